@@ -1,0 +1,1480 @@
+// hexopt_api.cu -- host runtime behind the C ABI of include/hexopt_gpu.h.
+//
+// One context = one CUDA stream + one batch of meshes resident in HBM.  Every compute stage is a
+// kernel launch over per-mesh segment tables (no block straddles two meshes, so every reduction
+// is per mesh and deterministic).  The host only uploads inputs, orders launches and downloads
+// results; there is no CPU compute path.
+#include <cuda_runtime.h>
+#include <cub/device/device_radix_sort.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/hexopt_gpu.h"
+#include "hexopt_bvh.h"
+#include "hexopt_kernels.h"
+
+using namespace hexopt;
+
+namespace {
+
+// ------------------------------------------------------------------ device buffer
+struct DBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t n) {
+    if (n == 0) n = 16;
+    if (n <= bytes) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    else p = nullptr;
+    return e;
+  }
+  template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+struct KindTable {
+  std::vector<Seg> segs;
+  DBuf dev;
+  int64_t nblk = 0;
+};
+
+struct StaticBvh {  // device LBVH over a fixed triangle set
+  DBuf child, parent, box, leaf_face, tri, counters;
+  int32_t n = 0;
+  BvhDev dev() const {
+    BvhDev b{};
+    b.n = n;
+    b.child = child.as<int32_t>();
+    b.box = box.as<float>();
+    b.leaf_face = leaf_face.as<int32_t>();
+    b.tri = tri.as<double>();
+    return b;
+  }
+};
+
+struct TargetHost {
+  bool set = false;
+  int64_t nv = 0, nf = 0;
+  std::vector<double> TV;
+  StaticBvh bvh;
+  DBuf TVd, FN, VNc, ENc, curve_ptr, curve_vs, curve_closed;
+  int64_t n_curves = 0;
+  double lo[3], hi[3];
+  std::vector<int64_t> ref_vs;  // vertices referenced by a face (target-local ids)
+};
+
+struct SurfaceHost {
+  bool set = false;
+  int64_t nf = 0;
+  DBuf F, child, parent, box, leaf_face, counters;
+  std::vector<int64_t> ref_vs;  // referenced vertices (global ids)
+};
+
+}  // namespace
+
+struct hexopt_ctx {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  int64_t launches = 0;
+  // batch
+  int n_meshes = 0;
+  int64_t NV = 0, NH = 0, NC = 0, NT = 0, NL = 0, NG = 0;
+  std::vector<MeshDesc> md;
+  DBuf md_d, sc_d;
+  std::vector<MeshScalars> sc;
+  DBuf X, hexv, gslot, Sinv, Ccoef, Bgen, aL;
+  DBuf b, diag, q64, ba, diaga, q64a;
+  DBuf d, r, p, q, invd, da, ra, pa, qa, invda;
+  DBuf stage, stage2, HJs, VJs, Xa, grad, Xbak;
+  bool adj_ready = false;
+  DBuf partials, counters;
+  DBuf c_ids, c_pos, t_ids, t_nrm, t_dis, l_ids, l_axis, l_orig, l_curve;
+  std::vector<int64_t> nC, nT, nL;
+  std::vector<double> lamC, lamT, lamL;
+  KindTable kind[8];
+  int block[8] = {128, 256, 256, 128, 128, 128, 128, 128};  // K_CONS follows K_VERT's size
+  // SLIM
+  hexopt_slim_params params{};
+  bool precomputed = false;
+  bool mixed = false;
+  // targets / surfaces
+  std::vector<TargetHost> tgt;
+  std::vector<SurfaceHost> surf;
+  DBuf tgt_d, surf_d, hm_d, tgt_vs_d, surf_vs_d;
+  std::vector<int64_t> tgt_vs_cnt, surf_vs_cnt;
+  bool haus_ready = false;
+  // feature alignment
+  double lamda0 = 0.05, HR = 0.005;
+  bool fa_ready = false;
+  bool use_graph = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool graph_hausdorff = false;
+  int64_t graph_launches = 0;
+};
+
+namespace {
+
+int fail(hexopt_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CK(call)                                                                            \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? HEXOPT_ERR_NOMEM : HEXOPT_ERR_CUDA, \
+                  "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);     \
+  } while (0)
+
+#define CKL()                                                                                 \
+  do {                                                                                        \
+    cudaError_t e_ = cudaGetLastError();                                                      \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail(ctx, HEXOPT_ERR_CUDA, "launch: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+template <typename T>
+cudaError_t upload(DBuf &buf, const T *src, size_t n, cudaStream_t st) {
+  cudaError_t e = buf.ensure(n * sizeof(T));
+  if (e != cudaSuccess) return e;
+  if (n && src) return cudaMemcpyAsync(buf.p, src, n * sizeof(T), cudaMemcpyHostToDevice, st);
+  return cudaSuccess;
+}
+
+// Build the segment table of one launch kind: counts per mesh, items numbered from item0.
+void build_kind(hexopt_ctx *c, int k, const std::vector<int64_t> &count, const std::vector<int64_t> &item0) {
+  KindTable &t = c->kind[k];
+  t.segs.clear();
+  const int B = c->block[k];
+  for (int m = 0; m < c->n_meshes; m++) {
+    const int64_t n = count[m];
+    const int64_t nb = std::max<int64_t>(1, (n + B - 1) / B);
+    c->md[m].kblk0[k] = (int64_t)t.segs.size();
+    c->md[m].knblk[k] = (int32_t)nb;
+    c->md[m].kitem0[k] = item0[m];
+    c->md[m].kcount[k] = n;
+    for (int64_t bk = 0; bk < nb; bk++) {
+      Seg s;
+      s.mesh = m;
+      s.blk_in_mesh = (int32_t)bk;
+      s.begin = item0[m] + bk * B;
+      s.end = std::min(item0[m] + n, s.begin + B);
+      if (s.begin > s.end) s.begin = s.end;
+      t.segs.push_back(s);
+    }
+  }
+  t.nblk = (int64_t)t.segs.size();
+}
+
+int rebuild_tables(hexopt_ctx *ctx) {
+  const int M = ctx->n_meshes;
+  ctx->block[K_CONS] = ctx->block[K_VERT];  // constraint launches use the vertex block size
+  std::vector<int64_t> cnt(M), it0(M);
+  int64_t off_c = 0, off_t = 0, off_l = 0;
+  for (int m = 0; m < M; m++) {
+    MeshDesc &d = ctx->md[m];
+    d.c_off = off_c; d.nc = ctx->nC[m];
+    d.t_off = off_t; d.nt = ctx->nT[m];
+    d.l_off = off_l; d.nl = ctx->nL[m];
+    off_c += d.nc; off_t += d.nt; off_l += d.nl;
+  }
+  ctx->NC = off_c; ctx->NT = off_t; ctx->NL = off_l;
+  for (int m = 0; m < M; m++) { cnt[m] = ctx->md[m].nh; it0[m] = ctx->md[m].h_off; }
+  build_kind(ctx, K_HEX, cnt, it0);
+  for (int m = 0; m < M; m++) { cnt[m] = ctx->md[m].nv + ctx->md[m].nl; it0[m] = ctx->md[m].v_off + ctx->md[m].l_off; }
+  build_kind(ctx, K_VERT, cnt, it0);
+  for (int m = 0; m < M; m++) {
+    cnt[m] = ctx->md[m].nc + ctx->md[m].nt + ctx->md[m].nl;
+    it0[m] = ctx->md[m].c_off + ctx->md[m].t_off + ctx->md[m].l_off;
+  }
+  build_kind(ctx, K_CONS, cnt, it0);
+  for (int m = 0; m < M; m++) { cnt[m] = ctx->md[m].nt; it0[m] = ctx->md[m].t_off; }
+  build_kind(ctx, K_PROJ, cnt, it0);
+  for (int m = 0; m < M; m++) { cnt[m] = ctx->md[m].nl; it0[m] = ctx->md[m].l_off; }
+  build_kind(ctx, K_LINE, cnt, it0);
+  {
+    int64_t o = 0;
+    for (int m = 0; m < M; m++) { cnt[m] = m < (int)ctx->tgt_vs_cnt.size() ? ctx->tgt_vs_cnt[m] : 0; it0[m] = o; o += cnt[m]; }
+    build_kind(ctx, K_TGTV, cnt, it0);
+    o = 0;
+    for (int m = 0; m < M; m++) { cnt[m] = m < (int)ctx->surf_vs_cnt.size() ? ctx->surf_vs_cnt[m] : 0; it0[m] = o; o += cnt[m]; }
+    build_kind(ctx, K_SURFV, cnt, it0);
+  }
+  for (int m = 0; m < M; m++) { cnt[m] = 0; it0[m] = 0; }
+  build_kind(ctx, K_SURFF, cnt, it0);
+  for (int m = 0; m < M; m++) {
+    MeshDesc &d = ctx->md[m];
+    d.hblk0 = d.kblk0[K_HEX]; d.nhblk = d.knblk[K_HEX];
+    d.vblk0 = d.kblk0[K_VERT]; d.nvblk = d.knblk[K_VERT];
+    d.cblk0 = d.kblk0[K_CONS]; d.ncblk = d.knblk[K_CONS];
+  }
+  int64_t maxblk = 0;
+  for (int k = 0; k < 8; k++) {
+    maxblk = std::max(maxblk, ctx->kind[k].nblk);
+    CK(upload(ctx->kind[k].dev, ctx->kind[k].segs.data(), ctx->kind[k].segs.size(), ctx->st));
+  }
+  CK(ctx->partials.ensure(sizeof(double) * (size_t)(maxblk + 1) * kMaxCand));
+  CK(upload(ctx->md_d, ctx->md.data(), ctx->md.size(), ctx->st));
+  return HEXOPT_OK;
+}
+
+KArgs make_args(hexopt_ctx *c) {
+  KArgs a{};
+  a.mesh = c->md_d.as<MeshDesc>();
+  a.sc = c->sc_d.as<MeshScalars>();
+  a.hseg = c->kind[K_HEX].dev.as<Seg>();
+  a.vseg = c->kind[K_VERT].dev.as<Seg>();
+  a.cseg = c->kind[K_CONS].dev.as<Seg>();
+  a.partials = c->partials.as<double>();
+  a.counters = c->counters.as<unsigned>();
+  a.hexv = c->hexv.as<uint32_t>();
+  a.gslot = c->gslot.as<int32_t>();
+  a.X = c->X.as<double>();
+  a.aL = c->aL.as<double>();
+  a.Sinv = c->Sinv.p;
+  a.Ccoef = c->Ccoef.p;
+  a.Bgen = c->Bgen.as<double>();
+  a.b = c->b.as<double>(); a.diag = c->diag.as<double>(); a.ba = c->ba.as<double>(); a.diaga = c->diaga.as<double>();
+  a.d = c->d.p; a.r = c->r.p; a.p = c->p.p; a.q = c->q.p; a.invd = c->invd.p;
+  a.da = c->da.p; a.ra = c->ra.p; a.pa = c->pa.p; a.qa = c->qa.p; a.invda = c->invda.p;
+  a.c_ids = c->c_ids.as<int32_t>(); a.c_pos = c->c_pos.as<double>();
+  a.t_ids = c->t_ids.as<int32_t>(); a.t_nrm = c->t_nrm.as<double>(); a.t_dis = c->t_dis.as<double>();
+  a.l_ids = c->l_ids.as<int32_t>(); a.l_axis = c->l_axis.as<double>(); a.l_orig = c->l_orig.as<double>();
+  a.energy = c->params.energy;
+  a.cg_max_iter = c->params.cg_max_iter;
+  a.ls_cand = c->params.ls_candidates;
+  a.cg_tol = c->params.cg_tol;
+  a.sc_exp_f = c->params.exp_factor;
+  a.hthreads = c->block[K_HEX];
+  a.vthreads = c->block[K_VERT];
+  a.Xa = c->Xa.as<double>();
+  a.grad = c->grad.as<double>();
+  return a;
+}
+
+int alloc_vectors(hexopt_ctx *ctx) {
+  const size_t nv4 = (size_t)std::max<int64_t>(ctx->NV, 1) * 4;
+  const size_t nl = (size_t)std::max<int64_t>(ctx->NL, 1);
+  const size_t vt = ctx->mixed ? sizeof(float) : sizeof(double);
+  for (DBuf *bf : {&ctx->b, &ctx->diag, &ctx->q64}) CK(bf->ensure(nv4 * sizeof(double)));
+  for (DBuf *bf : {&ctx->d, &ctx->r, &ctx->p, &ctx->q, &ctx->invd}) CK(bf->ensure(nv4 * vt));
+  for (DBuf *bf : {&ctx->ba, &ctx->diaga, &ctx->q64a, &ctx->aL}) CK(bf->ensure(nl * sizeof(double)));
+  for (DBuf *bf : {&ctx->da, &ctx->ra, &ctx->pa, &ctx->qa, &ctx->invda}) CK(bf->ensure(nl * vt));
+  const size_t nt = (size_t)((ctx->NH + 31) / 32 * 32) * 8;
+  CK(ctx->Sinv.ensure(nt * vt));
+  CK(ctx->Ccoef.ensure(nt * 6 * vt));
+  CK(ctx->Bgen.ensure((size_t)std::max<int64_t>(ctx->NG, 1) * 8 * 9 * sizeof(double)));
+  return HEXOPT_OK;
+}
+
+int push_scalars(hexopt_ctx *ctx) {
+  CK(upload(ctx->sc_d, ctx->sc.data(), ctx->sc.size(), ctx->st));
+  return HEXOPT_OK;
+}
+int pull_scalars(hexopt_ctx *ctx) {
+  CK(cudaMemcpyAsync(ctx->sc.data(), ctx->sc_d.p, sizeof(MeshScalars) * ctx->sc.size(), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
+// ------------------------------------------------------------------ SLIM stages
+template <typename ET, typename VT>
+int run_precompute(hexopt_ctx *ctx) {
+  KArgs a = make_args(ctx);
+  launch_precompute<ET, VT>(a, ctx->kind[K_HEX].nblk, ctx->st);
+  ctx->launches += 1;
+  CKL();
+  return HEXOPT_OK;
+}
+
+template <typename ET, typename VT>
+int run_iteration(hexopt_ctx *ctx) {
+  KArgs a = make_args(ctx);
+  cudaStream_t st = ctx->st;
+  const size_t nv4 = (size_t)ctx->NV * 4;
+  CK(cudaMemsetAsync(ctx->b.p, 0, nv4 * sizeof(double), st));
+  CK(cudaMemsetAsync(ctx->diag.p, 0, nv4 * sizeof(double), st));
+  CK(cudaMemsetAsync(ctx->q64.p, 0, nv4 * sizeof(double), st));
+  if (ctx->NL) CK(cudaMemsetAsync(ctx->q64a.p, 0, (size_t)ctx->NL * sizeof(double), st));
+  const int64_t hb = ctx->kind[K_HEX].nblk, vb = ctx->kind[K_VERT].nblk, cb = ctx->kind[K_CONS].nblk;
+  launch_local<ET, VT>(a, hb, st);
+  launch_soft_rhs<VT>(a, cb, st);
+  launch_residual_elems<ET, VT>(a, hb, ctx->q64.as<double>(), st);
+  launch_soft_residual<VT>(a, cb, ctx->q64.as<double>(), ctx->q64a.as<double>(), st);
+  launch_cg_start<VT>(a, vb, ctx->q64.as<double>(), ctx->q64a.as<double>(), st);
+  ctx->launches += 5;
+  for (int i = 0; i < ctx->params.cg_max_iter; i++) launch_cg_iter<VT>(a, hb, vb, cb, st);
+  ctx->launches += (int64_t)kLaunchesCgIter * ctx->params.cg_max_iter;
+  launch_line_search<ET, VT>(a, hb, vb, cb, st);
+  const int rounds = (kHalvings + 1 + ctx->params.ls_candidates - 1) / ctx->params.ls_candidates;
+  ctx->launches += 3 + 2 * rounds;
+  CKL();
+  return HEXOPT_OK;
+}
+
+int dispatch_precompute(hexopt_ctx *ctx) {
+  return ctx->mixed ? run_precompute<float, float>(ctx) : run_precompute<double, double>(ctx);
+}
+int dispatch_iteration(hexopt_ctx *ctx) {
+  return ctx->mixed ? run_iteration<float, float>(ctx) : run_iteration<double, double>(ctx);
+}
+
+void fill_report(const MeshScalars &S, hexopt_slim_report &r) {
+  r.energy = S.energy;
+  r.energy_quality = S.eq;
+  r.energy_soft = S.es;
+  r.cg_error = S.cg_error;
+  r.max_step = S.max_step;
+  r.step = S.step;
+  r.cg_iters = S.cg_iters;
+  r.halvings = S.halvings;
+  r.status = S.status;
+  r.pad = 0;
+}
+
+// ------------------------------------------------------------------ BVH builds
+int build_static_bvh(hexopt_ctx *ctx, StaticBvh &B, const std::vector<double> &tri, int64_t nf) {
+  B.n = (int32_t)nf;
+  if (nf == 0) return HEXOPT_OK;
+  CK(upload(B.tri, tri.data(), tri.size(), ctx->st));
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t f = 0; f < nf; f++)
+    for (int c = 0; c < 3; c++) {
+      const double *p = &tri[f * 9 + c * 3];
+      double cen = (tri[f * 9 + c] + tri[f * 9 + 3 + c] + tri[f * 9 + 6 + c]) / 3;
+      (void)p;
+      lo[c] = std::min(lo[c], cen);
+      hi[c] = std::max(hi[c], cen);
+    }
+  CK(B.child.ensure(sizeof(int32_t) * 2 * std::max<int64_t>(nf - 1, 1)));
+  CK(B.parent.ensure(sizeof(int32_t) * (2 * nf - 1)));
+  CK(B.box.ensure(sizeof(float) * 6 * (2 * nf - 1)));
+  CK(B.leaf_face.ensure(sizeof(int32_t) * nf));
+  CK(B.counters.ensure(sizeof(unsigned) * std::max<int64_t>(nf - 1, 1)));
+  CK(cudaMemsetAsync(B.counters.p, 0, sizeof(unsigned) * std::max<int64_t>(nf - 1, 1), ctx->st));
+  DBuf keys, keys2, tmp;
+  CK(keys.ensure(sizeof(unsigned long long) * nf));
+  CK(keys2.ensure(sizeof(unsigned long long) * nf));
+  BvhDev bd = B.dev();
+  bvh_morton(bd, lo, hi, keys.as<unsigned long long>(), ctx->st);
+  size_t tb = 0;
+  CK(cub::DeviceRadixSort::SortKeys(nullptr, tb, keys.as<unsigned long long>(), keys2.as<unsigned long long>(), (int)nf, 0, 64, ctx->st));
+  CK(tmp.ensure(tb));
+  CK(cub::DeviceRadixSort::SortKeys(tmp.p, tb, keys.as<unsigned long long>(), keys2.as<unsigned long long>(), (int)nf, 0, 64, ctx->st));
+  bvh_karras((int)nf, keys2.as<unsigned long long>(), B.child.as<int32_t>(), B.parent.as<int32_t>(), B.leaf_face.as<int32_t>(), ctx->st);
+  bd = B.dev();
+  bvh_refit(bd, B.box.as<float>(), B.parent.as<int32_t>(), B.counters.as<unsigned>(), ctx->st);
+  ctx->launches += 4;
+  CKL();
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
+int upload_targets_table(hexopt_ctx *ctx) {
+  std::vector<TargetDev> td(ctx->n_meshes);
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    TargetDev t{};
+    TargetHost &h = ctx->tgt[m];
+    if (h.set) {
+      t.bvh = h.bvh.dev();
+      t.TV = h.TVd.as<double>();
+      t.tri = h.bvh.tri.as<double>();
+      t.FN = h.FN.as<double>();
+      t.VNc = h.VNc.as<double>();
+      t.ENc = h.ENc.as<double>();
+      t.curve_ptr = h.curve_ptr.as<int64_t>();
+      t.curve_vs = h.curve_vs.as<int32_t>();
+      t.curve_closed = h.curve_closed.as<uint8_t>();
+    }
+    td[m] = t;
+  }
+  CK(upload(ctx->tgt_d, td.data(), td.size(), ctx->st));
+  std::vector<BvhDev> sd(ctx->n_meshes);
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    BvhDev b{};
+    SurfaceHost &s = ctx->surf[m];
+    if (s.set) {
+      b.n = (int32_t)s.nf;
+      b.child = s.child.as<int32_t>();
+      b.box = s.box.as<float>();
+      b.leaf_face = s.leaf_face.as<int32_t>();
+      b.F = s.F.as<int32_t>();
+      b.X = ctx->X.as<double>();
+    }
+    sd[m] = b;
+  }
+  CK(upload(ctx->surf_d, sd.data(), sd.size(), ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
+ProjArgs make_proj(hexopt_ctx *c, int kind) {
+  ProjArgs p{};
+  p.seg = c->kind[kind].dev.as<Seg>();
+  p.mesh = c->md_d.as<MeshDesc>();
+  p.sc = c->sc_d.as<MeshScalars>();
+  p.tgt = c->tgt_d.as<TargetDev>();
+  p.X = c->X.as<double>();
+  p.t_ids = c->t_ids.as<int32_t>(); p.t_nrm = c->t_nrm.as<double>(); p.t_dis = c->t_dis.as<double>();
+  p.l_ids = c->l_ids.as<int32_t>(); p.l_curve = c->l_curve.as<int32_t>();
+  p.l_axis = c->l_axis.as<double>(); p.l_orig = c->l_orig.as<double>();
+  return p;
+}
+
+HausArgs make_haus(hexopt_ctx *c, int kind) {
+  HausArgs h{};
+  h.seg = c->kind[kind].dev.as<Seg>();
+  h.mesh = c->md_d.as<MeshDesc>();
+  h.sc = c->sc_d.as<MeshScalars>();
+  h.tgt = c->tgt_d.as<TargetDev>();
+  h.surf = c->surf_d.as<BvhDev>();
+  h.hm = c->hm_d.as<HausMesh>();
+  h.X = c->X.as<double>();
+  h.tgt_vs = c->tgt_vs_d.as<int64_t>();
+  h.surf_vs = c->surf_vs_d.as<int64_t>();
+  h.partials = c->partials.as<double>();
+  h.counters = c->counters.as<unsigned>();
+  return h;
+}
+
+int run_projection(hexopt_ctx *ctx) {
+  if (ctx->NT) {
+    launch_project(make_proj(ctx, K_PROJ), ctx->kind[K_PROJ].nblk, ctx->st);
+    ctx->launches++;
+  }
+  if (ctx->NL) {
+    launch_curve_project(make_proj(ctx, K_LINE), ctx->kind[K_LINE].nblk, ctx->st);
+    ctx->launches++;
+  }
+  CKL();
+  return HEXOPT_OK;
+}
+
+int run_hausdorff(hexopt_ctx *ctx) {
+  // refit the dynamic surface trees at the current positions
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    SurfaceHost &s = ctx->surf[m];
+    if (!s.set || s.nf == 0) continue;
+    BvhDev b{};
+    b.n = (int32_t)s.nf;
+    b.child = s.child.as<int32_t>();
+    b.leaf_face = s.leaf_face.as<int32_t>();
+    b.F = s.F.as<int32_t>();
+    b.X = ctx->X.as<double>();
+    bvh_refit(b, s.box.as<float>(), s.parent.as<int32_t>(), s.counters.as<unsigned>(), ctx->st);
+    ctx->launches++;
+  }
+  launch_haus_bbox(make_haus(ctx, K_SURFV), ctx->kind[K_SURFV].nblk, ctx->st);
+  launch_haus_side(make_haus(ctx, K_TGTV), 0, ctx->kind[K_TGTV].nblk, ctx->st);
+  launch_haus_side(make_haus(ctx, K_SURFV), 1, ctx->kind[K_SURFV].nblk, ctx->st);
+  ctx->launches += 3;
+  CKL();
+  return HEXOPT_OK;
+}
+
+int check_ctx(hexopt_ctx *ctx) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  if (ctx->n_meshes <= 0) return fail(ctx, HEXOPT_ERR_STATE, "no meshes uploaded");
+  return HEXOPT_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+int hexopt_create(hexopt_ctx **out, int device) {
+  if (!out) return HEXOPT_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return HEXOPT_ERR_CUDA;
+  if (device < 0 || device >= n) return HEXOPT_ERR_ARG;
+  hexopt_ctx *ctx = new hexopt_ctx();
+  ctx->device = device;
+  e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return HEXOPT_ERR_CUDA;
+  }
+  ctx->params.energy = HEXOPT_SYMMETRIC_DIRICHLET;
+  ctx->params.precision = HEXOPT_FP64;
+  ctx->params.weight_opt = 1.0;
+  ctx->params.exp_factor = 5.0;
+  ctx->params.cg_max_iter = 20;
+  ctx->params.cg_tol = 1e-8;
+  ctx->params.ls_candidates = 4;
+  ctx->params.cube = 1;
+  *out = ctx;
+  return HEXOPT_OK;
+}
+
+void hexopt_destroy(hexopt_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+  delete ctx;
+}
+
+const char *hexopt_last_error(const hexopt_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int hexopt_sync(hexopt_ctx *ctx) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
+int64_t hexopt_num_vertices(const hexopt_ctx *ctx) { return ctx ? ctx->NV : 0; }
+int64_t hexopt_num_hexes(const hexopt_ctx *ctx) { return ctx ? ctx->NH : 0; }
+int hexopt_num_meshes(const hexopt_ctx *ctx) { return ctx ? ctx->n_meshes : 0; }
+int64_t hexopt_launch_count(const hexopt_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const int64_t *nh, const double *V,
+                         const uint32_t *H, const uint8_t *h_flag) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  if (n_meshes <= 0 || !nv || !nh || !V || !H) return fail(ctx, HEXOPT_ERR_ARG, "upload_meshes: bad arguments");
+  CK(cudaSetDevice(ctx->device));
+  int64_t NV = 0, NH = 0;
+  for (int m = 0; m < n_meshes; m++) {
+    if (nv[m] <= 0 || nh[m] <= 0) return fail(ctx, HEXOPT_ERR_ARG, "mesh %d: empty (nv=%lld nh=%lld)", m, (long long)nv[m], (long long)nh[m]);
+    NV += nv[m];
+    NH += nh[m];
+  }
+  if (NV >= (int64_t)UINT32_MAX) return fail(ctx, HEXOPT_ERR_ARG, "too many vertices in one batch");
+  // validate hex ids (host, integer pass over the input)
+  {
+    int64_t ho = 0;
+    for (int m = 0; m < n_meshes; m++) {
+      for (int64_t i = 0; i < 8 * nh[m]; i++)
+        if (H[8 * ho + i] >= (uint64_t)nv[m]) return fail(ctx, HEXOPT_ERR_ARG, "mesh %d: hex corner id out of range", m);
+      ho += nh[m];
+    }
+  }
+  ctx->n_meshes = n_meshes;
+  ctx->NV = NV;
+  ctx->NH = NH;
+  ctx->md.assign(n_meshes, MeshDesc{});
+  ctx->sc.assign(n_meshes, MeshScalars{});
+  ctx->nC.assign(n_meshes, 0); ctx->nT.assign(n_meshes, 0); ctx->nL.assign(n_meshes, 0);
+  ctx->lamC.assign(n_meshes, 0); ctx->lamT.assign(n_meshes, 0); ctx->lamL.assign(n_meshes, 0);
+  ctx->tgt.clear(); ctx->tgt.resize(n_meshes);
+  ctx->surf.clear(); ctx->surf.resize(n_meshes);
+  ctx->tgt_vs_cnt.assign(n_meshes, 0);
+  ctx->surf_vs_cnt.assign(n_meshes, 0);
+  ctx->precomputed = false;
+  ctx->fa_ready = false;
+  ctx->haus_ready = false;
+  if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+  // own-shape slots
+  std::vector<int32_t> gs(NH, -1);
+  int64_t ng = 0;
+  if (h_flag)
+    for (int64_t h = 0; h < NH; h++)
+      if (!h_flag[h]) gs[h] = (int32_t)ng++;
+  ctx->NG = ng;
+  int64_t vo = 0, ho = 0;
+  for (int m = 0; m < n_meshes; m++) {
+    ctx->md[m].v_off = vo; ctx->md[m].nv = nv[m];
+    ctx->md[m].h_off = ho; ctx->md[m].nh = nh[m];
+    vo += nv[m]; ho += nh[m];
+  }
+  // positions
+  CK(upload(ctx->stage, V, (size_t)NV * 3, ctx->st));
+  CK(ctx->X.ensure(sizeof(double) * 4 * NV));
+  launch_rows_to_aos4(ctx->stage.as<double>(), ctx->X.as<double>(), NV, ctx->st);
+  // hexes -> AoSoA with global ids
+  const int64_t NHp = (NH + 31) / 32 * 32;
+  CK(upload(ctx->stage2, H, (size_t)NH * 8, ctx->st));
+  CK(ctx->hexv.ensure(sizeof(uint32_t) * 8 * NHp));
+  CK(cudaMemsetAsync(ctx->hexv.p, 0, sizeof(uint32_t) * 8 * NHp, ctx->st));
+  for (int m = 0; m < n_meshes; m++)
+    launch_hex_to_aosoa_mesh(ctx->stage2.as<uint32_t>() + 8 * ctx->md[m].h_off, ctx->md[m].h_off, nh[m],
+                             (uint32_t)ctx->md[m].v_off, ctx->hexv.as<uint32_t>(), ctx->st);
+  ctx->launches += 1 + n_meshes;
+  CK(upload(ctx->gslot, gs.data(), gs.size(), ctx->st));
+  CK(ctx->counters.ensure(sizeof(unsigned) * n_meshes));
+  CK(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned) * n_meshes, ctx->st));
+  int rc = rebuild_tables(ctx);
+  if (rc) return rc;
+  CK(upload(ctx->sc_d, ctx->sc.data(), ctx->sc.size(), ctx->st));
+  CK(ctx->HJs.ensure(sizeof(double) * NH));
+  CK(cudaStreamSynchronize(ctx->st));
+  CKL();
+  return HEXOPT_OK;
+}
+
+int hexopt_set_positions(hexopt_ctx *ctx, const double *V) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!V) return fail(ctx, HEXOPT_ERR_ARG, "set_positions: NULL");
+  CK(upload(ctx->stage, V, (size_t)ctx->NV * 3, ctx->st));
+  launch_rows_to_aos4(ctx->stage.as<double>(), ctx->X.as<double>(), ctx->NV, ctx->st);
+  ctx->launches++;
+  CKL();
+  return HEXOPT_OK;
+}
+
+int hexopt_get_positions(hexopt_ctx *ctx, double *V) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!V) return fail(ctx, HEXOPT_ERR_ARG, "get_positions: NULL");
+  CK(ctx->stage.ensure(sizeof(double) * 3 * ctx->NV));
+  launch_aos4_to_rows(ctx->X.as<double>(), ctx->stage.as<double>(), ctx->NV, ctx->st);
+  ctx->launches++;
+  CK(cudaMemcpyAsync(V, ctx->stage.p, sizeof(double) * 3 * ctx->NV, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
+int hexopt_scaled_jacobian(hexopt_ctx *ctx, double *V_Js, double *H_Js, hexopt_quality *q) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  KArgs a = make_args(ctx);
+  double *vj = nullptr;
+  if (V_Js) {
+    CK(ctx->VJs.ensure(sizeof(double) * 8 * ctx->NH));
+    vj = ctx->VJs.as<double>();
+  }
+  launch_scaled_jacobian(a, ctx->kind[K_HEX].nblk, vj, ctx->HJs.as<double>(), ctx->st);
+  ctx->launches += 2;
+  CKL();
+  if (V_Js) CK(cudaMemcpyAsync(V_Js, vj, sizeof(double) * 8 * ctx->NH, cudaMemcpyDeviceToHost, ctx->st));
+  if (H_Js) CK(cudaMemcpyAsync(H_Js, ctx->HJs.p, sizeof(double) * ctx->NH, cudaMemcpyDeviceToHost, ctx->st));
+  rc = pull_scalars(ctx);
+  if (rc) return rc;
+  if (q)
+    for (int m = 0; m < ctx->n_meshes; m++) {
+      const MeshScalars &S = ctx->sc[m];
+      q[m].min_Jacobian = S.sj_min;
+      q[m].ave_Jacobian = S.sj_sum / (double)ctx->md[m].nh;
+      q[m].deviation_Jacobian = S.sj_dev;
+      q[m].n_inverted = S.n_inv;
+    }
+  return HEXOPT_OK;
+}
+
+static int set_list(hexopt_ctx *ctx, const int64_t *counts, std::vector<int64_t> &dst, const int32_t *ids,
+                    DBuf &ids_d, const char *what) {
+  int64_t tot = 0;
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    if (counts[m] < 0) return fail(ctx, HEXOPT_ERR_ARG, "%s: negative count", what);
+    for (int64_t i = 0; i < counts[m]; i++)
+      if (ids[tot + i] < 0 || ids[tot + i] >= ctx->md[m].nv) return fail(ctx, HEXOPT_ERR_ARG, "%s: vertex id out of range", what);
+    tot += counts[m];
+  }
+  dst.assign(counts, counts + ctx->n_meshes);
+  CK(upload(ids_d, ids, (size_t)tot, ctx->st));
+  return HEXOPT_OK;
+}
+
+int hexopt_set_corners(hexopt_ctx *ctx, const int64_t *nC, const int32_t *ids, const double *C) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  rc = set_list(ctx, nC, ctx->nC, ids, ctx->c_ids, "set_corners");
+  if (rc) return rc;
+  int64_t tot = 0;
+  for (int m = 0; m < ctx->n_meshes; m++) tot += nC[m];
+  CK(upload(ctx->c_pos, C, (size_t)tot * 3, ctx->st));
+  ctx->haus_ready = false;
+  return rebuild_tables(ctx);
+}
+
+int hexopt_set_tangents(hexopt_ctx *ctx, const int64_t *nT, const int32_t *ids, const double *normal, const double *dis) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  rc = set_list(ctx, nT, ctx->nT, ids, ctx->t_ids, "set_tangents");
+  if (rc) return rc;
+  int64_t tot = 0;
+  for (int m = 0; m < ctx->n_meshes; m++) tot += nT[m];
+  CK(upload(ctx->t_nrm, normal, (size_t)tot * 3, ctx->st));
+  CK(upload(ctx->t_dis, dis, (size_t)tot, ctx->st));
+  return rebuild_tables(ctx);
+}
+
+int hexopt_set_lines(hexopt_ctx *ctx, const int64_t *nL, const int32_t *ids, const double *axis, const double *origin) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  rc = set_list(ctx, nL, ctx->nL, ids, ctx->l_ids, "set_lines");
+  if (rc) return rc;
+  int64_t tot = 0;
+  for (int m = 0; m < ctx->n_meshes; m++) tot += nL[m];
+  CK(upload(ctx->l_axis, axis, (size_t)tot * 3, ctx->st));
+  CK(upload(ctx->l_orig, origin, (size_t)tot * 3, ctx->st));
+  ctx->NL = tot;
+  ctx->precomputed = false;  // unknown count changed
+  return rebuild_tables(ctx);
+}
+
+int hexopt_set_weights(hexopt_ctx *ctx, const double *lC, const double *lT, const double *lL) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  rc = pull_scalars(ctx);
+  if (rc) return rc;
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    if (lC) ctx->lamC[m] = ctx->sc[m].lamda_C = lC[m];
+    if (lT) ctx->lamT[m] = ctx->sc[m].lamda_T = lT[m];
+    if (lL) ctx->lamL[m] = ctx->sc[m].lamda_L = lL[m];
+  }
+  return push_scalars(ctx);
+}
+
+int hexopt_get_tangents(hexopt_ctx *ctx, double *normal, double *dis) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (ctx->NT) {
+    if (normal) CK(cudaMemcpyAsync(normal, ctx->t_nrm.p, sizeof(double) * 3 * ctx->NT, cudaMemcpyDeviceToHost, ctx->st));
+    if (dis) CK(cudaMemcpyAsync(dis, ctx->t_dis.p, sizeof(double) * ctx->NT, cudaMemcpyDeviceToHost, ctx->st));
+  }
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
+int hexopt_get_lines(hexopt_ctx *ctx, double *axis, double *origin) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (ctx->NL) {
+    if (axis) CK(cudaMemcpyAsync(axis, ctx->l_axis.p, sizeof(double) * 3 * ctx->NL, cudaMemcpyDeviceToHost, ctx->st));
+    if (origin) CK(cudaMemcpyAsync(origin, ctx->l_orig.p, sizeof(double) * 3 * ctx->NL, cudaMemcpyDeviceToHost, ctx->st));
+  }
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
+int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *p) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!p) return fail(ctx, HEXOPT_ERR_ARG, "slim_precompute: NULL params");
+  if (p->energy < 0 || p->energy > 5) return fail(ctx, HEXOPT_ERR_ARG, "unknown energy %d", p->energy);
+  if (p->precision != HEXOPT_FP64 && p->precision != HEXOPT_MIXED) return fail(ctx, HEXOPT_ERR_ARG, "unknown precision");
+  if (p->ls_candidates < 1 || p->ls_candidates > kMaxCand) return fail(ctx, HEXOPT_ERR_ARG, "ls_candidates must be 1..%d", kMaxCand);
+  if (p->cg_max_iter < 0) return fail(ctx, HEXOPT_ERR_ARG, "cg_max_iter < 0");
+  if (!p->cube) return fail(ctx, HEXOPT_ERR_UNSUPPORTED, "cube = 0 reference shapes (edge-averaged cuboids) are not implemented");
+  ctx->params = *p;
+  ctx->mixed = p->precision == HEXOPT_MIXED;
+  rc = alloc_vectors(ctx);
+  if (rc) return rc;
+  rc = pull_scalars(ctx);
+  if (rc) return rc;
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    MeshScalars &S = ctx->sc[m];
+    S.M = p->weight_opt;
+    S.prox = 0.00001 * p->weight_opt;  // slim_m.cpp:1118
+    S.exp_f = p->exp_factor;
+    S.status = 0;
+  }
+  rc = push_scalars(ctx);
+  if (rc) return rc;
+  rc = dispatch_precompute(ctx);
+  if (rc) return rc;
+  ctx->precomputed = true;
+  return HEXOPT_OK;
+}
+
+int hexopt_slim_iterate(hexopt_ctx *ctx, int iters, hexopt_slim_report *rep) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!ctx->precomputed) return fail(ctx, HEXOPT_ERR_STATE, "slim_iterate before slim_precompute");
+  for (int i = 0; i < iters; i++) {
+    rc = dispatch_iteration(ctx);
+    if (rc) return rc;
+  }
+  if (rep) {
+    rc = pull_scalars(ctx);
+    if (rc) return rc;
+    for (int m = 0; m < ctx->n_meshes; m++) fill_report(ctx->sc[m], rep[m]);
+  }
+  return HEXOPT_OK;
+}
+
+int hexopt_slim_m_opt(hexopt_ctx *ctx, const hexopt_slim_params *p, int iters, hexopt_slim_report *rep) {
+  int rc = hexopt_slim_precompute(ctx, p);
+  if (rc) return rc;
+  return hexopt_slim_iterate(ctx, iters, rep);
+}
+
+int hexopt_get_curve_params(hexopt_ctx *ctx, double *a_L) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (ctx->NL && a_L) CK(cudaMemcpyAsync(a_L, ctx->aL.p, sizeof(double) * ctx->NL, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
+// ---------------------------------------------------------------- targets / projection
+int hexopt_set_target(hexopt_ctx *ctx, int mesh, int64_t nv, const double *TV, int64_t nf, const int32_t *TF) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (mesh < 0 || mesh >= ctx->n_meshes) return fail(ctx, HEXOPT_ERR_ARG, "set_target: bad mesh");
+  if (nv <= 0 || nf <= 0 || !TV || !TF) return fail(ctx, HEXOPT_ERR_ARG, "set_target: empty target");
+  for (int64_t i = 0; i < 3 * nf; i++)
+    if (TF[i] < 0 || TF[i] >= nv) return fail(ctx, HEXOPT_ERR_ARG, "set_target: face id out of range");
+  TargetHost &t = ctx->tgt[mesh];
+  t.nv = nv;
+  t.nf = nf;
+  t.TV.assign(TV, TV + 3 * nv);
+  // triangle soup and the normals of build_aabb_tree (per_face_normals, per_vertex_normals with
+  // angle weights, per_edge_normals uniform -- left unnormalised as the reference leaves them).
+  std::vector<double> tri(9 * nf), FN(3 * nf, 0.0), VN(3 * nv, 0.0), VNc(9 * nf), ENc(9 * nf);
+  for (int64_t f = 0; f < nf; f++) {
+    for (int c = 0; c < 3; c++)
+      for (int d = 0; d < 3; d++) tri[9 * f + 3 * c + d] = TV[3 * (int64_t)TF[3 * f + c] + d];
+    const double *p0 = &tri[9 * f], *p1 = &tri[9 * f + 3], *p2 = &tri[9 * f + 6];
+    const double e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]}, e2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+    const double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    const double r = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (r != 0)
+      for (int d = 0; d < 3; d++) FN[3 * f + d] = n[d] / r;
+  }
+  for (int64_t f = 0; f < nf; f++) {
+    double L[3];
+    for (int c = 0; c < 3; c++) {
+      const double *a = &tri[9 * f + 3 * ((c + 1) % 3)], *b = &tri[9 * f + 3 * ((c + 2) % 3)];
+      L[c] = (a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]);
+    }
+    for (int d = 0; d < 3; d++) {
+      const double s1 = L[d], s2 = L[(d + 1) % 3], s3 = L[(d + 2) % 3];
+      const double ang = std::acos((s3 + s2 - s1) / (2. * std::sqrt(s3 * s2)));
+      for (int k = 0; k < 3; k++) VN[3 * (int64_t)TF[3 * f + d] + k] += ang * FN[3 * f + k];
+    }
+  }
+  for (int64_t v = 0; v < nv; v++) {
+    const double r = std::sqrt(VN[3 * v] * VN[3 * v] + VN[3 * v + 1] * VN[3 * v + 1] + VN[3 * v + 2] * VN[3 * v + 2]);
+    if (r > 0)
+      for (int d = 0; d < 3; d++) VN[3 * v + d] /= r;
+  }
+  // undirected edges: sort (min, max, face*3+corner)
+  std::vector<std::pair<uint64_t, int64_t>> E(3 * nf);
+  for (int64_t f = 0; f < nf; f++)
+    for (int c = 0; c < 3; c++) {
+      uint64_t a = (uint64_t)TF[3 * f + (c + 1) % 3], b = (uint64_t)TF[3 * f + (c + 2) % 3];
+      if (a > b) std::swap(a, b);
+      E[3 * f + c] = {a * (uint64_t)(nv + 1) + b, 3 * f + c};
+    }
+  std::sort(E.begin(), E.end());
+  for (size_t i = 0; i < E.size();) {
+    size_t j = i;
+    double s[3] = {0, 0, 0};
+    while (j < E.size() && E[j].first == E[i].first) {
+      const int64_t f = E[j].second / 3;
+      for (int d = 0; d < 3; d++) s[d] += FN[3 * f + d];
+      j++;
+    }
+    for (size_t k = i; k < j; k++)
+      for (int d = 0; d < 3; d++) ENc[9 * (E[k].second / 3) + 3 * (E[k].second % 3) + d] = s[d];
+    i = j;
+  }
+  for (int64_t f = 0; f < nf; f++)
+    for (int c = 0; c < 3; c++)
+      for (int d = 0; d < 3; d++) VNc[9 * f + 3 * c + d] = VN[3 * (int64_t)TF[3 * f + c] + d];
+  for (int d = 0; d < 3; d++) { t.lo[d] = INFINITY; t.hi[d] = -INFINITY; }
+  std::vector<uint8_t> used(nv, 0);
+  for (int64_t i = 0; i < 3 * nf; i++) used[TF[i]] = 1;
+  for (int64_t v = 0; v < nv; v++)
+    for (int d = 0; d < 3; d++) {
+      t.lo[d] = std::min(t.lo[d], TV[3 * v + d]);
+      t.hi[d] = std::max(t.hi[d], TV[3 * v + d]);
+    }
+  CK(upload(t.TVd, TV, (size_t)3 * nv, ctx->st));
+  CK(upload(t.FN, FN.data(), FN.size(), ctx->st));
+  CK(upload(t.VNc, VNc.data(), VNc.size(), ctx->st));
+  CK(upload(t.ENc, ENc.data(), ENc.size(), ctx->st));
+  rc = build_static_bvh(ctx, t.bvh, tri, nf);
+  if (rc) return rc;
+  t.set = true;
+  // referenced target vertices for the Hausdorff side 0 list
+  t.ref_vs.clear();
+  for (int64_t v = 0; v < nv; v++)
+    if (used[v]) t.ref_vs.push_back(v);
+  std::vector<int64_t> all;
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    ctx->tgt_vs_cnt[m] = ctx->tgt[m].set ? (int64_t)ctx->tgt[m].ref_vs.size() : 0;
+    if (ctx->tgt[m].set) all.insert(all.end(), ctx->tgt[m].ref_vs.begin(), ctx->tgt[m].ref_vs.end());
+  }
+  CK(upload(ctx->tgt_vs_d, all.data(), all.size(), ctx->st));
+  rc = rebuild_tables(ctx);
+  if (rc) return rc;
+  return upload_targets_table(ctx);
+}
+
+int hexopt_signed_distance(hexopt_ctx *ctx, int mesh, int64_t np, const double *P, double *S, int32_t *I, double *C,
+                           double *N) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (mesh < 0 || mesh >= ctx->n_meshes || !ctx->tgt[mesh].set) return fail(ctx, HEXOPT_ERR_STATE, "signed_distance: no target");
+  if (np < 0 || (np > 0 && (!P || !S || !I || !C || !N))) return fail(ctx, HEXOPT_ERR_ARG, "signed_distance: bad arguments");
+  if (np == 0) return HEXOPT_OK;
+  DBuf Pd, Sd, Id, Cd, Nd, stat;
+  CK(upload(Pd, P, (size_t)3 * np, ctx->st));
+  CK(Sd.ensure(sizeof(double) * np)); CK(Id.ensure(sizeof(int32_t) * np));
+  CK(Cd.ensure(sizeof(double) * 3 * np)); CK(Nd.ensure(sizeof(double) * 3 * np));
+  CK(stat.ensure(sizeof(int)));
+  CK(cudaMemsetAsync(stat.p, 0, sizeof(int), ctx->st));
+  std::vector<TargetDev> td(ctx->n_meshes);
+  CK(cudaMemcpyAsync(td.data(), ctx->tgt_d.p, sizeof(TargetDev) * ctx->n_meshes, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  launch_signed_distance(td[mesh], np, Pd.as<double>(), Sd.as<double>(), Id.as<int32_t>(), Cd.as<double>(), Nd.as<double>(),
+                         stat.as<int>(), ctx->st);
+  ctx->launches++;
+  CKL();
+  CK(cudaMemcpyAsync(S, Sd.p, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(I, Id.p, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(C, Cd.p, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(N, Nd.p, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, ctx->st));
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, stat.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (st) return fail(ctx, HEXOPT_ERR_NUMERIC, "signed_distance: BVH traversal stack overflow");
+  return HEXOPT_OK;
+}
+
+int hexopt_set_feature_sets(hexopt_ctx *ctx, const int64_t *n_regular, const int32_t *regular_ids,
+                            const int64_t *n_line, const int32_t *line_ids, const int32_t *line_curve,
+                            const int64_t *n_curves, const int64_t *curve_ptr, const int32_t *curve_vs,
+                            const uint8_t *curve_closed) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  int64_t nr = 0, nl = 0;
+  for (int m = 0; m < ctx->n_meshes; m++) { nr += n_regular[m]; nl += n_line[m]; }
+  std::vector<double> zn(3 * std::max<int64_t>(nr, 1), 0.0), zd(std::max<int64_t>(nr, 1), 0.0);
+  rc = hexopt_set_tangents(ctx, n_regular, regular_ids, zn.data(), zd.data());
+  if (rc) return rc;
+  std::vector<double> zl(3 * std::max<int64_t>(nl, 1), 0.0);
+  rc = hexopt_set_lines(ctx, n_line, line_ids, zl.data(), zl.data());
+  if (rc) return rc;
+  // per-mesh curves (concatenated per mesh; curve ids in line_curve are mesh-local)
+  int64_t co = 0, vo = 0, lo = 0;
+  std::vector<int32_t> lc(std::max<int64_t>(nl, 1));
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    const int64_t ncv = n_curves ? n_curves[m] : 0;
+    TargetHost &t = ctx->tgt[m];
+    if (n_line[m] > 0 && !t.set) return fail(ctx, HEXOPT_ERR_STATE, "mesh %d: feature lines need a target", m);
+    const int64_t *cp = curve_ptr + co + m;  // ncv + 1 entries per mesh
+    std::vector<int64_t> ptr(ncv + 1);
+    for (int64_t i = 0; i <= ncv; i++) ptr[i] = cp[i] - cp[0];
+    const int64_t nvs = ptr[ncv];
+    for (int64_t i = 0; i < nvs; i++)
+      if (curve_vs[vo + i] < 0 || curve_vs[vo + i] >= t.nv) return fail(ctx, HEXOPT_ERR_ARG, "mesh %d: curve vertex out of range", m);
+    for (int64_t i = 0; i < n_line[m]; i++) {
+      if (line_curve[lo + i] < 0 || line_curve[lo + i] >= ncv) return fail(ctx, HEXOPT_ERR_ARG, "mesh %d: line curve id out of range", m);
+      lc[lo + i] = line_curve[lo + i];
+    }
+    if (t.set) {
+      CK(upload(t.curve_ptr, ptr.data(), ptr.size(), ctx->st));
+      CK(upload(t.curve_vs, curve_vs + vo, (size_t)nvs, ctx->st));
+      std::vector<uint8_t> cl(std::max<int64_t>(ncv, 1), 0);
+      for (int64_t i = 0; i < ncv; i++) cl[i] = curve_closed[co + i];
+      CK(upload(t.curve_closed, cl.data(), cl.size(), ctx->st));
+      t.n_curves = ncv;
+    }
+    co += ncv;
+    vo += nvs;
+    lo += n_line[m];
+  }
+  CK(upload(ctx->l_curve, lc.data(), lc.size(), ctx->st));
+  return upload_targets_table(ctx);
+}
+
+int hexopt_project_features(hexopt_ctx *ctx) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  return run_projection(ctx);
+}
+
+// ---------------------------------------------------------------- Hausdorff
+int hexopt_set_surface(hexopt_ctx *ctx, int mesh, int64_t nf, const int32_t *F) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (mesh < 0 || mesh >= ctx->n_meshes || nf <= 0 || !F) return fail(ctx, HEXOPT_ERR_ARG, "set_surface: bad arguments");
+  const int64_t nv = ctx->md[mesh].nv, vo = ctx->md[mesh].v_off;
+  std::vector<int32_t> G(3 * nf);
+  std::vector<uint8_t> used(nv, 0);
+  for (int64_t i = 0; i < 3 * nf; i++) {
+    if (F[i] < 0 || F[i] >= nv) return fail(ctx, HEXOPT_ERR_ARG, "set_surface: vertex id out of range");
+    G[i] = (int32_t)(F[i] + vo);
+    used[F[i]] = 1;
+  }
+  SurfaceHost &s = ctx->surf[mesh];
+  s.nf = nf;
+  s.ref_vs.clear();
+  for (int64_t v = 0; v < nv; v++)
+    if (used[v]) s.ref_vs.push_back(vo + v);
+  CK(upload(s.F, G.data(), G.size(), ctx->st));
+  // topology from the current positions' centroids
+  std::vector<double> tri(9 * nf);
+  std::vector<double> Xh(3 * nv);
+  CK(ctx->stage.ensure(sizeof(double) * 3 * ctx->NV));
+  launch_aos4_to_rows(ctx->X.as<double>(), ctx->stage.as<double>(), ctx->NV, ctx->st);
+  ctx->launches++;
+  CK(cudaMemcpyAsync(Xh.data(), ctx->stage.as<double>() + 3 * vo, sizeof(double) * 3 * nv, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  for (int64_t f = 0; f < nf; f++)
+    for (int c = 0; c < 3; c++)
+      for (int d = 0; d < 3; d++) tri[9 * f + 3 * c + d] = Xh[3 * (int64_t)F[3 * f + c] + d];
+  StaticBvh tmp;
+  rc = build_static_bvh(ctx, tmp, tri, nf);
+  if (rc) return rc;
+  // adopt the topology (child / parent / leaf order); boxes are refitted from X on use
+  std::swap(s.child.p, tmp.child.p); std::swap(s.child.bytes, tmp.child.bytes);
+  std::swap(s.parent.p, tmp.parent.p); std::swap(s.parent.bytes, tmp.parent.bytes);
+  std::swap(s.box.p, tmp.box.p); std::swap(s.box.bytes, tmp.box.bytes);
+  std::swap(s.leaf_face.p, tmp.leaf_face.p); std::swap(s.leaf_face.bytes, tmp.leaf_face.bytes);
+  std::swap(s.counters.p, tmp.counters.p); std::swap(s.counters.bytes, tmp.counters.bytes);
+  s.set = true;
+  std::vector<int64_t> all;
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    ctx->surf_vs_cnt[m] = ctx->surf[m].set ? (int64_t)ctx->surf[m].ref_vs.size() : 0;
+    if (ctx->surf[m].set) all.insert(all.end(), ctx->surf[m].ref_vs.begin(), ctx->surf[m].ref_vs.end());
+  }
+  CK(upload(ctx->surf_vs_d, all.data(), all.size(), ctx->st));
+  rc = rebuild_tables(ctx);
+  if (rc) return rc;
+  return upload_targets_table(ctx);
+}
+
+static int prepare_haus(hexopt_ctx *ctx) {
+  for (int m = 0; m < ctx->n_meshes; m++)
+    if (!ctx->tgt[m].set || !ctx->surf[m].set) return fail(ctx, HEXOPT_ERR_STATE, "mesh %d: Hausdorff needs set_target and set_surface", m);
+  std::vector<HausMesh> hm(ctx->n_meshes);
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    HausMesh h{};
+    for (int d = 0; d < 3; d++) { h.tgt_lo[d] = ctx->tgt[m].lo[d]; h.tgt_hi[d] = ctx->tgt[m].hi[d]; }
+    hm[m] = h;
+  }
+  CK(upload(ctx->hm_d, hm.data(), hm.size(), ctx->st));
+  ctx->haus_ready = true;
+  return HEXOPT_OK;
+}
+
+int hexopt_hausdorff_meshes(hexopt_ctx *ctx, double *diag, double *max_dist, double *ave_dist) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!ctx->haus_ready) {
+    rc = prepare_haus(ctx);
+    if (rc) return rc;
+  }
+  rc = run_hausdorff(ctx);
+  if (rc) return rc;
+  std::vector<HausMesh> hm(ctx->n_meshes);
+  CK(cudaMemcpyAsync(hm.data(), ctx->hm_d.p, sizeof(HausMesh) * ctx->n_meshes, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    if (diag) diag[m] = hm[m].diag;
+    if (max_dist) max_dist[m] = hm[m].max_dist;
+    if (ave_dist) ave_dist[m] = hm[m].ave_dist;
+  }
+  return HEXOPT_OK;
+}
+
+
+// ---------------------------------------------------------------- standalone distances
+static int ep_side(hexopt_ctx *ctx, const BvhDev &b, const double *P, const int64_t *ids, int64_t n, double upper,
+                   double *out3, DBuf &dist, DBuf &stat) {
+  CK(dist.ensure(sizeof(double) * std::max<int64_t>(n, 1)));
+  launch_ep_points(b, P, ids, n, upper, dist.as<double>(), stat.as<int>(), ctx->st);
+  launch_maxmean(dist.as<double>(), n, upper, out3, ctx->st);
+  ctx->launches += 2;
+  CKL();
+  return HEXOPT_OK;
+}
+
+int hexopt_hausdorff(hexopt_ctx *ctx, int64_t nv0, const double *V0, int64_t nf0, const int32_t *F0, int64_t nv1,
+                     const double *V1, int64_t nf1, const int32_t *F1, double *diag, double *max_dist,
+                     double *ave_dist) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  if (nv0 <= 0 || nv1 <= 0 || nf0 <= 0 || nf1 <= 0 || !V0 || !V1 || !F0 || !F1)
+    return fail(ctx, HEXOPT_ERR_ARG, "hausdorff: empty mesh");
+  for (int64_t i = 0; i < 3 * nf0; i++) if (F0[i] < 0 || F0[i] >= nv0) return fail(ctx, HEXOPT_ERR_ARG, "hausdorff: F0 id out of range");
+  for (int64_t i = 0; i < 3 * nf1; i++) if (F1[i] < 0 || F1[i] >= nv1) return fail(ctx, HEXOPT_ERR_ARG, "hausdorff: F1 id out of range");
+  CK(cudaSetDevice(ctx->device));
+  // union bbox of both vertex sets, inflated by 2% of its diagonal (metro_hausdorff.cpp:455-462)
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t v = 0; v < nv0; v++) for (int d = 0; d < 3; d++) { lo[d] = std::min(lo[d], V0[3 * v + d]); hi[d] = std::max(hi[d], V0[3 * v + d]); }
+  for (int64_t v = 0; v < nv1; v++) for (int d = 0; d < 3; d++) { lo[d] = std::min(lo[d], V1[3 * v + d]); hi[d] = std::max(hi[d], V1[3 * v + d]); }
+  const double e0 = hi[0] - lo[0], e1 = hi[1] - lo[1], e2 = hi[2] - lo[2];
+  const double off = std::sqrt(e0 * e0 + e1 * e1 + e2 * e2) * 0.02;
+  const double f0 = e0 + 2 * off, f1 = e1 + 2 * off, f2 = e2 + 2 * off;
+  const double D = std::sqrt(f0 * f0 + f1 * f1 + f2 * f2);
+  std::vector<double> tri0(9 * nf0), tri1(9 * nf1);
+  std::vector<uint8_t> u0(nv0, 0), u1(nv1, 0);
+  for (int64_t f = 0; f < nf0; f++) for (int c = 0; c < 3; c++) { u0[F0[3 * f + c]] = 1; for (int d = 0; d < 3; d++) tri0[9 * f + 3 * c + d] = V0[3 * (int64_t)F0[3 * f + c] + d]; }
+  for (int64_t f = 0; f < nf1; f++) for (int c = 0; c < 3; c++) { u1[F1[3 * f + c]] = 1; for (int d = 0; d < 3; d++) tri1[9 * f + 3 * c + d] = V1[3 * (int64_t)F1[3 * f + c] + d]; }
+  std::vector<int64_t> r0, r1;
+  for (int64_t v = 0; v < nv0; v++) if (u0[v]) r0.push_back(v);
+  for (int64_t v = 0; v < nv1; v++) if (u1[v]) r1.push_back(v);
+  StaticBvh B0, B1;
+  int rc = build_static_bvh(ctx, B0, tri0, nf0);
+  if (rc) return rc;
+  rc = build_static_bvh(ctx, B1, tri1, nf1);
+  if (rc) return rc;
+  DBuf P0, P1, I0, I1, dist, stat, out;
+  CK(upload(P0, V0, (size_t)3 * nv0, ctx->st));
+  CK(upload(P1, V1, (size_t)3 * nv1, ctx->st));
+  CK(upload(I0, r0.data(), r0.size(), ctx->st));
+  CK(upload(I1, r1.data(), r1.size(), ctx->st));
+  CK(stat.ensure(sizeof(int)));
+  CK(cudaMemsetAsync(stat.p, 0, sizeof(int), ctx->st));
+  CK(out.ensure(sizeof(double) * 6));
+  rc = ep_side(ctx, B1.dev(), P0.as<double>(), I0.as<int64_t>(), (int64_t)r0.size(), D, out.as<double>(), dist, stat);
+  if (rc) return rc;
+  DBuf dist2;
+  rc = ep_side(ctx, B0.dev(), P1.as<double>(), I1.as<int64_t>(), (int64_t)r1.size(), D, out.as<double>() + 3, dist2, stat);
+  if (rc) return rc;
+  double h[6];
+  int st = 0;
+  CK(cudaMemcpyAsync(h, out.p, sizeof h, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(&st, stat.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (st) return fail(ctx, HEXOPT_ERR_NUMERIC, "hausdorff: BVH traversal stack overflow");
+  if (diag) *diag = D;
+  if (max_dist) *max_dist = std::max(h[0], h[3]);
+  if (ave_dist) *ave_dist = std::max(h[4] / h[5], h[1] / h[2]);
+  return HEXOPT_OK;
+}
+
+int hexopt_point_face_distance(hexopt_ctx *ctx, int64_t np, const double *P, int64_t nv, const double *V, int64_t nf,
+                               const int32_t *F, double *dist) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  if (np < 0 || nv <= 0 || nf <= 0 || !V || !F || (np > 0 && (!P || !dist))) return fail(ctx, HEXOPT_ERR_ARG, "point_face_distance: bad arguments");
+  for (int64_t i = 0; i < 3 * nf; i++) if (F[i] < 0 || F[i] >= nv) return fail(ctx, HEXOPT_ERR_ARG, "point_face_distance: id out of range");
+  if (np == 0) return HEXOPT_OK;
+  CK(cudaSetDevice(ctx->device));
+  std::vector<double> tri(9 * nf);
+  for (int64_t f = 0; f < nf; f++) for (int c = 0; c < 3; c++) for (int d = 0; d < 3; d++) tri[9 * f + 3 * c + d] = V[3 * (int64_t)F[3 * f + c] + d];
+  StaticBvh B;
+  int rc = build_static_bvh(ctx, B, tri, nf);
+  if (rc) return rc;
+  DBuf Pd, Dd, stat;
+  CK(upload(Pd, P, (size_t)3 * np, ctx->st));
+  CK(Dd.ensure(sizeof(double) * np));
+  CK(stat.ensure(sizeof(int)));
+  CK(cudaMemsetAsync(stat.p, 0, sizeof(int), ctx->st));
+  launch_ep_points(B.dev(), Pd.as<double>(), nullptr, np, INFINITY, Dd.as<double>(), stat.as<int>(), ctx->st);
+  ctx->launches++;
+  CKL();
+  int st = 0;
+  CK(cudaMemcpyAsync(dist, Dd.p, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(&st, stat.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (st) return fail(ctx, HEXOPT_ERR_NUMERIC, "point_face_distance: BVH traversal stack overflow");
+  return HEXOPT_OK;
+}
+
+// ---------------------------------------------------------------- feature alignment
+int hexopt_fa_begin(hexopt_ctx *ctx, const hexopt_slim_params *p, double lamda0, double hausdorff_ratio_t) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!p) return fail(ctx, HEXOPT_ERR_ARG, "fa_begin: NULL params");
+  ctx->lamda0 = lamda0;
+  ctx->HR = hausdorff_ratio_t;
+  // validate and allocate with a precompute at the current positions
+  rc = hexopt_slim_precompute(ctx, p);
+  if (rc) return rc;
+  rc = pull_scalars(ctx);
+  if (rc) return rc;
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    MeshScalars &S = ctx->sc[m];
+    S.lamda_C = S.lamda_T = S.lamda_L = lamda0;  // fc.lamda_C = fc.lamda_L = fc.lamda_T = LAMDA (:3811)
+    S.lamda0 = lamda0;
+    S.fa_iter = 0;
+    S.max_sat = 0;
+    S.HR = hausdorff_ratio_t;
+  }
+  rc = push_scalars(ctx);
+  if (rc) return rc;
+  if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+  ctx->fa_ready = true;
+  return HEXOPT_OK;
+}
+
+static int fa_enqueue(hexopt_ctx *ctx, int do_hausdorff) {
+  int rc = run_projection(ctx);
+  if (rc) return rc;
+  rc = dispatch_precompute(ctx);
+  if (rc) return rc;
+  rc = dispatch_iteration(ctx);
+  if (rc) return rc;
+  launch_fa_schedule(ctx->sc_d.as<MeshScalars>(), ctx->n_meshes, ctx->lamda0, 1e16, ctx->st);
+  KArgs a = make_args(ctx);
+  launch_scaled_jacobian(a, ctx->kind[K_HEX].nblk, nullptr, ctx->HJs.as<double>(), ctx->st);
+  ctx->launches += 3;
+  if (do_hausdorff) {
+    rc = run_hausdorff(ctx);
+    if (rc) return rc;
+    launch_fa_haus_flag(ctx->sc_d.as<MeshScalars>(), ctx->hm_d.as<HausMesh>(), ctx->n_meshes, ctx->st);
+    ctx->launches++;
+  }
+  CKL();
+  return HEXOPT_OK;
+}
+
+int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_report *rep) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!ctx->fa_ready) return fail(ctx, HEXOPT_ERR_STATE, "feature_alignment_step before fa_begin");
+  if (do_hausdorff && !ctx->haus_ready) {
+    rc = prepare_haus(ctx);
+    if (rc) return rc;
+  }
+  if (ctx->use_graph) {
+    if (ctx->graph_exec && ctx->graph_hausdorff != (do_hausdorff != 0)) {
+      cudaGraphExecDestroy(ctx->graph_exec);
+      ctx->graph_exec = nullptr;
+    }
+    if (!ctx->graph_exec) {
+      cudaGraph_t g;
+      const int64_t l0 = ctx->launches;
+      CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+      rc = fa_enqueue(ctx, do_hausdorff);
+      cudaGraph_t gg = nullptr;
+      cudaError_t e = cudaStreamEndCapture(ctx->st, &gg);
+      if (rc) return rc;
+      if (e != cudaSuccess) return fail(ctx, HEXOPT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+      g = gg;
+      CK(cudaGraphInstantiate(&ctx->graph_exec, g, 0));
+      cudaGraphDestroy(g);
+      ctx->graph_hausdorff = do_hausdorff != 0;
+      ctx->graph_launches = ctx->launches - l0;  // kernels in one replay
+      ctx->launches = l0;                        // capture executed nothing
+    }
+    CK(cudaGraphLaunch(ctx->graph_exec, ctx->st));
+    ctx->launches += ctx->graph_launches;
+  } else {
+    rc = fa_enqueue(ctx, do_hausdorff);
+    if (rc) return rc;
+  }
+  if (rep) {
+    rc = pull_scalars(ctx);
+    if (rc) return rc;
+    for (int m = 0; m < ctx->n_meshes; m++) {
+      const MeshScalars &S = ctx->sc[m];
+      fill_report(S, rep[m].slim);
+      rep[m].quality.min_Jacobian = S.sj_min;
+      rep[m].quality.ave_Jacobian = S.sj_sum / (double)ctx->md[m].nh;
+      rep[m].quality.deviation_Jacobian = -1;  // the step skips the deviation pass
+      rep[m].quality.n_inverted = S.n_inv;
+      rep[m].lamda = S.lamda_C;
+      rep[m].hausdorff_diag = do_hausdorff ? S.haus_diag : -1;
+      rep[m].hausdorff_max = do_hausdorff ? S.haus_max : -1;
+      rep[m].hausdorff_ave = do_hausdorff ? S.haus_ave : -1;
+    }
+  }
+  return HEXOPT_OK;
+}
+
+int hexopt_use_graph(hexopt_ctx *ctx, int on) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  ctx->use_graph = on != 0;
+  if (!ctx->use_graph && ctx->graph_exec) {
+    cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+  }
+  return HEXOPT_OK;
+}
+
+// ---------------------------------------------------------------- adjoint
+int hexopt_energy_fwd(hexopt_ctx *ctx, const double *X, double *E) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!ctx->precomputed) return fail(ctx, HEXOPT_ERR_STATE, "energy_fwd before slim_precompute");
+  if (ctx->params.energy != HEXOPT_SYMMETRIC_DIRICHLET) return fail(ctx, HEXOPT_ERR_UNSUPPORTED, "adjoint: symmetric Dirichlet only");
+  CK(ctx->Xa.ensure(sizeof(double) * 4 * ctx->NV));
+  if (X) {
+    CK(upload(ctx->stage, X, (size_t)3 * ctx->NV, ctx->st));
+    launch_rows_to_aos4(ctx->stage.as<double>(), ctx->Xa.as<double>(), ctx->NV, ctx->st);
+  } else {
+    CK(cudaMemcpyAsync(ctx->Xa.p, ctx->X.p, sizeof(double) * 4 * ctx->NV, cudaMemcpyDeviceToDevice, ctx->st));
+  }
+  KArgs a = make_args(ctx);
+  if (ctx->mixed) launch_energy_fwd<float>(a, ctx->kind[K_HEX].nblk, ctx->kind[K_CONS].nblk, ctx->st);
+  else launch_energy_fwd<double>(a, ctx->kind[K_HEX].nblk, ctx->kind[K_CONS].nblk, ctx->st);
+  ctx->launches += 3;
+  CKL();
+  rc = pull_scalars(ctx);
+  if (rc) return rc;
+  if (E)
+    for (int m = 0; m < ctx->n_meshes; m++) E[m] = ctx->sc[m].adj_eq + ctx->sc[m].adj_es;
+  ctx->adj_ready = true;
+  return HEXOPT_OK;
+}
+
+int hexopt_energy_bwd(hexopt_ctx *ctx, double *grad) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!ctx->adj_ready) return fail(ctx, HEXOPT_ERR_STATE, "energy_bwd before energy_fwd");
+  CK(ctx->grad.ensure(sizeof(double) * 4 * ctx->NV));
+  CK(cudaMemsetAsync(ctx->grad.p, 0, sizeof(double) * 4 * ctx->NV, ctx->st));
+  KArgs a = make_args(ctx);
+  if (ctx->mixed) launch_energy_bwd<float>(a, ctx->kind[K_HEX].nblk, ctx->kind[K_CONS].nblk, ctx->st);
+  else launch_energy_bwd<double>(a, ctx->kind[K_HEX].nblk, ctx->kind[K_CONS].nblk, ctx->st);
+  ctx->launches += 2;
+  CKL();
+  if (grad) {
+    CK(ctx->stage.ensure(sizeof(double) * 3 * ctx->NV));
+    launch_aos4_to_rows(ctx->grad.as<double>(), ctx->stage.as<double>(), ctx->NV, ctx->st);
+    ctx->launches++;
+    CK(cudaMemcpyAsync(grad, ctx->stage.p, sizeof(double) * 3 * ctx->NV, cudaMemcpyDeviceToHost, ctx->st));
+  }
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
+// ---------------------------------------------------------------- tuning
+int hexopt_set_block_size(hexopt_ctx *ctx, int kind, int threads) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  if (kind == 0) {
+    if (threads != 32 && threads != 64 && threads != 128) return fail(ctx, HEXOPT_ERR_ARG, "hex block size must be 32, 64 or 128");
+    ctx->block[K_HEX] = threads;
+  } else if (kind == 1) {
+    if (threads != 64 && threads != 128 && threads != 256) return fail(ctx, HEXOPT_ERR_ARG, "vertex block size must be 64, 128 or 256");
+    ctx->block[K_VERT] = threads;
+  } else {
+    return fail(ctx, HEXOPT_ERR_ARG, "unknown kind");
+  }
+  if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+  if (ctx->n_meshes > 0) return rebuild_tables(ctx);
+  return HEXOPT_OK;
+}
+
+// Times one SLIM iteration for each (hex block, vertex block, line-search candidates) setting on
+// a copy of the positions, keeps the fastest, restores the positions and scalars.
+int hexopt_autotune(hexopt_ctx *ctx) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!ctx->precomputed) return fail(ctx, HEXOPT_ERR_STATE, "autotune before slim_precompute");
+  CK(ctx->Xbak.ensure(sizeof(double) * 4 * ctx->NV));
+  CK(cudaMemcpyAsync(ctx->Xbak.p, ctx->X.p, sizeof(double) * 4 * ctx->NV, cudaMemcpyDeviceToDevice, ctx->st));
+  rc = pull_scalars(ctx);
+  if (rc) return rc;
+  const std::vector<MeshScalars> sc0 = ctx->sc;
+  const int hb[2] = {64, 128}, vb[2] = {128, 256}, lc[3] = {2, 4, 8};
+  float best = INFINITY;
+  int bh = ctx->block[K_HEX], bv = ctx->block[K_VERT], bl = ctx->params.ls_candidates;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
+      for (int k = 0; k < 3; k++) {
+        ctx->block[K_HEX] = hb[i];
+        ctx->block[K_VERT] = vb[j];
+        ctx->params.ls_candidates = lc[k];
+        rc = rebuild_tables(ctx);
+        if (rc) return rc;
+        float ms = 0;
+        for (int rep = 0; rep < 2; rep++) {
+          CK(cudaMemcpyAsync(ctx->X.p, ctx->Xbak.p, sizeof(double) * 4 * ctx->NV, cudaMemcpyDeviceToDevice, ctx->st));
+          ctx->sc = sc0;
+          rc = push_scalars(ctx);
+          if (rc) return rc;
+          CK(cudaEventRecord(e0, ctx->st));
+          rc = dispatch_iteration(ctx);
+          if (rc) return rc;
+          CK(cudaEventRecord(e1, ctx->st));
+          CK(cudaEventSynchronize(e1));
+          CK(cudaEventElapsedTime(&ms, e0, e1));
+        }
+        if (ms < best) { best = ms; bh = hb[i]; bv = vb[j]; bl = lc[k]; }
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->block[K_HEX] = bh;
+  ctx->block[K_VERT] = bv;
+  ctx->params.ls_candidates = bl;
+  rc = rebuild_tables(ctx);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(ctx->X.p, ctx->Xbak.p, sizeof(double) * 4 * ctx->NV, cudaMemcpyDeviceToDevice, ctx->st));
+  ctx->sc = sc0;
+  rc = push_scalars(ctx);
+  if (rc) return rc;
+  if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
+int hexopt_get_tuning(const hexopt_ctx *ctx, int *hex_block, int *vert_block, int *ls_candidates) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  if (hex_block) *hex_block = ctx->block[K_HEX];
+  if (vert_block) *vert_block = ctx->block[K_VERT];
+  if (ls_candidates) *ls_candidates = ctx->params.ls_candidates;
+  return HEXOPT_OK;
+}
+
+// ---------------------------------------------------------------- aabb.h value types
+void hexopt_aabb_merge(hexopt_aabb *a, const hexopt_aabb *b) {
+  for (int d = 0; d < 3; d++) {
+    a->min[d] = std::min(a->min[d], b->min[d]);
+    a->max[d] = std::max(a->max[d], b->max[d]);
+  }
+}
+double hexopt_aabb_squared_distance(const hexopt_aabb *a, const double *p) {
+  double s = 0;
+  for (int d = 0; d < 3; d++) {
+    double e = 0;
+    if (p[d] < a->min[d]) e = a->min[d] - p[d];
+    else if (p[d] > a->max[d]) e = p[d] - a->max[d];
+    s += e * e;
+  }
+  return s;
+}
+// slab test (AABB::rayIntersect, aabb.h:21-48): 1 on hit with the entry/exit parameters
+int hexopt_aabb_ray_intersect(const hexopt_aabb *a, const hexopt_ray *r, double *nearT, double *farT) {
+  double n = -INFINITY, f = INFINITY;
+  for (int i = 0; i < 3; i++) {
+    const double origin = r->o[i], minVal = a->min[i], maxVal = a->max[i];
+    if (r->d[i] == 0) {
+      if (origin < minVal || origin > maxVal) return 0;
+    } else {
+      double t1 = (minVal - origin) * r->dRcp[i], t2 = (maxVal - origin) * r->dRcp[i];
+      if (t1 > t2) std::swap(t1, t2);
+      n = std::max(t1, n);
+      f = std::min(t2, f);
+      if (!(n <= f)) return 0;
+    }
+  }
+  if (nearT) *nearT = n;
+  if (farT) *farT = f;
+  return r->mint <= f && n <= r->maxt;
+}
+int hexopt_aabb_largest_axis(const hexopt_aabb *a) {
+  const double e0 = a->max[0] - a->min[0], e1 = a->max[1] - a->min[1], e2 = a->max[2] - a->min[2];
+  if (e0 >= e1 && e0 >= e2) return 0;
+  if (e1 >= e2) return 1;
+  return 2;
+}
+double hexopt_aabb_surface_area(const hexopt_aabb *a) {
+  const double e0 = a->max[0] - a->min[0], e1 = a->max[1] - a->min[1], e2 = a->max[2] - a->min[2];
+  return 2.0 * (e0 * e1 + e1 * e2 + e2 * e0);
+}
+
+}  // extern "C"

@@ -1,0 +1,86 @@
+// hexopt_bvh.h -- LBVH / target / Hausdorff structures shared by the runtime and k_bvh.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "hexopt_dev.h"
+
+namespace hexopt {
+
+// A linear BVH over n triangles.  Internal nodes 0..n-2 (root 0), leaves in sorted order; a
+// child id >= 0 is an internal node, < 0 is leaf ~id.  Boxes: (2n-1) x 6 floats, internal nodes
+// first then leaves.  Static trees read triangles from `tri` (9 doubles per face id); dynamic
+// trees gather them from the positions X through F (3 global vertex ids per face).
+struct BvhDev {
+  int32_t n;
+  int32_t pad;
+  const int32_t *child;
+  const float *box;
+  const int32_t *leaf_face;
+  const double *tri;
+  const int32_t *F;
+  const double *X;
+};
+
+// A mesh's target triangle mesh (mf.tri / tri_tree): geometry, per-face normals of
+// build_aabb_tree, and the feature curves as polylines over its vertices.
+struct TargetDev {
+  BvhDev bvh;
+  const double *TV;       // target vertices, rows of 3
+  const double *tri;      // 9 doubles per face
+  const double *FN;       // face normals (3 per face)
+  const double *VNc;      // angle-weighted vertex normal of each corner (9 per face)
+  const double *ENc;      // uniform edge normal of the edge opposite each corner (9 per face)
+  const int64_t *curve_ptr;
+  const int32_t *curve_vs;
+  const uint8_t *curve_closed;
+};
+
+struct ProjArgs {
+  const Seg *seg;
+  const MeshDesc *mesh;
+  MeshScalars *sc;
+  const TargetDev *tgt;
+  const double *X;
+  const int32_t *t_ids;
+  double *t_nrm, *t_dis;
+  const int32_t *l_ids, *l_curve;
+  double *l_axis, *l_orig;
+};
+
+struct HausMesh {
+  double tgt_lo[3], tgt_hi[3];  // bbox of the target vertices (static)
+  double diag;                  // inflated bbox diagonal of both surfaces
+  double side_max[2], side_mean[2];
+  double max_dist, ave_dist;
+};
+
+struct HausArgs {
+  const Seg *seg;
+  const MeshDesc *mesh;
+  MeshScalars *sc;
+  const TargetDev *tgt;
+  const BvhDev *surf;       // per mesh: dynamic BVH over the boundary triangles
+  HausMesh *hm;
+  const double *X;
+  const int64_t *tgt_vs;    // K_TGTV items: referenced target vertices (target-local ids)
+  const int64_t *surf_vs;   // K_SURFV items: referenced surface vertices (global ids)
+  double *partials;
+  unsigned *counters;
+};
+
+void bvh_morton(const BvhDev &b, const double lo[3], const double hi[3], unsigned long long *keys, cudaStream_t st);
+void bvh_karras(int n, const unsigned long long *keys, int32_t *child, int32_t *parent, int32_t *leaf_face,
+                cudaStream_t st);
+void bvh_refit(const BvhDev &b, float *box, const int32_t *parent, unsigned *counters, cudaStream_t st);
+void launch_project(const ProjArgs &p, int64_t nblk, cudaStream_t st);
+void launch_curve_project(const ProjArgs &p, int64_t nblk, cudaStream_t st);
+void launch_signed_distance(const TargetDev &t, int64_t np, const double *P, double *S, int32_t *I, double *C,
+                            double *N, int *status, cudaStream_t st);
+void launch_haus_bbox(const HausArgs &h, int64_t nblk, cudaStream_t st);
+void launch_haus_side(const HausArgs &h, int side, int64_t nblk, cudaStream_t st);
+void launch_ep_points(const BvhDev &b, const double *P, const int64_t *ids, int64_t n, double upper, double *dist,
+                      int *status, cudaStream_t st);
+void launch_maxmean(const double *dist, int64_t n, double upper, double *out3, cudaStream_t st);
+void launch_fa_haus_flag(MeshScalars *sc, const HausMesh *hm, int n, cudaStream_t st);
+
+}  // namespace hexopt

@@ -1,0 +1,127 @@
+// hexopt_elem.cuh -- per-hex element helpers shared by the SLIM and adjoint kernels: vertex
+// gathers (AoS4), corner-tet edge matrices, the cube-corner signed permutation J = E R_k^T / s and
+// its transpose for scattering forces, and the general (own-shape) J = E B.
+#pragma once
+#include "hexopt_common.cuh"
+#include "hexopt_kernels.h"
+
+namespace hexopt {
+
+// ------------------------------------------------------------------------------- helpers
+__device__ __forceinline__ void load_pos(const double *X, uint32_t v, double p[3]) {
+  const double2 a = __ldg(reinterpret_cast<const double2 *>(X + 4 * (int64_t)v));
+  const double b = __ldg(X + 4 * (int64_t)v + 2);
+  p[0] = a.x; p[1] = a.y; p[2] = b;
+}
+template <typename T>
+__device__ __forceinline__ void load_vec(const T *Y, uint32_t v, T p[3]) {
+  p[0] = Y[4 * (int64_t)v]; p[1] = Y[4 * (int64_t)v + 1]; p[2] = Y[4 * (int64_t)v + 2];
+}
+__device__ __forceinline__ void load_vec(const float *Y, uint32_t v, float p[3]) {
+  const float4 a = *reinterpret_cast<const float4 *>(Y + 4 * (int64_t)v);
+  p[0] = a.x; p[1] = a.y; p[2] = a.z;
+}
+__device__ __forceinline__ void atomic_add3(double *Y, uint32_t v, double a, double b, double c) {
+  atomicAdd(Y + 4 * (int64_t)v, a); atomicAdd(Y + 4 * (int64_t)v + 1, b); atomicAdd(Y + 4 * (int64_t)v + 2, c);
+}
+__device__ __forceinline__ void atomic_add3(float *Y, uint32_t v, float a, float b, float c) {
+  atomicAdd(reinterpret_cast<float4 *>(Y + 4 * (int64_t)v), make_float4(a, b, c, 0.f));
+}
+
+// Edge matrix of corner tet k as columns (E[:, j] = P[tet_v(k,j+1)] - P[tet_v(k,0)]), from the
+// hex corner gather hv[].  Positions are FP64; the subtraction happens in FP64 before any cast.
+template <int K>
+__device__ __forceinline__ void tet_edges(const double *X, const uint32_t hv[8], double E[3][3]) {
+  double p0[3];
+  load_pos(X, hv[tet_v(K, 0)], p0);
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    double q[3];
+    load_pos(X, hv[tet_v(K, j + 1)], q);
+    E[0][j] = q[0] - p0[0]; E[1][j] = q[1] - p0[1]; E[2][j] = q[2] - p0[2];
+  }
+}
+template <int K, typename T>
+__device__ __forceinline__ void tet_edges_vec(const T *Y, const uint32_t hv[8], T E[3][3]) {
+  T p0[3];
+  load_vec(Y, hv[tet_v(K, 0)], p0);
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    T q[3];
+    load_vec(Y, hv[tet_v(K, j + 1)], q);
+    E[0][j] = q[0] - p0[0]; E[1][j] = q[1] - p0[1]; E[2][j] = q[2] - p0[2];
+  }
+}
+
+// J = E R_k^T (cube-corner tet k): J[:, edge_axis(k,j)] = edge_sign(k,j) * E[:, j]
+template <int K, typename T, typename S>
+__device__ __forceinline__ void cube_J(const S E[3][3], T scale, T J[3][3]) {
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int a = edge_axis(K, j);
+    const T sg = T(edge_sign(K, j)) * scale;
+#pragma unroll
+    for (int r = 0; r < 3; r++) J[r][a] = T(E[r][j]) * sg;
+  }
+}
+// Forces of a cube tet from the stress Q (3x3): f_{j+1} = sign * Q[:, axis_j], f_0 = -sum.
+template <int K, typename T, typename A>
+__device__ __forceinline__ void cube_scatter(const T Q[3][3], T scale, A F[8][3]) {
+  A f0[3] = {0, 0, 0};
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int a = edge_axis(K, j);
+    const T sg = T(edge_sign(K, j)) * scale;
+    const int c = tet_v(K, j + 1);
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      A v = A(Q[r][a] * sg);
+      F[c][r] += v;
+      f0[r] += v;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 3; r++) F[tet_v(K, 0)][r] -= f0[r];
+}
+// General (own-shape) tet: J = E B, forces G = Q B^T (columns are f_1..f_3).
+template <int K, typename T, typename S>
+__device__ __forceinline__ void gen_J(const S E[3][3], const double *B, T J[3][3]) {
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) J[r][c] = T(E[r][0]) * T(B[0 * 3 + c]) + T(E[r][1]) * T(B[1 * 3 + c]) + T(E[r][2]) * T(B[2 * 3 + c]);
+}
+template <int K, typename T, typename A>
+__device__ __forceinline__ void gen_scatter(const T Q[3][3], const double *B, A F[8][3]) {
+  A f0[3] = {0, 0, 0};
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int c = tet_v(K, j + 1);
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      A v = A(Q[r][0] * T(B[j * 3 + 0]) + Q[r][1] * T(B[j * 3 + 1]) + Q[r][2] * T(B[j * 3 + 2]));
+      F[c][r] += v;
+      f0[r] += v;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 3; r++) F[tet_v(K, 0)][r] -= f0[r];
+}
+
+// symmetric 3x3 stored as (xx, yy, zz, xy, xz, yz) times a 3x3
+template <typename T>
+__device__ __forceinline__ void sym_mul(const T c[6], const T J[3][3], T Q[3][3]) {
+#pragma unroll
+  for (int col = 0; col < 3; col++) {
+    Q[0][col] = c[0] * J[0][col] + c[3] * J[1][col] + c[4] * J[2][col];
+    Q[1][col] = c[3] * J[0][col] + c[1] * J[1][col] + c[5] * J[2][col];
+    Q[2][col] = c[4] * J[0][col] + c[5] * J[1][col] + c[2] * J[2][col];
+  }
+}
+
+__device__ __forceinline__ void load_hex(const uint32_t *hexv, int64_t h, uint32_t hv[8]) {
+#pragma unroll
+  for (int c = 0; c < 8; c++) hv[c] = __ldg(hexv + hex_idx(h, c));
+}
+
+}  // namespace hexopt

@@ -1,0 +1,78 @@
+// hexopt_kernels.h -- kernel argument block and launcher declarations (host + device).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "hexopt_dev.h"
+
+namespace hexopt {
+
+// Everything a kernel may touch, passed by value.  Vector pointers whose scalar type depends on
+// the arithmetic mode are void*.
+struct KArgs {
+  // batch tables
+  const MeshDesc *mesh;
+  MeshScalars *sc;
+  const Seg *hseg, *vseg, *cseg;
+  double *partials;
+  unsigned *counters;
+  // geometry
+  const uint32_t *hexv;  // AoSoA corners
+  const int32_t *gslot;  // per hex: -1 cube target, else own-shape slot
+  double *X;             // positions AoS4 FP64
+  double *aL;            // curve parameters (FP64)
+  void *Sinv;            // per tet 1/cbrt(6 vol) (ET, AoSoA NC=1)
+  void *Ccoef;           // per tet C_t (ET, AoSoA NC=6)
+  double *Bgen;          // own-shape rest inverses, 9 per tet
+  // linear system (FP64 accumulation)
+  double *b, *diag, *ba, *diaga;
+  // CG vectors (VT)
+  void *d, *r, *p, *q, *invd;
+  void *da, *ra, *pa, *qa, *invda;
+  // constraints
+  const int32_t *c_ids; const double *c_pos;
+  const int32_t *t_ids; double *t_nrm; double *t_dis;
+  const int32_t *l_ids; double *l_axis; double *l_orig;
+  // parameters
+  int energy;
+  int cg_max_iter;
+  int ls_cand;
+  int pad_;
+  double cg_tol;
+  double sc_exp_f;
+  int hthreads;   // block size of hex-kind launches (<= 128)
+  int vthreads;   // block size of vertex / constraint launches (<= 256)
+  // adjoint
+  double *Xa;     // evaluation point (AoS4 FP64)
+  double *grad;   // dE/dX (AoS4 FP64)
+};
+
+template <typename ET, typename VT> void launch_precompute(const KArgs &a, int64_t nblk, cudaStream_t st);
+template <typename ET, typename VT> void launch_local(const KArgs &a, int64_t nblk, cudaStream_t st);
+template <typename ET, typename VT> void launch_residual_elems(const KArgs &a, int64_t nblk, double *q64, cudaStream_t st);
+template <typename ET, typename VT> void launch_spmv_elems(const KArgs &a, int64_t nblk, cudaStream_t st);
+template <typename VT> void launch_soft_rhs(const KArgs &a, int64_t nblk, cudaStream_t st);
+template <typename VT> void launch_soft_residual(const KArgs &a, int64_t nblk, double *q64, double *q64a, cudaStream_t st);
+template <typename VT> void launch_soft_spmv(const KArgs &a, int64_t nblk, cudaStream_t st);
+template <typename VT> void launch_cg_start(const KArgs &a, int64_t nblk, const double *q64, const double *q64a, cudaStream_t st);
+template <typename VT> void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st);
+template <typename ET, typename VT> void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st);
+
+// Launches per call of the launchers above (for the launch count).
+constexpr int kLaunchesCgIter = 5;
+
+// ---- adjoint (k_adjoint.cu) ----
+template <typename ET> void launch_energy_fwd(const KArgs &a, int64_t hblk, int64_t cblk, cudaStream_t st);
+template <typename ET> void launch_energy_bwd(const KArgs &a, int64_t hblk, int64_t cblk, cudaStream_t st);
+
+// ---- quality (k_quality.cu) ----
+void launch_scaled_jacobian(const KArgs &a, int64_t hblk, double *V_Js, double *H_Js, cudaStream_t st);
+// weight schedule + report packing for the feature-alignment step
+void launch_fa_schedule(MeshScalars *sc, int n_meshes, double lamda0, double bound, cudaStream_t st);
+
+// ---- layout helpers (k_layout.cu) ----
+void launch_rows_to_aos4(const double *src, double *dst, int64_t n, cudaStream_t st);
+void launch_aos4_to_rows(const double *src, double *dst, int64_t n, cudaStream_t st);
+void launch_hex_to_aosoa_mesh(const uint32_t *src, int64_t h0, int64_t nh, uint32_t voff, uint32_t *dst,
+                              cudaStream_t st);
+
+}  // namespace hexopt

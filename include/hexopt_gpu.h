@@ -1,0 +1,217 @@
+/*
+ * hexopt_gpu.h -- C ABI of libhexopt_gpu.so, the GB300 (sm_103a) implementation of the
+ * octree hex mesher's geometric-optimisation hot path.
+ *
+ * Every entry point returns an int status (HEXOPT_OK == 0); hexopt_last_error() gives the
+ * message of the last failure.  Arguments are plain pointers and sizes; unless a name says
+ * "_device", pointers are host memory.  Array conventions: vertices are row-major n x 3
+ * doubles (x, y, z per vertex); hexes are 8 uint32 corner ids per hex in the reference's
+ * corner order (hex_ref_shape, global_types.h:208-218); ids inside per-mesh arrays are local
+ * to their mesh.  A context holds one batch of meshes (n_meshes >= 1) resident in HBM and a
+ * CUDA stream; calls on one context are not re-entrant.
+ *
+ * Correspondence with the reference interface this library stands in for (file:line inside the
+ * reference project):
+ *   hexopt_scaled_jacobian        <- bool scaled_jacobian(Mesh&, Mesh_Quality&)        global_functions.h:81
+ *   hexopt_slim_precompute        <- slim_precompute(V, F, V_init, SLIMData&, SLIM_ENERGY, Tetralize_Set)
+ *                                                                                      slim_m.h:102-108
+ *   hexopt_slim_iterate           <- slim_solve2(SLIMData&, iter_num, type) fixed-N branch  slim_m.h:114
+ *   hexopt_slim_m_opt             <- optimization::slim_m_opt(Tetralize_Set&, iter, type)   optimization.h:32
+ *   hexopt_signed_distance        <- igl::signed_distance_pseudonormal (called by dirty_graph_projection,
+ *                                    grid_hex_meshing.cpp:4031-4078) over build_aabb_tree  (:4231-4248)
+ *   hexopt_project_features       <- dirty_graph_projection               grid_hex_meshing.cpp:3954-4082
+ *   hexopt_hausdorff              <- void compute(const Mesh&, const Mesh&, double& diag, double& max,
+ *                                    double& ave)                                       metro_hausdorff.h:37
+ *   hexopt_feature_alignment_step <- one pass of the feature_alignment loop   grid_hex_meshing.cpp:3855-3882
+ *   hexopt_aabb_*                 <- struct AABB / struct Ray                             aabb.h:5-115
+ */
+#ifndef HEXOPT_GPU_H
+#define HEXOPT_GPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define HEXOPT_API __attribute__((visibility("default")))
+#else
+#define HEXOPT_API
+#endif
+
+/* ---- status codes ---- */
+#define HEXOPT_OK 0
+#define HEXOPT_ERR_ARG 1         /* invalid argument (sizes, ids out of range, NULL) */
+#define HEXOPT_ERR_CUDA 2        /* a CUDA call failed */
+#define HEXOPT_ERR_STATE 3       /* call order (e.g. iterate before precompute) */
+#define HEXOPT_ERR_NUMERIC 4     /* NaN/Inf or degenerate element detected on the device */
+#define HEXOPT_ERR_UNSUPPORTED 5 /* option outside what this build implements */
+#define HEXOPT_ERR_NOMEM 6       /* device allocation failed */
+
+/* ---- per-mesh device status bits (hexopt_slim_report.status) ---- */
+#define HEXOPT_STATUS_NONFINITE_ENERGY 1  /* line search met only NaN/Inf energies */
+#define HEXOPT_STATUS_DEGENERATE_TET 2    /* zero-volume tet at precompute (reference: Inf/NaN) */
+#define HEXOPT_STATUS_CG_BREAKDOWN 4      /* p^T A p <= 0 in the PCG */
+#define HEXOPT_STATUS_BVH_OVERFLOW 8      /* a BVH traversal stack overflowed */
+
+/* ---- SLIM_ENERGY (global_types.h:58-66) ---- */
+#define HEXOPT_ARAP 0
+#define HEXOPT_LOG_ARAP 1
+#define HEXOPT_SYMMETRIC_DIRICHLET 2
+#define HEXOPT_CONFORMAL 3
+#define HEXOPT_EXP_CONFORMAL 4
+#define HEXOPT_EXP_SYMMETRIC_DIRICHLET 5
+
+/* ---- arithmetic modes ---- */
+#define HEXOPT_FP64 0  /* plain: every stage in FP64 */
+#define HEXOPT_MIXED 1 /* FP32 local step / energy / SpMV, FP64 accumulation, FP64-refined PCG */
+
+typedef struct hexopt_ctx hexopt_ctx;
+
+/* Mesh_Quality subset (global_types.h:487-511). */
+typedef struct hexopt_quality {
+  double min_Jacobian;
+  double ave_Jacobian;
+  double deviation_Jacobian;
+  int64_t n_inverted; /* hexes whose minimum corner scaled Jacobian is < 0 */
+} hexopt_quality;
+
+typedef struct hexopt_slim_params {
+  int energy;          /* SLIM_ENERGY; the reference's feature alignment uses SYMMETRIC_DIRICHLET */
+  int precision;       /* HEXOPT_FP64 or HEXOPT_MIXED */
+  double weight_opt;   /* SLIMData::weight_opt: M per tet, proximal term 1e-5 * weight_opt */
+  double exp_factor;   /* SLIMData::exp_factor (slim_m_opt sets 5.0) */
+  int cg_max_iter;     /* 20 (slim_m.cpp:495) */
+  double cg_tol;       /* 1e-8 (slim_m.cpp:494) */
+  int ls_candidates;   /* step sizes evaluated per line-search pass, 1..8 (same result, fewer passes) */
+  int cube;            /* compute_referenceMesh 'cube' flag: 1 in feature alignment */
+} hexopt_slim_params;
+
+typedef struct hexopt_slim_report {
+  double energy;         /* SLIMData::energy (total / mesh_area) */
+  double energy_quality; /* SLIMData::engery_quality */
+  double energy_soft;    /* SLIMData::engery_soft */
+  double cg_error;       /* relative residual estimate of the last CG */
+  double max_step;       /* flip-avoiding step bound of the last line search */
+  double step;           /* accepted step */
+  int32_t cg_iters;
+  int32_t halvings;
+  int32_t status;        /* HEXOPT_STATUS_* bits */
+  int32_t pad;
+} hexopt_slim_report;
+
+typedef struct hexopt_fa_report {
+  hexopt_slim_report slim;
+  hexopt_quality quality;     /* scaled Jacobian after the step */
+  double lamda;               /* feature weight after the schedule update */
+  double hausdorff_diag, hausdorff_max, hausdorff_ave; /* when requested, else -1 */
+} hexopt_fa_report;
+
+/* ---- context ---- */
+HEXOPT_API int hexopt_create(hexopt_ctx **ctx, int device);
+HEXOPT_API void hexopt_destroy(hexopt_ctx *ctx);
+HEXOPT_API const char *hexopt_last_error(const hexopt_ctx *ctx);
+/* Synchronises the context's stream. */
+HEXOPT_API int hexopt_sync(hexopt_ctx *ctx);
+
+/* ---- meshes ----
+ * Uploads a batch: mesh m has nv[m] vertices and nh[m] hexes; V and H are the meshes' arrays
+ * concatenated.  h_flag (may be NULL = all 1) marks hexes whose target is a cube of equal volume
+ * (1) or their own shape at precompute time (0), as compute_referenceMesh's H_flag. */
+HEXOPT_API int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const int64_t *nh, const double *V,
+                         const uint32_t *H, const uint8_t *h_flag);
+HEXOPT_API int hexopt_set_positions(hexopt_ctx *ctx, const double *V);
+HEXOPT_API int hexopt_get_positions(hexopt_ctx *ctx, double *V);
+HEXOPT_API int64_t hexopt_num_vertices(const hexopt_ctx *ctx);
+HEXOPT_API int64_t hexopt_num_hexes(const hexopt_ctx *ctx);
+HEXOPT_API int hexopt_num_meshes(const hexopt_ctx *ctx);
+
+/* ---- quality: scaled_jacobian (global_functions.cpp:2309-2356) for every mesh ----
+ * V_Js (8 per hex) and H_Js (1 per hex) may be NULL; q has n_meshes entries. */
+HEXOPT_API int hexopt_scaled_jacobian(hexopt_ctx *ctx, double *V_Js, double *H_Js, hexopt_quality *q);
+
+/* ---- soft constraints (Feature_Constraints, global_types.h:583-610) ----
+ * Per-mesh counts, concatenated arrays, mesh-local vertex ids. */
+HEXOPT_API int hexopt_set_corners(hexopt_ctx *ctx, const int64_t *nC, const int32_t *ids, const double *C);
+HEXOPT_API int hexopt_set_tangents(hexopt_ctx *ctx, const int64_t *nT, const int32_t *ids, const double *normal,
+                        const double *dis);
+HEXOPT_API int hexopt_set_lines(hexopt_ctx *ctx, const int64_t *nL, const int32_t *ids, const double *axis,
+                     const double *origin);
+/* lamda_C / lamda_T / lamda_L per mesh (n_meshes each) */
+HEXOPT_API int hexopt_set_weights(hexopt_ctx *ctx, const double *lamda_C, const double *lamda_T, const double *lamda_L);
+HEXOPT_API int hexopt_get_tangents(hexopt_ctx *ctx, double *normal, double *dis);
+HEXOPT_API int hexopt_get_lines(hexopt_ctx *ctx, double *axis, double *origin);
+
+/* ---- SLIM ---- */
+HEXOPT_API int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *params);
+/* iters fixed-count SLIM iterations (slim_solve2, slim_m.cpp:1269-1288); rep: n_meshes or NULL */
+HEXOPT_API int hexopt_slim_iterate(hexopt_ctx *ctx, int iters, hexopt_slim_report *rep);
+/* slim_precompute + iterate, as optimization::slim_m_opt(ts, iters, -1) */
+HEXOPT_API int hexopt_slim_m_opt(hexopt_ctx *ctx, const hexopt_slim_params *params, int iters, hexopt_slim_report *rep);
+/* curve parameters a_L after the last solve (sum of nL) */
+HEXOPT_API int hexopt_get_curve_params(hexopt_ctx *ctx, double *a_L);
+
+/* ---- closest point on a target triangle mesh ----
+ * Target of mesh m: triangles TF over TV (mesh-local ids), built into a GPU LBVH with the face,
+ * angle-weighted vertex and uniform edge normals of build_aabb_tree. */
+HEXOPT_API int hexopt_set_target(hexopt_ctx *ctx, int mesh, int64_t nv, const double *TV, int64_t nf, const int32_t *TF);
+/* signed_distance_pseudonormal of np host points against mesh m's target. */
+HEXOPT_API int hexopt_signed_distance(hexopt_ctx *ctx, int mesh, int64_t np, const double *P, double *S, int32_t *I, double *C,
+                           double *N);
+
+/* Feature projection sets (dirty_graph_projection): per mesh the regular boundary vertices that
+ * get tangent planes (ids), the line vertices with their curve (line_ids, line_curve) and the
+ * feature curves as polylines over the target's vertices (curve_ptr / curve_vs, closed flag). */
+HEXOPT_API int hexopt_set_feature_sets(hexopt_ctx *ctx, const int64_t *n_regular, const int32_t *regular_ids,
+                            const int64_t *n_line, const int32_t *line_ids, const int32_t *line_curve,
+                            const int64_t *n_curves, const int64_t *curve_ptr, const int32_t *curve_vs,
+                            const uint8_t *curve_closed);
+/* Recomputes tangent planes and line targets from the current positions. */
+HEXOPT_API int hexopt_project_features(hexopt_ctx *ctx);
+
+/* ---- Hausdorff (metro_hausdorff.cpp:358-506): vertex-sampled, two-sided ---- */
+HEXOPT_API int hexopt_hausdorff(hexopt_ctx *ctx, int64_t nv0, const double *V0, int64_t nf0, const int32_t *F0, int64_t nv1,
+                     const double *V1, int64_t nf1, const int32_t *F1, double *diag, double *max_dist,
+                     double *ave_dist);
+/* The hex mesh's boundary surface of mesh m (extract_surface_conforming_mesh: boundary quads split
+ * 0-1-2 / 2-3-0, global_functions.cpp:1021-1060) as nf triangles over the mesh's vertices. */
+HEXOPT_API int hexopt_set_surface(hexopt_ctx *ctx, int mesh, int64_t nf, const int32_t *F);
+/* Between each mesh's target and its boundary surface at the current positions (n_meshes each). */
+HEXOPT_API int hexopt_hausdorff_meshes(hexopt_ctx *ctx, double *diag, double *max_dist, double *ave_dist);
+/* One-sided distances of np host points to the triangles (V, F): min over faces of vcg's
+ * PointDistanceEP (the sample distance of the uniform-area Hausdorff mode). */
+HEXOPT_API int hexopt_point_face_distance(hexopt_ctx *ctx, int64_t np, const double *P, int64_t nv, const double *V, int64_t nf,
+                               const int32_t *F, double *dist);
+
+/* ---- the optimiser iteration: one pass of feature_alignment's loop body ----
+ * projection -> slim_precompute -> one SLIM iteration -> weight schedule -> scaled Jacobian
+ * (-> Hausdorff when do_hausdorff).  lamda0 = feature_weight * MESHRATIO (0.05), upper bound 1e16. */
+HEXOPT_API int hexopt_fa_begin(hexopt_ctx *ctx, const hexopt_slim_params *params, double lamda0, double hausdorff_ratio_t);
+HEXOPT_API int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_report *rep);
+/* Captures one step (without report download) in a CUDA graph and replays it; 1 = on. */
+HEXOPT_API int hexopt_use_graph(hexopt_ctx *ctx, int on);
+
+/* ---- adjoint of the total energy (symmetric Dirichlet over corner tets + soft terms) ----
+ * With the operator frozen at the last precompute: E per mesh, and dE/dX (n x 3, all meshes). */
+HEXOPT_API int hexopt_energy_fwd(hexopt_ctx *ctx, const double *X, double *E);
+HEXOPT_API int hexopt_energy_bwd(hexopt_ctx *ctx, double *grad);
+
+/* ---- launch tuning ---- */
+HEXOPT_API int hexopt_set_block_size(hexopt_ctx *ctx, int kind, int threads); /* kind 0 hex, 1 vertex */
+HEXOPT_API int hexopt_autotune(hexopt_ctx *ctx);
+HEXOPT_API int hexopt_get_tuning(const hexopt_ctx *ctx, int *hex_block, int *vert_block, int *ls_candidates);
+/* Kernel launches issued by this context since creation (for the bench's launch count). */
+HEXOPT_API int64_t hexopt_launch_count(const hexopt_ctx *ctx);
+
+/* ---- aabb.h value types (Ray / AABB, aabb.h:5-115) on the host ---- */
+typedef struct hexopt_aabb { double min[3], max[3]; } hexopt_aabb;
+typedef struct hexopt_ray { double o[3], d[3], dRcp[3]; double mint, maxt; } hexopt_ray;
+HEXOPT_API void hexopt_aabb_merge(hexopt_aabb *a, const hexopt_aabb *b);
+HEXOPT_API double hexopt_aabb_squared_distance(const hexopt_aabb *a, const double *p);
+HEXOPT_API int hexopt_aabb_ray_intersect(const hexopt_aabb *a, const hexopt_ray *r, double *nearT, double *farT);
+HEXOPT_API int hexopt_aabb_largest_axis(const hexopt_aabb *a);
+HEXOPT_API double hexopt_aabb_surface_area(const hexopt_aabb *a);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

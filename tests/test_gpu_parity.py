@@ -1,0 +1,283 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's golden vectors and the
+CPU oracle on the same seeded inputs.
+
+Tolerances (from the required parity bar): scaled Jacobian and inversion flags bit-exact (FP64
+path); per-element energies 1e-5 relative; positions after N iterations 1e-6 of the bbox
+diagonal (FP64 mode); Hausdorff 1e-5 of the diagonal.  The mixed-precision mode is checked
+against the FP64 oracle with the tolerance stated at each test."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def hx():
+    import build
+    build.build()
+    import hexopt
+    return hexopt
+
+
+@pytest.fixture(scope="module")
+def ctx(hx):
+    c = hx.Context(0)
+    yield c
+    c.close()
+
+
+def diag_of(V):
+    return float(np.linalg.norm(V.max(0) - V.min(0)))
+
+
+def jittered(n, sigma, seed):
+    from hexopt import meshgen
+    V, H = meshgen.grid_hex(n)
+    b = meshgen.grid_boundary_mask(n)
+    return meshgen.jitter(V, ~b, 1.0 / n, seed, sigma=sigma), H, b
+
+
+# ------------------------------------------------------------------ scaled Jacobian
+def test_scaled_jacobian_bitexact_vs_reference(ctx):
+    z = load_golden("scaled_jacobian")
+    ctx.upload([(z["V"], z["H"])])
+    vj, hj, q = ctx.scaled_jacobian(per_corner=True)
+    np.testing.assert_allclose(vj, z["V_Js"], rtol=0, atol=1e-15)
+    assert np.array_equal(hj < 0, z["H_Js"] < 0)
+    assert q[0]["inverted"] == int(z["stats"][3])
+    np.testing.assert_allclose([q[0]["min"], q[0]["ave"], q[0]["dev"]], z["stats"][:3], rtol=1e-12)
+
+
+def test_scaled_jacobian_bitexact_vs_oracle_batched(ctx, oracle):
+    meshes = [jittered(n, 0.35, 100 + n)[:2] for n in (6, 9, 4)]
+    ctx.upload(meshes)
+    vj, hj, q = ctx.scaled_jacobian(per_corner=True)
+    o = 0
+    for m, (V, H) in enumerate(meshes):
+        r = oracle.scaled_jacobian(V, H)
+        assert np.array_equal(vj[8 * o:8 * (o + len(H))], r["V_Js"])
+        assert np.array_equal(hj[o:o + len(H)] < 0, r["H_Js"] < 0)
+        assert q[m]["inverted"] == r["inverted"]
+        assert q[m]["min"] == r["min"]
+        o += len(H)
+
+
+# ------------------------------------------------------------------ SLIM
+def load_slim(ctx, z):
+    ctx.upload([(z["V"], z["H"])], h_flag=z.get("h_flag"))
+    ctx.set_corners([z["ids_C"]], [z["C_"]])
+    ctx.set_tangents([z["ids_T"]], [z["normal_T"]], [z["dis_T"]])
+    ctx.set_lines([z["ids_L"]], [z["Axa_L"]], [z["origin_L"]])
+    ctx.set_weights(float(z["lamda_C"]), float(z["lamda_T"]), float(z["lamda_L"]))
+
+
+@pytest.mark.parametrize("name", ["slim_fa_1", "slim_fa_3", "slim_fa_strong", "slim_fa_hflag"])
+def test_slim_fp64_matches_reference(ctx, hx, name):
+    z = load_golden(name)
+    load_slim(ctx, z)
+    rep = ctx.slim_m_opt(int(z["iters"]), precision=hx.FP64, weight_opt=0.001)
+    Vg = ctx.get_positions()
+    d = diag_of(z["V"])
+    assert np.abs(Vg - z["V_o"]).max() <= 1e-6 * d
+    np.testing.assert_allclose([rep[0]["energy"], rep[0]["energy_quality"], rep[0]["energy_soft"]], z["out"], rtol=1e-5)
+    assert rep[0]["status"] == 0
+
+
+@pytest.mark.parametrize("name", ["slim_fa_1", "slim_fa_3", "slim_fa_strong"])
+def test_slim_mixed_error_vs_reference(ctx, hx, name):
+    """Mixed precision (FP32 local step / SpMV / energies, FP64 residual, positions and
+    reductions): positions within 1e-5 of the diagonal, energy within 1e-4 relative."""
+    z = load_golden(name)
+    load_slim(ctx, z)
+    rep = ctx.slim_m_opt(int(z["iters"]), precision=hx.MIXED, weight_opt=0.001)
+    Vg = ctx.get_positions()
+    d = diag_of(z["V"])
+    err = np.abs(Vg - z["V_o"]).max() / d
+    print(f"{name}: mixed position error {err:.3e} diag, energy rel err "
+          f"{abs(rep[0]['energy'] - z['out'][0]) / z['out'][0]:.3e}")
+    assert err <= 1e-5
+    assert abs(rep[0]["energy"] - z["out"][0]) <= 1e-4 * abs(z["out"][0])
+
+
+def test_slim_larger_grid_vs_oracle(ctx, hx, oracle):
+    V, H, b = jittered(14, 0.2, 5)
+    ids = np.nonzero(b)[0].astype(np.int32)
+    nrm = V[ids] - 0.5
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    dis = (nrm * (0.5 + 0.58 * nrm)).sum(1)
+    ctx.upload([(V, H)])
+    ctx.set_tangents([ids], [nrm], [dis])
+    ctx.set_weights(0.5, 0.5, 0.5)
+    rep = ctx.slim_m_opt(3, precision=hx.FP64, weight_opt=0.001)
+    Vg = ctx.get_positions()
+    prob = oracle.SlimProblem(V, H, ids_T=ids, normal_T=nrm, dis_T=dis, lamda_T=0.5, weight_opt=0.001)
+    Vo, _, info = oracle.slim_m_opt(prob, 3)
+    assert np.abs(Vg - Vo).max() <= 1e-6 * diag_of(V)
+    assert rep[0]["energy"] == pytest.approx(info["energy"], rel=1e-6)
+    assert rep[0]["cg_iters"] == info["cg_iters"]
+
+
+def test_batched_meshes_equal_individual_runs(ctx, hx, oracle):
+    probs = []
+    for n, seed in ((5, 1), (7, 2), (4, 3)):
+        V, H, b = jittered(n, 0.15, seed)
+        ids = np.nonzero(b)[0].astype(np.int32)
+        nrm = V[ids] - 0.5
+        nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+        dis = (nrm * (0.5 + 0.55 * nrm)).sum(1)
+        probs.append((V, H, ids, nrm, dis))
+    ctx.upload([(p[0], p[1]) for p in probs])
+    ctx.set_tangents([p[2] for p in probs], [p[3] for p in probs], [p[4] for p in probs])
+    ctx.set_weights([0.05, 1.0, 10.0], [0.05, 1.0, 10.0], [0.05, 1.0, 10.0])
+    rep = ctx.slim_m_opt(2, precision=hx.FP64, weight_opt=0.001)
+    Vg = ctx.get_positions()
+    o = 0
+    for m, (p, lam) in enumerate(zip(probs, (0.05, 1.0, 10.0))):
+        prob = oracle.SlimProblem(p[0], p[1], ids_T=p[2], normal_T=p[3], dis_T=p[4], lamda_T=lam, weight_opt=0.001)
+        Vo, _, info = oracle.slim_m_opt(prob, 2)
+        assert np.abs(Vg[o:o + len(p[0])] - Vo).max() <= 1e-6 * diag_of(p[0])
+        assert rep[m]["energy"] == pytest.approx(info["energy"], rel=1e-6)
+        o += len(p[0])
+
+
+# ------------------------------------------------------------------ projection / Hausdorff
+@pytest.mark.parametrize("name", ["signed_distance", "signed_distance_cyl"])
+def test_signed_distance_matches_reference(ctx, hx, name):
+    z = load_golden(name)
+    from hexopt import meshgen
+    ctx.upload([meshgen.grid_hex(1)])
+    ctx.set_target(0, z["TV"], z["TF"])
+    S, I, Cc, N = ctx.signed_distance(0, z["P"])
+    np.testing.assert_allclose(S, z["S"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(Cc, z["C"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(N, z["N"], rtol=0, atol=1e-12)
+
+
+def test_hausdorff_matches_reference(ctx):
+    z = load_golden("hausdorff")
+    for V1, F1, out in ((z["V1"], z["F1"], z["out"]), (z["BV"], z["BF"], z["out_b"])):
+        dg, mx, av = ctx.hausdorff(z["V0"], z["F0"], V1, F1)
+        assert dg == pytest.approx(out[0], rel=1e-12)
+        assert abs(mx - out[1]) <= 1e-5 * out[0]
+        assert abs(av - out[2]) <= 1e-5 * out[0]
+        assert mx == pytest.approx(out[1], rel=1e-9) and av == pytest.approx(out[2], rel=1e-9)
+
+
+def test_point_face_distance_matches_oracle(ctx, oracle):
+    from hexopt import meshgen
+    TV, TF = meshgen.superellipsoid(5000)
+    P = np.random.default_rng(3).uniform(-0.2, 1.2, (2000, 3))
+    d = ctx.point_face_distance(P, TV, TF)
+    np.testing.assert_allclose(d, oracle.point_face_distance(P, TV, TF), rtol=1e-12, atol=1e-15)
+
+
+def test_hausdorff_meshes_matches_oracle(ctx, hx, oracle):
+    from hexopt import workloads
+    p = workloads.cylinder()
+    workloads.load(ctx, [p])
+    dg, mx, av = ctx.hausdorff_meshes()
+    Vs = p["V"]
+    ref = oracle.hausdorff(p["TV"], p["TF"], Vs, p["surface"])
+    assert abs(dg[0] - ref[0]) <= 1e-12 * ref[0]
+    assert abs(mx[0] - ref[1]) <= 1e-5 * ref[0] and abs(av[0] - ref[2]) <= 1e-5 * ref[0]
+
+
+# ------------------------------------------------------------------ feature alignment
+@pytest.mark.parametrize("graph", [False, True])
+def test_feature_alignment_cylinder_vs_oracle(ctx, hx, graph):
+    import fa_oracle
+    from hexopt import workloads
+    p = workloads.cylinder()
+    workloads.load(ctx, [p])
+    ctx.use_graph(graph)
+    ctx.fa_begin(lamda0=0.05, precision=hx.FP64, weight_opt=0.001)
+    for _ in range(3):
+        r = ctx.fa_step(hausdorff=True)
+    ctx.use_graph(False)
+    Vg = ctx.get_positions()
+    Vo, info, lam = fa_oracle.fa_steps(p, 3)
+    assert np.abs(Vg - Vo).max() <= 1e-6 * diag_of(p["V"])
+    assert r[0]["lamda"] == pytest.approx(lam, rel=1e-6)
+    assert r[0]["energy"] == pytest.approx(info["energy"], rel=1e-6)
+    assert r[0]["hausdorff_max"] > 0
+
+
+def test_feature_alignment_grid_vs_oracle(ctx, hx):
+    import fa_oracle
+    from hexopt import workloads
+    p = workloads.grid_superellipsoid(n=10, sigma=0.2, seed=4, n_tri=4000)
+    workloads.load(ctx, [p])
+    ctx.fa_begin(lamda0=0.05, precision=hx.FP64, weight_opt=0.001)
+    for _ in range(2):
+        r = ctx.fa_step(hausdorff=False)
+    Vg = ctx.get_positions()
+    Vo, info, lam = fa_oracle.fa_steps(p, 2)
+    assert np.abs(Vg - Vo).max() <= 1e-6 * diag_of(p["V"])
+    assert r[0]["lamda"] == pytest.approx(lam, rel=1e-6)
+
+
+# ------------------------------------------------------------------ adjoint
+def test_adjoint_matches_oracle_and_central_differences(ctx, hx, oracle):
+    """Relative agreement 1e-4 with FP64 central differences (h = 1e-6) on seeded coordinates and
+    1e-9 with the oracle's analytic gradient."""
+    z = load_golden("slim_fa_1")
+    load_slim(ctx, z)
+    ctx.slim_precompute(precision=hx.FP64, weight_opt=0.001)
+    X = z["V"] + np.random.default_rng(9).normal(0, 0.01, z["V"].shape)
+    E = ctx.energy_fwd(X)
+    G = ctx.energy_bwd()
+    prob = oracle.SlimProblem(z["V"], z["H"], ids_C=z["ids_C"], C_=z["C_"], lamda_C=float(z["lamda_C"]),
+                              ids_T=z["ids_T"], normal_T=z["normal_T"], dis_T=z["dis_T"], lamda_T=float(z["lamda_T"]),
+                              ids_L=z["ids_L"], Axa_L=z["Axa_L"], origin_L=z["origin_L"], lamda_L=float(z["lamda_L"]))
+    aL = np.zeros(len(z["ids_L"]))
+    Eo = oracle.slim_energy(prob, X, aL)[0]
+    assert E[0] == pytest.approx(Eo, rel=1e-10)
+    Go = oracle.slim_energy_grad(prob, X, aL)
+    np.testing.assert_allclose(G, Go, rtol=1e-9, atol=1e-9 * np.abs(Go).max())
+    rng = np.random.default_rng(10)
+    idx = rng.choice(X.size, size=60, replace=False)
+    h = 1e-6
+    for k in idx:
+        Xp = X.copy(); Xp.flat[k] += h
+        Xm = X.copy(); Xm.flat[k] -= h
+        fd = (oracle.slim_energy(prob, Xp, aL)[0] - oracle.slim_energy(prob, Xm, aL)[0]) / (2 * h)
+        assert abs(G.flat[k] - fd) <= 1e-4 * max(abs(fd), 1e-3 * np.abs(G).max())
+
+
+# ------------------------------------------------------------------ runtime behaviour
+def test_autotune_preserves_results(ctx, hx):
+    z = load_golden("slim_fa_3")
+    load_slim(ctx, z)
+    ctx.slim_precompute(precision=hx.FP64, weight_opt=0.001)
+    cfg = ctx.autotune()
+    assert cfg["hex_block"] in (64, 128) and cfg["ls_candidates"] in (2, 4, 8)
+    rep = ctx.slim_iterate(int(z["iters"]))
+    assert np.abs(ctx.get_positions() - z["V_o"]).max() <= 1e-6 * diag_of(z["V"])
+
+
+def test_invalid_arguments_raise(ctx, hx):
+    V, H, b = jittered(3, 0.1, 1)
+    bad = H.copy()
+    bad[0, 0] = len(V) + 5
+    with pytest.raises(hx.HexoptError, match="out of range"):
+        ctx.upload([(V, bad)])
+    ctx.upload([(V, H)])
+    with pytest.raises(hx.HexoptError):
+        ctx.set_tangents([[len(V)]], [[0, 0, 1]], [0.0])
+    c2 = hx.Context(0)
+    c2.upload([(V, H)])
+    with pytest.raises(hx.HexoptError, match="before slim_precompute"):
+        c2.slim_iterate(1)
+    c2.close()
+
+
+def test_degenerate_tet_sets_status(ctx, hx):
+    from hexopt import meshgen
+    V, H = meshgen.grid_hex(2)
+    V = V.copy()
+    V[13] = V[12]  # collapse an edge of interior hexes: zero-volume corner tets
+    ctx.upload([(V, H)])
+    rep = ctx.slim_m_opt(1, precision=hx.FP64, weight_opt=0.001)
+    assert rep[0]["status"] & 2
