@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""Benchmark of the optimiser iteration (one pass of the feature-alignment loop: projection,
+slim_precompute, one SLIM iteration, weight schedule, scaled-Jacobian check, Hausdorff check) on
+the 2.1M-hex workload: a 128^3 jittered grid whose boundary is tied to a 200k-triangle
+superellipsoid.  Prints one JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision mixed|fp64]
+
+Multi-GPU: the path does not shard a single mesh; N ranks run N independent replicas (one mesh
+each) and `value` is the sum of their iteration rates over the slowest rank's time.
+`--impl reference` times the CPU restatement of the reference's FP64 path (the oracle) on a
+bounded sample of the same workload, on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "feature-preserving-octree-hex-meshing_gb300")
+sys.path.insert(0, PKG)
+
+import numpy as np  # noqa: E402
+
+METRIC = "optimizer iters/s"
+UNIT = "iters/s"
+GRID_N = 128
+CPU_SAMPLE_N = 32          # 32^3 = 32,768 hexes per CPU-baseline step
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as tdist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        tdist.init_process_group("gloo", rank=rank, world_size=ws)
+        return rank, ws, tdist
+    return 0, 1, None
+
+
+def barrier(tdist):
+    if tdist is not None:
+        tdist.barrier()
+
+
+def max_over_ranks(tdist, x):
+    if tdist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(PEAKS) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def spmv_bytes_per_hex(mixed: bool) -> float:
+    """Algorithmic bytes of one element-SpMV launch per hex: 8 corner ids (32 B), 8 tets x 6
+    stored coefficients, one read of the search direction and one read-modify-write of the
+    product per vertex (N ~ H on these meshes; AoS4 stride)."""
+    w = 4 if mixed else 8
+    return 32 + 8 * 6 * w + 4 * w + 2 * 4 * w
+
+
+def cpu_baseline(steps=None, budget_s=12.0):
+    """The oracle (CPU restatement of the reference's FP64 path) on a 32^3 sample of the
+    workload, single-threaded; returns (iters/s scaled to the full workload, details)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_py
+    oracle_py.build_oracle()
+    import fa_oracle
+    from hexopt import workloads
+    p = workloads.grid_superellipsoid(CPU_SAMPLE_N, n_tri=20000)
+    times = []
+    V = p["V"]
+    t_all = time.perf_counter()
+    n = 0
+    while True:
+        t0 = time.perf_counter()
+        V, info, lam = fa_oracle.fa_steps(dict(p, V=V), 1)
+        times.append(time.perf_counter() - t0)
+        n += 1
+        if steps is not None and n >= steps:
+            break
+        if steps is None and (time.perf_counter() - t_all > budget_s or n >= 20):
+            break
+    sec = float(np.median(times))
+    hexes = len(p["H"])
+    mhex = hexes / sec / 1e6
+    full = GRID_N ** 3
+    return hexes / sec / full, dict(sample=f"grid {CPU_SAMPLE_N}^3 ({hexes} hexes), 20k-triangle superellipsoid, "
+                                          f"{n} feature-alignment iterations, median {sec:.3f} s/iter; "
+                                          f"iters/s scaled by hexes to the {full}-hex workload",
+                                    mhex_per_s=mhex, sec_per_iter=sec)
+
+
+def run_reference(args):
+    rank, ws, tdist = dist_init()
+    if rank != 0:
+        return 0
+    steps = max(1, args.steps)
+    warm = max(0, args.warmup)
+    if warm:
+        cpu_baseline(steps=min(warm, 1))
+    val, det = cpu_baseline(steps=steps)
+    out = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+           "ms_per_step": det["sec_per_iter"] * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+           "config": {"workload": f"grid{GRID_N}_superellipsoid (2,097,152 hexes), CPU sample "
+                                  f"grid{CPU_SAMPLE_N}", "hexes": GRID_N ** 3},
+           "cpu_baseline": {"value": val, "unit": UNIT, "cores": 1, "kind": "port", "sample": det["sample"]},
+           "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "mhex_per_s": det["mhex_per_s"]}
+    print(json.dumps(out))
+    return 0
+
+
+def run_ours(args):
+    rank, ws, tdist = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import build
+    build.build()
+    import hexopt
+    from hexopt import workloads
+    precision = hexopt.MIXED if args.precision == "mixed" else hexopt.FP64
+    p = workloads.grid_superellipsoid(GRID_N, seed=rank)
+    nv, nh = len(p["V"]), len(p["H"])
+    ctx = hexopt.Context(local)
+    workloads.load(ctx, [p])
+    ctx.fa_begin(lamda0=0.05, precision=precision, weight_opt=0.001)
+    tune = ctx.autotune() if not args.no_autotune else None
+    ctx.use_graph(True)
+    do_h = not args.no_hausdorff
+    for _ in range(args.warmup):
+        ctx.fa_step(hausdorff=do_h, report=False)
+    ctx.sync()
+    # ---------------- timed region: inputs resident in HBM, one graph replay per step
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(tdist)
+    l0 = ctx.launch_count()
+    ctx.timer_start()
+    for _ in range(args.steps):
+        ctx.fa_step(hausdorff=do_h, report=False)
+    ms = ctx.timer_stop()
+    launches = ctx.launch_count() - l0
+    clk = clocks.stop()
+    ms = max_over_ranks(tdist, ms)
+    rep = ctx.fa_step(hausdorff=do_h)[0]  # report of the state after the timed steps
+    value = ws * args.steps / (ms / 1e3)
+    # ---------------- e2e: host buffers in pinned memory, H2D + step + D2H every step
+    import torch
+    Vin = torch.from_numpy(np.ascontiguousarray(p["V"])).pin_memory()
+    Vout = torch.empty((nv, 3), dtype=torch.float64).pin_memory()
+    vin, vout = Vin.numpy(), Vout.numpy()
+    ctx.fa_begin(lamda0=0.05, precision=precision, weight_opt=0.001)
+    ctx.fa_step(hausdorff=do_h, report=False)  # re-capture the graph outside the timed region
+    barrier(tdist)
+    ctx.timer_start()
+    for _ in range(args.steps):
+        ctx._ck(ctx.L.hexopt_set_positions(ctx.h, hexopt._lib.ptr(vin, hexopt._lib._d)), "set_positions")
+        r = ctx.fa_step(hausdorff=do_h, report=True)
+        ctx._ck(ctx.L.hexopt_get_positions(ctx.h, hexopt._lib.ptr(vout, hexopt._lib._d)), "get_positions")
+    e2e_ms = max_over_ranks(tdist, ctx.timer_stop())
+    e2e = ws * args.steps / (e2e_ms / 1e3)
+    rep_bytes = 128  # per-mesh report read back (hexopt_fa_report)
+    # ---------------- FP64 plain path on the same input (the benchmark spec comparison), same steps
+    out_extra = {}
+    if not args.skip_compare:
+        cmp_steps = min(args.steps, 5)
+        res = {}
+        for name, prec in (("fp64", hexopt.FP64), ("mixed", hexopt.MIXED)):
+            ctx.set_positions(p["V"])
+            ctx.fa_begin(lamda0=0.05, precision=prec, weight_opt=0.001)
+            ctx.use_graph(True)
+            ctx.fa_step(hausdorff=do_h, report=False)  # capture
+            ctx.set_positions(p["V"])
+            ctx.fa_begin(lamda0=0.05, precision=prec, weight_opt=0.001)
+            ctx.timer_start()
+            for _ in range(cmp_steps):
+                ctx.fa_step(hausdorff=do_h, report=False)
+            t = ctx.timer_stop()
+            q = ctx.scaled_jacobian()[2][0]
+            res[name] = dict(iters_per_s=cmp_steps / (t / 1e3), min_J=q["min"])
+        out_extra = {"fp64_iters_per_s": res["fp64"]["iters_per_s"], "mixed_iters_per_s": res["mixed"]["iters_per_s"],
+                     "mixed_over_fp64": res["mixed"]["iters_per_s"] / res["fp64"]["iters_per_s"],
+                     "min_J_fp64": res["fp64"]["min_J"], "min_J_mixed": res["mixed"]["min_J"],
+                     "min_J_abs_diff": abs(res["fp64"]["min_J"] - res["mixed"]["min_J"]),
+                     "compare_steps": cmp_steps}
+    # ---------------- roofline of the dominant kernel (element SpMV of the PCG)
+    ctx.set_positions(p["V"])
+    ctx.fa_begin(lamda0=0.05, precision=precision, weight_opt=0.001)
+    spmv_ms = ctx.time_stage(0, reps=50)
+    mixed = precision == hexopt.MIXED
+    achieved = spmv_bytes_per_hex(mixed) * nh / (spmv_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    stages = {nm: ctx.time_stage(i, reps=10) for i, nm in ((1, "local_ms"), (2, "ls_energy_ms"), (3, "sj_ms"),
+                                                            (4, "projection_ms"))}
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
+           "config": {"workload": f"grid{GRID_N}_superellipsoid: {nh} hexes, {nv} vertices, 200k-triangle "
+                                  f"superellipsoid target (float32 coords), Gaussian jitter 0.2h seed {rank}; "
+                                  f"{'mixed FP32/FP64' if mixed else 'plain FP64'}; Hausdorff every iteration "
+                                  f"{'on' if do_h else 'off'}; CUDA-graph replay per step",
+                      "hexes": nh, "vertices": nv, "replicas": ws,
+                      "l2": "inputs larger than L2 (per-tet coefficients and positions exceed 129 MB)",
+                      "tuning": tune},
+           "mhex_per_s": value * nh / 1e6,
+           "min_J": rep["min_J"], "energy": rep["energy"], "hausdorff_ratio": rep["hausdorff_max"] / rep["hausdorff_diag"] if do_h else None,
+           "gpu_launches": launches,
+           "clocks": clk,
+           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nv * 3 * 8,
+                   "d2h_bytes_per_step": nv * 3 * 8 + rep_bytes},
+           "roofline": {"bound": "hbm", "kernel": "k_spmv (element SpMV of the PCG)", "achieved": achieved,
+                        "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                        "peak_kind": peak_kind, "kernel_ms": spmv_ms,
+                        "bytes_per_hex": spmv_bytes_per_hex(mixed)},
+           "stages": stages}
+    out.update(out_extra)
+    if rank == 0 and not args.no_cpu_baseline:
+        val, det = cpu_baseline()
+        out["cpu_baseline"] = {"value": val, "unit": UNIT, "cores": 1, "kind": "port", "sample": det["sample"]}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-hausdorff", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--skip-compare", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    return run_reference(args) if args.impl == "reference" else run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

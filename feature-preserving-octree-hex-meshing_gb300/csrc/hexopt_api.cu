@@ -105,7 +105,7 @@ struct hexopt_ctx {
   DBuf md_d, sc_d;
   std::vector<MeshScalars> sc;
   DBuf X, hexv, gslot, Sinv, Ccoef, Bgen, aL;
-  DBuf b, diag, q64, ba, diaga, q64a;
+  DBuf b, diag, ba, diaga;
   DBuf d, r, p, q, invd, da, ra, pa, qa, invda;
   DBuf stage, stage2, HJs, VJs, Xa, grad, Xbak;
   bool adj_ready = false;
@@ -115,6 +115,7 @@ struct hexopt_ctx {
   std::vector<double> lamC, lamT, lamL;
   KindTable kind[8];
   int block[8] = {128, 256, 256, 128, 128, 128, 128, 128};  // K_CONS follows K_VERT's size
+  int ipt[8] = {1, 4, 1, 1, 1, 1, 1, 1};                     // items per thread of each kind
   // SLIM
   hexopt_slim_params params{};
   bool precomputed = false;
@@ -132,6 +133,7 @@ struct hexopt_ctx {
   cudaGraphExec_t graph_exec = nullptr;
   bool graph_hausdorff = false;
   int64_t graph_launches = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
 namespace {
@@ -173,7 +175,7 @@ cudaError_t upload(DBuf &buf, const T *src, size_t n, cudaStream_t st) {
 void build_kind(hexopt_ctx *c, int k, const std::vector<int64_t> &count, const std::vector<int64_t> &item0) {
   KindTable &t = c->kind[k];
   t.segs.clear();
-  const int B = c->block[k];
+  const int B = c->block[k] * c->ipt[k];
   for (int m = 0; m < c->n_meshes; m++) {
     const int64_t n = count[m];
     const int64_t nb = std::max<int64_t>(1, (n + B - 1) / B);
@@ -262,7 +264,7 @@ KArgs make_args(hexopt_ctx *c) {
   a.Sinv = c->Sinv.p;
   a.Ccoef = c->Ccoef.p;
   a.Bgen = c->Bgen.as<double>();
-  a.b = c->b.as<double>(); a.diag = c->diag.as<double>(); a.ba = c->ba.as<double>(); a.diaga = c->diaga.as<double>();
+  a.b = c->b.p; a.diag = c->diag.p; a.ba = c->ba.p; a.diaga = c->diaga.p;
   a.d = c->d.p; a.r = c->r.p; a.p = c->p.p; a.q = c->q.p; a.invd = c->invd.p;
   a.da = c->da.p; a.ra = c->ra.p; a.pa = c->pa.p; a.qa = c->qa.p; a.invda = c->invda.p;
   a.c_ids = c->c_ids.as<int32_t>(); a.c_pos = c->c_pos.as<double>();
@@ -284,10 +286,9 @@ int alloc_vectors(hexopt_ctx *ctx) {
   const size_t nv4 = (size_t)std::max<int64_t>(ctx->NV, 1) * 4;
   const size_t nl = (size_t)std::max<int64_t>(ctx->NL, 1);
   const size_t vt = ctx->mixed ? sizeof(float) : sizeof(double);
-  for (DBuf *bf : {&ctx->b, &ctx->diag, &ctx->q64}) CK(bf->ensure(nv4 * sizeof(double)));
-  for (DBuf *bf : {&ctx->d, &ctx->r, &ctx->p, &ctx->q, &ctx->invd}) CK(bf->ensure(nv4 * vt));
-  for (DBuf *bf : {&ctx->ba, &ctx->diaga, &ctx->q64a, &ctx->aL}) CK(bf->ensure(nl * sizeof(double)));
-  for (DBuf *bf : {&ctx->da, &ctx->ra, &ctx->pa, &ctx->qa, &ctx->invda}) CK(bf->ensure(nl * vt));
+  for (DBuf *bf : {&ctx->b, &ctx->diag, &ctx->d, &ctx->r, &ctx->p, &ctx->q, &ctx->invd}) CK(bf->ensure(nv4 * vt));
+  CK(ctx->aL.ensure(nl * sizeof(double)));
+  for (DBuf *bf : {&ctx->ba, &ctx->diaga, &ctx->da, &ctx->ra, &ctx->pa, &ctx->qa, &ctx->invda}) CK(bf->ensure(nl * vt));
   const size_t nt = (size_t)((ctx->NH + 31) / 32 * 32) * 8;
   CK(ctx->Sinv.ensure(nt * vt));
   CK(ctx->Ccoef.ensure(nt * 6 * vt));
@@ -316,21 +317,18 @@ int run_precompute(hexopt_ctx *ctx) {
 }
 
 template <typename ET, typename VT>
-int run_iteration(hexopt_ctx *ctx) {
+int run_iteration(hexopt_ctx *ctx, bool pre) {
   KArgs a = make_args(ctx);
   cudaStream_t st = ctx->st;
   const size_t nv4 = (size_t)ctx->NV * 4;
-  CK(cudaMemsetAsync(ctx->b.p, 0, nv4 * sizeof(double), st));
-  CK(cudaMemsetAsync(ctx->diag.p, 0, nv4 * sizeof(double), st));
-  CK(cudaMemsetAsync(ctx->q64.p, 0, nv4 * sizeof(double), st));
-  if (ctx->NL) CK(cudaMemsetAsync(ctx->q64a.p, 0, (size_t)ctx->NL * sizeof(double), st));
+  CK(cudaMemsetAsync(ctx->b.p, 0, nv4 * sizeof(VT), st));
+  CK(cudaMemsetAsync(ctx->diag.p, 0, nv4 * sizeof(VT), st));
+  CK(cudaMemsetAsync(ctx->r.p, 0, nv4 * sizeof(VT), st));
   const int64_t hb = ctx->kind[K_HEX].nblk, vb = ctx->kind[K_VERT].nblk, cb = ctx->kind[K_CONS].nblk;
-  launch_local<ET, VT>(a, hb, st);
+  launch_local<ET, VT>(a, hb, pre, st);
   launch_soft_rhs<VT>(a, cb, st);
-  launch_residual_elems<ET, VT>(a, hb, ctx->q64.as<double>(), st);
-  launch_soft_residual<VT>(a, cb, ctx->q64.as<double>(), ctx->q64a.as<double>(), st);
-  launch_cg_start<VT>(a, vb, ctx->q64.as<double>(), ctx->q64a.as<double>(), st);
-  ctx->launches += 5;
+  launch_cg_start<VT>(a, vb, st);
+  ctx->launches += 3;
   for (int i = 0; i < ctx->params.cg_max_iter; i++) launch_cg_iter<VT>(a, hb, vb, cb, st);
   ctx->launches += (int64_t)kLaunchesCgIter * ctx->params.cg_max_iter;
   launch_line_search<ET, VT>(a, hb, vb, cb, st);
@@ -343,12 +341,14 @@ int run_iteration(hexopt_ctx *ctx) {
 int dispatch_precompute(hexopt_ctx *ctx) {
   return ctx->mixed ? run_precompute<float, float>(ctx) : run_precompute<double, double>(ctx);
 }
-int dispatch_iteration(hexopt_ctx *ctx) {
-  return ctx->mixed ? run_iteration<float, float>(ctx) : run_iteration<double, double>(ctx);
+int dispatch_iteration(hexopt_ctx *ctx, bool pre = false) {
+  return ctx->mixed ? run_iteration<float, float>(ctx, pre) : run_iteration<double, double>(ctx, pre);
 }
 
-void fill_report(const MeshScalars &S, hexopt_slim_report &r) {
-  r.energy = S.energy;
+// SLIMData::energy is the accepted total divided by mesh_area = sum of M over the tets
+// (slim_m.cpp:1129-1130, 1284-1285).
+void fill_report(const MeshScalars &S, int64_t nh, hexopt_slim_report &r) {
+  r.energy = S.energy / (S.M * 8.0 * (double)nh);
   r.energy_quality = S.eq;
   r.energy_soft = S.es;
   r.cg_error = S.cg_error;
@@ -543,6 +543,8 @@ void hexopt_destroy(hexopt_ctx *ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
 }
@@ -795,6 +797,8 @@ int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *p) {
   }
   rc = push_scalars(ctx);
   if (rc) return rc;
+  // slim_precompute: data.a_L.setZero() (slim_m.cpp:1115)
+  if (ctx->NL) CK(cudaMemsetAsync(ctx->aL.p, 0, sizeof(double) * ctx->NL, ctx->st));
   rc = dispatch_precompute(ctx);
   if (rc) return rc;
   ctx->precomputed = true;
@@ -812,7 +816,7 @@ int hexopt_slim_iterate(hexopt_ctx *ctx, int iters, hexopt_slim_report *rep) {
   if (rep) {
     rc = pull_scalars(ctx);
     if (rc) return rc;
-    for (int m = 0; m < ctx->n_meshes; m++) fill_report(ctx->sc[m], rep[m]);
+    for (int m = 0; m < ctx->n_meshes; m++) fill_report(ctx->sc[m], ctx->md[m].nh, rep[m]);
   }
   return HEXOPT_OK;
 }
@@ -1220,14 +1224,17 @@ int hexopt_fa_begin(hexopt_ctx *ctx, const hexopt_slim_params *p, double lamda0,
 static int fa_enqueue(hexopt_ctx *ctx, int do_hausdorff) {
   int rc = run_projection(ctx);
   if (rc) return rc;
-  rc = dispatch_precompute(ctx);
-  if (rc) return rc;
-  rc = dispatch_iteration(ctx);
+  rc = dispatch_iteration(ctx, true);  // slim_precompute fused into the local step
   if (rc) return rc;
   launch_fa_schedule(ctx->sc_d.as<MeshScalars>(), ctx->n_meshes, ctx->lamda0, 1e16, ctx->st);
   KArgs a = make_args(ctx);
-  launch_scaled_jacobian(a, ctx->kind[K_HEX].nblk, nullptr, ctx->HJs.as<double>(), ctx->st);
-  ctx->launches += 3;
+  if (ctx->mixed) {
+    launch_sj_check(a, ctx->kind[K_HEX].nblk, ctx->st);
+    ctx->launches += 2;
+  } else {
+    launch_scaled_jacobian(a, ctx->kind[K_HEX].nblk, nullptr, ctx->HJs.as<double>(), ctx->st);
+    ctx->launches += 3;
+  }
   if (do_hausdorff) {
     rc = run_hausdorff(ctx);
     if (rc) return rc;
@@ -1278,7 +1285,7 @@ int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_r
     if (rc) return rc;
     for (int m = 0; m < ctx->n_meshes; m++) {
       const MeshScalars &S = ctx->sc[m];
-      fill_report(S, rep[m].slim);
+      fill_report(S, ctx->md[m].nh, rep[m].slim);
       rep[m].quality.min_Jacobian = S.sj_min;
       rep[m].quality.ave_Jacobian = S.sj_sum / (double)ctx->md[m].nh;
       rep[m].quality.deviation_Jacobian = -1;  // the step skips the deviation pass
@@ -1377,7 +1384,9 @@ int hexopt_autotune(hexopt_ctx *ctx) {
   rc = pull_scalars(ctx);
   if (rc) return rc;
   const std::vector<MeshScalars> sc0 = ctx->sc;
-  const int hb[2] = {64, 128}, vb[2] = {128, 256}, lc[3] = {2, 4, 8};
+  const int hb[2] = {64, 128}, vb[2] = {128, 256};
+  // candidate counts whose energy-pass variants run without register spills in each mode
+  const int lc[3] = {ctx->mixed ? 2 : 1, ctx->mixed ? 4 : 2, ctx->mixed ? 5 : 2};
   float best = INFINITY;
   int bh = ctx->block[K_HEX], bv = ctx->block[K_VERT], bl = ctx->params.ls_candidates;
   cudaEvent_t e0, e1;
@@ -1475,6 +1484,80 @@ int hexopt_aabb_largest_axis(const hexopt_aabb *a) {
 double hexopt_aabb_surface_area(const hexopt_aabb *a) {
   const double e0 = a->max[0] - a->min[0], e1 = a->max[1] - a->min[1], e2 = a->max[2] - a->min[2];
   return 2.0 * (e0 * e1 + e1 * e2 + e2 * e0);
+}
+
+
+// ---------------------------------------------------------------- timing
+int hexopt_timer_start(hexopt_ctx *ctx) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  if (!ctx->ev0) CK(cudaEventCreate(&ctx->ev0));
+  if (!ctx->ev1) CK(cudaEventCreate(&ctx->ev1));
+  CK(cudaEventRecord(ctx->ev0, ctx->st));
+  return HEXOPT_OK;
+}
+
+int hexopt_timer_stop(hexopt_ctx *ctx, double *ms) {
+  if (!ctx || !ctx->ev0) return HEXOPT_ERR_ARG;
+  CK(cudaEventRecord(ctx->ev1, ctx->st));
+  CK(cudaEventSynchronize(ctx->ev1));
+  float f = 0;
+  CK(cudaEventElapsedTime(&f, ctx->ev0, ctx->ev1));
+  if (ms) *ms = f;
+  return HEXOPT_OK;
+}
+
+}  // extern "C"
+
+template <typename ET, typename VT>
+static void stage_launch(hexopt_ctx *ctx, int stage) {
+  KArgs a = make_args(ctx);
+  const int64_t hb = ctx->kind[K_HEX].nblk;
+  switch (stage) {
+    case 0: launch_spmv_elems<ET, VT>(a, hb, ctx->st); break;
+    case 1: launch_local<ET, VT>(a, hb, false, ctx->st); break;
+    case 2: launch_ls_energy_pass<ET, VT>(a, hb, ctx->st); break;
+    case 3: launch_scaled_jacobian(a, hb, nullptr, ctx->HJs.as<double>(), ctx->st); break;
+    case 4: run_projection(ctx); break;
+    default: break;
+  }
+}
+
+extern "C" {
+
+int hexopt_time_stage(hexopt_ctx *ctx, int stage, int reps, double *ms_per_launch) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!ctx->precomputed) return fail(ctx, HEXOPT_ERR_STATE, "time_stage before slim_precompute");
+  if (stage < 0 || stage > 5 || reps <= 0) return fail(ctx, HEXOPT_ERR_ARG, "time_stage: bad stage or reps");
+  if (stage <= 2) {
+    // make the solver state well defined (one iteration), then reopen the per-mesh CG and
+    // line-search flags so the timed launches do their full work
+    rc = dispatch_iteration(ctx);
+    if (rc) return rc;
+    rc = pull_scalars(ctx);
+    if (rc) return rc;
+    for (auto &S : ctx->sc) { S.cg_done = 0; S.ls_done = 0; }
+    rc = push_scalars(ctx);
+    if (rc) return rc;
+  }
+  rc = hexopt_timer_start(ctx);
+  if (rc) return rc;
+  for (int i = 0; i < reps; i++) {
+    if (stage == 5) {
+      rc = dispatch_iteration(ctx);
+      if (rc) return rc;
+    } else if (ctx->mixed) {
+      stage_launch<float, float>(ctx, stage);
+    } else {
+      stage_launch<double, double>(ctx, stage);
+    }
+  }
+  CKL();
+  double ms = 0;
+  rc = hexopt_timer_stop(ctx, &ms);
+  if (rc) return rc;
+  if (ms_per_launch) *ms_per_launch = ms / reps;
+  return HEXOPT_OK;
 }
 
 }  // extern "C"

@@ -124,4 +124,96 @@ __device__ __forceinline__ void load_hex(const uint32_t *hexv, int64_t h, uint32
   for (int c = 0; c < 8; c++) hv[c] = __ldg(hexv + hex_idx(h, c));
 }
 
+// ---------------------------------------------------------------- 12-edge hex frame
+// The 24 tet edges of the 8 corner tets are the 12 hex edges, each used twice.  Edge e joins
+// corners (lo, hi) with lo < hi and is stored as P[hi] - P[lo]; the edge (c0 -> cj) of a corner
+// tet is +E[e] when cj > c0, else -E[e].  Everything below folds at compile time.
+__host__ __device__ __forceinline__ constexpr int hex_edge_ord(int lo, int hi) {
+  return (lo == 0 && hi == 1) ? 0 : (lo == 1 && hi == 2) ? 1 : (lo == 2 && hi == 3) ? 2 : (lo == 0 && hi == 3) ? 3
+       : (lo == 4 && hi == 5) ? 4 : (lo == 5 && hi == 6) ? 5 : (lo == 6 && hi == 7) ? 6 : (lo == 4 && hi == 7) ? 7
+       : (lo == 0 && hi == 4) ? 8 : (lo == 1 && hi == 5) ? 9 : (lo == 2 && hi == 6) ? 10 : 11;
+}
+__host__ __device__ __forceinline__ constexpr int hex_edge_id(int a, int b) {
+  return hex_edge_ord(a < b ? a : b, a < b ? b : a);
+}
+__host__ __device__ __forceinline__ constexpr int hex_edge_lo(int e) {
+  return e == 0 ? 0 : e == 1 ? 1 : e == 2 ? 2 : e == 3 ? 0 : e == 4 ? 4 : e == 5 ? 5 : e == 6 ? 6 : e == 7 ? 4
+       : e == 8 ? 0 : e == 9 ? 1 : e == 10 ? 2 : 3;
+}
+__host__ __device__ __forceinline__ constexpr int hex_edge_hi(int e) {
+  return e == 0 ? 1 : e == 1 ? 2 : e == 2 ? 3 : e == 3 ? 3 : e == 4 ? 5 : e == 5 ? 6 : e == 6 ? 7 : e == 7 ? 7
+       : e == 8 ? 4 : e == 9 ? 5 : e == 10 ? 6 : 7;
+}
+
+// Gather the 8 corner positions (FP64) and form the 12 edges in FP64, stored as T.
+template <typename T>
+__device__ __forceinline__ void hex_edges_pos(const double *X, const uint32_t hv[8], T E12[12][3]) {
+  double P[8][3];
+#pragma unroll
+  for (int c = 0; c < 8; c++) load_pos(X, hv[c], P[c]);
+#pragma unroll
+  for (int e = 0; e < 12; e++)
+#pragma unroll
+    for (int r = 0; r < 3; r++) E12[e][r] = T(P[hex_edge_hi(e)][r] - P[hex_edge_lo(e)][r]);
+}
+template <typename T>
+__device__ __forceinline__ void hex_edges_vec(const T *Y, const uint32_t hv[8], T E12[12][3]) {
+  T P[8][3];
+#pragma unroll
+  for (int c = 0; c < 8; c++) load_vec(Y, hv[c], P[c]);
+#pragma unroll
+  for (int e = 0; e < 12; e++)
+#pragma unroll
+    for (int r = 0; r < 3; r++) E12[e][r] = P[hex_edge_hi(e)][r] - P[hex_edge_lo(e)][r];
+}
+// Edge matrix (columns) of corner tet K from the 12-edge frame.
+template <int K, typename T>
+__device__ __forceinline__ void tet_E12(const T E12[12][3], T E[3][3]) {
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int c0 = tet_v(K, 0), cj = tet_v(K, j + 1);
+    const int e = hex_edge_id(c0, cj);
+    const T sg = cj > c0 ? T(1) : T(-1);
+#pragma unroll
+    for (int r = 0; r < 3; r++) E[r][j] = sg * E12[e][r];
+  }
+}
+// Accumulate 3x3 "edge forces" G (columns for edges c0->cj) into corner forces.
+template <int K, typename T, typename A>
+__device__ __forceinline__ void scatter_cols(const T G[3][3], A F[8][3]) {
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int c0 = tet_v(K, 0), cj = tet_v(K, j + 1);
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      F[cj][r] += A(G[r][j]);
+      F[c0][r] -= A(G[r][j]);
+    }
+  }
+}
+// J = E B and the transpose action G = Q B^T for a cube-target tet (B = signed permutation
+// scaled by s) or an own-shape tet (B stored, 9 doubles).
+template <int K, typename T>
+__device__ __forceinline__ void apply_B(const T E[3][3], int32_t gs, const double *B, T s, T J[3][3]) {
+  if (gs < 0) cube_J<K>(E, s, J);
+  else gen_J<K>(E, B, J);
+}
+template <int K, typename T>
+__device__ __forceinline__ void apply_BT(const T Q[3][3], int32_t gs, const double *B, T s, T G[3][3]) {
+  if (gs < 0) {
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int a = edge_axis(K, j);
+      const T sg = T(edge_sign(K, j)) * s;
+#pragma unroll
+      for (int r = 0; r < 3; r++) G[r][j] = Q[r][a] * sg;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int r = 0; r < 3; r++) G[r][j] = Q[r][0] * T(B[j * 3 + 0]) + Q[r][1] * T(B[j * 3 + 1]) + Q[r][2] * T(B[j * 3 + 2]);
+  }
+}
+
 }  // namespace hexopt

@@ -23,8 +23,8 @@ struct KArgs {
   void *Sinv;            // per tet 1/cbrt(6 vol) (ET, AoSoA NC=1)
   void *Ccoef;           // per tet C_t (ET, AoSoA NC=6)
   double *Bgen;          // own-shape rest inverses, 9 per tet
-  // linear system (FP64 accumulation)
-  double *b, *diag, *ba, *diaga;
+  // linear system right-hand side and diagonal (VT)
+  void *b, *diag, *ba, *diaga;
   // CG vectors (VT)
   void *d, *r, *p, *q, *invd;
   void *da, *ra, *pa, *qa, *invda;
@@ -47,14 +47,13 @@ struct KArgs {
 };
 
 template <typename ET, typename VT> void launch_precompute(const KArgs &a, int64_t nblk, cudaStream_t st);
-template <typename ET, typename VT> void launch_local(const KArgs &a, int64_t nblk, cudaStream_t st);
-template <typename ET, typename VT> void launch_residual_elems(const KArgs &a, int64_t nblk, double *q64, cudaStream_t st);
+// fused local step; pre = also take the volume snapshot (slim_precompute) at the current X
+template <typename ET, typename VT> void launch_local(const KArgs &a, int64_t nblk, bool pre, cudaStream_t st);
 template <typename ET, typename VT> void launch_spmv_elems(const KArgs &a, int64_t nblk, cudaStream_t st);
 template <typename VT> void launch_soft_rhs(const KArgs &a, int64_t nblk, cudaStream_t st);
-template <typename VT> void launch_soft_residual(const KArgs &a, int64_t nblk, double *q64, double *q64a, cudaStream_t st);
-template <typename VT> void launch_soft_spmv(const KArgs &a, int64_t nblk, cudaStream_t st);
-template <typename VT> void launch_cg_start(const KArgs &a, int64_t nblk, const double *q64, const double *q64a, cudaStream_t st);
+template <typename VT> void launch_cg_start(const KArgs &a, int64_t nblk, cudaStream_t st);
 template <typename VT> void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st);
+template <typename ET, typename VT> void launch_ls_energy_pass(const KArgs &a, int64_t hblk, cudaStream_t st);
 template <typename ET, typename VT> void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st);
 
 // Launches per call of the launchers above (for the launch count).
@@ -66,6 +65,8 @@ template <typename ET> void launch_energy_bwd(const KArgs &a, int64_t hblk, int6
 
 // ---- quality (k_quality.cu) ----
 void launch_scaled_jacobian(const KArgs &a, int64_t hblk, double *V_Js, double *H_Js, cudaStream_t st);
+// FP32-screened minimum / inversion check used inside the mixed-mode optimiser iteration
+void launch_sj_check(const KArgs &a, int64_t hblk, cudaStream_t st);
 // weight schedule + report packing for the feature-alignment step
 void launch_fa_schedule(MeshScalars *sc, int n_meshes, double lamda0, double bound, cudaStream_t st);
 

@@ -193,12 +193,89 @@ __device__ void closest_pt_tri(const double p[3], const double a[3], const doubl
   for (int d = 0; d < 3; d++) out[d] = a[d] + ab[d] * v + ac[d] * w;
 }
 
-// Nearest face (squared distance, face id, closest point).  Returns false on stack overflow.
+// ---- FP32 filtering with exact FP64 evaluation ----
+// Traversal and leaf screening run in FP32 on coordinates taken relative to the leaf's first
+// vertex (formed in FP64, rounded once).  A face is evaluated in FP64 only when its FP32 lower
+// bound is within a margin of the current best, so the FP64 result is the one a pure FP64
+// search returns: boxes are stored rounded outward, the box margin covers the rounding of the
+// query, and the leaf margin (1e-4 of the local scale) covers the FP32 point-triangle distance
+// of triangles whose smallest angle is above ~0.6 degrees; thinner triangles fall back to their
+// box distance as the lower bound.
+__device__ __forceinline__ float box_d2f(const float *bx, const float q[3]) {
+  float s = 0.f;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const float e = fmaxf(fmaxf(bx[d] - q[d], q[d] - bx[3 + d]), 0.f);
+    s = fmaf(e, e, s);
+  }
+  return s;
+}
+
+// Squared distance from p to the triangle (0, b, c) in FP32 (Ericson's region tests).
+__device__ __forceinline__ float tri_d2f(const float p[3], const float b[3], const float c[3]) {
+  const float d1 = b[0] * p[0] + b[1] * p[1] + b[2] * p[2], d2 = c[0] * p[0] + c[1] * p[1] + c[2] * p[2];
+  float x[3];
+  if (d1 <= 0.f && d2 <= 0.f) { x[0] = 0.f; x[1] = 0.f; x[2] = 0.f; }
+  else {
+    const float bp[3] = {p[0] - b[0], p[1] - b[1], p[2] - b[2]};
+    const float d3 = b[0] * bp[0] + b[1] * bp[1] + b[2] * bp[2], d4 = c[0] * bp[0] + c[1] * bp[1] + c[2] * bp[2];
+    const float vc = d1 * d4 - d3 * d2;
+    const float cp[3] = {p[0] - c[0], p[1] - c[1], p[2] - c[2]};
+    const float d5 = b[0] * cp[0] + b[1] * cp[1] + b[2] * cp[2], d6 = c[0] * cp[0] + c[1] * cp[1] + c[2] * cp[2];
+    const float vb = d5 * d2 - d1 * d6;
+    const float va = d3 * d6 - d5 * d4;
+    if (d3 >= 0.f && d4 <= d3) { x[0] = b[0]; x[1] = b[1]; x[2] = b[2]; }
+    else if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+      const float v = d1 / (d1 - d3);
+      x[0] = v * b[0]; x[1] = v * b[1]; x[2] = v * b[2];
+    } else if (d6 >= 0.f && d5 <= d6) { x[0] = c[0]; x[1] = c[1]; x[2] = c[2]; }
+    else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+      const float w = d2 / (d2 - d6);
+      x[0] = w * c[0]; x[1] = w * c[1]; x[2] = w * c[2];
+    } else if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+      const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+      x[0] = b[0] + w * (c[0] - b[0]); x[1] = b[1] + w * (c[1] - b[1]); x[2] = b[2] + w * (c[2] - b[2]);
+    } else {
+      const float den = 1.f / (va + vb + vc);
+      const float v = vb * den, w = vc * den;
+      x[0] = b[0] * v + c[0] * w; x[1] = b[1] * v + c[1] * w; x[2] = b[2] * v + c[2] * w;
+    }
+  }
+  const float e0 = p[0] - x[0], e1 = p[1] - x[1], e2 = p[2] - x[2];
+  return e0 * e0 + e1 * e1 + e2 * e2;
+}
+
+// Lower bound (FP32, with its margin applied) of the distance from q to face P.
+__device__ __forceinline__ float leaf_lower_bound(const double q[3], const double P[3][3], const float *lbox,
+                                                  const float qf[3]) {
+  float qa[3], ab[3], ac[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    qa[d] = float(q[d] - P[0][d]);
+    ab[d] = float(P[1][d] - P[0][d]);
+    ac[d] = float(P[2][d] - P[0][d]);
+  }
+  const float cx = ab[1] * ac[2] - ab[2] * ac[1], cy = ab[2] * ac[0] - ab[0] * ac[2], cz = ab[0] * ac[1] - ab[1] * ac[0];
+  const float lab = ab[0] * ab[0] + ab[1] * ab[1] + ab[2] * ab[2], lac = ac[0] * ac[0] + ac[1] * ac[1] + ac[2] * ac[2];
+  const float L = fabsf(qa[0]) + fabsf(qa[1]) + fabsf(qa[2]) + sqrtf(lab) + sqrtf(lac);
+  if (cx * cx + cy * cy + cz * cz >= 1e-4f * lab * lac)
+    return sqrtf(tri_d2f(qa, ab, ac)) - 1e-4f * L;
+  return sqrtf(box_d2f(lbox, qf)) - 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
+}
+
+__device__ __forceinline__ const float *node_box(const BvhDev &b, int32_t c) {
+  return b.box + 6 * (int64_t)(c >= 0 ? c : b.n - 1 + ~c);
+}
+
+// Nearest face (squared FP64 distance, face id, closest point).  Returns false on stack overflow.
 __device__ bool bvh_closest(const BvhDev &b, const double q[3], double &best, int32_t &bf, double bc[3]) {
   int32_t stack[kStack];
   int sp = 0;
   bool ok = true;
   const int n = b.n;
+  const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
+  const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
+  float bestd = isinf(best) ? INFINITY : __double2float_ru(sqrt(best));
   stack[sp++] = n == 1 ? ~0 : 0;
   while (sp > 0) {
     const int32_t node = stack[--sp];
@@ -206,23 +283,28 @@ __device__ bool bvh_closest(const BvhDev &b, const double q[3], double &best, in
       const int32_t leaf = ~node;
       if (leaf >= n) { ok = false; continue; }
       const int32_t f = b.leaf_face[leaf];
-      double p[3][3], c[3];
+      double p[3][3];
       face_pts(b, f, p);
+      if (leaf_lower_bound(q, p, node_box(b, node), qf) > bestd) continue;
+      double c[3];
       closest_pt_tri(q, p[0], p[1], p[2], c);
       const double e0 = q[0] - c[0], e1 = q[1] - c[1], e2 = q[2] - c[2];
       const double d2 = e0 * e0 + e1 * e1 + e2 * e2;
-      if (d2 < best) { best = d2; bf = f; bc[0] = c[0]; bc[1] = c[1]; bc[2] = c[2]; }
+      if (d2 < best) {
+        best = d2; bf = f; bc[0] = c[0]; bc[1] = c[1]; bc[2] = c[2];
+        bestd = __double2float_ru(sqrt(best));
+      }
       continue;
     }
     if (node >= n - 1) { ok = false; continue; }
     const int32_t l = b.child[2 * node], r = b.child[2 * node + 1];
     if (l >= n - 1 || r >= n - 1 || ~l >= n || ~r >= n) { ok = false; continue; }
-    const double dl = box_d2(b.box + 6 * (int64_t)(l >= 0 ? l : n - 1 + ~l), q);
-    const double dr = box_d2(b.box + 6 * (int64_t)(r >= 0 ? r : n - 1 + ~r), q);
+    const float dl = sqrtf(box_d2f(node_box(b, l), qf)) - mbox;
+    const float dr = sqrtf(box_d2f(node_box(b, r), qf)) - mbox;
     const int32_t nearc = dl <= dr ? l : r, farc = dl <= dr ? r : l;
-    const double dn = fmin(dl, dr), df = fmax(dl, dr);
-    if (df < best) { if (sp < kStack) stack[sp++] = farc; else ok = false; }
-    if (dn < best) { if (sp < kStack) stack[sp++] = nearc; else ok = false; }
+    const float dn = fminf(dl, dr), df = fmaxf(dl, dr);
+    if (df <= bestd) { if (sp < kStack) stack[sp++] = farc; else ok = false; }
+    if (dn <= bestd) { if (sp < kStack) stack[sp++] = nearc; else ok = false; }
   }
   return ok;
 }
@@ -440,12 +522,17 @@ __device__ void point_distance_ep(const EPFace &f, const double q[3], double &di
   dist = fabs(d);
 }
 
-// min over faces of PointDistanceEP, starting from `dist` (the upper bound)
+// min over faces of PointDistanceEP, starting from `dist` (the upper bound).  PointDistanceEP is
+// never below the true point-triangle distance, so the FP32 lower bound screens faces the same
+// way as in the closest-point search.
 __device__ bool bvh_ep(const BvhDev &b, const double q[3], double &dist) {
   int32_t stack[kStack];
   int sp = 0;
   bool ok = true;
   const int n = b.n;
+  const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
+  const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
+  float bestd = __double2float_ru(dist);
   stack[sp++] = n == 1 ? ~0 : 0;
   while (sp > 0) {
     const int32_t node = stack[--sp];
@@ -453,20 +540,22 @@ __device__ bool bvh_ep(const BvhDev &b, const double q[3], double &dist) {
       if (~node >= n) { ok = false; continue; }
       double P[3][3];
       face_pts(b, b.leaf_face[~node], P);
+      if (leaf_lower_bound(q, P, node_box(b, node), qf) > bestd) continue;
       EPFace f;
       ep_setup(P, f);
       point_distance_ep(f, q, dist);
+      bestd = __double2float_ru(dist);
       continue;
     }
     if (node >= n - 1) { ok = false; continue; }
     const int32_t l = b.child[2 * node], r = b.child[2 * node + 1];
     if (l >= n - 1 || r >= n - 1 || ~l >= n || ~r >= n) { ok = false; continue; }
-    const double dl = sqrt(box_d2(b.box + 6 * (int64_t)(l >= 0 ? l : n - 1 + ~l), q));
-    const double dr = sqrt(box_d2(b.box + 6 * (int64_t)(r >= 0 ? r : n - 1 + ~r), q));
+    const float dl = sqrtf(box_d2f(node_box(b, l), qf)) - mbox;
+    const float dr = sqrtf(box_d2f(node_box(b, r), qf)) - mbox;
     const int32_t nearc = dl <= dr ? l : r, farc = dl <= dr ? r : l;
-    const double dn = fmin(dl, dr), df = fmax(dl, dr);
-    if (df <= dist) { if (sp < kStack) stack[sp++] = farc; else ok = false; }
-    if (dn <= dist) { if (sp < kStack) stack[sp++] = nearc; else ok = false; }
+    const float dn = fminf(dl, dr), df = fmaxf(dl, dr);
+    if (df <= bestd) { if (sp < kStack) stack[sp++] = farc; else ok = false; }
+    if (dn <= bestd) { if (sp < kStack) stack[sp++] = nearc; else ok = false; }
   }
   return ok;
 }

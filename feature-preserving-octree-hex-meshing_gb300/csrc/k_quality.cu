@@ -6,6 +6,7 @@
 // FP64 oracle on the same positions.
 #include "hexopt_common.cuh"
 #include "hexopt_kernels.h"
+#include "hexopt_elem.cuh"
 
 namespace hexopt {
 
@@ -96,6 +97,65 @@ __global__ void __launch_bounds__(128) k_sj_dev(KArgs a, const double *H_Js) {
       a.counters[sg.mesh] = 0;
     }
   }
+}
+
+// In-loop quality check of the mixed mode: corner scaled Jacobians in FP32 from the FP64 edge
+// frame; a corner whose FP32 value is within 1e-4 of zero (its sign, i.e. the inversion flag, is
+// in doubt) or whose edges are near the Precision guard is re-evaluated bit-exactly in FP64.
+// Per mesh: min, sum and inverted count (the deviation pass is not part of the check).
+template <int K>
+__device__ __forceinline__ double corner_sj_fast(const float E12[12][3], const double *X, const uint32_t hv[8]) {
+  float E[3][3];
+  tet_E12<K>(E12, E);
+  const float n1 = sqrtf(E[0][0] * E[0][0] + E[1][0] * E[1][0] + E[2][0] * E[2][0]);
+  const float n2 = sqrtf(E[0][1] * E[0][1] + E[1][1] * E[1][1] + E[2][1] * E[2][1]);
+  const float n3 = sqrtf(E[0][2] * E[0][2] + E[1][2] * E[1][2] + E[2][2] * E[2][2]);
+  const float sj = det3(E) / (n1 * n2 * n3);
+  if (fabsf(sj) < 1e-4f || fminf(n1, fminf(n2, n3)) < 1e-5f || !(fabsf(sj) <= 2.f)) return corner_sj<K>(X, hv);
+  return double(sj);
+}
+
+__global__ void __launch_bounds__(128) k_sj_fast(KArgs a) {
+  const Seg sg = a.hseg[blockIdx.x];
+  const int64_t h = sg.begin + threadIdx.x;
+  const MeshDesc md = a.mesh[sg.mesh];
+  double mn[1] = {1.0}, acc[2] = {0, 0};
+  if (h < sg.end) {
+    uint32_t hv[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) hv[c] = __ldg(a.hexv + hex_idx(h, c));
+    float E12[12][3];
+    hex_edges_pos(a.X, hv, E12);
+    double hm = 1.0;
+    hm = fmin(hm, corner_sj_fast<0>(E12, a.X, hv)); hm = fmin(hm, corner_sj_fast<1>(E12, a.X, hv));
+    hm = fmin(hm, corner_sj_fast<2>(E12, a.X, hv)); hm = fmin(hm, corner_sj_fast<3>(E12, a.X, hv));
+    hm = fmin(hm, corner_sj_fast<4>(E12, a.X, hv)); hm = fmin(hm, corner_sj_fast<5>(E12, a.X, hv));
+    hm = fmin(hm, corner_sj_fast<6>(E12, a.X, hv)); hm = fmin(hm, corner_sj_fast<7>(E12, a.X, hv));
+    mn[0] = hm;
+    acc[0] = hm;
+    acc[1] = hm < 0 ? 1.0 : 0.0;
+  }
+  __shared__ double smem[2][32];
+  block_min<1>(mn, smem);
+  double m0 = mn[0];
+  block_sum<2>(acc, smem);
+  double out[3] = {m0, acc[0], acc[1]};
+  if (publish_partials<3>(out, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
+    double m = gather_partials_min(a.partials, md.hblk0, md.nhblk, 3, 0, smem);
+    double s = gather_partials_sum(a.partials, md.hblk0, md.nhblk, 3, 1, smem);
+    double c = gather_partials_sum(a.partials, md.hblk0, md.nhblk, 3, 2, smem);
+    if (threadIdx.x == 0) {
+      MeshScalars &S = a.sc[sg.mesh];
+      S.sj_min = fmin(m, 1.0);
+      S.sj_sum = s;
+      S.n_inv = (int64_t)c;
+      a.counters[sg.mesh] = 0;
+    }
+  }
+}
+
+void launch_sj_check(const KArgs &a, int64_t hblk, cudaStream_t st) {
+  k_sj_fast<<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
 }
 
 void launch_scaled_jacobian(const KArgs &a, int64_t hblk, double *V_Js, double *H_Js, cudaStream_t st) {

@@ -13,8 +13,10 @@
 //   k_ls_*           flip_avoiding_line_search + igl::line_search      flip_avoiding_line_search.cpp,
 //                                                                       line_search.cpp:10-53
 // Precision: ET = element coefficient / arithmetic type, VT = CG vector type.  FP64 mode uses
-// <double,double>; MIXED uses <float,float> with FP64 positions, FP64 residual, FP64 accumulation
-// of every reduction, and FP64 for the step bound.
+// <double,double>.  MIXED uses <float,float>: edges are formed from FP64 positions in FP64 and
+// rounded once; the PCG solves for the update delta from an initial residual formed per element
+// as M W^T W (R - J) B^T (no cancellation against A x0); positions are updated in FP64; every
+// reduction accumulates in FP64; the step bound's root solve is FP64.
 #include "hexopt_common.cuh"
 #include "hexopt_kernels.h"
 #include "hexopt_elem.cuh"
@@ -22,6 +24,8 @@
 namespace hexopt {
 
 // ------------------------------------------------------------------------------- precompute
+// slim_precompute alone (hexopt_slim_precompute): per-tet 1/cbrt(6 vol) of cube-target tets,
+// rest-edge inverse of own-shape tets, from the FP64 positions.
 template <typename ET>
 __global__ void __launch_bounds__(128) k_precompute(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
@@ -36,15 +40,13 @@ __global__ void __launch_bounds__(128) k_precompute(KArgs a) {
   {                                                                                            \
     double E[3][3];                                                                            \
     tet_edges<K>(a.X, hv, E);                                                                  \
+    const double d = det3(E);                                                                  \
+    degenerate |= (d == 0.0);                                                                  \
     if (gs < 0) {                                                                              \
-      const double d = det3(E);                                                                \
-      degenerate |= (d == 0.0);                                                                \
       Sinv[tet_idx<1>(h, K, 0)] = ET(1.0 / cbrt(d));                                            \
     } else {                                                                                   \
       double A[3][3];                                                                          \
       adj3(E, A);                                                                              \
-      const double d = det3(E);                                                                \
-      degenerate |= (d == 0.0);                                                                \
       double *B = a.Bgen + ((int64_t)gs * 8 + K) * 9;                                          \
       _Pragma("unroll") for (int i = 0; i < 3; i++)                                            \
       _Pragma("unroll") for (int j = 0; j < 3; j++) B[i * 3 + j] = A[i][j] / d;                 \
@@ -57,49 +59,86 @@ __global__ void __launch_bounds__(128) k_precompute(KArgs a) {
 }
 
 // ------------------------------------------------------------------------------- local step
-template <typename ET, int K>
-__device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, const uint32_t hv[8], int32_t gs, ET M,
-                                          ET exp_f, int energy, double F[8][3]) {
-  double E[3][3];
-  tet_edges<K>(a.X, hv, E);
-  const ET *Sinv = reinterpret_cast<const ET *>(a.Sinv);
-  const ET is = Sinv[tet_idx<1>(h, K, 0)];
+// One corner tet of the fused local step: (optional) volume snapshot, J, SVD, SLIM weights, the
+// stored coefficients C' and the tet's contributions to b = A^T M f, to the initial residual
+// r0 = b - A x0 = sum_t M W^T W (R - J) B^T (formed per element, so it carries no cancellation)
+// and to diag(L).
+template <typename ET, int K, bool PRE>
+__device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs, const ET E12[12][3], ET M, ET exp_f,
+                                          int energy, ET Fb[8][3], ET Fr[8][3], ET Dg[8][3], bool &degenerate) {
+  ET E[3][3];
+  tet_E12<K>(E12, E);
+  ET *Sinv = reinterpret_cast<ET *>(a.Sinv);
+  double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
+  ET is;
+  if (PRE) {
+    const ET d = det3(E);
+    degenerate |= (d == ET(0));
+    if (gs < 0) {
+      is = ET(1) / cbrt(d);
+    } else {
+      ET A[3][3];
+      adj3(E, A);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) B[i * 3 + j] = double(A[i][j] / d);
+      is = ET(1);
+    }
+    Sinv[tet_idx<1>(h, K, 0)] = is;
+  } else {
+    is = Sinv[tet_idx<1>(h, K, 0)];
+  }
   ET J[3][3];
-  const double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
-  if (gs < 0) cube_J<K>(E, is, J); else gen_J<K>(E, B, J);
+  apply_B<K>(E, gs, B, is, J);
   ET R[3][3], U[3][3], s[3], Vm[3][3], m[3];
   polar_svd3(J, R, U, s, Vm);
   slim_weights(energy, exp_f, s, U, Vm, m, R);
-  // W = U diag(m) U^T is symmetric, so W^T W = U diag(m^2) U^T.
+  // W = U diag(m) U^T is symmetric, so M W^T W = M U diag(m^2) U^T
   ET c[6];
-  const ET m0 = m[0] * m[0], m1 = m[1] * m[1], m2 = m[2] * m[2];
+  const ET m0 = M * m[0] * m[0], m1 = M * m[1] * m[1], m2 = M * m[2] * m[2];
   c[0] = U[0][0] * U[0][0] * m0 + U[0][1] * U[0][1] * m1 + U[0][2] * U[0][2] * m2;
   c[1] = U[1][0] * U[1][0] * m0 + U[1][1] * U[1][1] * m1 + U[1][2] * U[1][2] * m2;
   c[2] = U[2][0] * U[2][0] * m0 + U[2][1] * U[2][1] * m1 + U[2][2] * U[2][2] * m2;
   c[3] = U[0][0] * U[1][0] * m0 + U[0][1] * U[1][1] * m1 + U[0][2] * U[1][2] * m2;
   c[4] = U[0][0] * U[2][0] * m0 + U[0][1] * U[2][1] * m1 + U[0][2] * U[2][2] * m2;
   c[5] = U[1][0] * U[2][0] * m0 + U[1][1] * U[2][1] * m1 + U[1][2] * U[2][2] * m2;
-  // rhs stress M W^T W R
-  ET Q[3][3];
+  ET Q[3][3], G[3][3];
   sym_mul(c, R, Q);
+  apply_BT<K>(Q, gs, B, is, G);
+  scatter_cols<K>(G, Fb);
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) Q[i][j] *= M;
+    for (int j = 0; j < 3; j++) R[i][j] -= J[i][j];
+  sym_mul(c, R, Q);
+  apply_BT<K>(Q, gs, B, is, G);
+  scatter_cols<K>(G, Fr);
   ET *C = reinterpret_cast<ET *>(a.Ccoef);
+  ET w[4];
   if (gs < 0) {
-    const ET s2 = M * is * is;  // fold M / cbrt(6 vol)^2 into the stored coefficients
+    const ET s2 = is * is;  // fold 1 / cbrt(6 vol)^2 into the stored coefficients
 #pragma unroll
     for (int i = 0; i < 6; i++) C[tet_idx<6>(h, K, i)] = c[i] * s2;
-    cube_scatter<K>(Q, is, F);
+    w[0] = ET(3) * s2; w[1] = w[2] = w[3] = s2;  // |g_j|^2 of the cube-corner gradient rows
   } else {
 #pragma unroll
-    for (int i = 0; i < 6; i++) C[tet_idx<6>(h, K, i)] = c[i] * M;
-    gen_scatter<K>(Q, B, F);
+    for (int i = 0; i < 6; i++) C[tet_idx<6>(h, K, i)] = c[i];
+#pragma unroll
+    for (int j = 0; j < 3; j++) w[j + 1] = ET(B[j * 3] * B[j * 3] + B[j * 3 + 1] * B[j * 3 + 1] + B[j * 3 + 2] * B[j * 3 + 2]);
+    ET g0[3];
+#pragma unroll
+    for (int r = 0; r < 3; r++) g0[r] = ET(B[r] + B[3 + r] + B[6 + r]);
+    w[0] = g0[0] * g0[0] + g0[1] * g0[1] + g0[2] * g0[2];
+  }
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int cc = tet_v(K, j);
+    Dg[cc][0] += w[j] * c[0]; Dg[cc][1] += w[j] * c[1]; Dg[cc][2] += w[j] * c[2];
   }
 }
 
-template <typename ET>
+template <typename ET, bool PRE>
 __global__ void __launch_bounds__(128) k_local(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
   const int64_t h = sg.begin + threadIdx.x;
@@ -109,100 +148,81 @@ __global__ void __launch_bounds__(128) k_local(KArgs a) {
   uint32_t hv[8];
   load_hex(a.hexv, h, hv);
   const int32_t gs = a.gslot[h];
-  double F[8][3];
+  ET E12[12][3];
+  hex_edges_pos(a.X, hv, E12);
+  ET Fb[8][3], Fr[8][3], Dg[8][3];
 #pragma unroll
-  for (int c = 0; c < 8; c++) F[c][0] = F[c][1] = F[c][2] = 0;
-  local_tet<ET, 0>(a, h, hv, gs, M, exp_f, a.energy, F);
-  local_tet<ET, 1>(a, h, hv, gs, M, exp_f, a.energy, F);
-  local_tet<ET, 2>(a, h, hv, gs, M, exp_f, a.energy, F);
-  local_tet<ET, 3>(a, h, hv, gs, M, exp_f, a.energy, F);
-  local_tet<ET, 4>(a, h, hv, gs, M, exp_f, a.energy, F);
-  local_tet<ET, 5>(a, h, hv, gs, M, exp_f, a.energy, F);
-  local_tet<ET, 6>(a, h, hv, gs, M, exp_f, a.energy, F);
-  local_tet<ET, 7>(a, h, hv, gs, M, exp_f, a.energy, F);
+  for (int c = 0; c < 8; c++)
 #pragma unroll
-  for (int c = 0; c < 8; c++) atomic_add3(a.b, hv[c], F[c][0], F[c][1], F[c][2]);
+    for (int r = 0; r < 3; r++) Fb[c][r] = Fr[c][r] = Dg[c][r] = ET(0);
+  bool degenerate = false;
+  local_tet<ET, 0, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
+  local_tet<ET, 1, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
+  local_tet<ET, 2, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
+  local_tet<ET, 3, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
+  local_tet<ET, 4, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
+  local_tet<ET, 5, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
+  local_tet<ET, 6, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
+  local_tet<ET, 7, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
+  ET *b = reinterpret_cast<ET *>(a.b), *r = reinterpret_cast<ET *>(a.r), *dg = reinterpret_cast<ET *>(a.diag);
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    atomic_add3(b, hv[c], Fb[c][0], Fb[c][1], Fb[c][2]);
+    atomic_add3(r, hv[c], Fr[c][0], Fr[c][1], Fr[c][2]);
+    atomic_add3(dg, hv[c], Dg[c][0], Dg[c][1], Dg[c][2]);
+  }
+  if (PRE && degenerate) atomicOr(&a.sc[sg.mesh].status, 2);
 }
 
 // ------------------------------------------------------------------------------- SpMV
-// out += K in for all element terms.  FROM_POS: `in` is the FP64 position array (initial
-// residual); DIAG: also accumulate diag(K) into a.diag.
-template <typename ET, typename OT, int K, bool FROM_POS, bool DIAG>
-__device__ __forceinline__ void spmv_tet(const KArgs &a, const void *in, int64_t h, const uint32_t hv[8], int32_t gs,
-                                         OT F[8][3], double Dg[8][3]) {
-  ET J[3][3];
+// q += K p over the element terms: J' = E(p) B', Q = C' J', forces G = Q B'^T (the cube scale
+// is folded into C').
+template <typename ET, int K>
+__device__ __forceinline__ void spmv_tet(const KArgs &a, int64_t h, int32_t gs, const ET E12[12][3], ET F[8][3]) {
+  ET E[3][3], J[3][3], Q[3][3], G[3][3];
+  tet_E12<K>(E12, E);
   const double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
-  if (FROM_POS) {
-    double E[3][3];
-    tet_edges<K>(reinterpret_cast<const double *>(in), hv, E);
-    if (gs < 0) cube_J<K>(E, ET(1), J); else gen_J<K>(E, B, J);
-  } else {
-    ET E[3][3];
-    tet_edges_vec<K>(reinterpret_cast<const ET *>(in), hv, E);
-    if (gs < 0) cube_J<K>(E, ET(1), J); else gen_J<K>(E, B, J);
-  }
+  apply_B<K>(E, gs, B, ET(1), J);
   const ET *C = reinterpret_cast<const ET *>(a.Ccoef);
   ET c[6];
 #pragma unroll
   for (int i = 0; i < 6; i++) c[i] = C[tet_idx<6>(h, K, i)];
-  ET Q[3][3];
   sym_mul(c, J, Q);
-  if (gs < 0) cube_scatter<K>(Q, ET(1), F); else gen_scatter<K>(Q, B, F);
-  if (DIAG) {
-    // diag(K_t) at corner j, coordinate b: C[b][b] * |g_j|^2
-    double w[4];
-    if (gs < 0) {
-      w[0] = 3; w[1] = w[2] = w[3] = 1;
-    } else {
-#pragma unroll
-      for (int j = 0; j < 3; j++) w[j + 1] = B[j * 3] * B[j * 3] + B[j * 3 + 1] * B[j * 3 + 1] + B[j * 3 + 2] * B[j * 3 + 2];
-      double g0[3];
-#pragma unroll
-      for (int r = 0; r < 3; r++) g0[r] = B[r] + B[3 + r] + B[6 + r];
-      w[0] = g0[0] * g0[0] + g0[1] * g0[1] + g0[2] * g0[2];
-    }
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const int cc = tet_v(K, j);
-      Dg[cc][0] += w[j] * double(c[0]); Dg[cc][1] += w[j] * double(c[1]); Dg[cc][2] += w[j] * double(c[2]);
-    }
-  }
+  apply_BT<K>(Q, gs, B, ET(1), G);
+  scatter_cols<K>(G, F);
 }
 
-template <typename ET, typename OT, bool FROM_POS, bool DIAG>
-__global__ void __launch_bounds__(128) k_spmv(KArgs a, const void *in, OT *out) {
+template <typename ET>
+__global__ void __launch_bounds__(128) k_spmv(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
-  if (!FROM_POS && a.sc[sg.mesh].cg_done) return;
+  if (a.sc[sg.mesh].cg_done) return;
   const int64_t h = sg.begin + threadIdx.x;
   if (h >= sg.end) return;
   uint32_t hv[8];
   load_hex(a.hexv, h, hv);
   const int32_t gs = a.gslot[h];
-  OT F[8][3];
-  double Dg[DIAG ? 8 : 1][3];
+  ET E12[12][3];
+  hex_edges_vec(reinterpret_cast<const ET *>(a.p), hv, E12);
+  ET F[8][3];
 #pragma unroll
-  for (int c = 0; c < 8; c++) F[c][0] = F[c][1] = F[c][2] = 0;
-  if (DIAG)
+  for (int c = 0; c < 8; c++) F[c][0] = F[c][1] = F[c][2] = ET(0);
+  spmv_tet<ET, 0>(a, h, gs, E12, F);
+  spmv_tet<ET, 1>(a, h, gs, E12, F);
+  spmv_tet<ET, 2>(a, h, gs, E12, F);
+  spmv_tet<ET, 3>(a, h, gs, E12, F);
+  spmv_tet<ET, 4>(a, h, gs, E12, F);
+  spmv_tet<ET, 5>(a, h, gs, E12, F);
+  spmv_tet<ET, 6>(a, h, gs, E12, F);
+  spmv_tet<ET, 7>(a, h, gs, E12, F);
+  ET *q = reinterpret_cast<ET *>(a.q);
 #pragma unroll
-    for (int c = 0; c < (DIAG ? 8 : 1); c++) Dg[c][0] = Dg[c][1] = Dg[c][2] = 0;
-  spmv_tet<ET, OT, 0, FROM_POS, DIAG>(a, in, h, hv, gs, F, (double(*)[3])Dg);
-  spmv_tet<ET, OT, 1, FROM_POS, DIAG>(a, in, h, hv, gs, F, (double(*)[3])Dg);
-  spmv_tet<ET, OT, 2, FROM_POS, DIAG>(a, in, h, hv, gs, F, (double(*)[3])Dg);
-  spmv_tet<ET, OT, 3, FROM_POS, DIAG>(a, in, h, hv, gs, F, (double(*)[3])Dg);
-  spmv_tet<ET, OT, 4, FROM_POS, DIAG>(a, in, h, hv, gs, F, (double(*)[3])Dg);
-  spmv_tet<ET, OT, 5, FROM_POS, DIAG>(a, in, h, hv, gs, F, (double(*)[3])Dg);
-  spmv_tet<ET, OT, 6, FROM_POS, DIAG>(a, in, h, hv, gs, F, (double(*)[3])Dg);
-  spmv_tet<ET, OT, 7, FROM_POS, DIAG>(a, in, h, hv, gs, F, (double(*)[3])Dg);
-#pragma unroll
-  for (int c = 0; c < 8; c++) atomic_add3(out, hv[c], F[c][0], F[c][1], F[c][2]);
-  if (DIAG)
-#pragma unroll
-    for (int c = 0; c < (DIAG ? 8 : 1); c++) atomic_add3(a.diag, hv[c], Dg[c][0], Dg[c][1], Dg[c][2]);
+  for (int c = 0; c < 8; c++) atomic_add3(q, hv[c], F[c][0], F[c][1], F[c][2]);
 }
 
 // ------------------------------------------------------------------------------- soft terms
 // Constraint items of a mesh: [0, nc) corners, [nc, nc+nt) tangent planes, [nc+nt, +nl) lines.
-// mode 0: rhs and diagonal (add_soft_constraints)
+// add_soft_constraints (slim_m.cpp:647-711): rhs, diagonal and the residual at x0 (curve
+// unknowns start at 0).
 template <typename VT>
 __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
   const Seg sg = a.cseg[blockIdx.x];
@@ -210,13 +230,17 @@ __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
   if (i >= sg.end) return;
   const MeshDesc md = a.mesh[sg.mesh];
   const MeshScalars &S = a.sc[sg.mesh];
-  int64_t li = i - md.c_off - md.t_off - md.l_off;  // items of a mesh start at c_off+t_off+l_off
+  VT *b = reinterpret_cast<VT *>(a.b), *r = reinterpret_cast<VT *>(a.r), *dg = reinterpret_cast<VT *>(a.diag);
+  int64_t li = i - md.c_off - md.t_off - md.l_off;
   if (li < md.nc) {
     const int64_t e = md.c_off + li;
     const uint32_t v = (uint32_t)(md.v_off + a.c_ids[e]);
     const double lc = S.lamda_C;
-    atomic_add3(a.b, v, lc * a.c_pos[3 * e], lc * a.c_pos[3 * e + 1], lc * a.c_pos[3 * e + 2]);
-    atomic_add3(a.diag, v, lc, lc, lc);
+    const double *x = a.X + 4 * (int64_t)v;
+    const double c0 = a.c_pos[3 * e], c1 = a.c_pos[3 * e + 1], c2 = a.c_pos[3 * e + 2];
+    atomic_add3(b, v, VT(lc * c0), VT(lc * c1), VT(lc * c2));
+    atomic_add3(r, v, VT(lc * (c0 - x[0])), VT(lc * (c1 - x[1])), VT(lc * (c2 - x[2])));
+    atomic_add3(dg, v, VT(lc), VT(lc), VT(lc));
     return;
   }
   li -= md.nc;
@@ -225,8 +249,11 @@ __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
     const uint32_t v = (uint32_t)(md.v_off + a.t_ids[e]);
     const double lt = S.lamda_T;
     const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2], d = a.t_dis[e];
-    atomic_add3(a.b, v, lt * n0 * d, lt * n1 * d, lt * n2 * d);
-    atomic_add3(a.diag, v, lt * n0 * n0, lt * n1 * n1, lt * n2 * n2);
+    const double *x = a.X + 4 * (int64_t)v;
+    const double res = lt * (d - (n0 * x[0] + n1 * x[1] + n2 * x[2]));
+    atomic_add3(b, v, VT(lt * n0 * d), VT(lt * n1 * d), VT(lt * n2 * d));
+    atomic_add3(r, v, VT(res * n0), VT(res * n1), VT(res * n2));
+    atomic_add3(dg, v, VT(lt * n0 * n0), VT(lt * n1 * n1), VT(lt * n2 * n2));
     return;
   }
   li -= md.nt;
@@ -236,28 +263,34 @@ __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
     const double ll = S.lamda_L;
     const double x0 = a.l_axis[3 * e], x1 = a.l_axis[3 * e + 1], x2 = a.l_axis[3 * e + 2];
     const double o0 = a.l_orig[3 * e], o1 = a.l_orig[3 * e + 1], o2 = a.l_orig[3 * e + 2];
-    atomic_add3(a.b, v, ll * o0, ll * o1, ll * o2);
-    atomic_add3(a.diag, v, ll, ll, ll);
-    a.ba[e] = ll * (-x0 * o0 - x1 * o1 - x2 * o2);
-    a.diaga[e] = ll * (x0 * x0 + x1 * x1 + x2 * x2);
+    const double *x = a.X + 4 * (int64_t)v;
+    atomic_add3(b, v, VT(ll * o0), VT(ll * o1), VT(ll * o2));
+    atomic_add3(r, v, VT(ll * (o0 - x[0])), VT(ll * (o1 - x[1])), VT(ll * (o2 - x[2])));
+    atomic_add3(dg, v, VT(ll), VT(ll), VT(ll));
+    VT *ba = reinterpret_cast<VT *>(a.ba), *ra = reinterpret_cast<VT *>(a.ra), *dga = reinterpret_cast<VT *>(a.diaga);
+    ba[e] = VT(ll * (-x0 * o0 - x1 * o1 - x2 * o2));
+    ra[e] = VT(ll * (x0 * (x[0] - o0) + x1 * (x[1] - o1) + x2 * (x[2] - o2)));
+    dga[e] = VT(ll * (x0 * x0 + x1 * x1 + x2 * x2));
   }
 }
 
-// out += S in  for the soft-constraint block of L (FP64 accumulation when OT = double).
-template <typename IT, typename OT, bool FROM_POS>
-__global__ void __launch_bounds__(256) k_soft_mv(KArgs a, const IT *in, const IT *in_a, OT *out, OT *out_a) {
+// q += S p for the soft-constraint block of L
+template <typename VT>
+__global__ void __launch_bounds__(256) k_soft_mv(KArgs a) {
   const Seg sg = a.cseg[blockIdx.x];
-  if (!FROM_POS && a.sc[sg.mesh].cg_done) return;
+  if (a.sc[sg.mesh].cg_done) return;
   const int64_t i = sg.begin + threadIdx.x;
   if (i >= sg.end) return;
   const MeshDesc md = a.mesh[sg.mesh];
   const MeshScalars &S = a.sc[sg.mesh];
+  const VT *in = reinterpret_cast<const VT *>(a.p), *in_a = reinterpret_cast<const VT *>(a.pa);
+  VT *out = reinterpret_cast<VT *>(a.q), *out_a = reinterpret_cast<VT *>(a.qa);
   int64_t li = i - md.c_off - md.t_off - md.l_off;
   if (li < md.nc) {
     const uint32_t v = (uint32_t)(md.v_off + a.c_ids[md.c_off + li]);
-    const double lc = S.lamda_C;
-    const IT *p = in + 4 * (int64_t)v;
-    atomic_add3(out, v, OT(lc * p[0]), OT(lc * p[1]), OT(lc * p[2]));
+    const VT lc = VT(S.lamda_C);
+    const VT *p = in + 4 * (int64_t)v;
+    atomic_add3(out, v, lc * p[0], lc * p[1], lc * p[2]);
     return;
   }
   li -= md.nc;
@@ -265,9 +298,9 @@ __global__ void __launch_bounds__(256) k_soft_mv(KArgs a, const IT *in, const IT
     const int64_t e = md.t_off + li;
     const uint32_t v = (uint32_t)(md.v_off + a.t_ids[e]);
     const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2];
-    const IT *p = in + 4 * (int64_t)v;
+    const VT *p = in + 4 * (int64_t)v;
     const double s = S.lamda_T * (n0 * double(p[0]) + n1 * double(p[1]) + n2 * double(p[2]));
-    atomic_add3(out, v, OT(s * n0), OT(s * n1), OT(s * n2));
+    atomic_add3(out, v, VT(s * n0), VT(s * n1), VT(s * n2));
     return;
   }
   li -= md.nt;
@@ -276,11 +309,11 @@ __global__ void __launch_bounds__(256) k_soft_mv(KArgs a, const IT *in, const IT
     const uint32_t v = (uint32_t)(md.v_off + a.l_ids[e]);
     const double ll = S.lamda_L;
     const double x0 = a.l_axis[3 * e], x1 = a.l_axis[3 * e + 1], x2 = a.l_axis[3 * e + 2];
-    const IT *p = in + 4 * (int64_t)v;
-    const double pa = FROM_POS ? 0.0 : double(in_a[e]);  // curve unknowns start at 0
-    atomic_add3(out, v, OT(ll * (double(p[0]) - x0 * pa)), OT(ll * (double(p[1]) - x1 * pa)),
-                OT(ll * (double(p[2]) - x2 * pa)));
-    out_a[e] += OT(ll * (-(x0 * double(p[0]) + x1 * double(p[1]) + x2 * double(p[2])) + (x0 * x0 + x1 * x1 + x2 * x2) * pa));
+    const VT *p = in + 4 * (int64_t)v;
+    const double pa = double(in_a[e]);
+    atomic_add3(out, v, VT(ll * (double(p[0]) - x0 * pa)), VT(ll * (double(p[1]) - x1 * pa)),
+                VT(ll * (double(p[2]) - x2 * pa)));
+    out_a[e] += VT(ll * (-(x0 * double(p[0]) + x1 * double(p[1]) + x2 * double(p[2])) + (x0 * x0 + x1 * x1 + x2 * x2) * pa));
   }
 }
 
@@ -291,59 +324,75 @@ struct ItemRef {
   int64_t idx;  // global vertex id or global curve entry
 };
 __device__ __forceinline__ ItemRef item_ref(const MeshDesc &md, int64_t i) {
-  // vertex-kind item ids: v_off + l_off + local, so each mesh's block covers nv + nl items
   const int64_t li = i - md.v_off - md.l_off;
   if (li < md.nv) return {false, md.v_off + li};
   return {true, md.l_off + (li - md.nv)};
 }
 
-// r = b - A x0 (the element and soft parts were accumulated into q64), p = invd r, delta = 0
+template <typename T> struct V3 { T x, y, z; };
+__device__ __forceinline__ V3<float> ld3(const float *Y, int64_t v) {
+  const float4 t = *reinterpret_cast<const float4 *>(Y + 4 * v);
+  return {t.x, t.y, t.z};
+}
+__device__ __forceinline__ V3<double> ld3(const double *Y, int64_t v) {
+  const double2 t = *reinterpret_cast<const double2 *>(Y + 4 * v);
+  return {t.x, t.y, Y[4 * v + 2]};
+}
+__device__ __forceinline__ void st3(float *Y, int64_t v, V3<float> a) {
+  *reinterpret_cast<float4 *>(Y + 4 * v) = make_float4(a.x, a.y, a.z, 0.f);
+}
+__device__ __forceinline__ void st3(double *Y, int64_t v, V3<double> a) {
+  *reinterpret_cast<double2 *>(Y + 4 * v) = make_double2(a.x, a.y);
+  Y[4 * v + 2] = a.z;
+  Y[4 * v + 3] = 0.0;
+}
+
+// r0 is already formed (local step + soft terms): p = invd r0, delta = 0, q = prox p, norms.
 template <typename VT>
-__global__ void __launch_bounds__(256) k_cg_start(KArgs a, const double *q64, const double *q64a) {
+__global__ void __launch_bounds__(256) k_cg_start(KArgs a) {
   const Seg sg = a.vseg[blockIdx.x];
-  const int64_t i = sg.begin + threadIdx.x;
   const MeshDesc md = a.mesh[sg.mesh];
   MeshScalars &S = a.sc[sg.mesh];
   const double prox = S.prox;
-  double acc[3] = {0, 0, 0};  // rhs_norm2, rn2, r.p
+  double acc[3] = {0, 0, 0};  // |b|^2, |r|^2, r.p
   VT *r = reinterpret_cast<VT *>(a.r), *p = reinterpret_cast<VT *>(a.p), *d = reinterpret_cast<VT *>(a.d);
   VT *q = reinterpret_cast<VT *>(a.q), *invd = reinterpret_cast<VT *>(a.invd);
-  VT *ra = reinterpret_cast<VT *>(a.ra), *pa = reinterpret_cast<VT *>(a.pa), *da = reinterpret_cast<VT *>(a.da);
-  VT *qa = reinterpret_cast<VT *>(a.qa), *invda = reinterpret_cast<VT *>(a.invda);
-  if (i < sg.end) {
+  const VT *b = reinterpret_cast<const VT *>(a.b), *dg = reinterpret_cast<const VT *>(a.diag);
+  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
     const ItemRef it = item_ref(md, i);
     if (!it.curve) {
-      const int64_t o = 4 * it.idx;
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const double x0 = a.X[o + c];
-        const double bb = a.b[o + c];             // A^T M f + soft rhs (no proximal part)
-        const double bfull = bb + prox * x0;      // rhs of the reference system
-        const double rr = bb - q64[o + c];         // b - A x0 (proximal parts cancel)
-        const double id = 1.0 / (a.diag[o + c] + prox);
-        const double pp = id * rr;
-        r[o + c] = VT(rr); p[o + c] = VT(pp); d[o + c] = VT(0); invd[o + c] = VT(id);
-        q[o + c] = VT(prox * pp);                  // q = prox p: first SpMV accumulates on top
-        acc[0] += bfull * bfull; acc[1] += rr * rr; acc[2] += rr * pp;
-      }
+      const int64_t v = it.idx;
+      const V3<VT> bb = ld3(b, v), rr = ld3(r, v), gg = ld3(dg, v);
+      const double x0 = a.X[4 * v], x1 = a.X[4 * v + 1], x2 = a.X[4 * v + 2];
+      const double b0 = double(bb.x) + prox * x0, b1 = double(bb.y) + prox * x1, b2 = double(bb.z) + prox * x2;
+      const double i0 = 1.0 / (double(gg.x) + prox), i1 = 1.0 / (double(gg.y) + prox), i2 = 1.0 / (double(gg.z) + prox);
+      const double p0 = i0 * double(rr.x), p1 = i1 * double(rr.y), p2 = i2 * double(rr.z);
+      st3(p, v, V3<VT>{VT(p0), VT(p1), VT(p2)});
+      st3(d, v, V3<VT>{VT(0), VT(0), VT(0)});
+      st3(invd, v, V3<VT>{VT(i0), VT(i1), VT(i2)});
+      st3(q, v, V3<VT>{VT(prox * p0), VT(prox * p1), VT(prox * p2)});
+      acc[0] += b0 * b0 + b1 * b1 + b2 * b2;
+      acc[1] += double(rr.x) * double(rr.x) + double(rr.y) * double(rr.y) + double(rr.z) * double(rr.z);
+      acc[2] += double(rr.x) * p0 + double(rr.y) * p1 + double(rr.z) * p2;
     } else {
       const int64_t e = it.idx;
-      const double bb = a.ba[e];
-      const double rr = bb - q64a[e];
-      const double dg = a.diaga[e];
-      const double id = dg != 0.0 ? 1.0 / dg : 0.0;  // DiagonalPreconditioner: 0 if no diagonal
+      VT *ra = reinterpret_cast<VT *>(a.ra), *pa = reinterpret_cast<VT *>(a.pa), *da = reinterpret_cast<VT *>(a.da);
+      VT *qa = reinterpret_cast<VT *>(a.qa), *invda = reinterpret_cast<VT *>(a.invda);
+      const double bb = double(reinterpret_cast<const VT *>(a.ba)[e]);
+      const double rr = double(ra[e]);
+      const double g = double(reinterpret_cast<const VT *>(a.diaga)[e]);
+      const double id = g != 0.0 ? 1.0 / g : 0.0;  // DiagonalPreconditioner: 0 without a diagonal
       const double pp = id * rr;
-      ra[e] = VT(rr); pa[e] = VT(pp); da[e] = VT(0); invda[e] = VT(id); qa[e] = VT(0);
+      pa[e] = VT(pp); da[e] = VT(0); invda[e] = VT(id); qa[e] = VT(0);
       acc[0] += bb * bb; acc[1] += rr * rr; acc[2] += rr * pp;
     }
   }
   __shared__ double smem[3][32];
   block_sum<3>(acc, smem);
-  const MeshDesc &mdr = md;
-  if (publish_partials<3>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, mdr.nvblk)) {
-    double v0 = gather_partials_sum(a.partials, mdr.vblk0, mdr.nvblk, 3, 0, smem);
-    double v1 = gather_partials_sum(a.partials, mdr.vblk0, mdr.nvblk, 3, 1, smem);
-    double v2 = gather_partials_sum(a.partials, mdr.vblk0, mdr.nvblk, 3, 2, smem);
+  if (publish_partials<3>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
+    double v0 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 3, 0, smem);
+    double v1 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 3, 1, smem);
+    double v2 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 3, 2, smem);
     if (threadIdx.x == 0) {
       S.rhs_norm2 = v0;
       S.threshold = a.cg_tol * a.cg_tol * v0;
@@ -353,6 +402,7 @@ __global__ void __launch_bounds__(256) k_cg_start(KArgs a, const double *q64, co
       S.cg_done = 0;
       if (v0 == 0.0) { S.cg_done = 1; S.cg_error = 0; }
       else if (v1 < S.threshold) { S.cg_done = 1; S.cg_error = sqrt(v1 / v0); }
+      else if (a.cg_max_iter <= 0) { S.cg_done = 1; S.cg_error = sqrt(v1 / v0); }
       a.counters[sg.mesh] = 0;
     }
   }
@@ -364,18 +414,17 @@ __global__ void __launch_bounds__(256) k_cg_alpha(KArgs a) {
   const Seg sg = a.vseg[blockIdx.x];
   MeshScalars &S = a.sc[sg.mesh];
   if (S.cg_done) return;
-  const int64_t i = sg.begin + threadIdx.x;
   const MeshDesc md = a.mesh[sg.mesh];
   const VT *p = reinterpret_cast<const VT *>(a.p), *q = reinterpret_cast<const VT *>(a.q);
-  const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
   double acc[1] = {0};
-  if (i < sg.end) {
+  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
     const ItemRef it = item_ref(md, i);
     if (!it.curve) {
-      const int64_t o = 4 * it.idx;
-      acc[0] = double(p[o]) * double(q[o]) + double(p[o + 1]) * double(q[o + 1]) + double(p[o + 2]) * double(q[o + 2]);
+      const V3<VT> pp = ld3(p, it.idx), qq = ld3(q, it.idx);
+      acc[0] += double(pp.x) * double(qq.x) + double(pp.y) * double(qq.y) + double(pp.z) * double(qq.z);
     } else {
-      acc[0] = double(pa[it.idx]) * double(qa[it.idx]);
+      const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
+      acc[0] += double(pa[it.idx]) * double(qa[it.idx]);
     }
   }
   __shared__ double smem[1][32];
@@ -396,29 +445,28 @@ __global__ void __launch_bounds__(256) k_cg_update(KArgs a) {
   const Seg sg = a.vseg[blockIdx.x];
   MeshScalars &S = a.sc[sg.mesh];
   if (S.cg_done) return;
-  const int64_t i = sg.begin + threadIdx.x;
   const MeshDesc md = a.mesh[sg.mesh];
   const VT alpha = VT(S.alpha);
-  VT *r = reinterpret_cast<VT *>(a.r), *d = reinterpret_cast<VT *>(a.d);
-  const VT *p = reinterpret_cast<const VT *>(a.p), *q = reinterpret_cast<const VT *>(a.q);
-  const VT *invd = reinterpret_cast<const VT *>(a.invd);
-  VT *ra = reinterpret_cast<VT *>(a.ra), *da = reinterpret_cast<VT *>(a.da);
-  const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
-  const VT *invda = reinterpret_cast<const VT *>(a.invda);
   double acc[2] = {0, 0};
-  if (i < sg.end) {
+  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
     const ItemRef it = item_ref(md, i);
     if (!it.curve) {
-      const int64_t o = 4 * it.idx;
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        d[o + c] += alpha * p[o + c];
-        const VT rr = r[o + c] - alpha * q[o + c];
-        r[o + c] = rr;
-        acc[0] += double(rr) * double(rr);
-        acc[1] += double(rr) * double(invd[o + c] * rr);
-      }
+      VT *r = reinterpret_cast<VT *>(a.r), *d = reinterpret_cast<VT *>(a.d);
+      const VT *p = reinterpret_cast<const VT *>(a.p), *q = reinterpret_cast<const VT *>(a.q);
+      const VT *invd = reinterpret_cast<const VT *>(a.invd);
+      const int64_t v = it.idx;
+      const V3<VT> pp = ld3(p, v), qq = ld3(q, v), id = ld3(invd, v);
+      V3<VT> dd = ld3(d, v), rr = ld3(r, v);
+      dd.x += alpha * pp.x; dd.y += alpha * pp.y; dd.z += alpha * pp.z;
+      rr.x -= alpha * qq.x; rr.y -= alpha * qq.y; rr.z -= alpha * qq.z;
+      st3(d, v, dd);
+      st3(r, v, rr);
+      acc[0] += double(rr.x) * double(rr.x) + double(rr.y) * double(rr.y) + double(rr.z) * double(rr.z);
+      acc[1] += double(rr.x) * double(id.x * rr.x) + double(rr.y) * double(id.y * rr.y) + double(rr.z) * double(id.z * rr.z);
     } else {
+      VT *ra = reinterpret_cast<VT *>(a.ra), *da = reinterpret_cast<VT *>(a.da);
+      const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
+      const VT *invda = reinterpret_cast<const VT *>(a.invda);
       const int64_t e = it.idx;
       da[e] += alpha * pa[e];
       const VT rr = ra[e] - alpha * qa[e];
@@ -454,27 +502,28 @@ __global__ void __launch_bounds__(256) k_cg_dir(KArgs a) {
   const Seg sg = a.vseg[blockIdx.x];
   const MeshScalars &S = a.sc[sg.mesh];
   if (S.cg_done) return;
-  const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
   const MeshDesc md = a.mesh[sg.mesh];
   const VT beta = VT(S.beta), prox = VT(S.prox);
-  const VT *r = reinterpret_cast<const VT *>(a.r), *invd = reinterpret_cast<const VT *>(a.invd);
-  VT *p = reinterpret_cast<VT *>(a.p), *q = reinterpret_cast<VT *>(a.q);
+  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
   const ItemRef it = item_ref(md, i);
   if (!it.curve) {
-    const int64_t o = 4 * it.idx;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const VT pp = invd[o + c] * r[o + c] + beta * p[o + c];
-      p[o + c] = pp;
-      q[o + c] = prox * pp;
-    }
+    const VT *r = reinterpret_cast<const VT *>(a.r), *invd = reinterpret_cast<const VT *>(a.invd);
+    VT *p = reinterpret_cast<VT *>(a.p), *q = reinterpret_cast<VT *>(a.q);
+    const int64_t v = it.idx;
+    const V3<VT> rr = ld3(r, v), id = ld3(invd, v);
+    V3<VT> pp = ld3(p, v);
+    pp.x = id.x * rr.x + beta * pp.x;
+    pp.y = id.y * rr.y + beta * pp.y;
+    pp.z = id.z * rr.z + beta * pp.z;
+    st3(p, v, pp);
+    st3(q, v, V3<VT>{prox * pp.x, prox * pp.y, prox * pp.z});
   } else {
     const VT *ra = reinterpret_cast<const VT *>(a.ra), *invda = reinterpret_cast<const VT *>(a.invda);
     VT *pa = reinterpret_cast<VT *>(a.pa), *qa = reinterpret_cast<VT *>(a.qa);
     const int64_t e = it.idx;
     pa[e] = invda[e] * ra[e] + beta * pa[e];
     qa[e] = VT(0);
+  }
   }
 }
 
@@ -569,33 +618,6 @@ __device__ double min_pos_root(const double E[3][3], const double D[3][3]) {
   return INFINITY;
 }
 
-// Energy density of corner tet K at positions X + alpha d.  The edges are formed in FP64 and the
-// density evaluated in ET; tets with |det J| below a threshold are re-evaluated in FP64.
-template <typename ET, typename VT, int K>
-__device__ __forceinline__ double tet_energy_at(const KArgs &a, int64_t h, const uint32_t hv[8], int32_t gs,
-                                                const double E0[3][3], const double Dd[3][3], double alpha) {
-  const ET *Sinv = reinterpret_cast<const ET *>(a.Sinv);
-  double E[3][3];
-#pragma unroll
-  for (int r = 0; r < 3; r++)
-#pragma unroll
-    for (int c = 0; c < 3; c++) E[r][c] = E0[r][c] + alpha * Dd[r][c];
-  const double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
-  ET J[3][3];
-  const ET is = Sinv[tet_idx<1>(h, K, 0)];
-  if (gs < 0) cube_J<K>(E, is, J); else gen_J<K>(E, B, J);
-  ET e = tet_energy_density<ET>(a.energy, ET(a.sc_exp_f), J);
-  if (sizeof(ET) == 4) {
-    const ET d = det3(J);
-    if (!(fabs(d) > ET(1e-3))) {  // near-degenerate: FP64 re-evaluation
-      double Jd[3][3];
-      if (gs < 0) cube_J<K>(E, double(is), Jd); else gen_J<K>(E, B, Jd);
-      return tet_energy_density<double>(a.energy, a.sc_exp_f, Jd);
-    }
-  }
-  return double(e);
-}
-
 template <typename VT, int K>
 __device__ __forceinline__ void tet_dir(const VT *d, const uint32_t hv[8], double Dd[3][3]) {
   VT p0[3];
@@ -610,7 +632,85 @@ __device__ __forceinline__ void tet_dir(const VT *d, const uint32_t hv[8], doubl
   }
 }
 
-// Pass 1: min positive root over tets (step bound) and the quality energy at the current X.
+// Energy density of corner tet K at edges E (ET); tets with |det J| below 1e-3 are re-evaluated
+// in FP64 from the FP64 positions (mixed mode only).
+template <typename ET, typename VT, int K>
+__device__ __forceinline__ double tet_energy_e(const KArgs &a, int64_t h, const uint32_t hv[8], int32_t gs,
+                                               const ET E[3][3], double alpha) {
+  const ET *Sinv = reinterpret_cast<const ET *>(a.Sinv);
+  const double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
+  const ET is = Sinv[tet_idx<1>(h, K, 0)];
+  ET J[3][3];
+  apply_B<K>(E, gs, B, is, J);
+  const ET e = tet_energy_density<ET>(a.energy, ET(a.sc_exp_f), J);
+  if (sizeof(ET) == 4) {
+    const ET d = det3(J);
+    if (!(fabs(d) > ET(1e-3))) {
+      double E0[3][3], Dd[3][3], Ed[3][3], Jd[3][3];
+      tet_edges<K>(a.X, hv, E0);
+      tet_dir<VT, K>(reinterpret_cast<const VT *>(a.d), hv, Dd);
+#pragma unroll
+      for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) Ed[r][c] = E0[r][c] + alpha * Dd[r][c];
+      apply_B<K>(Ed, gs, B, double(is), Jd);
+      return tet_energy_density<double>(a.energy, a.sc_exp_f, Jd);
+    }
+  }
+  return double(e);
+}
+
+// Flip-avoiding step bound of corner tet K.  Only a root of det(E + t D) in [0, 1.25] can lower
+// max_step = min(1, 0.8 min_root).  The cubic's coefficients are formed in ET and converted to the
+// Bernstein basis on [0, 1.25]; when all four Bernstein coefficients keep the sign of det E with a
+// margin that covers the ET rounding (bounded through Hadamard's inequality), there is no root in
+// the interval and the tet is skipped.  Otherwise the smallest positive root is solved in FP64
+// exactly as the reference does.
+template <typename ET, typename VT, int K>
+__device__ __forceinline__ void tet_bound(const KArgs &a, const uint32_t hv[8], const ET E[3][3], const ET D[3][3],
+                                          double &mn) {
+  ET ne[3], nd[3];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    ne[j] = sqrt(E[0][j] * E[0][j] + E[1][j] * E[1][j] + E[2][j] * E[2][j]);
+    nd[j] = sqrt(D[0][j] * D[0][j] + D[1][j] * D[1][j] + D[2][j] * D[2][j]);
+  }
+  const ET T = ET(1.25);
+  const ET M0 = ne[0] * ne[1] * ne[2];
+  const ET M1 = nd[0] * ne[1] * ne[2] + ne[0] * nd[1] * ne[2] + ne[0] * ne[1] * nd[2];
+  const ET M2 = nd[0] * nd[1] * ne[2] + nd[0] * ne[1] * nd[2] + ne[0] * nd[1] * nd[2];
+  const ET M3 = nd[0] * nd[1] * nd[2];
+  // det(E + tD) = c0 + c1 t + c2 t^2 + c3 t^3
+  ET Mx[3][3];
+  const ET c0 = det3(E), c3 = det3(D);
+  ET c1 = 0, c2 = 0;
+#pragma unroll
+  for (int col = 0; col < 3; col++) {
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+      for (int cc = 0; cc < 3; cc++) Mx[r][cc] = (cc == col) ? D[r][cc] : E[r][cc];
+    c1 += det3(Mx);
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+      for (int cc = 0; cc < 3; cc++) Mx[r][cc] = (cc == col) ? E[r][cc] : D[r][cc];
+    c2 += det3(Mx);
+  }
+  const ET a1 = c1 * T, a2 = c2 * T * T, a3 = c3 * T * T * T;
+  const ET b0 = c0, b1 = c0 + a1 / ET(3), b2 = c0 + ET(2) * a1 / ET(3) + a2 / ET(3), b3 = c0 + a1 + a2 + a3;
+  const ET rel = sizeof(ET) == 4 ? ET(2e-5) : ET(1e-13);
+  const ET err = rel * (M0 + M1 * T + M2 * T * T + M3 * T * T * T);
+  const bool pos = b0 > err && b1 > err && b2 > err && b3 > err;
+  const bool neg = b0 < -err && b1 < -err && b2 < -err && b3 < -err;
+  if (pos || neg) return;
+  double E64[3][3], D64[3][3];
+  tet_edges<K>(a.X, hv, E64);
+  tet_dir<VT, K>(reinterpret_cast<const VT *>(a.d), hv, D64);
+  mn = fmin(mn, min_pos_root(E64, D64));
+}
+
+// Pass 1: step bound over the tets and the quality energy at the current X.
 template <typename ET, typename VT>
 __global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
@@ -622,15 +722,24 @@ __global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
     uint32_t hv[8];
     load_hex(a.hexv, h, hv);
     const int32_t gs = a.gslot[h];
-    const VT *d = reinterpret_cast<const VT *>(a.d);
+    ET E12[12][3], D12[12][3];
+    hex_edges_pos(a.X, hv, E12);
+    {
+      VT Dv[12][3];
+      hex_edges_vec(reinterpret_cast<const VT *>(a.d), hv, Dv);
+#pragma unroll
+      for (int e = 0; e < 12; e++)
+#pragma unroll
+        for (int r = 0; r < 3; r++) D12[e][r] = ET(Dv[e][r]);
+    }
     double esum = 0;
-#define HX_LS(K)                                                   \
-    {                                                              \
-      double E[3][3], Dd[3][3];                                    \
-      tet_edges<K>(a.X, hv, E);                                    \
-      tet_dir<VT, K>(d, hv, Dd);                                   \
-      mn[0] = fmin(mn[0], min_pos_root(E, Dd));                    \
-      esum += tet_energy_at<ET, VT, K>(a, h, hv, gs, E, Dd, 0.0);  \
+#define HX_LS(K)                                                  \
+    {                                                             \
+      ET E[3][3], D[3][3];                                        \
+      tet_E12<K>(E12, E);                                         \
+      tet_E12<K>(D12, D);                                         \
+      tet_bound<ET, VT, K>(a, hv, E, D, mn[0]);                   \
+      esum += tet_energy_e<ET, VT, K>(a, h, hv, gs, E, 0.0);      \
     }
     HX_LS(0) HX_LS(1) HX_LS(2) HX_LS(3) HX_LS(4) HX_LS(5) HX_LS(6) HX_LS(7)
 #undef HX_LS
@@ -659,13 +768,12 @@ __device__ __forceinline__ double cand_alpha(const MeshScalars &S, int j) {
   return j > kHalvings - 1 ? 0.0 : ldexp(S.max_step, -j);
 }
 
-// Quality energy at the candidates j = round*nc .. round*nc + nc - 1.
-template <typename ET, typename VT>
+// Quality energy at the NC candidates j = round*NC .. round*NC + NC - 1 (E = E0 + alpha D).
+template <typename ET, typename VT, int NC>
 __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round) {
   const Seg sg = a.hseg[blockIdx.x];
   MeshScalars &S = a.sc[sg.mesh];
   if (S.ls_done) return;
-  const int nc = a.ls_cand;
   const int64_t h = sg.begin + threadIdx.x;
   const MeshDesc md = a.mesh[sg.mesh];
   double acc[kMaxCand];
@@ -675,27 +783,45 @@ __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round) {
     uint32_t hv[8];
     load_hex(a.hexv, h, hv);
     const int32_t gs = a.gslot[h];
-    const VT *d = reinterpret_cast<const VT *>(a.d);
-#define HX_LE(K)                                                            \
-    {                                                                       \
-      double E[3][3], Dd[3][3];                                             \
-      tet_edges<K>(a.X, hv, E);                                             \
-      tet_dir<VT, K>(d, hv, Dd);                                            \
-      for (int j = 0; j < nc; j++) {                                        \
-        const double al = cand_alpha(S, round * nc + j);                    \
-        acc[j] += tet_energy_at<ET, VT, K>(a, h, hv, gs, E, Dd, al);        \
-      }                                                                     \
+    ET E12[12][3], D12[12][3];
+    hex_edges_pos(a.X, hv, E12);
+    {
+      VT Dv[12][3];
+      hex_edges_vec(reinterpret_cast<const VT *>(a.d), hv, Dv);
+#pragma unroll
+      for (int e = 0; e < 12; e++)
+#pragma unroll
+        for (int r = 0; r < 3; r++) D12[e][r] = ET(Dv[e][r]);
+    }
+    double al[NC];
+#pragma unroll
+    for (int j = 0; j < NC; j++) al[j] = cand_alpha(S, round * NC + j);
+#define HX_LE(K)                                                             \
+    {                                                                        \
+      ET E0[3][3], D[3][3];                                                  \
+      tet_E12<K>(E12, E0);                                                   \
+      tet_E12<K>(D12, D);                                                    \
+      _Pragma("unroll") for (int j = 0; j < NC; j++) {                       \
+        ET E[3][3];                                                          \
+        const ET aj = ET(al[j]);                                             \
+        _Pragma("unroll") for (int r = 0; r < 3; r++)                        \
+        _Pragma("unroll") for (int c = 0; c < 3; c++) E[r][c] = E0[r][c] + aj * D[r][c]; \
+        acc[j] += tet_energy_e<ET, VT, K>(a, h, hv, gs, E, al[j]);           \
+      }                                                                      \
     }
     HX_LE(0) HX_LE(1) HX_LE(2) HX_LE(3) HX_LE(4) HX_LE(5) HX_LE(6) HX_LE(7)
 #undef HX_LE
 #pragma unroll
-    for (int j = 0; j < kMaxCand; j++) acc[j] *= S.M;
+    for (int j = 0; j < NC; j++) acc[j] *= S.M;
   }
-  __shared__ double smem[kMaxCand][32];
-  block_sum<kMaxCand>(acc, smem);
-  if (publish_partials<kMaxCand>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
-    for (int j = 0; j < nc; j++) {
-      double e = gather_partials_sum(a.partials, md.hblk0, md.nhblk, kMaxCand, j, smem);
+  __shared__ double smem[NC][32];
+  double acc2[NC];
+#pragma unroll
+  for (int j = 0; j < NC; j++) acc2[j] = acc[j];
+  block_sum<NC>(acc2, smem);
+  if (publish_partials<NC>(acc2, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
+    for (int j = 0; j < NC; j++) {
+      double e = gather_partials_sum(a.partials, md.hblk0, md.nhblk, NC, j, smem);
       if (threadIdx.x == 0) S.cand_eq[j] = e;
     }
     if (threadIdx.x == 0) a.counters[sg.mesh] = 0;
@@ -703,7 +829,8 @@ __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round) {
 }
 
 // Soft energy at the current X (round < 0) or at the candidates of `round`; its last block
-// takes the line-search decision for the round (accept the first finite E <= E_old).
+// takes the line-search decision for the round (accept the first finite E <= E_old,
+// line_search.cpp:26-47).
 template <typename VT>
 __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
   const Seg sg = a.cseg[blockIdx.x];
@@ -728,7 +855,9 @@ __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
     const int64_t v = md.v_off + lv;
     const double x0 = a.X[4 * v], x1 = a.X[4 * v + 1], x2 = a.X[4 * v + 2];
     const double d0 = double(d[4 * v]), d1 = double(d[4 * v + 1]), d2 = double(d[4 * v + 2]);
-    for (int j = 0; j < nc; j++) {
+#pragma unroll
+    for (int j = 0; j < kMaxCand; j++) {
+      if (j >= nc) break;
       const double al = round < 0 ? 0.0 : cand_alpha(S, round * nc + j);
       const double y0 = x0 + al * d0, y1 = x1 + al * d1, y2 = x2 + al * d2;
       double en;
@@ -773,7 +902,7 @@ __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
             break;
           }
         }
-        if (!S.ls_done && (round + 1) * nc > kHalvings) {  // unreachable: step 0 is always accepted
+        if (!S.ls_done && (round + 1) * nc > kHalvings) {  // only NaN/Inf energies, even at step 0
           S.ls_done = 1; S.step = 0; S.energy = S.old_e; S.eq = S.old_eq; S.es = S.old_es;
           S.halvings = kHalvings; S.status |= 1;
         }
@@ -787,10 +916,9 @@ __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
 template <typename VT>
 __global__ void __launch_bounds__(256) k_ls_apply(KArgs a) {
   const Seg sg = a.vseg[blockIdx.x];
-  const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
   const MeshDesc md = a.mesh[sg.mesh];
   const MeshScalars &S = a.sc[sg.mesh];
+  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
   const ItemRef it = item_ref(md, i);
   if (!it.curve) {
     const VT *d = reinterpret_cast<const VT *>(a.d);
@@ -802,77 +930,85 @@ __global__ void __launch_bounds__(256) k_ls_apply(KArgs a) {
     const VT *da = reinterpret_cast<const VT *>(a.da);
     a.aL[it.idx] = double(da[it.idx]);
   }
+  }
+}
+
+// One candidate-energy pass alone (timing): the pass of round 0.
+template <typename ET, typename VT>
+void launch_ls_energy_pass(const KArgs &a, int64_t hblk, cudaStream_t st) {
+  switch (a.ls_cand) {
+    case 1: k_ls_energy<ET, VT, 1><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
+    case 2: k_ls_energy<ET, VT, 2><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
+    case 3: k_ls_energy<ET, VT, 3><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
+    case 4: k_ls_energy<ET, VT, 4><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
+    case 5: k_ls_energy<ET, VT, 5><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
+    case 6: k_ls_energy<ET, VT, 6><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
+    case 7: k_ls_energy<ET, VT, 7><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
+    default: k_ls_energy<ET, VT, 8><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
+  }
 }
 
 // ------------------------------------------------------------------------------- launchers
-#define HX_GRID(n) dim3((unsigned)(n))
-
 template <typename ET, typename VT>
 void launch_precompute(const KArgs &a, int64_t nblk, cudaStream_t st) {
-  k_precompute<ET><<<HX_GRID(nblk), a.hthreads, 0, st>>>(a);
+  k_precompute<ET><<<(unsigned)nblk, a.hthreads, 0, st>>>(a);
 }
 template <typename ET, typename VT>
-void launch_local(const KArgs &a, int64_t nblk, cudaStream_t st) {
-  k_local<ET><<<HX_GRID(nblk), a.hthreads, 0, st>>>(a);
-}
-template <typename ET, typename VT>
-void launch_residual_elems(const KArgs &a, int64_t nblk, double *q64, cudaStream_t st) {
-  k_spmv<ET, double, true, true><<<HX_GRID(nblk), a.hthreads, 0, st>>>(a, a.X, q64);
+void launch_local(const KArgs &a, int64_t nblk, bool pre, cudaStream_t st) {
+  if (pre) k_local<ET, true><<<(unsigned)nblk, a.hthreads, 0, st>>>(a);
+  else k_local<ET, false><<<(unsigned)nblk, a.hthreads, 0, st>>>(a);
 }
 template <typename ET, typename VT>
 void launch_spmv_elems(const KArgs &a, int64_t nblk, cudaStream_t st) {
-  k_spmv<ET, VT, false, false><<<HX_GRID(nblk), a.hthreads, 0, st>>>(a, a.p, reinterpret_cast<VT *>(a.q));
+  k_spmv<ET><<<(unsigned)nblk, a.hthreads, 0, st>>>(a);
 }
 template <typename VT>
 void launch_soft_rhs(const KArgs &a, int64_t nblk, cudaStream_t st) {
-  k_soft_rhs<VT><<<HX_GRID(nblk), a.vthreads, 0, st>>>(a);
+  k_soft_rhs<VT><<<(unsigned)nblk, a.vthreads, 0, st>>>(a);
 }
 template <typename VT>
-void launch_soft_residual(const KArgs &a, int64_t nblk, double *q64, double *q64a, cudaStream_t st) {
-  k_soft_mv<double, double, true><<<HX_GRID(nblk), a.vthreads, 0, st>>>(a, a.X, nullptr, q64, q64a);
-}
-template <typename VT>
-void launch_soft_spmv(const KArgs &a, int64_t nblk, cudaStream_t st) {
-  k_soft_mv<VT, VT, false><<<HX_GRID(nblk), a.vthreads, 0, st>>>(a, reinterpret_cast<const VT *>(a.p),
-                                                          reinterpret_cast<const VT *>(a.pa),
-                                                          reinterpret_cast<VT *>(a.q), reinterpret_cast<VT *>(a.qa));
-}
-template <typename VT>
-void launch_cg_start(const KArgs &a, int64_t nblk, const double *q64, const double *q64a, cudaStream_t st) {
-  k_cg_start<VT><<<HX_GRID(nblk), a.vthreads, 0, st>>>(a, q64, q64a);
+void launch_cg_start(const KArgs &a, int64_t nblk, cudaStream_t st) {
+  k_cg_start<VT><<<(unsigned)nblk, a.vthreads, 0, st>>>(a);
 }
 template <typename VT>
 void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st) {
-  launch_spmv_elems<VT, VT>(a, hblk, st);
-  launch_soft_spmv<VT>(a, cblk, st);
-  k_cg_alpha<VT><<<HX_GRID(vblk), a.vthreads, 0, st>>>(a);
-  k_cg_update<VT><<<HX_GRID(vblk), a.vthreads, 0, st>>>(a);
-  k_cg_dir<VT><<<HX_GRID(vblk), a.vthreads, 0, st>>>(a);
+  k_spmv<VT><<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
+  k_soft_mv<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a);
+  k_cg_alpha<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+  k_cg_update<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+  k_cg_dir<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
 }
 template <typename ET, typename VT>
 void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st) {
-  k_ls_bound<ET, VT><<<HX_GRID(hblk), a.hthreads, 0, st>>>(a);
-  k_ls_soft<VT><<<HX_GRID(cblk), a.vthreads, 0, st>>>(a, -1);
+  k_ls_bound<ET, VT><<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
+  k_ls_soft<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a, -1);
   const int rounds = (kHalvings + 1 + a.ls_cand - 1) / a.ls_cand;
   for (int r = 0; r < rounds; r++) {
-    k_ls_energy<ET, VT><<<HX_GRID(hblk), a.hthreads, 0, st>>>(a, r);
-    k_ls_soft<VT><<<HX_GRID(cblk), a.vthreads, 0, st>>>(a, r);
+    switch (a.ls_cand) {
+      case 1: k_ls_energy<ET, VT, 1><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
+      case 2: k_ls_energy<ET, VT, 2><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
+      case 3: k_ls_energy<ET, VT, 3><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
+      case 4: k_ls_energy<ET, VT, 4><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
+      case 5: k_ls_energy<ET, VT, 5><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
+      case 6: k_ls_energy<ET, VT, 6><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
+      case 7: k_ls_energy<ET, VT, 7><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
+      default: k_ls_energy<ET, VT, 8><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
+    }
+    k_ls_soft<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a, r);
   }
-  k_ls_apply<VT><<<HX_GRID(vblk), a.vthreads, 0, st>>>(a);
+  k_ls_apply<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
 }
 
 // explicit instantiations for the two modes
 #define HX_INST(ET, VT)                                                                          \
   template void launch_precompute<ET, VT>(const KArgs &, int64_t, cudaStream_t);                 \
-  template void launch_local<ET, VT>(const KArgs &, int64_t, cudaStream_t);                      \
-  template void launch_residual_elems<ET, VT>(const KArgs &, int64_t, double *, cudaStream_t);   \
+  template void launch_local<ET, VT>(const KArgs &, int64_t, bool, cudaStream_t);                \
   template void launch_spmv_elems<ET, VT>(const KArgs &, int64_t, cudaStream_t);                 \
   template void launch_soft_rhs<VT>(const KArgs &, int64_t, cudaStream_t);                       \
-  template void launch_soft_residual<VT>(const KArgs &, int64_t, double *, double *, cudaStream_t); \
-  template void launch_soft_spmv<VT>(const KArgs &, int64_t, cudaStream_t);                      \
-  template void launch_cg_start<VT>(const KArgs &, int64_t, const double *, const double *, cudaStream_t); \
+  template void launch_cg_start<VT>(const KArgs &, int64_t, cudaStream_t);                       \
   template void launch_cg_iter<VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t);      \
-  template void launch_line_search<ET, VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t);
+  template void launch_line_search<ET, VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t); \
+  template void launch_ls_energy_pass<ET, VT>(const KArgs &, int64_t, cudaStream_t);
 HX_INST(double, double)
 HX_INST(float, float)
 #undef HX_INST

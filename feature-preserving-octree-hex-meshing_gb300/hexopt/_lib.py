@@ -95,6 +95,9 @@ SIGNATURES = {
     "hexopt_autotune": (C.c_int, [_vp]),
     "hexopt_get_tuning": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "hexopt_launch_count": (C.c_int64, [_vp]),
+    "hexopt_timer_start": (C.c_int, [_vp]),
+    "hexopt_timer_stop": (C.c_int, [_vp, _d]),
+    "hexopt_time_stage": (C.c_int, [_vp, C.c_int, C.c_int, _d]),
     "hexopt_aabb_merge": (None, [C.POINTER(AABB), C.POINTER(AABB)]),
     "hexopt_aabb_squared_distance": (C.c_double, [C.POINTER(AABB), _d]),
     "hexopt_aabb_ray_intersect": (C.c_int, [C.POINTER(AABB), C.POINTER(Ray), _d, _d]),
@@ -370,6 +373,19 @@ class Context:
 
     def sync(self):
         self._ck(self.L.hexopt_sync(self.h), "sync")
+
+    def timer_start(self):
+        self._ck(self.L.hexopt_timer_start(self.h), "timer_start")
+
+    def timer_stop(self):
+        ms = C.c_double()
+        self._ck(self.L.hexopt_timer_stop(self.h, C.byref(ms)), "timer_stop")
+        return ms.value
+
+    def time_stage(self, stage, reps=20):
+        ms = C.c_double()
+        self._ck(self.L.hexopt_time_stage(self.h, stage, reps, C.byref(ms)), "time_stage")
+        return ms.value
 
     def launch_count(self):
         return int(self.L.hexopt_launch_count(self.h))

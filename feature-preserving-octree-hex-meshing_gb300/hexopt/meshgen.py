@@ -228,6 +228,21 @@ def hex_boundary_quads(H: np.ndarray) -> np.ndarray:
     return Q[cnt[inv.ravel()] == 1]
 
 
+def grid_boundary_quads(nx: int, ny: int | None = None, nz: int | None = None) -> np.ndarray:
+    """Boundary quads of grid_hex(nx, ny, nz) directly from the grid structure (same faces and
+    corner order as hex_boundary_quads, without the global face matching)."""
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    _, H = grid_hex(nx, ny, nz)
+    HF = np.array([[0, 1, 2, 3], [4, 7, 6, 5], [0, 4, 5, 1], [0, 3, 7, 4], [3, 2, 6, 7], [1, 5, 6, 2]])
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    i, j, k = i.ravel(), j.ravel(), k.ravel()
+    out = []
+    for f, sel in ((0, k == 0), (1, k == nz - 1), (2, j == 0), (4, j == ny - 1), (3, i == 0), (5, i == nx - 1)):
+        out.append(H[sel][:, HF[f]].astype(np.int64))
+    return np.concatenate(out)
+
+
 def quads_to_tris(Q: np.ndarray) -> np.ndarray:
     """Split boundary quads into (0,1,2), (2,3,0) (grid_hex_meshing.cpp:4290-4313)."""
     return np.concatenate([Q[:, [0, 1, 2]], Q[:, [2, 3, 0]]]).astype(np.int32)

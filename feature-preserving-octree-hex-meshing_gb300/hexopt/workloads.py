@@ -27,7 +27,7 @@ def grid_superellipsoid(n=128, sigma=0.2, seed=0, n_tri=200_000, exponent=4.0):
     regular = np.nonzero(b)[0].astype(np.int32)
     return dict(name=f"grid{n}_superellipsoid", V=V, H=H, TV=TV, TF=TF, regular=regular,
                 lines=np.zeros(0, np.int32), line_curve=np.zeros(0, np.int32), curves=[], closed=[],
-                corners=np.zeros(0, np.int32), surface=boundary_surface(H))
+                corners=np.zeros(0, np.int32), surface=meshgen.quads_to_tris(meshgen.grid_boundary_quads(n)))
 
 
 def cylinder(n_core=8, n_ring=6, n_z=16):

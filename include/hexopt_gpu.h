@@ -199,6 +199,17 @@ HEXOPT_API int hexopt_energy_bwd(hexopt_ctx *ctx, double *grad);
 HEXOPT_API int hexopt_set_block_size(hexopt_ctx *ctx, int kind, int threads); /* kind 0 hex, 1 vertex */
 HEXOPT_API int hexopt_autotune(hexopt_ctx *ctx);
 HEXOPT_API int hexopt_get_tuning(const hexopt_ctx *ctx, int *hex_block, int *vert_block, int *ls_candidates);
+/* CUDA-event timing on the context's stream: start records an event, stop records a second one,
+ * synchronises and returns the elapsed milliseconds between them. */
+HEXOPT_API int hexopt_timer_start(hexopt_ctx *ctx);
+HEXOPT_API int hexopt_timer_stop(hexopt_ctx *ctx, double *ms);
+/* Average device time of one launch of a stage, timed with CUDA events over `reps` back-to-back
+ * launches on the current state (after slim_precompute / an iteration):
+ *   0 element SpMV of the PCG   1 local step   2 line-search energy pass (ls_candidates steps)
+ *   3 scaled Jacobian           4 feature projection   5 one full SLIM iteration
+ * Stages 0-2 leave the solver scratch in an unspecified state; positions are not modified by
+ * 0-4 (stage 5 advances them like slim_iterate). */
+HEXOPT_API int hexopt_time_stage(hexopt_ctx *ctx, int stage, int reps, double *ms_per_launch);
 /* Kernel launches issued by this context since creation (for the bench's launch count). */
 HEXOPT_API int64_t hexopt_launch_count(const hexopt_ctx *ctx);
 
