@@ -60,7 +60,7 @@ struct KindTable {
 };
 
 struct StaticBvh {  // device LBVH over a fixed triangle set
-  DBuf child, parent, box, leaf_face, tri, counters;
+  DBuf child, parent, box, leaf_face, tri, counters, node, leafd;
   int32_t n = 0;
   BvhDev dev() const {
     BvhDev b{};
@@ -69,6 +69,8 @@ struct StaticBvh {  // device LBVH over a fixed triangle set
     b.box = box.as<float>();
     b.leaf_face = leaf_face.as<int32_t>();
     b.tri = tri.as<double>();
+    b.node = node.as<float4>();
+    b.leafd = leafd.as<float4>();
     return b;
   }
 };
@@ -87,7 +89,7 @@ struct TargetHost {
 struct SurfaceHost {
   bool set = false;
   int64_t nf = 0;
-  DBuf F, child, parent, box, leaf_face, counters;
+  DBuf F, child, parent, box, leaf_face, counters, node, leafd;
   std::vector<int64_t> ref_vs;  // referenced vertices (global ids)
 };
 
@@ -114,6 +116,7 @@ struct hexopt_ctx {
   std::vector<int64_t> nC, nT, nL;
   std::vector<double> lamC, lamT, lamL;
   KindTable kind[8];
+  // items per block: hex 128, unknowns 256 x ipt, constraints 256, queries 128
   int block[8] = {128, 256, 256, 128, 128, 128, 128, 128};  // K_CONS follows K_VERT's size
   int ipt[8] = {1, 4, 1, 1, 1, 1, 1, 1};                     // items per thread of each kind
   // SLIM
@@ -124,6 +127,7 @@ struct hexopt_ctx {
   std::vector<TargetHost> tgt;
   std::vector<SurfaceHost> surf;
   DBuf tgt_d, surf_d, hm_d, tgt_vs_d, surf_vs_d;
+  DBuf ovf_item, ovf_mesh, ovf_count, ovf_best, ovf_face, ovf_pt, hdist;
   std::vector<int64_t> tgt_vs_cnt, surf_vs_cnt;
   bool haus_ready = false;
   // feature alignment
@@ -196,6 +200,8 @@ void build_kind(hexopt_ctx *c, int k, const std::vector<int64_t> &count, const s
   t.nblk = (int64_t)t.segs.size();
 }
 
+int ensure_query_buffers(hexopt_ctx *ctx);
+
 int rebuild_tables(hexopt_ctx *ctx) {
   const int M = ctx->n_meshes;
   ctx->block[K_CONS] = ctx->block[K_VERT];  // constraint launches use the vertex block size
@@ -245,7 +251,7 @@ int rebuild_tables(hexopt_ctx *ctx) {
   }
   CK(ctx->partials.ensure(sizeof(double) * (size_t)(maxblk + 1) * kMaxCand));
   CK(upload(ctx->md_d, ctx->md.data(), ctx->md.size(), ctx->st));
-  return HEXOPT_OK;
+  return ensure_query_buffers(ctx);
 }
 
 KArgs make_args(hexopt_ctx *c) {
@@ -380,6 +386,8 @@ int build_static_bvh(hexopt_ctx *ctx, StaticBvh &B, const std::vector<double> &t
   CK(B.leaf_face.ensure(sizeof(int32_t) * nf));
   CK(B.counters.ensure(sizeof(unsigned) * std::max<int64_t>(nf - 1, 1)));
   CK(cudaMemsetAsync(B.counters.p, 0, sizeof(unsigned) * std::max<int64_t>(nf - 1, 1), ctx->st));
+  CK(B.node.ensure(sizeof(float4) * 4 * std::max<int64_t>(nf - 1, 1)));
+  CK(B.leafd.ensure(sizeof(float4) * 3 * nf));
   DBuf keys, keys2, tmp;
   CK(keys.ensure(sizeof(unsigned long long) * nf));
   CK(keys2.ensure(sizeof(unsigned long long) * nf));
@@ -391,8 +399,9 @@ int build_static_bvh(hexopt_ctx *ctx, StaticBvh &B, const std::vector<double> &t
   CK(cub::DeviceRadixSort::SortKeys(tmp.p, tb, keys.as<unsigned long long>(), keys2.as<unsigned long long>(), (int)nf, 0, 64, ctx->st));
   bvh_karras((int)nf, keys2.as<unsigned long long>(), B.child.as<int32_t>(), B.parent.as<int32_t>(), B.leaf_face.as<int32_t>(), ctx->st);
   bd = B.dev();
-  bvh_refit(bd, B.box.as<float>(), B.parent.as<int32_t>(), B.counters.as<unsigned>(), ctx->st);
-  ctx->launches += 4;
+  bvh_refit(bd, B.box.as<float>(), B.parent.as<int32_t>(), B.counters.as<unsigned>(), B.node.as<float4>(),
+            B.leafd.as<float4>(), ctx->st);
+  ctx->launches += 5;
   CKL();
   CK(cudaStreamSynchronize(ctx->st));
   return HEXOPT_OK;
@@ -428,6 +437,8 @@ int upload_targets_table(hexopt_ctx *ctx) {
       b.leaf_face = s.leaf_face.as<int32_t>();
       b.F = s.F.as<int32_t>();
       b.X = ctx->X.as<double>();
+      b.node = s.node.as<float4>();
+      b.leafd = s.leafd.as<float4>();
     }
     sd[m] = b;
   }
@@ -436,8 +447,37 @@ int upload_targets_table(hexopt_ctx *ctx) {
   return HEXOPT_OK;
 }
 
+int ensure_query_buffers(hexopt_ctx *ctx) {
+  int64_t n = 1;
+  for (int k : {K_PROJ, K_TGTV, K_SURFV}) {
+    int64_t tot = 0;
+    for (int m = 0; m < ctx->n_meshes; m++) tot += ctx->md[m].kcount[k];
+    n = std::max(n, tot);
+  }
+  CK(ctx->ovf_item.ensure(sizeof(int64_t) * n));
+  CK(ctx->ovf_mesh.ensure(sizeof(int32_t) * n));
+  CK(ctx->ovf_count.ensure(sizeof(unsigned)));
+  CK(ctx->ovf_best.ensure(sizeof(double) * n));
+  CK(ctx->ovf_face.ensure(sizeof(int32_t) * n));
+  CK(ctx->ovf_pt.ensure(sizeof(double) * 3 * n));
+  CK(ctx->hdist.ensure(sizeof(double) * n));
+  return HEXOPT_OK;
+}
+
+Overflow make_ovf(hexopt_ctx *c) {
+  Overflow o{};
+  o.item = c->ovf_item.as<int64_t>();
+  o.mesh = c->ovf_mesh.as<int32_t>();
+  o.count = c->ovf_count.as<unsigned>();
+  o.best = c->ovf_best.as<double>();
+  o.face = c->ovf_face.as<int32_t>();
+  o.pt = c->ovf_pt.as<double>();
+  return o;
+}
+
 ProjArgs make_proj(hexopt_ctx *c, int kind) {
   ProjArgs p{};
+  p.ovf = make_ovf(c);
   p.seg = c->kind[kind].dev.as<Seg>();
   p.mesh = c->md_d.as<MeshDesc>();
   p.sc = c->sc_d.as<MeshScalars>();
@@ -451,6 +491,8 @@ ProjArgs make_proj(hexopt_ctx *c, int kind) {
 
 HausArgs make_haus(hexopt_ctx *c, int kind) {
   HausArgs h{};
+  h.ovf = make_ovf(c);
+  h.dist = c->hdist.as<double>();
   h.seg = c->kind[kind].dev.as<Seg>();
   h.mesh = c->md_d.as<MeshDesc>();
   h.sc = c->sc_d.as<MeshScalars>();
@@ -468,7 +510,7 @@ HausArgs make_haus(hexopt_ctx *c, int kind) {
 int run_projection(hexopt_ctx *ctx) {
   if (ctx->NT) {
     launch_project(make_proj(ctx, K_PROJ), ctx->kind[K_PROJ].nblk, ctx->st);
-    ctx->launches++;
+    ctx->launches += 2;
   }
   if (ctx->NL) {
     launch_curve_project(make_proj(ctx, K_LINE), ctx->kind[K_LINE].nblk, ctx->st);
@@ -489,13 +531,16 @@ int run_hausdorff(hexopt_ctx *ctx) {
     b.leaf_face = s.leaf_face.as<int32_t>();
     b.F = s.F.as<int32_t>();
     b.X = ctx->X.as<double>();
-    bvh_refit(b, s.box.as<float>(), s.parent.as<int32_t>(), s.counters.as<unsigned>(), ctx->st);
-    ctx->launches++;
+    b.node = s.node.as<float4>();
+    b.leafd = s.leafd.as<float4>();
+    bvh_refit(b, s.box.as<float>(), s.parent.as<int32_t>(), s.counters.as<unsigned>(), s.node.as<float4>(),
+              s.leafd.as<float4>(), ctx->st);
+    ctx->launches += 2;
   }
   launch_haus_bbox(make_haus(ctx, K_SURFV), ctx->kind[K_SURFV].nblk, ctx->st);
   launch_haus_side(make_haus(ctx, K_TGTV), 0, ctx->kind[K_TGTV].nblk, ctx->st);
   launch_haus_side(make_haus(ctx, K_SURFV), 1, ctx->kind[K_SURFV].nblk, ctx->st);
-  ctx->launches += 3;
+  ctx->launches += 7;
   CKL();
   return HEXOPT_OK;
 }
@@ -1054,6 +1099,8 @@ int hexopt_set_surface(hexopt_ctx *ctx, int mesh, int64_t nf, const int32_t *F) 
   std::swap(s.box.p, tmp.box.p); std::swap(s.box.bytes, tmp.box.bytes);
   std::swap(s.leaf_face.p, tmp.leaf_face.p); std::swap(s.leaf_face.bytes, tmp.leaf_face.bytes);
   std::swap(s.counters.p, tmp.counters.p); std::swap(s.counters.bytes, tmp.counters.bytes);
+  std::swap(s.node.p, tmp.node.p); std::swap(s.node.bytes, tmp.node.bytes);
+  std::swap(s.leafd.p, tmp.leafd.p); std::swap(s.leafd.bytes, tmp.leafd.bytes);
   s.set = true;
   std::vector<int64_t> all;
   for (int m = 0; m < ctx->n_meshes; m++) {
@@ -1386,7 +1433,7 @@ int hexopt_autotune(hexopt_ctx *ctx) {
   const std::vector<MeshScalars> sc0 = ctx->sc;
   const int hb[2] = {64, 128}, vb[2] = {128, 256};
   // candidate counts whose energy-pass variants run without register spills in each mode
-  const int lc[3] = {ctx->mixed ? 2 : 1, ctx->mixed ? 4 : 2, ctx->mixed ? 5 : 2};
+  const int lc[3] = {1, 2, ctx->mixed ? 4 : 2};
   float best = INFINITY;
   int bh = ctx->block[K_HEX], bv = ctx->block[K_VERT], bl = ctx->params.ls_candidates;
   cudaEvent_t e0, e1;

@@ -19,6 +19,22 @@ struct BvhDev {
   const double *tri;
   const int32_t *F;
   const double *X;
+  // packed internal nodes, 64 B each: both children's boxes and ids in one record
+  // (lo/hi of the left box, lo/hi of the right box, left id, right id)
+  const float4 *node;
+  // per leaf (sorted order), 48 B: first vertex and the two edges from it in FP32 -- the
+  // screening data of the leaf's triangle
+  const float4 *leafd;
+};
+
+// Queries that exceed the per-thread traversal budget are finished by a warp-cooperative pass.
+struct Overflow {
+  int64_t *item;     // query item ids
+  int32_t *mesh;     // their meshes
+  unsigned *count;   // number of entries
+  double *best;      // per query item: best (squared for closest point) distance found so far
+  int32_t *face;     // per query item: face of that best (closest point)
+  double *pt;        // per query item: closest point (3)
 };
 
 // A mesh's target triangle mesh (mf.tri / tri_tree): geometry, per-face normals of
@@ -36,6 +52,7 @@ struct TargetDev {
 };
 
 struct ProjArgs {
+  Overflow ovf;
   const Seg *seg;
   const MeshDesc *mesh;
   MeshScalars *sc;
@@ -55,6 +72,8 @@ struct HausMesh {
 };
 
 struct HausArgs {
+  Overflow ovf;
+  double *dist;             // per sample item of the side being processed
   const Seg *seg;
   const MeshDesc *mesh;
   MeshScalars *sc;
@@ -71,12 +90,16 @@ struct HausArgs {
 void bvh_morton(const BvhDev &b, const double lo[3], const double hi[3], unsigned long long *keys, cudaStream_t st);
 void bvh_karras(int n, const unsigned long long *keys, int32_t *child, int32_t *parent, int32_t *leaf_face,
                 cudaStream_t st);
-void bvh_refit(const BvhDev &b, float *box, const int32_t *parent, unsigned *counters, cudaStream_t st);
+// refit boxes bottom-up and rewrite the packed node records
+void bvh_refit(const BvhDev &b, float *box, const int32_t *parent, unsigned *counters, float4 *node, float4 *leafd,
+               cudaStream_t st);
+// both passes of the tangent-plane projection
 void launch_project(const ProjArgs &p, int64_t nblk, cudaStream_t st);
 void launch_curve_project(const ProjArgs &p, int64_t nblk, cudaStream_t st);
 void launch_signed_distance(const TargetDev &t, int64_t np, const double *P, double *S, int32_t *I, double *C,
                             double *N, int *status, cudaStream_t st);
 void launch_haus_bbox(const HausArgs &h, int64_t nblk, cudaStream_t st);
+// both passes of one Hausdorff side (per-sample distances into h.dist) and its reduction
 void launch_haus_side(const HausArgs &h, int side, int64_t nblk, cudaStream_t st);
 void launch_ep_points(const BvhDev &b, const double *P, const int64_t *ids, int64_t n, double upper, double *dist,
                       int *status, cudaStream_t st);

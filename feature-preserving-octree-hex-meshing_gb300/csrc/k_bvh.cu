@@ -104,13 +104,22 @@ __global__ void k_karras(int n, const unsigned long long *keys, int32_t *child, 
 __device__ __forceinline__ float down(double x) { float f = __double2float_rd(x); return f; }
 __device__ __forceinline__ float up(double x) { float f = __double2float_ru(x); return f; }
 
-// Leaf boxes and bottom-up union.  counters: n - 1 zeros on entry, zeros again on exit.
-__global__ void k_refit(BvhDev b, float *box, const int32_t *parent, unsigned *counters) {
+// Leaf boxes, leaf screening frames and bottom-up union.  counters: n - 1 zeros on entry, zeros
+// again on exit.
+__global__ void k_refit(BvhDev b, float *box, const int32_t *parent, unsigned *counters, float4 *leafd) {
   const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= b.n) return;
   const int n = b.n;
   double p[3][3];
   face_pts(b, b.leaf_face[k], p);
+  {
+    const float ax = float(p[0][0]), ay = float(p[0][1]), az = float(p[0][2]);
+    const float bx = float(p[1][0] - p[0][0]), by = float(p[1][1] - p[0][1]), bz = float(p[1][2] - p[0][2]);
+    const float cx = float(p[2][0] - p[0][0]), cy = float(p[2][1] - p[0][1]), cz = float(p[2][2] - p[0][2]);
+    leafd[3 * (int64_t)k] = make_float4(ax, ay, az, bx);
+    leafd[3 * (int64_t)k + 1] = make_float4(by, bz, cx, cy);
+    leafd[3 * (int64_t)k + 2] = make_float4(cz, 0.f, 0.f, 0.f);
+  }
   float *lb = box + 6 * (int64_t)(n - 1 + k);
 #pragma unroll
   for (int d = 0; d < 3; d++) {
@@ -245,213 +254,25 @@ __device__ __forceinline__ float tri_d2f(const float p[3], const float b[3], con
   return e0 * e0 + e1 * e1 + e2 * e2;
 }
 
-// Lower bound (FP32, with its margin applied) of the distance from q to face P.
-__device__ __forceinline__ float leaf_lower_bound(const double q[3], const double P[3][3], const float *lbox,
-                                                  const float qf[3]) {
-  float qa[3], ab[3], ac[3];
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    qa[d] = float(q[d] - P[0][d]);
-    ab[d] = float(P[1][d] - P[0][d]);
-    ac[d] = float(P[2][d] - P[0][d]);
-  }
+// Lower bound (FP32, margin applied) of the distance from the query to leaf `leaf`'s triangle,
+// from its FP32 screening frame; `boxd` (the leaf box bound) is used for thin triangles.  The
+// margin covers the FP32 evaluation: 1e-4 of the local scale plus the rounding of absolute
+// coordinates (relative 1e-6).
+__device__ __forceinline__ float leaf_lower_bound(const float4 *leafd, int32_t leaf, const float qf[3], float boxd) {
+  const float4 u = __ldg(leafd + 3 * (int64_t)leaf), v = __ldg(leafd + 3 * (int64_t)leaf + 1),
+               w = __ldg(leafd + 3 * (int64_t)leaf + 2);
+  const float qa[3] = {qf[0] - u.x, qf[1] - u.y, qf[2] - u.z};
+  const float ab[3] = {u.w, v.x, v.y}, ac[3] = {v.z, v.w, w.x};
   const float cx = ab[1] * ac[2] - ab[2] * ac[1], cy = ab[2] * ac[0] - ab[0] * ac[2], cz = ab[0] * ac[1] - ab[1] * ac[0];
   const float lab = ab[0] * ab[0] + ab[1] * ab[1] + ab[2] * ab[2], lac = ac[0] * ac[0] + ac[1] * ac[1] + ac[2] * ac[2];
-  const float L = fabsf(qa[0]) + fabsf(qa[1]) + fabsf(qa[2]) + sqrtf(lab) + sqrtf(lac);
-  if (cx * cx + cy * cy + cz * cz >= 1e-4f * lab * lac)
-    return sqrtf(tri_d2f(qa, ab, ac)) - 1e-4f * L;
-  return sqrtf(box_d2f(lbox, qf)) - 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
-}
-
-__device__ __forceinline__ const float *node_box(const BvhDev &b, int32_t c) {
-  return b.box + 6 * (int64_t)(c >= 0 ? c : b.n - 1 + ~c);
-}
-
-// Nearest face (squared FP64 distance, face id, closest point).  Returns false on stack overflow.
-__device__ bool bvh_closest(const BvhDev &b, const double q[3], double &best, int32_t &bf, double bc[3]) {
-  int32_t stack[kStack];
-  int sp = 0;
-  bool ok = true;
-  const int n = b.n;
-  const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
-  const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
-  float bestd = isinf(best) ? INFINITY : __double2float_ru(sqrt(best));
-  stack[sp++] = n == 1 ? ~0 : 0;
-  while (sp > 0) {
-    const int32_t node = stack[--sp];
-    if (node < 0) {
-      const int32_t leaf = ~node;
-      if (leaf >= n) { ok = false; continue; }
-      const int32_t f = b.leaf_face[leaf];
-      double p[3][3];
-      face_pts(b, f, p);
-      if (leaf_lower_bound(q, p, node_box(b, node), qf) > bestd) continue;
-      double c[3];
-      closest_pt_tri(q, p[0], p[1], p[2], c);
-      const double e0 = q[0] - c[0], e1 = q[1] - c[1], e2 = q[2] - c[2];
-      const double d2 = e0 * e0 + e1 * e1 + e2 * e2;
-      if (d2 < best) {
-        best = d2; bf = f; bc[0] = c[0]; bc[1] = c[1]; bc[2] = c[2];
-        bestd = __double2float_ru(sqrt(best));
-      }
-      continue;
-    }
-    if (node >= n - 1) { ok = false; continue; }
-    const int32_t l = b.child[2 * node], r = b.child[2 * node + 1];
-    if (l >= n - 1 || r >= n - 1 || ~l >= n || ~r >= n) { ok = false; continue; }
-    const float dl = sqrtf(box_d2f(node_box(b, l), qf)) - mbox;
-    const float dr = sqrtf(box_d2f(node_box(b, r), qf)) - mbox;
-    const int32_t nearc = dl <= dr ? l : r, farc = dl <= dr ? r : l;
-    const float dn = fminf(dl, dr), df = fmaxf(dl, dr);
-    if (df <= bestd) { if (sp < kStack) stack[sp++] = farc; else ok = false; }
-    if (dn <= bestd) { if (sp < kStack) stack[sp++] = nearc; else ok = false; }
+  if (cx * cx + cy * cy + cz * cz >= 1e-4f * lab * lac) {
+    const float L = fabsf(qa[0]) + fabsf(qa[1]) + fabsf(qa[2]) + sqrtf(lab) + sqrtf(lac);
+    const float abs_scale = 1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]);
+    return sqrtf(tri_d2f(qa, ab, ac)) - 1e-4f * L - 1e-6f * abs_scale;
   }
-  return ok;
+  return boxd;
 }
 
-// pseudonormal_test: normal at the closest point c of face f (vertex / edge / face normal).
-__device__ void pseudonormal(const TargetDev &t, int32_t f, const double c[3], double n[3]) {
-  double A[3], B[3], C[3];
-#pragma unroll
-  for (int d = 0; d < 3; d++) { A[d] = t.tri[(int64_t)f * 9 + d]; B[d] = t.tri[(int64_t)f * 9 + 3 + d]; C[d] = t.tri[(int64_t)f * 9 + 6 + d]; }
-  const double e1[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]}, e2[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
-  const double x0 = e1[1] * e2[2] - e1[2] * e2[1], x1 = e1[2] * e2[0] - e1[0] * e2[2], x2 = e1[0] * e2[1] - e1[1] * e2[0];
-  const double area = sqrt(x0 * x0 + x1 * x1 + x2 * x2);  // doublearea
-  const double epsilon = 1e-12;
-  int kind = 0, which = 0;  // 0 face, 1 vertex (which corner), 2 edge (opposite which corner)
-  if (area > 1e-4) {
-    const double v2[3] = {c[0] - A[0], c[1] - A[1], c[2] - A[2]};
-    const double d00 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2], d01 = e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2];
-    const double d11 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
-    const double d20 = v2[0] * e1[0] + v2[1] * e1[1] + v2[2] * e1[2], d21 = v2[0] * e2[0] + v2[1] * e2[1] + v2[2] * e2[2];
-    const double den = d00 * d11 - d01 * d01;
-    double bb[3];
-    bb[1] = (d11 * d20 - d01 * d21) / den;
-    bb[2] = (d00 * d21 - d01 * d20) / den;
-    bb[0] = 1.0 - (bb[1] + bb[2]);
-    const int type = (bb[0] <= epsilon) + (bb[1] <= epsilon) + (bb[2] <= epsilon);
-    if (type == 2) {
-      kind = 1;
-      which = bb[0] > epsilon ? 0 : (bb[1] > epsilon ? 1 : 2);
-    } else if (type == 1) {
-      kind = 2;
-      which = bb[0] <= epsilon ? 0 : (bb[1] <= epsilon ? 1 : 2);
-    }
-  } else {
-    const double *P[3] = {A, B, C};
-    bool found = false;
-    for (int v = 0; v < 3 && !found; v++) {
-      const double dx = c[0] - P[v][0], dy = c[1] - P[v][1], dz = c[2] - P[v][2];
-      if (sqrt(dx * dx + dy * dy + dz * dz) < epsilon) { found = true; kind = 1; which = v; }
-    }
-    for (int e = 0; e < 3 && !found; e++) {
-      const double *s = P[(e + 1) % 3], *dd = P[(e + 2) % 3];
-      const double dms[3] = {dd[0] - s[0], dd[1] - s[1], dd[2] - s[2]};
-      const double smp[3] = {s[0] - c[0], s[1] - c[1], s[2] - c[2]};
-      const double vl = dms[0] * dms[0] + dms[1] * dms[1] + dms[2] * dms[2];
-      const double tt = -(dms[0] * smp[0] + dms[1] * smp[1] + dms[2] * smp[2]) / vl;
-      double sq;
-      if (tt < 0) {
-        sq = smp[0] * smp[0] + smp[1] * smp[1] + smp[2] * smp[2];
-      } else if (tt > 1) {
-        const double z0 = c[0] - dd[0], z1 = c[1] - dd[1], z2 = c[2] - dd[2];
-        sq = z0 * z0 + z1 * z1 + z2 * z2;
-      } else {
-        const double pr0 = (1.0 - tt) * s[0] + tt * dd[0], pr1 = (1.0 - tt) * s[1] + tt * dd[1], pr2 = (1.0 - tt) * s[2] + tt * dd[2];
-        const double m0 = c[0] - pr0, m1 = c[1] - pr1, m2 = c[2] - pr2;
-        sq = m0 * m0 + m1 * m1 + m2 * m2;
-      }
-      if (sqrt(sq) < epsilon) { found = true; kind = 2; which = e; }
-    }
-  }
-  const double *src = kind == 0 ? t.FN + 3 * (int64_t)f : kind == 1 ? t.VNc + 9 * (int64_t)f + 3 * which : t.ENc + 9 * (int64_t)f + 3 * which;
-  n[0] = src[0]; n[1] = src[1]; n[2] = src[2];
-}
-
-// Tangent planes of the regular boundary vertices (dirty_graph_projection, :4031-4078):
-// normal_T = pseudonormal, dis_T = normal_T . closest point.
-__global__ void __launch_bounds__(128) k_project(ProjArgs p) {
-  const Seg sg = p.seg[blockIdx.x];
-  const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
-  const MeshDesc md = p.mesh[sg.mesh];
-  const TargetDev &t = p.tgt[sg.mesh];
-  const int64_t e = md.t_off + (i - md.kitem0[K_PROJ]);
-  const int64_t v = md.v_off + p.t_ids[e];
-  const double q[3] = {p.X[4 * v], p.X[4 * v + 1], p.X[4 * v + 2]};
-  double best = INFINITY, c[3] = {0, 0, 0}, n[3] = {0, 0, 0};
-  int32_t f = -1;
-  if (t.bvh.n > 0 && !bvh_closest(t.bvh, q, best, f, c)) atomicOr(&p.sc[sg.mesh].status, 8);
-  if (f >= 0) pseudonormal(t, f, c, n);
-  p.t_nrm[3 * e] = n[0]; p.t_nrm[3 * e + 1] = n[1]; p.t_nrm[3 * e + 2] = n[2];
-  p.t_dis[e] = n[0] * c[0] + n[1] * c[1] + n[2] * c[2];
-}
-
-// signed_distance_pseudonormal for arbitrary query points (rows) against mesh m's target
-__global__ void __launch_bounds__(128) k_signed_distance(TargetDev t, int64_t np, const double *P, double *S,
-                                                         int32_t *I, double *C, double *N, int *status) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= np) return;
-  const double q[3] = {P[3 * i], P[3 * i + 1], P[3 * i + 2]};
-  double best = INFINITY, c[3] = {0, 0, 0}, n[3] = {0, 0, 0};
-  int32_t f = -1;
-  if (t.bvh.n > 0 && !bvh_closest(t.bvh, q, best, f, c)) atomicOr(status, 8);
-  double s = 1;
-  if (f >= 0) {
-    pseudonormal(t, f, c, n);
-    s = ((q[0] - c[0]) * n[0] + (q[1] - c[1]) * n[1] + (q[2] - c[2]) * n[2]) >= 0 ? 1. : -1.;
-  }
-  S[i] = s * sqrt(best);
-  I[i] = f;
-  C[3 * i] = c[0]; C[3 * i + 1] = c[1]; C[3 * i + 2] = c[2];
-  N[3 * i] = n[0]; N[3 * i + 1] = n[1]; N[3 * i + 2] = n[2];
-}
-
-// Feature lines (dirty_graph_projection LINE branch, :3963-4025): nearest curve segment by
-// point_line_projection (global_functions.cpp:3454-3465), ties to the lower segment index.
-__global__ void __launch_bounds__(128) k_curve_project(ProjArgs p) {
-  const Seg sg = p.seg[blockIdx.x];
-  const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
-  const MeshDesc md = p.mesh[sg.mesh];
-  const TargetDev &t = p.tgt[sg.mesh];
-  const int64_t e = md.l_off + (i - md.kitem0[K_LINE]);
-  const int64_t v = md.v_off + p.l_ids[e];
-  const double q[3] = {p.X[4 * v], p.X[4 * v + 1], p.X[4 * v + 2]};
-  const int32_t cu = p.l_curve[e];
-  const int64_t c0 = t.curve_ptr[cu], c1 = t.curve_ptr[cu + 1];
-  const int64_t size = c1 - c0;
-  const int64_t len = t.curve_closed[cu] ? size : size - 1;
-  double best = INFINITY, pv[3] = {0, 0, 0}, tg[3] = {1, 0, 0};
-  for (int64_t j = 0; j < len; j++) {
-    const double *a = t.TV + 3 * (int64_t)t.curve_vs[c0 + j];
-    const double *b = t.TV + 3 * (int64_t)t.curve_vs[c0 + (j + 1) % size];
-    const double vv1[3] = {q[0] - a[0], q[1] - a[1], q[2] - a[2]}, v21[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
-    const double n2 = v21[0] * v21[0] + v21[1] * v21[1] + v21[2] * v21[2];
-    const double tt = n2 >= 1.e-7 ? (vv1[0] * v21[0] + vv1[1] * v21[1] + vv1[2] * v21[2]) / n2 : 0.0;
-    double pp[3];
-    if (tt >= 0.0 && tt <= 1.0) { pp[0] = a[0] + tt * v21[0]; pp[1] = a[1] + tt * v21[1]; pp[2] = a[2] + tt * v21[2]; }
-    else if (tt < 0.0) { pp[0] = a[0]; pp[1] = a[1]; pp[2] = a[2]; }
-    else { pp[0] = b[0]; pp[1] = b[1]; pp[2] = b[2]; }
-    const double dx = q[0] - pp[0], dy = q[1] - pp[1], dz = q[2] - pp[2];
-    const double dist = sqrt(dx * dx + dy * dy + dz * dz);
-    if (dist < best) {
-      best = dist;
-      pv[0] = pp[0]; pv[1] = pp[1]; pv[2] = pp[2];
-      const double ln = sqrt(n2);
-      tg[0] = v21[0] / ln; tg[1] = v21[1] / ln; tg[2] = v21[2] / ln;
-    }
-  }
-  if (len <= 0 && size > 0) {  // single-vertex curve: nearest curve vertex
-    const double *a = t.TV + 3 * (int64_t)t.curve_vs[c0];
-    pv[0] = a[0]; pv[1] = a[1]; pv[2] = a[2];
-    tg[0] = 1; tg[1] = 0; tg[2] = 0;
-  }
-  p.l_orig[3 * e] = pv[0]; p.l_orig[3 * e + 1] = pv[1]; p.l_orig[3 * e + 2] = pv[2];
-  p.l_axis[3 * e] = tg[0]; p.l_axis[3 * e + 1] = tg[1]; p.l_axis[3 * e + 2] = tg[2];
-}
-
-// ------------------------------------------------------------------------------- Hausdorff
 struct EPFace {
   double p[3][3], edge[3][3], dir[3], off, darea;
   int axis;
@@ -522,44 +343,391 @@ __device__ void point_distance_ep(const EPFace &f, const double q[3], double &di
   dist = fabs(d);
 }
 
-// min over faces of PointDistanceEP, starting from `dist` (the upper bound).  PointDistanceEP is
-// never below the true point-triangle distance, so the FP32 lower bound screens faces the same
-// way as in the closest-point search.
-__device__ bool bvh_ep(const BvhDev &b, const double q[3], double &dist) {
-  int32_t stack[kStack];
-  int sp = 0;
-  bool ok = true;
+
+// ---- traversal over packed nodes ----
+// Each internal node is one 64-byte record with both children's boxes and ids, so a step is one
+// dependent load.  Stack entries carry the box lower bound they were pushed with, so entries made
+// obsolete by a later improvement are dropped when popped.
+struct NodeRec { float lb[6], rb[6]; int32_t l, r; };
+__device__ __forceinline__ NodeRec load_node(const float4 *node, int32_t i) {
+  const float4 a = __ldg(node + 4 * (int64_t)i), b = __ldg(node + 4 * (int64_t)i + 1), c = __ldg(node + 4 * (int64_t)i + 2),
+               d = __ldg(node + 4 * (int64_t)i + 3);
+  NodeRec r;
+  r.lb[0] = a.x; r.lb[1] = a.y; r.lb[2] = a.z; r.lb[3] = a.w; r.lb[4] = b.x; r.lb[5] = b.y;
+  r.rb[0] = b.z; r.rb[1] = b.w; r.rb[2] = c.x; r.rb[3] = c.y; r.rb[4] = c.z; r.rb[5] = c.w;
+  r.l = __float_as_int(d.x); r.r = __float_as_int(d.y);
+  return r;
+}
+
+// Leaf evaluation shared by both traversals.  MODE 0: closest point (squared distance, strict
+// improvement); MODE 1: PointDistanceEP from the current best as the upper bound.
+template <int MODE>
+__device__ __forceinline__ bool eval_leaf(const BvhDev &b, int32_t leaf, float boxd, const double q[3], const float qf[3],
+                                          float bestd, double best, double &cand, int32_t &cf, double cc[3]) {
+  if (leaf_lower_bound(b.leafd, leaf, qf, boxd) > bestd) return false;
+  const int32_t f = b.leaf_face[leaf];
+  double P[3][3];
+  face_pts(b, f, P);
+  if (MODE == 0) {
+    double c[3];
+    closest_pt_tri(q, P[0], P[1], P[2], c);
+    const double e0 = q[0] - c[0], e1 = q[1] - c[1], e2 = q[2] - c[2];
+    cand = e0 * e0 + e1 * e1 + e2 * e2;
+    cf = f;
+    cc[0] = c[0]; cc[1] = c[1]; cc[2] = c[2];
+  } else {
+    EPFace fe;
+    ep_setup(P, fe);
+    double dd = best;
+    point_distance_ep(fe, q, dd);
+    cand = dd;
+  }
+  return true;
+}
+
+template <int MODE>
+__device__ __forceinline__ float dist_bound(double x) {
+  if (isinf(x)) return INFINITY;
+  return MODE == 0 ? __double2float_ru(sqrt(x)) : __double2float_ru(x);
+}
+
+// Per-thread depth-first traversal with at most `budget` pops.  Returns 0 when done, 1 on stack
+// overflow (result may be incomplete), 2 when the budget ran out (best is a valid upper bound).
+template <int MODE>
+__device__ int thread_traverse(const BvhDev &b, const double q[3], double &best, int32_t &bf, double bc[3],
+                               int budget) {
   const int n = b.n;
   const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
   const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
-  float bestd = __double2float_ru(dist);
-  stack[sp++] = n == 1 ? ~0 : 0;
+  float bestd = dist_bound<MODE>(best);
+  if (n == 1) {
+    double cand = INFINITY, cc[3];
+    int32_t cf = -1;
+    if (eval_leaf<MODE>(b, 0, -INFINITY, q, qf, bestd, best, cand, cf, cc) && cand < best) {
+      best = cand;
+      if (MODE == 0) { bf = cf; bc[0] = cc[0]; bc[1] = cc[1]; bc[2] = cc[2]; }
+    }
+    return 0;
+  }
+  int32_t sn[kStack];
+  float sd[kStack];
+  int sp = 0, pops = 0;
+  bool ok = true;
+  sn[sp] = 0; sd[sp] = 0.f; sp++;
   while (sp > 0) {
-    const int32_t node = stack[--sp];
+    if (pops >= budget) return 2;
+    --sp;
+    const int32_t node = sn[sp];
+    const float d = sd[sp];
+    pops++;
+    if (d > bestd) continue;
     if (node < 0) {
-      if (~node >= n) { ok = false; continue; }
-      double P[3][3];
-      face_pts(b, b.leaf_face[~node], P);
-      if (leaf_lower_bound(q, P, node_box(b, node), qf) > bestd) continue;
-      EPFace f;
-      ep_setup(P, f);
-      point_distance_ep(f, q, dist);
-      bestd = __double2float_ru(dist);
+      const int32_t leaf = ~node;
+      if (leaf >= n) { ok = false; continue; }
+      double cand = INFINITY, cc[3];
+      int32_t cf = -1;
+      if (eval_leaf<MODE>(b, leaf, d, q, qf, bestd, best, cand, cf, cc) && cand < best) {
+        best = cand;
+        if (MODE == 0) { bf = cf; bc[0] = cc[0]; bc[1] = cc[1]; bc[2] = cc[2]; }
+        bestd = dist_bound<MODE>(best);
+      }
       continue;
     }
     if (node >= n - 1) { ok = false; continue; }
-    const int32_t l = b.child[2 * node], r = b.child[2 * node + 1];
-    if (l >= n - 1 || r >= n - 1 || ~l >= n || ~r >= n) { ok = false; continue; }
-    const float dl = sqrtf(box_d2f(node_box(b, l), qf)) - mbox;
-    const float dr = sqrtf(box_d2f(node_box(b, r), qf)) - mbox;
-    const int32_t nearc = dl <= dr ? l : r, farc = dl <= dr ? r : l;
-    const float dn = fminf(dl, dr), df = fmaxf(dl, dr);
-    if (df <= bestd) { if (sp < kStack) stack[sp++] = farc; else ok = false; }
-    if (dn <= bestd) { if (sp < kStack) stack[sp++] = nearc; else ok = false; }
+    const NodeRec r = load_node(b.node, node);
+    if (r.l >= n - 1 || r.r >= n - 1 || ~r.l >= n || ~r.r >= n) { ok = false; continue; }
+    const float dl = sqrtf(box_d2f(r.lb, qf)) - mbox;
+    const float dr = sqrtf(box_d2f(r.rb, qf)) - mbox;
+    const bool lnear = dl <= dr;
+    const int32_t nearc = lnear ? r.l : r.r, farc = lnear ? r.r : r.l;
+    const float dn = lnear ? dl : dr, df = lnear ? dr : dl;
+    if (df <= bestd) { if (sp < kStack) { sn[sp] = farc; sd[sp] = df; sp++; } else ok = false; }
+    if (dn <= bestd) { if (sp < kStack) { sn[sp] = nearc; sd[sp] = dn; sp++; } else ok = false; }
   }
-  return ok;
+  return ok ? 0 : 1;
 }
 
+// Warp-cooperative traversal for the queries left over by the per-thread pass: one query per
+// warp, up to 32 frontier entries per step (one per lane), LIFO frontier in shared memory.
+constexpr int kWarpStack = 1024;
+
+__device__ __forceinline__ int warp_excl_scan(int v, int &total) {
+  const int lane = threadIdx.x & 31;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  total = __shfl_sync(0xffffffffu, x, 31);
+  return x - v;
+}
+
+template <int MODE>
+__device__ bool warp_traverse(const BvhDev &b, const double q[3], int32_t *sn, float *sd, double &best, int32_t &bf,
+                              double bc[3]) {
+  const int lane = threadIdx.x & 31;
+  const int n = b.n;
+  const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
+  const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
+  float bestd = dist_bound<MODE>(best);
+  bool ok = true;
+  int sz = 1;
+  if (lane == 0) { sn[0] = n == 1 ? ~0 : 0; sd[0] = -INFINITY; }
+  __syncwarp();
+  for (int guard = 0; sz > 0 && guard < 4 * (2 * n + 64); guard++) {
+    const int take = sz < 32 ? sz : 32;
+    const bool has = lane < take;
+    const int32_t node = has ? sn[sz - take + lane] : 0;
+    const float d = has ? sd[sz - take + lane] : INFINITY;
+    __syncwarp();
+    sz -= take;
+    double cand = INFINITY;
+    int32_t cf = -1;
+    double cc[3] = {0, 0, 0};
+    int32_t push[2];
+    float pd[2];
+    int np = 0;
+    if (has && d <= bestd) {
+      if (node < 0) {
+        const int32_t leaf = ~node;
+        if (leaf < n) eval_leaf<MODE>(b, leaf, d, q, qf, bestd, best, cand, cf, cc);
+        else ok = false;
+      } else if (node < n - 1) {
+        const NodeRec r = load_node(b.node, node);
+        if (r.l >= n - 1 || r.r >= n - 1 || ~r.l >= n || ~r.r >= n) {
+          ok = false;
+        } else {
+          const float dl = sqrtf(box_d2f(r.lb, qf)) - mbox;
+          const float dr = sqrtf(box_d2f(r.rb, qf)) - mbox;
+          const bool lnear = dl <= dr;
+          const float dn = lnear ? dl : dr, df = lnear ? dr : dl;
+          if (df <= bestd) { push[np] = lnear ? r.r : r.l; pd[np] = df; np++; }
+          if (dn <= bestd) { push[np] = lnear ? r.l : r.r; pd[np] = dn; np++; }
+        }
+      } else {
+        ok = false;
+      }
+    }
+    double m = cand;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (m < best) {
+      if (MODE == 0) {
+        const unsigned who = __ballot_sync(0xffffffffu, cand == m);
+        const int src = __ffs(who) - 1;
+        bf = __shfl_sync(0xffffffffu, cf, src);
+        bc[0] = __shfl_sync(0xffffffffu, cc[0], src);
+        bc[1] = __shfl_sync(0xffffffffu, cc[1], src);
+        bc[2] = __shfl_sync(0xffffffffu, cc[2], src);
+      }
+      best = m;
+      bestd = dist_bound<MODE>(best);
+    }
+    int total;
+    const int off = warp_excl_scan(np, total);
+    const int room = kWarpStack - sz;
+    for (int k = 0; k < np; k++)
+      if (off + k < room) { sn[sz + off + k] = push[k]; sd[sz + off + k] = pd[k]; }
+    if (total > room) ok = false;
+    __syncwarp();
+    sz += total < room ? total : room;
+  }
+  if (sz > 0) ok = false;
+  return __all_sync(0xffffffffu, ok);
+}
+
+constexpr int kThreadBudget = 64;   // pops per query before handing over to the warp pass
+__device__ __forceinline__ unsigned warps_total() { return gridDim.x * (blockDim.x >> 5); }
+__device__ __forceinline__ unsigned warp_global() { return blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); }
+
+__device__ __forceinline__ void push_overflow(const Overflow &o, int64_t item, int32_t mesh) {
+  const unsigned k = atomicAdd(o.count, 1u);
+  o.item[k] = item;
+  o.mesh[k] = mesh;
+}
+
+// pseudonormal_test: normal at the closest point c of face f (vertex / edge / face normal).
+__device__ void pseudonormal(const TargetDev &t, int32_t f, const double c[3], double n[3]) {
+  double A[3], B[3], C[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) { A[d] = t.tri[(int64_t)f * 9 + d]; B[d] = t.tri[(int64_t)f * 9 + 3 + d]; C[d] = t.tri[(int64_t)f * 9 + 6 + d]; }
+  const double e1[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]}, e2[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
+  const double x0 = e1[1] * e2[2] - e1[2] * e2[1], x1 = e1[2] * e2[0] - e1[0] * e2[2], x2 = e1[0] * e2[1] - e1[1] * e2[0];
+  const double area = sqrt(x0 * x0 + x1 * x1 + x2 * x2);  // doublearea
+  const double epsilon = 1e-12;
+  int kind = 0, which = 0;  // 0 face, 1 vertex (which corner), 2 edge (opposite which corner)
+  if (area > 1e-4) {
+    const double v2[3] = {c[0] - A[0], c[1] - A[1], c[2] - A[2]};
+    const double d00 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2], d01 = e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2];
+    const double d11 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+    const double d20 = v2[0] * e1[0] + v2[1] * e1[1] + v2[2] * e1[2], d21 = v2[0] * e2[0] + v2[1] * e2[1] + v2[2] * e2[2];
+    const double den = d00 * d11 - d01 * d01;
+    double bb[3];
+    bb[1] = (d11 * d20 - d01 * d21) / den;
+    bb[2] = (d00 * d21 - d01 * d20) / den;
+    bb[0] = 1.0 - (bb[1] + bb[2]);
+    const int type = (bb[0] <= epsilon) + (bb[1] <= epsilon) + (bb[2] <= epsilon);
+    if (type == 2) {
+      kind = 1;
+      which = bb[0] > epsilon ? 0 : (bb[1] > epsilon ? 1 : 2);
+    } else if (type == 1) {
+      kind = 2;
+      which = bb[0] <= epsilon ? 0 : (bb[1] <= epsilon ? 1 : 2);
+    }
+  } else {
+    const double *P[3] = {A, B, C};
+    bool found = false;
+    for (int v = 0; v < 3 && !found; v++) {
+      const double dx = c[0] - P[v][0], dy = c[1] - P[v][1], dz = c[2] - P[v][2];
+      if (sqrt(dx * dx + dy * dy + dz * dz) < epsilon) { found = true; kind = 1; which = v; }
+    }
+    for (int e = 0; e < 3 && !found; e++) {
+      const double *s = P[(e + 1) % 3], *dd = P[(e + 2) % 3];
+      const double dms[3] = {dd[0] - s[0], dd[1] - s[1], dd[2] - s[2]};
+      const double smp[3] = {s[0] - c[0], s[1] - c[1], s[2] - c[2]};
+      const double vl = dms[0] * dms[0] + dms[1] * dms[1] + dms[2] * dms[2];
+      const double tt = -(dms[0] * smp[0] + dms[1] * smp[1] + dms[2] * smp[2]) / vl;
+      double sq;
+      if (tt < 0) {
+        sq = smp[0] * smp[0] + smp[1] * smp[1] + smp[2] * smp[2];
+      } else if (tt > 1) {
+        const double z0 = c[0] - dd[0], z1 = c[1] - dd[1], z2 = c[2] - dd[2];
+        sq = z0 * z0 + z1 * z1 + z2 * z2;
+      } else {
+        const double pr0 = (1.0 - tt) * s[0] + tt * dd[0], pr1 = (1.0 - tt) * s[1] + tt * dd[1], pr2 = (1.0 - tt) * s[2] + tt * dd[2];
+        const double m0 = c[0] - pr0, m1 = c[1] - pr1, m2 = c[2] - pr2;
+        sq = m0 * m0 + m1 * m1 + m2 * m2;
+      }
+      if (sqrt(sq) < epsilon) { found = true; kind = 2; which = e; }
+    }
+  }
+  const double *src = kind == 0 ? t.FN + 3 * (int64_t)f : kind == 1 ? t.VNc + 9 * (int64_t)f + 3 * which : t.ENc + 9 * (int64_t)f + 3 * which;
+  n[0] = src[0]; n[1] = src[1]; n[2] = src[2];
+}
+
+// Tangent planes of the regular boundary vertices (dirty_graph_projection, :4031-4078):
+// normal_T = pseudonormal, dis_T = normal_T . closest point.
+__device__ __forceinline__ void write_tangent(const ProjArgs &p, const TargetDev &t, int64_t e, int32_t f,
+                                              const double c[3]) {
+  double n[3] = {0, 0, 0};
+  if (f >= 0) pseudonormal(t, f, c, n);
+  p.t_nrm[3 * e] = n[0]; p.t_nrm[3 * e + 1] = n[1]; p.t_nrm[3 * e + 2] = n[2];
+  p.t_dis[e] = n[0] * c[0] + n[1] * c[1] + n[2] * c[2];
+}
+
+__global__ void __launch_bounds__(128) k_project(ProjArgs p) {
+  const Seg sg = p.seg[blockIdx.x];
+  const int64_t i = sg.begin + threadIdx.x;
+  if (i >= sg.end) return;
+  const MeshDesc md = p.mesh[sg.mesh];
+  const TargetDev &t = p.tgt[sg.mesh];
+  const int64_t e = md.t_off + (i - md.kitem0[K_PROJ]);
+  const int64_t v = md.v_off + p.t_ids[e];
+  const double q[3] = {p.X[4 * v], p.X[4 * v + 1], p.X[4 * v + 2]};
+  double best = INFINITY, c[3] = {0, 0, 0};
+  int32_t f = -1;
+  int st = 0;
+  if (t.bvh.n > 0) st = thread_traverse<0>(t.bvh, q, best, f, c, kThreadBudget);
+  if (st == 2) {
+    p.ovf.best[i] = best; p.ovf.face[i] = f;
+    p.ovf.pt[3 * i] = c[0]; p.ovf.pt[3 * i + 1] = c[1]; p.ovf.pt[3 * i + 2] = c[2];
+    push_overflow(p.ovf, i, sg.mesh);
+    return;
+  }
+  if (st == 1) atomicOr(&p.sc[sg.mesh].status, 8);
+  write_tangent(p, t, e, f, c);
+}
+
+__global__ void __launch_bounds__(128) k_project_warp(ProjArgs p) {
+  __shared__ int32_t sn[4][kWarpStack];
+  __shared__ float sd[4][kWarpStack];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned cnt = *p.ovf.count;
+  for (unsigned k = warp_global(); k < cnt; k += warps_total()) {
+    const int64_t i = p.ovf.item[k];
+    const int32_t m = p.ovf.mesh[k];
+    const MeshDesc md = p.mesh[m];
+    const TargetDev &t = p.tgt[m];
+    const int64_t e = md.t_off + (i - md.kitem0[K_PROJ]);
+    const int64_t v = md.v_off + p.t_ids[e];
+    const double q[3] = {p.X[4 * v], p.X[4 * v + 1], p.X[4 * v + 2]};
+    double best = p.ovf.best[i], c[3] = {p.ovf.pt[3 * i], p.ovf.pt[3 * i + 1], p.ovf.pt[3 * i + 2]};
+    int32_t f = p.ovf.face[i];
+    const bool ok = warp_traverse<0>(t.bvh, q, sn[w], sd[w], best, f, c);
+    if (lane == 0) {
+      if (!ok) atomicOr(&p.sc[m].status, 8);
+      write_tangent(p, t, e, f, c);
+    }
+    __syncwarp();
+  }
+}
+
+// signed_distance_pseudonormal for arbitrary query points (rows) against mesh m's target
+__global__ void __launch_bounds__(128) k_signed_distance(TargetDev t, int64_t np, const double *P, double *S,
+                                                         int32_t *I, double *C, double *N, int *status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const double q[3] = {P[3 * i], P[3 * i + 1], P[3 * i + 2]};
+  double best = INFINITY, c[3] = {0, 0, 0}, n[3] = {0, 0, 0};
+  int32_t f = -1;
+  if (t.bvh.n > 0 && thread_traverse<0>(t.bvh, q, best, f, c, 1 << 30) != 0) atomicOr(status, 8);
+  double s = 1;
+  if (f >= 0) {
+    pseudonormal(t, f, c, n);
+    s = ((q[0] - c[0]) * n[0] + (q[1] - c[1]) * n[1] + (q[2] - c[2]) * n[2]) >= 0 ? 1. : -1.;
+  }
+  S[i] = s * sqrt(best);
+  I[i] = f;
+  C[3 * i] = c[0]; C[3 * i + 1] = c[1]; C[3 * i + 2] = c[2];
+  N[3 * i] = n[0]; N[3 * i + 1] = n[1]; N[3 * i + 2] = n[2];
+}
+
+// Feature lines (dirty_graph_projection LINE branch, :3963-4025): nearest curve segment by
+// point_line_projection (global_functions.cpp:3454-3465), ties to the lower segment index.
+__global__ void __launch_bounds__(128) k_curve_project(ProjArgs p) {
+  const Seg sg = p.seg[blockIdx.x];
+  const int64_t i = sg.begin + threadIdx.x;
+  if (i >= sg.end) return;
+  const MeshDesc md = p.mesh[sg.mesh];
+  const TargetDev &t = p.tgt[sg.mesh];
+  const int64_t e = md.l_off + (i - md.kitem0[K_LINE]);
+  const int64_t v = md.v_off + p.l_ids[e];
+  const double q[3] = {p.X[4 * v], p.X[4 * v + 1], p.X[4 * v + 2]};
+  const int32_t cu = p.l_curve[e];
+  const int64_t c0 = t.curve_ptr[cu], c1 = t.curve_ptr[cu + 1];
+  const int64_t size = c1 - c0;
+  const int64_t len = t.curve_closed[cu] ? size : size - 1;
+  double best = INFINITY, pv[3] = {0, 0, 0}, tg[3] = {1, 0, 0};
+  for (int64_t j = 0; j < len; j++) {
+    const double *a = t.TV + 3 * (int64_t)t.curve_vs[c0 + j];
+    const double *b = t.TV + 3 * (int64_t)t.curve_vs[c0 + (j + 1) % size];
+    const double vv1[3] = {q[0] - a[0], q[1] - a[1], q[2] - a[2]}, v21[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    const double n2 = v21[0] * v21[0] + v21[1] * v21[1] + v21[2] * v21[2];
+    const double tt = n2 >= 1.e-7 ? (vv1[0] * v21[0] + vv1[1] * v21[1] + vv1[2] * v21[2]) / n2 : 0.0;
+    double pp[3];
+    if (tt >= 0.0 && tt <= 1.0) { pp[0] = a[0] + tt * v21[0]; pp[1] = a[1] + tt * v21[1]; pp[2] = a[2] + tt * v21[2]; }
+    else if (tt < 0.0) { pp[0] = a[0]; pp[1] = a[1]; pp[2] = a[2]; }
+    else { pp[0] = b[0]; pp[1] = b[1]; pp[2] = b[2]; }
+    const double dx = q[0] - pp[0], dy = q[1] - pp[1], dz = q[2] - pp[2];
+    const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+    if (dist < best) {
+      best = dist;
+      pv[0] = pp[0]; pv[1] = pp[1]; pv[2] = pp[2];
+      const double ln = sqrt(n2);
+      tg[0] = v21[0] / ln; tg[1] = v21[1] / ln; tg[2] = v21[2] / ln;
+    }
+  }
+  if (len <= 0 && size > 0) {  // single-vertex curve: nearest curve vertex
+    const double *a = t.TV + 3 * (int64_t)t.curve_vs[c0];
+    pv[0] = a[0]; pv[1] = a[1]; pv[2] = a[2];
+    tg[0] = 1; tg[1] = 0; tg[2] = 0;
+  }
+  p.l_orig[3 * e] = pv[0]; p.l_orig[3 * e + 1] = pv[1]; p.l_orig[3 * e + 2] = pv[2];
+  p.l_axis[3 * e] = tg[0]; p.l_axis[3 * e + 1] = tg[1]; p.l_axis[3 * e + 2] = tg[2];
+}
+
+// ------------------------------------------------------------------------------- Hausdorff
 // bbox of the referenced surface vertices at the current positions (per mesh), combined with the
 // static target bbox -> inflated diagonal (the distance upper bound).
 __global__ void __launch_bounds__(256) k_haus_bbox(HausArgs h) {
@@ -595,47 +763,92 @@ __global__ void __launch_bounds__(256) k_haus_bbox(HausArgs h) {
 }
 
 // One side of the vertex-sampled Hausdorff: SIDE 0 = target vertices vs surface faces,
-// SIDE 1 = surface vertices vs target faces.
+// SIDE 1 = surface vertices vs target faces.  Per-sample distance into h.dist (left at the upper
+// bound when no face is closer), finished by the warp pass for samples over budget, then reduced.
+template <int SIDE>
+__device__ __forceinline__ void haus_query(const HausArgs &h, int64_t i, int32_t m, double q[3], const BvhDev *&b) {
+  if (SIDE == 0) {
+    const int64_t v = h.tgt_vs[i];
+    const TargetDev &t = h.tgt[m];
+    q[0] = t.TV[3 * v]; q[1] = t.TV[3 * v + 1]; q[2] = t.TV[3 * v + 2];
+    b = &h.surf[m];
+  } else {
+    const int64_t v = h.surf_vs[i];
+    q[0] = h.X[4 * v]; q[1] = h.X[4 * v + 1]; q[2] = h.X[4 * v + 2];
+    b = &h.tgt[m].bvh;
+  }
+}
+
 template <int SIDE>
 __global__ void __launch_bounds__(128) k_haus_side(HausArgs h) {
   const Seg sg = h.seg[blockIdx.x];
   const int64_t i = sg.begin + threadIdx.x;
+  if (i >= sg.end) return;
+  double q[3];
+  const BvhDev *b;
+  haus_query<SIDE>(h, i, sg.mesh, q, b);
+  double dist = h.hm[sg.mesh].diag;
+  int32_t fd = -1;
+  double cd[3];
+  int st = 0;
+  if (b->n > 0) st = thread_traverse<1>(*b, q, dist, fd, cd, kThreadBudget);
+  if (st == 2) {
+    h.ovf.best[i] = dist;
+    push_overflow(h.ovf, i, sg.mesh);
+    return;
+  }
+  if (st == 1) atomicOr(&h.sc[sg.mesh].status, 8);
+  h.dist[i] = dist;
+}
+
+template <int SIDE>
+__global__ void __launch_bounds__(128) k_haus_warp(HausArgs h) {
+  __shared__ int32_t sn[4][kWarpStack];
+  __shared__ float sd[4][kWarpStack];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned cnt = *h.ovf.count;
+  for (unsigned k = warp_global(); k < cnt; k += warps_total()) {
+    const int64_t i = h.ovf.item[k];
+    const int32_t m = h.ovf.mesh[k];
+    double q[3];
+    const BvhDev *b;
+    haus_query<SIDE>(h, i, m, q, b);
+    double dist = h.ovf.best[i];
+    int32_t fd = -1;
+    double cd[3];
+    const bool ok = warp_traverse<1>(*b, q, sn[w], sd[w], dist, fd, cd);
+    if (lane == 0) {
+      if (!ok) atomicOr(&h.sc[m].status, 8);
+      h.dist[i] = dist;
+    }
+    __syncwarp();
+  }
+}
+
+// max / mean of one side (AddSample, sampling.h:224-256: samples at the upper bound are dropped)
+template <int SIDE>
+__global__ void __launch_bounds__(256) k_haus_reduce(HausArgs h) {
+  const Seg sg = h.seg[blockIdx.x];
   const MeshDesc md = h.mesh[sg.mesh];
   HausMesh &hm = h.hm[sg.mesh];
   const double upper = hm.diag;
-  double mx[1] = {-INFINITY}, acc[2] = {0, 0};
-  if (i < sg.end) {
-    double q[3];
-    if (SIDE == 0) {
-      const int64_t v = h.tgt_vs[i];
-      const TargetDev &t = h.tgt[sg.mesh];
-      q[0] = t.TV[3 * v]; q[1] = t.TV[3 * v + 1]; q[2] = t.TV[3 * v + 2];
-    } else {
-      const int64_t v = h.surf_vs[i];
-      q[0] = h.X[4 * v]; q[1] = h.X[4 * v + 1]; q[2] = h.X[4 * v + 2];
-    }
-    double dist = upper;
-    const BvhDev &b = SIDE == 0 ? h.surf[sg.mesh] : h.tgt[sg.mesh].bvh;
-    if (b.n > 0 && !bvh_ep(b, q, dist)) atomicOr(&h.sc[sg.mesh].status, 8);
-    if (dist != upper) { mx[0] = dist; acc[0] = dist; acc[1] = 1; }
+  double mx[1] = {INFINITY}, acc[2] = {0, 0};
+  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
+    const double d = h.dist[i];
+    if (d != upper) { mx[0] = fmin(mx[0], -d); acc[0] += d; acc[1] += 1; }
   }
   __shared__ double smem[2][32];
-  double nm[1] = {-mx[0]};
-  block_min<1>(nm, smem);
-  const double bm = -nm[0];
+  block_min<1>(mx, smem);
+  const double bm = mx[0];
   block_sum<2>(acc, smem);
   double out[3] = {bm, acc[0], acc[1]};
   const int kind = SIDE == 0 ? K_TGTV : K_SURFV;
   if (publish_partials<3>(out, h.partials, blockIdx.x, h.counters + sg.mesh, md.knblk[kind])) {
-    double m = -INFINITY;
-    for (int b = threadIdx.x; b < md.knblk[kind]; b += blockDim.x)
-      m = fmax(m, __ldcg(&h.partials[(md.kblk0[kind] + b) * 3]));
-    double t[1] = {-m};
-    block_min<1>(t, smem);
+    double m = gather_partials_min(h.partials, md.kblk0[kind], md.knblk[kind], 3, 0, smem);
     double s = gather_partials_sum(h.partials, md.kblk0[kind], md.knblk[kind], 3, 1, smem);
     double c = gather_partials_sum(h.partials, md.kblk0[kind], md.knblk[kind], 3, 2, smem);
     if (threadIdx.x == 0) {
-      hm.side_max[SIDE] = -t[0];
+      hm.side_max[SIDE] = -m;
       hm.side_mean[SIDE] = s / c;
       if (SIDE == 1) {
         hm.max_dist = fmax(hm.side_max[0], hm.side_max[1]);
@@ -654,7 +867,9 @@ __global__ void __launch_bounds__(128) k_ep_points(BvhDev b, const double *P, co
   const int64_t v = ids ? ids[i] : i;
   const double q[3] = {P[3 * v], P[3 * v + 1], P[3 * v + 2]};
   double d = upper;
-  if (b.n > 0 && !bvh_ep(b, q, d)) atomicOr(status, 8);
+  int32_t fd = -1;
+  double cd[3];
+  if (b.n > 0 && thread_traverse<1>(b, q, d, fd, cd, 1 << 30) != 0) atomicOr(status, 8);
   dist[i] = d;
 }
 
@@ -684,6 +899,19 @@ __global__ void k_fa_haus_flag(MeshScalars *sc, const HausMesh *hm, int n) {
 }
 
 // ------------------------------------------------------------------------------- launchers
+// internal node records (64 B): both child boxes and child ids
+__global__ void k_pack(int n, const int32_t *child, const float *box, float4 *node) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int32_t l = child[2 * i], r = child[2 * i + 1];
+  const float *bl = box + 6 * (int64_t)(l >= 0 ? l : n - 1 + ~l);
+  const float *br = box + 6 * (int64_t)(r >= 0 ? r : n - 1 + ~r);
+  node[4 * (int64_t)i] = make_float4(bl[0], bl[1], bl[2], bl[3]);
+  node[4 * (int64_t)i + 1] = make_float4(bl[4], bl[5], br[0], br[1]);
+  node[4 * (int64_t)i + 2] = make_float4(br[2], br[3], br[4], br[5]);
+  node[4 * (int64_t)i + 3] = make_float4(__int_as_float(l), __int_as_float(r), 0.f, 0.f);
+}
+
 void launch_ep_points(const BvhDev &b, const double *P, const int64_t *ids, int64_t n, double upper, double *dist,
                       int *status, cudaStream_t st) {
   if (n > 0) k_ep_points<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(b, P, ids, n, upper, dist, status);
@@ -703,11 +931,18 @@ void bvh_karras(int n, const unsigned long long *keys, int32_t *child, int32_t *
                 cudaStream_t st) {
   if (n > 0) k_karras<<<(n + 255) / 256, 256, 0, st>>>(n, keys, child, parent, leaf_face);
 }
-void bvh_refit(const BvhDev &b, float *box, const int32_t *parent, unsigned *counters, cudaStream_t st) {
-  if (b.n > 0) k_refit<<<(b.n + 127) / 128, 128, 0, st>>>(b, box, parent, counters);
+void bvh_refit(const BvhDev &b, float *box, const int32_t *parent, unsigned *counters, float4 *node, float4 *leafd,
+               cudaStream_t st) {
+  if (b.n <= 0) return;
+  k_refit<<<(b.n + 127) / 128, 128, 0, st>>>(b, box, parent, counters, leafd);
+  if (b.n > 1) k_pack<<<(b.n + 254) / 256, 256, 0, st>>>(b.n, b.child, box, node);
 }
+static const unsigned kWarpGrid = 912;  // persistent warp-pass grid (152 SMs x 6 blocks of 4 warps)
 void launch_project(const ProjArgs &p, int64_t nblk, cudaStream_t st) {
-  if (nblk > 0) k_project<<<(unsigned)nblk, 128, 0, st>>>(p);
+  if (nblk <= 0) return;
+  cudaMemsetAsync(p.ovf.count, 0, sizeof(unsigned), st);
+  k_project<<<(unsigned)nblk, 128, 0, st>>>(p);
+  k_project_warp<<<kWarpGrid, 128, 0, st>>>(p);
 }
 void launch_curve_project(const ProjArgs &p, int64_t nblk, cudaStream_t st) {
   if (nblk > 0) k_curve_project<<<(unsigned)nblk, 128, 0, st>>>(p);
@@ -717,11 +952,19 @@ void launch_signed_distance(const TargetDev &t, int64_t np, const double *P, dou
   if (np > 0) k_signed_distance<<<(unsigned)((np + 127) / 128), 128, 0, st>>>(t, np, P, S, I, C, N, status);
 }
 void launch_haus_bbox(const HausArgs &h, int64_t nblk, cudaStream_t st) {
-  k_haus_bbox<<<(unsigned)nblk, 256, 0, st>>>(h);
+  k_haus_bbox<<<(unsigned)nblk, 128, 0, st>>>(h);
 }
 void launch_haus_side(const HausArgs &h, int side, int64_t nblk, cudaStream_t st) {
-  if (side == 0) k_haus_side<0><<<(unsigned)nblk, 128, 0, st>>>(h);
-  else k_haus_side<1><<<(unsigned)nblk, 128, 0, st>>>(h);
+  cudaMemsetAsync(h.ovf.count, 0, sizeof(unsigned), st);
+  if (side == 0) {
+    k_haus_side<0><<<(unsigned)nblk, 128, 0, st>>>(h);
+    k_haus_warp<0><<<kWarpGrid, 128, 0, st>>>(h);
+    k_haus_reduce<0><<<(unsigned)nblk, 128, 0, st>>>(h);
+  } else {
+    k_haus_side<1><<<(unsigned)nblk, 128, 0, st>>>(h);
+    k_haus_warp<1><<<kWarpGrid, 128, 0, st>>>(h);
+    k_haus_reduce<1><<<(unsigned)nblk, 128, 0, st>>>(h);
+  }
 }
 
 }  // namespace hexopt

@@ -769,62 +769,64 @@ __device__ __forceinline__ double cand_alpha(const MeshScalars &S, int j) {
 }
 
 // Quality energy at the NC candidates j = round*NC .. round*NC + NC - 1 (E = E0 + alpha D).
+// Persistent launch: a fixed grid walks the hex segments, so the rounds after the line search
+// has accepted a step cost one scalar read per segment.
 template <typename ET, typename VT, int NC>
-__global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round) {
-  const Seg sg = a.hseg[blockIdx.x];
-  MeshScalars &S = a.sc[sg.mesh];
-  if (S.ls_done) return;
-  const int64_t h = sg.begin + threadIdx.x;
-  const MeshDesc md = a.mesh[sg.mesh];
-  double acc[kMaxCand];
+__global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t nseg) {
+  __shared__ double smem[NC][32];
+  for (int64_t sb = blockIdx.x; sb < nseg; sb += gridDim.x) {
+    const Seg sg = a.hseg[sb];
+    MeshScalars &S = a.sc[sg.mesh];
+    if (S.ls_done) continue;
+    const int64_t h = sg.begin + threadIdx.x;
+    const MeshDesc md = a.mesh[sg.mesh];
+    double acc[NC];
 #pragma unroll
-  for (int j = 0; j < kMaxCand; j++) acc[j] = 0;
-  if (h < sg.end) {
-    uint32_t hv[8];
-    load_hex(a.hexv, h, hv);
-    const int32_t gs = a.gslot[h];
-    ET E12[12][3], D12[12][3];
-    hex_edges_pos(a.X, hv, E12);
-    {
-      VT Dv[12][3];
-      hex_edges_vec(reinterpret_cast<const VT *>(a.d), hv, Dv);
+    for (int j = 0; j < NC; j++) acc[j] = 0;
+    if (h < sg.end) {
+      uint32_t hv[8];
+      load_hex(a.hexv, h, hv);
+      const int32_t gs = a.gslot[h];
+      ET E12[12][3], D12[12][3];
+      hex_edges_pos(a.X, hv, E12);
+      {
+        VT Dv[12][3];
+        hex_edges_vec(reinterpret_cast<const VT *>(a.d), hv, Dv);
 #pragma unroll
-      for (int e = 0; e < 12; e++)
+        for (int e = 0; e < 12; e++)
 #pragma unroll
-        for (int r = 0; r < 3; r++) D12[e][r] = ET(Dv[e][r]);
-    }
-    double al[NC];
+          for (int r = 0; r < 3; r++) D12[e][r] = ET(Dv[e][r]);
+      }
+      double al[NC];
 #pragma unroll
-    for (int j = 0; j < NC; j++) al[j] = cand_alpha(S, round * NC + j);
+      for (int j = 0; j < NC; j++) al[j] = cand_alpha(S, round * NC + j);
 #define HX_LE(K)                                                             \
-    {                                                                        \
-      ET E0[3][3], D[3][3];                                                  \
-      tet_E12<K>(E12, E0);                                                   \
-      tet_E12<K>(D12, D);                                                    \
-      _Pragma("unroll") for (int j = 0; j < NC; j++) {                       \
-        ET E[3][3];                                                          \
-        const ET aj = ET(al[j]);                                             \
-        _Pragma("unroll") for (int r = 0; r < 3; r++)                        \
-        _Pragma("unroll") for (int c = 0; c < 3; c++) E[r][c] = E0[r][c] + aj * D[r][c]; \
-        acc[j] += tet_energy_e<ET, VT, K>(a, h, hv, gs, E, al[j]);           \
-      }                                                                      \
-    }
-    HX_LE(0) HX_LE(1) HX_LE(2) HX_LE(3) HX_LE(4) HX_LE(5) HX_LE(6) HX_LE(7)
+      {                                                                      \
+        ET E0[3][3], D[3][3];                                                \
+        tet_E12<K>(E12, E0);                                                 \
+        tet_E12<K>(D12, D);                                                  \
+        _Pragma("unroll") for (int j = 0; j < NC; j++) {                     \
+          ET E[3][3];                                                        \
+          const ET aj = ET(al[j]);                                           \
+          _Pragma("unroll") for (int r = 0; r < 3; r++)                      \
+          _Pragma("unroll") for (int c = 0; c < 3; c++) E[r][c] = E0[r][c] + aj * D[r][c]; \
+          acc[j] += tet_energy_e<ET, VT, K>(a, h, hv, gs, E, al[j]);         \
+        }                                                                    \
+      }
+      HX_LE(0) HX_LE(1) HX_LE(2) HX_LE(3) HX_LE(4) HX_LE(5) HX_LE(6) HX_LE(7)
 #undef HX_LE
 #pragma unroll
-    for (int j = 0; j < NC; j++) acc[j] *= S.M;
-  }
-  __shared__ double smem[NC][32];
-  double acc2[NC];
-#pragma unroll
-  for (int j = 0; j < NC; j++) acc2[j] = acc[j];
-  block_sum<NC>(acc2, smem);
-  if (publish_partials<NC>(acc2, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
-    for (int j = 0; j < NC; j++) {
-      double e = gather_partials_sum(a.partials, md.hblk0, md.nhblk, NC, j, smem);
-      if (threadIdx.x == 0) S.cand_eq[j] = e;
+      for (int j = 0; j < NC; j++) acc[j] *= S.M;
     }
-    if (threadIdx.x == 0) a.counters[sg.mesh] = 0;
+    block_sum<NC>(acc, smem);
+    if (publish_partials<NC>(acc, a.partials, sb, a.counters + sg.mesh, md.nhblk)) {
+      for (int j = 0; j < NC; j++) {
+        double e = gather_partials_sum(a.partials, md.hblk0, md.nhblk, NC, j, smem);
+        if (threadIdx.x == 0) S.cand_eq[j] = e;
+      }
+      if (threadIdx.x == 0) a.counters[sg.mesh] = 0;
+    }
+    __syncthreads();
   }
 }
 
@@ -933,18 +935,21 @@ __global__ void __launch_bounds__(256) k_ls_apply(KArgs a) {
   }
 }
 
+// Persistent grid size: enough blocks to fill the GPU (152 SMs x 6), never more than segments.
+static inline unsigned pgrid(int64_t nseg) { return (unsigned)(nseg < 912 ? nseg : 912); }
+
 // One candidate-energy pass alone (timing): the pass of round 0.
 template <typename ET, typename VT>
 void launch_ls_energy_pass(const KArgs &a, int64_t hblk, cudaStream_t st) {
   switch (a.ls_cand) {
-    case 1: k_ls_energy<ET, VT, 1><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
-    case 2: k_ls_energy<ET, VT, 2><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
-    case 3: k_ls_energy<ET, VT, 3><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
-    case 4: k_ls_energy<ET, VT, 4><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
-    case 5: k_ls_energy<ET, VT, 5><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
-    case 6: k_ls_energy<ET, VT, 6><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
-    case 7: k_ls_energy<ET, VT, 7><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
-    default: k_ls_energy<ET, VT, 8><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, 0); break;
+    case 1: k_ls_energy<ET, VT, 1><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
+    case 2: k_ls_energy<ET, VT, 2><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
+    case 3: k_ls_energy<ET, VT, 3><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
+    case 4: k_ls_energy<ET, VT, 4><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
+    case 5: k_ls_energy<ET, VT, 5><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
+    case 6: k_ls_energy<ET, VT, 6><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
+    case 7: k_ls_energy<ET, VT, 7><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
+    default: k_ls_energy<ET, VT, 8><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
   }
 }
 
@@ -985,14 +990,14 @@ void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk
   const int rounds = (kHalvings + 1 + a.ls_cand - 1) / a.ls_cand;
   for (int r = 0; r < rounds; r++) {
     switch (a.ls_cand) {
-      case 1: k_ls_energy<ET, VT, 1><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
-      case 2: k_ls_energy<ET, VT, 2><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
-      case 3: k_ls_energy<ET, VT, 3><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
-      case 4: k_ls_energy<ET, VT, 4><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
-      case 5: k_ls_energy<ET, VT, 5><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
-      case 6: k_ls_energy<ET, VT, 6><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
-      case 7: k_ls_energy<ET, VT, 7><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
-      default: k_ls_energy<ET, VT, 8><<<(unsigned)hblk, a.hthreads, 0, st>>>(a, r); break;
+      case 1: k_ls_energy<ET, VT, 1><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
+      case 2: k_ls_energy<ET, VT, 2><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
+      case 3: k_ls_energy<ET, VT, 3><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
+      case 4: k_ls_energy<ET, VT, 4><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
+      case 5: k_ls_energy<ET, VT, 5><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
+      case 6: k_ls_energy<ET, VT, 6><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
+      case 7: k_ls_energy<ET, VT, 7><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
+      default: k_ls_energy<ET, VT, 8><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
     }
     k_ls_soft<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a, r);
   }
