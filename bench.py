@@ -112,6 +112,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def profiler(on: bool):
+    """cudaProfilerStart/Stop around the timed region, so that `ncu --profile-from-start off`
+    lists exactly the timed launches (a no-op without a profiler attached)."""
+    import torch
+    rt = torch.cuda.cudart()
+    (rt.cudaProfilerStart if on else rt.cudaProfilerStop)()
+
+
 def peaks():
     try:
         with open(PEAKS) as f:
@@ -191,7 +199,7 @@ def run_ours(args):
     import hexopt
     from hexopt import workloads
     precision = hexopt.MIXED if args.precision == "mixed" else hexopt.FP64
-    p = workloads.grid_superellipsoid(GRID_N, seed=rank)
+    p = workloads.grid_superellipsoid(args.grid, seed=rank)
     nv, nh = len(p["V"]), len(p["H"])
     ctx = hexopt.Context(local)
     workloads.load(ctx, [p])
@@ -207,10 +215,12 @@ def run_ours(args):
     clocks.start()
     barrier(tdist)
     l0 = ctx.launch_count()
+    profiler(True)
     ctx.timer_start()
     for _ in range(args.steps):
         ctx.fa_step(hausdorff=do_h, report=False)
     ms = ctx.timer_stop()
+    profiler(False)
     launches = ctx.launch_count() - l0
     clk = clocks.stop()
     ms = max_over_ranks(tdist, ms)
@@ -267,7 +277,7 @@ def run_ours(args):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
-           "config": {"workload": f"grid{GRID_N}_superellipsoid: {nh} hexes, {nv} vertices, 200k-triangle "
+           "config": {"workload": f"grid{args.grid}_superellipsoid: {nh} hexes, {nv} vertices, 200k-triangle "
                                   f"superellipsoid target (float32 coords), Gaussian jitter 0.2h seed {rank}; "
                                   f"{'mixed FP32/FP64' if mixed else 'plain FP64'}; Hausdorff every iteration "
                                   f"{'on' if do_h else 'off'}; CUDA-graph replay per step",
@@ -306,6 +316,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--skip-compare", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, default=GRID_N,
+                    help="grid cells per axis (128 = the 2.1M-hex workload; smaller only for profiler captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     return run_reference(args) if args.impl == "reference" else run_ours(args)

@@ -23,8 +23,10 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 if not os.path.exists(NVCC):
     NVCC = "nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no FP contraction, so host-side FP64 set-up (target normals, tables) rounds the same
+# on x86 and aarch64 and like the reference's CPU build
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-         f"-I{INCLUDE}", f"-I{CSRC}"]
+         "-Xcompiler", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 
 def _sources():

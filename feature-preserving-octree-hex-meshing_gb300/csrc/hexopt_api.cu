@@ -1563,7 +1563,10 @@ static void stage_launch(hexopt_ctx *ctx, int stage) {
     case 0: launch_spmv_elems<ET, VT>(a, hb, ctx->st); break;
     case 1: launch_local<ET, VT>(a, hb, false, ctx->st); break;
     case 2: launch_ls_energy_pass<ET, VT>(a, hb, ctx->st); break;
-    case 3: launch_scaled_jacobian(a, hb, nullptr, ctx->HJs.as<double>(), ctx->st); break;
+    case 3:  // the per-iteration quality check as the loop runs it
+      if (ctx->mixed) launch_sj_check(a, hb, ctx->st);
+      else launch_scaled_jacobian(a, hb, nullptr, ctx->HJs.as<double>(), ctx->st);
+      break;
     case 4: run_projection(ctx); break;
     default: break;
   }

@@ -118,7 +118,13 @@ __global__ void k_refit(BvhDev b, float *box, const int32_t *parent, unsigned *c
     const float cx = float(p[2][0] - p[0][0]), cy = float(p[2][1] - p[0][1]), cz = float(p[2][2] - p[0][2]);
     leafd[3 * (int64_t)k] = make_float4(ax, ay, az, bx);
     leafd[3 * (int64_t)k + 1] = make_float4(by, bz, cx, cy);
-    leafd[3 * (int64_t)k + 2] = make_float4(cz, 0.f, 0.f, 0.f);
+    // unit normal of (p1 - p0) x (p2 - p0), formed in FP64 and rounded once
+    const double ux = p[1][0] - p[0][0], uy = p[1][1] - p[0][1], uz = p[1][2] - p[0][2];
+    const double vx = p[2][0] - p[0][0], vy = p[2][1] - p[0][1], vz = p[2][2] - p[0][2];
+    double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+    const double nn = sqrt(nx * nx + ny * ny + nz * nz);
+    if (nn > 0) { nx /= nn; ny /= nn; nz /= nn; }
+    leafd[3 * (int64_t)k + 2] = make_float4(cz, float(nx), float(ny), float(nz));
   }
   float *lb = box + 6 * (int64_t)(n - 1 + k);
 #pragma unroll
@@ -159,57 +165,70 @@ __device__ __forceinline__ double box_d2(const float *bx, const double q[3]) {
   return s;
 }
 
-// Ericson's closest point on triangle (Real-Time Collision Detection 5.1.5), FP64.
+// FP64 arithmetic with every product and sum rounded on its own (no fused multiply-add), in the
+// operation order of the reference's CPU code, so the exact evaluations below give its bits.
+__device__ __forceinline__ double nmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double nadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double nsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ndot(const double *a, const double *b) {
+  return nadd(nadd(nmul(a[0], b[0]), nmul(a[1], b[1])), nmul(a[2], b[2]));
+}
+__device__ __forceinline__ void nsub3(const double *a, const double *b, double *o) {
+  o[0] = nsub(a[0], b[0]); o[1] = nsub(a[1], b[1]); o[2] = nsub(a[2], b[2]);
+}
+__device__ __forceinline__ void ncross(const double *a, const double *b, double *o) {
+  o[0] = nsub(nmul(a[1], b[2]), nmul(a[2], b[1]));
+  o[1] = nsub(nmul(a[2], b[0]), nmul(a[0], b[2]));
+  o[2] = nsub(nmul(a[0], b[1]), nmul(a[1], b[0]));
+}
+
+// Ericson's closest point on triangle (Real-Time Collision Detection 5.1.5), FP64, as
+// igl::point_simplex_squared_distance (point_simplex_squared_distance.cpp:25-130).
 __device__ void closest_pt_tri(const double p[3], const double a[3], const double b[3], const double c[3],
                                double out[3]) {
   double ab[3], ac[3], ap[3], bp[3], cp[3];
-#pragma unroll
-  for (int d = 0; d < 3; d++) { ab[d] = b[d] - a[d]; ac[d] = c[d] - a[d]; ap[d] = p[d] - a[d]; }
-  const double d1 = ab[0] * ap[0] + ab[1] * ap[1] + ab[2] * ap[2], d2 = ac[0] * ap[0] + ac[1] * ap[1] + ac[2] * ap[2];
+  nsub3(b, a, ab); nsub3(c, a, ac); nsub3(p, a, ap);
+  const double d1 = ndot(ab, ap), d2 = ndot(ac, ap);
   if (d1 <= 0.0 && d2 <= 0.0) { out[0] = a[0]; out[1] = a[1]; out[2] = a[2]; return; }
-#pragma unroll
-  for (int d = 0; d < 3; d++) bp[d] = p[d] - b[d];
-  const double d3 = ab[0] * bp[0] + ab[1] * bp[1] + ab[2] * bp[2], d4 = ac[0] * bp[0] + ac[1] * bp[1] + ac[2] * bp[2];
+  nsub3(p, b, bp);
+  const double d3 = ndot(ab, bp), d4 = ndot(ac, bp);
   if (d3 >= 0.0 && d4 <= d3) { out[0] = b[0]; out[1] = b[1]; out[2] = b[2]; return; }
-  const double vc = d1 * d4 - d3 * d2;
+  const double vc = nsub(nmul(d1, d4), nmul(d3, d2));
   if (!(a[0] == b[0] && a[1] == b[1] && a[2] == b[2]) && vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
-    const double v = d1 / (d1 - d3);
+    const double v = d1 / nsub(d1, d3);
 #pragma unroll
-    for (int d = 0; d < 3; d++) out[d] = a[d] + v * ab[d];
+    for (int d = 0; d < 3; d++) out[d] = nadd(a[d], nmul(v, ab[d]));
     return;
   }
-#pragma unroll
-  for (int d = 0; d < 3; d++) cp[d] = p[d] - c[d];
-  const double d5 = ab[0] * cp[0] + ab[1] * cp[1] + ab[2] * cp[2], d6 = ac[0] * cp[0] + ac[1] * cp[1] + ac[2] * cp[2];
+  nsub3(p, c, cp);
+  const double d5 = ndot(ab, cp), d6 = ndot(ac, cp);
   if (d6 >= 0.0 && d5 <= d6) { out[0] = c[0]; out[1] = c[1]; out[2] = c[2]; return; }
-  const double vb = d5 * d2 - d1 * d6;
+  const double vb = nsub(nmul(d5, d2), nmul(d1, d6));
   if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
-    const double w = d2 / (d2 - d6);
+    const double w = d2 / nsub(d2, d6);
 #pragma unroll
-    for (int d = 0; d < 3; d++) out[d] = a[d] + w * ac[d];
+    for (int d = 0; d < 3; d++) out[d] = nadd(a[d], nmul(w, ac[d]));
     return;
   }
-  const double va = d3 * d6 - d5 * d4;
-  if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0) {
-    const double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+  const double va = nsub(nmul(d3, d6), nmul(d5, d4));
+  const double d43 = nsub(d4, d3), d56 = nsub(d5, d6);
+  if (va <= 0.0 && d43 >= 0.0 && d56 >= 0.0) {
+    const double w = d43 / nadd(d43, d56);
 #pragma unroll
-    for (int d = 0; d < 3; d++) out[d] = b[d] + w * (c[d] - b[d]);
+    for (int d = 0; d < 3; d++) out[d] = nadd(b[d], nmul(w, nsub(c[d], b[d])));
     return;
   }
-  const double denom = 1.0 / (va + vb + vc);
-  const double v = vb * denom, w = vc * denom;
+  const double denom = 1.0 / nadd(nadd(va, vb), vc);
+  const double v = nmul(vb, denom), w = nmul(vc, denom);
 #pragma unroll
-  for (int d = 0; d < 3; d++) out[d] = a[d] + ab[d] * v + ac[d] * w;
+  for (int d = 0; d < 3; d++) out[d] = nadd(nadd(a[d], nmul(ab[d], v)), nmul(ac[d], w));
 }
 
 // ---- FP32 filtering with exact FP64 evaluation ----
 // Traversal and leaf screening run in FP32 on coordinates taken relative to the leaf's first
-// vertex (formed in FP64, rounded once).  A face is evaluated in FP64 only when its FP32 lower
-// bound is within a margin of the current best, so the FP64 result is the one a pure FP64
-// search returns: boxes are stored rounded outward, the box margin covers the rounding of the
-// query, and the leaf margin (1e-4 of the local scale) covers the FP32 point-triangle distance
-// of triangles whose smallest angle is above ~0.6 degrees; thinner triangles fall back to their
-// box distance as the lower bound.
+// vertex (formed in FP64, rounded once); only the leaves that FP32 cannot rule out are evaluated
+// in FP64, so the FP64 result is the one a pure FP64 search returns.  Boxes are stored rounded
+// outward and the box margin covers the rounding of the query.
 __device__ __forceinline__ float box_d2f(const float *bx, const float q[3]) {
   float s = 0.f;
 #pragma unroll
@@ -220,57 +239,105 @@ __device__ __forceinline__ float box_d2f(const float *bx, const float q[3]) {
   return s;
 }
 
-// Squared distance from p to the triangle (0, b, c) in FP32 (Ericson's region tests).
-__device__ __forceinline__ float tri_d2f(const float p[3], const float b[3], const float c[3]) {
-  const float d1 = b[0] * p[0] + b[1] * p[1] + b[2] * p[2], d2 = c[0] * p[0] + c[1] * p[1] + c[2] * p[2];
-  float x[3];
-  if (d1 <= 0.f && d2 <= 0.f) { x[0] = 0.f; x[1] = 0.f; x[2] = 0.f; }
-  else {
-    const float bp[3] = {p[0] - b[0], p[1] - b[1], p[2] - b[2]};
-    const float d3 = b[0] * bp[0] + b[1] * bp[1] + b[2] * bp[2], d4 = c[0] * bp[0] + c[1] * bp[1] + c[2] * bp[2];
-    const float vc = d1 * d4 - d3 * d2;
-    const float cp[3] = {p[0] - c[0], p[1] - c[1], p[2] - c[2]};
-    const float d5 = b[0] * cp[0] + b[1] * cp[1] + b[2] * cp[2], d6 = c[0] * cp[0] + c[1] * cp[1] + c[2] * cp[2];
-    const float vb = d5 * d2 - d1 * d6;
-    const float va = d3 * d6 - d5 * d4;
-    if (d3 >= 0.f && d4 <= d3) { x[0] = b[0]; x[1] = b[1]; x[2] = b[2]; }
-    else if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
-      const float v = d1 / (d1 - d3);
-      x[0] = v * b[0]; x[1] = v * b[1]; x[2] = v * b[2];
-    } else if (d6 >= 0.f && d5 <= d6) { x[0] = c[0]; x[1] = c[1]; x[2] = c[2]; }
-    else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
-      const float w = d2 / (d2 - d6);
-      x[0] = w * c[0]; x[1] = w * c[1]; x[2] = w * c[2];
-    } else if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
-      const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
-      x[0] = b[0] + w * (c[0] - b[0]); x[1] = b[1] + w * (c[1] - b[1]); x[2] = b[2] + w * (c[2] - b[2]);
-    } else {
-      const float den = 1.f / (va + vb + vc);
-      const float v = vb * den, w = vc * den;
-      x[0] = b[0] * v + c[0] * w; x[1] = b[1] * v + c[1] * w; x[2] = b[2] * v + c[2] * w;
-    }
-  }
-  const float e0 = p[0] - x[0], e1 = p[1] - x[1], e2 = p[2] - x[2];
-  return e0 * e0 + e1 * e1 + e2 * e2;
+// FP32 segment distance |q - (v1 + t (v2 - v1))|, t clamped to [0, 1] (the ps_dist below).
+__device__ __forceinline__ float seg_df(const float q[3], const float v1[3], const float v2[3]) {
+  const float e[3] = {v2[0] - v1[0], v2[1] - v1[1], v2[2] - v1[2]};
+  const float w[3] = {q[0] - v1[0], q[1] - v1[1], q[2] - v1[2]};
+  const float ee = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+  float t = ee > 0.f ? (w[0] * e[0] + w[1] * e[1] + w[2] * e[2]) / ee : 0.f;
+  t = fminf(fmaxf(t, 0.f), 1.f);
+  const float d0 = w[0] - e[0] * t, d1 = w[1] - e[1] * t, d2 = w[2] - e[2] * t;
+  return sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
 }
 
-// Lower bound (FP32, margin applied) of the distance from the query to leaf `leaf`'s triangle,
-// from its FP32 screening frame; `boxd` (the leaf box bound) is used for thin triangles.  The
-// margin covers the FP32 evaluation: 1e-4 of the local scale plus the rounding of absolute
-// coordinates (relative 1e-6).
-__device__ __forceinline__ float leaf_lower_bound(const float4 *leafd, int32_t leaf, const float qf[3], float boxd) {
+// ((v2 - v1) x (p - v1)) . n: the edge test of PointDistanceEP without its dominant-axis scaling
+// (the projected 2-D cross product divided by n[axis] equals this for p in the plane).
+__device__ __forceinline__ float edge_side(const float v1[3], const float v2[3], const float p[3], const float n[3]) {
+  const float e[3] = {v2[0] - v1[0], v2[1] - v1[1], v2[2] - v1[2]};
+  const float w[3] = {p[0] - v1[0], p[1] - v1[1], p[2] - v1[2]};
+  return (e[1] * w[2] - e[2] * w[1]) * n[0] + (e[2] * w[0] - e[0] * w[2]) * n[1] + (e[0] * w[1] - e[1] * w[0]) * n[2];
+}
+
+// FP32 bounds [lo, hi] of the exact FP64 distance from the query to leaf `leaf`'s triangle under
+// the metric of MODE, from the leaf's FP32 screening frame (first vertex, the two edges from it,
+// unit normal formed in FP64).  m = 1e-4 of the local scale plus 1e-6 of the absolute
+// coordinates covers the FP32 evaluation; an edge test is decided only outside its error band
+// (tb per unit edge length).
+//   MODE 0 (Euclidean, the projection metric): the distance is the plane distance |d| when the
+//     projection is inside, else the smallest of the three edge-segment distances, and it never
+//     exceeds that smallest segment distance.  lo takes |d| when the projection may be inside,
+//     hi only when it is inside for sure -- valid for any triangle shape.
+//   MODE 1 (PointDistanceEP, the Hausdorff metric): follows the first failing edge test rather
+//     than the nearest feature, so it can exceed the Euclidean distance; the FP64 branch is
+//     replayed in FP32 and hi is INFINITY where a test falls inside its band (lo = |d| - m, as
+//     the metric always measures to a point in the plane of the triangle).
+// Triangles whose smallest angle is below ~1e-6 rad take `boxd` as lo and the largest vertex
+// distance as hi (both metrics measure to a point of the triangle).
+template <int MODE>
+__device__ __forceinline__ void leaf_bounds(const float4 *leafd, int32_t leaf, const float qf[3], float boxd, float &lo,
+                                            float &hi) {
   const float4 u = __ldg(leafd + 3 * (int64_t)leaf), v = __ldg(leafd + 3 * (int64_t)leaf + 1),
                w = __ldg(leafd + 3 * (int64_t)leaf + 2);
   const float qa[3] = {qf[0] - u.x, qf[1] - u.y, qf[2] - u.z};
   const float ab[3] = {u.w, v.x, v.y}, ac[3] = {v.z, v.w, w.x};
   const float cx = ab[1] * ac[2] - ab[2] * ac[1], cy = ab[2] * ac[0] - ab[0] * ac[2], cz = ab[0] * ac[1] - ab[1] * ac[0];
   const float lab = ab[0] * ab[0] + ab[1] * ab[1] + ab[2] * ab[2], lac = ac[0] * ac[0] + ac[1] * ac[1] + ac[2] * ac[2];
-  if (cx * cx + cy * cy + cz * cz >= 1e-4f * lab * lac) {
-    const float L = fabsf(qa[0]) + fabsf(qa[1]) + fabsf(qa[2]) + sqrtf(lab) + sqrtf(lac);
-    const float abs_scale = 1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]);
-    return sqrtf(tri_d2f(qa, ab, ac)) - 1e-4f * L - 1e-6f * abs_scale;
+  const float c2 = cx * cx + cy * cy + cz * cz;
+  const float L = fabsf(qa[0]) + fabsf(qa[1]) + fabsf(qa[2]) + sqrtf(lab) + sqrtf(lac);
+  const float abs_scale = 1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]);
+  const float m = 1e-4f * L + 1e-6f * abs_scale;
+  if (!(c2 >= 1e-12f * lab * lac)) {
+    const float qb[3] = {qa[0] - ab[0], qa[1] - ab[1], qa[2] - ab[2]}, qc[3] = {qa[0] - ac[0], qa[1] - ac[1], qa[2] - ac[2]};
+    const float da = qa[0] * qa[0] + qa[1] * qa[1] + qa[2] * qa[2], db = qb[0] * qb[0] + qb[1] * qb[1] + qb[2] * qb[2],
+                dc = qc[0] * qc[0] + qc[1] * qc[1] + qc[2] * qc[2];
+    lo = boxd;
+    hi = sqrtf(fmaxf(fmaxf(da, db), dc)) + m;
+    return;
   }
-  return boxd;
+  const float n[3] = {w.y, w.z, w.w};
+  const float d = n[0] * qa[0] + n[1] * qa[1] + n[2] * qa[2];
+  const float ad = fabsf(d);
+  const float p[3] = {qa[0] - n[0] * d, qa[1] - n[1] * d, qa[2] - n[2] * d};
+  const float P0[3] = {0.f, 0.f, 0.f};
+  const float tb = m + 3e-6f * abs_scale;
+  const float lbc = sqrtf((ac[0] - ab[0]) * (ac[0] - ab[0]) + (ac[1] - ab[1]) * (ac[1] - ab[1]) + (ac[2] - ab[2]) * (ac[2] - ab[2]));
+  const float t0 = tb * lbc, t1 = tb * sqrtf(lac), t2 = tb * sqrtf(lab);
+  const float b0 = edge_side(ab, ac, p, n), b1 = edge_side(ac, P0, p, n), b2 = edge_side(P0, ab, p, n);
+  if (MODE == 0) {
+    const float smin = fminf(fminf(seg_df(qa, ab, ac), seg_df(qa, ac, P0)), seg_df(qa, P0, ab));
+    const bool maybe_in = b0 > -t0 && b1 > -t1 && b2 > -t2;
+    const bool surely_in = b0 > t0 && b1 > t1 && b2 > t2;
+    lo = (maybe_in ? fminf(ad, smin) : smin) - m;
+    hi = (surely_in ? fminf(ad, smin) : smin) + m;
+    return;
+  }
+  lo = ad - m;
+  hi = INFINITY;
+  float val;
+  if (fabsf(b0) <= t0) return;
+  if (b0 < 0.f) { val = seg_df(qa, ab, ac); }
+  else if (fabsf(b1) <= t1) return;
+  else if (b1 < 0.f) { val = seg_df(qa, ac, P0); }
+  else if (fabsf(b2) <= t2) return;
+  else if (b2 < 0.f) { val = seg_df(qa, P0, ab); }
+  else {
+    // all three tests pass: interior unless the smallest is under 1e-6 of twice the area
+    const float T = 1e-6f * sqrtf(c2);
+    const float bm = fminf(fminf(b0, b1), b2);
+    const float tm = fmaxf(fmaxf(t0, t1), t2) + 1e-4f * T;
+    if (bm > T + tm) val = ad;
+    else if (bm < T - tm) {
+      // the smallest test picks the edge; a near tie between two of them is undecided
+      const int k = (bm == b0) ? 0 : (bm == b1 ? 1 : 2);
+      const float o1 = k == 0 ? b1 : b0, o2 = k == 2 ? b1 : b2;
+      if (fminf(o1, o2) - bm <= 2.f * tm) return;
+      val = k == 0 ? seg_df(qa, ab, ac) : (k == 1 ? seg_df(qa, ac, P0) : seg_df(qa, P0, ab));
+    } else {
+      return;
+    }
+  }
+  lo = fmaxf(lo, val - m);
+  hi = val + m;
 }
 
 struct EPFace {
@@ -283,17 +350,12 @@ __device__ void ep_setup(const double P[3][3], EPFace &e) {
   for (int c = 0; c < 3; c++)
 #pragma unroll
     for (int d = 0; d < 3; d++) e.p[c][d] = P[c][d];
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    e.edge[0][d] = P[1][d] - P[0][d];
-    e.edge[1][d] = P[2][d] - P[1][d];
-    e.edge[2][d] = P[0][d] - P[2][d];
-  }
-  e.dir[0] = e.edge[0][1] * e.edge[1][2] - e.edge[0][2] * e.edge[1][1];
-  e.dir[1] = e.edge[0][2] * e.edge[1][0] - e.edge[0][0] * e.edge[1][2];
-  e.dir[2] = e.edge[0][0] * e.edge[1][1] - e.edge[0][1] * e.edge[1][0];
-  e.off = e.dir[0] * P[0][0] + e.dir[1] * P[0][1] + e.dir[2] * P[0][2];
-  const double nn = sqrt(e.dir[0] * e.dir[0] + e.dir[1] * e.dir[1] + e.dir[2] * e.dir[2]);
+  nsub3(P[1], P[0], e.edge[0]);
+  nsub3(P[2], P[1], e.edge[1]);
+  nsub3(P[0], P[2], e.edge[2]);
+  ncross(e.edge[0], e.edge[1], e.dir);
+  e.off = ndot(e.dir, P[0]);
+  const double nn = sqrt(ndot(e.dir, e.dir));
   if (nn > 0) { e.dir[0] /= nn; e.dir[1] /= nn; e.dir[2] /= nn; e.off /= nn; }
   const double nx = fabs(e.dir[0]), ny = fabs(e.dir[1]), nz = fabs(e.dir[2]);
   double s;
@@ -303,36 +365,40 @@ __device__ void ep_setup(const double P[3][3], EPFace &e) {
 #pragma unroll
   for (int c = 0; c < 3; c++)
 #pragma unroll
-    for (int d = 0; d < 3; d++) e.edge[c][d] *= s;
-  const double a0 = P[1][0] - P[0][0], a1 = P[1][1] - P[0][1], a2 = P[1][2] - P[0][2];
-  const double b0 = P[2][0] - P[0][0], b1 = P[2][1] - P[0][1], b2 = P[2][2] - P[0][2];
-  const double c0 = a1 * b2 - a2 * b1, c1 = a2 * b0 - a0 * b2, c2 = a0 * b1 - a1 * b0;
-  e.darea = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+    for (int d = 0; d < 3; d++) e.edge[c][d] = nmul(e.edge[c][d], s);
+  double a[3], b[3], x[3];
+  nsub3(P[1], P[0], a);
+  nsub3(P[2], P[0], b);
+  ncross(a, b, x);
+  e.darea = sqrt(ndot(x, x));
 }
 
 __device__ __forceinline__ double ps_dist(const double q[3], const double *v1, const double *v2) {
-  const double e[3] = {v2[0] - v1[0], v2[1] - v1[1], v2[2] - v1[2]};
-  double t = ((q[0] - v1[0]) * e[0] + (q[1] - v1[1]) * e[1] + (q[2] - v1[2]) * e[2]) / (e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+  double e[3], qv[3], pp[3];
+  nsub3(v2, v1, e);
+  nsub3(q, v1, qv);
+  double t = ndot(qv, e) / ndot(e, e);
   t = t < 0 ? 0 : (t > 1 ? 1 : t);
-  const double d0 = q[0] - (v1[0] + e[0] * t), d1 = q[1] - (v1[1] + e[1] * t), d2 = q[2] - (v1[2] + e[2] * t);
-  return sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+#pragma unroll
+  for (int d = 0; d < 3; d++) pp[d] = nsub(q[d], nadd(v1[d], nmul(e[d], t)));
+  return sqrt(ndot(pp, pp));
 }
 
 __device__ void point_distance_ep(const EPFace &f, const double q[3], double &dist) {
   const double EPS = 0.000001;
-  const double d = f.dir[0] * q[0] + f.dir[1] * q[1] + f.dir[2] * q[2] - f.off;
+  const double d = nsub(ndot(f.dir, q), f.off);
   if (d > dist || d < -dist) return;
-  const double p[3] = {q[0] - f.dir[0] * d, q[1] - f.dir[1] * d, q[2] - f.dir[2] * d};
+  const double p[3] = {nsub(q[0], nmul(f.dir[0], d)), nsub(q[1], nmul(f.dir[1], d)), nsub(q[2], nmul(f.dir[2], d))};
   const int i1 = f.axis == 0 ? 1 : (f.axis == 1 ? 2 : 0), i2 = f.axis == 0 ? 2 : (f.axis == 1 ? 0 : 1);
-  const double b0 = f.edge[1][i1] * (p[i2] - f.p[1][i2]) - f.edge[1][i2] * (p[i1] - f.p[1][i1]);
+  const double b0 = nsub(nmul(f.edge[1][i1], nsub(p[i2], f.p[1][i2])), nmul(f.edge[1][i2], nsub(p[i1], f.p[1][i1])));
   if (b0 <= 0) { const double x = ps_dist(q, f.p[1], f.p[2]); if (dist > x) dist = x; return; }
-  const double b1 = f.edge[2][i1] * (p[i2] - f.p[2][i2]) - f.edge[2][i2] * (p[i1] - f.p[2][i1]);
+  const double b1 = nsub(nmul(f.edge[2][i1], nsub(p[i2], f.p[2][i2])), nmul(f.edge[2][i2], nsub(p[i1], f.p[2][i1])));
   if (b1 <= 0) { const double x = ps_dist(q, f.p[2], f.p[0]); if (dist > x) dist = x; return; }
-  const double b2 = f.edge[0][i1] * (p[i2] - f.p[0][i2]) - f.edge[0][i2] * (p[i1] - f.p[0][i1]);
+  const double b2 = nsub(nmul(f.edge[0][i1], nsub(p[i2], f.p[0][i2])), nmul(f.edge[0][i2], nsub(p[i1], f.p[0][i1])));
   if (b2 <= 0) { const double x = ps_dist(q, f.p[0], f.p[1]); if (dist > x) dist = x; return; }
   double b = fmin(b0, b1);
   b = fmin(b, b2);
-  if (b < EPS * f.darea) {
+  if (b < nmul(EPS, f.darea)) {
     double bt;
     if (b == b0) bt = ps_dist(q, f.p[1], f.p[2]);
     else if (b == b1) bt = ps_dist(q, f.p[2], f.p[0]);
@@ -342,7 +408,6 @@ __device__ void point_distance_ep(const EPFace &f, const double q[3], double &di
   }
   dist = fabs(d);
 }
-
 
 // ---- traversal over packed nodes ----
 // Each internal node is one 64-byte record with both children's boxes and ids, so a step is one
@@ -359,36 +424,65 @@ __device__ __forceinline__ NodeRec load_node(const float4 *node, int32_t i) {
   return r;
 }
 
-// Leaf evaluation shared by both traversals.  MODE 0: closest point (squared distance, strict
-// improvement); MODE 1: PointDistanceEP from the current best as the upper bound.
+// Exact FP64 evaluation of one leaf against the running best.  MODE 0: closest point (squared
+// distance, strict improvement); MODE 1: PointDistanceEP from the current best as the upper bound.
 template <int MODE>
-__device__ __forceinline__ bool eval_leaf(const BvhDev &b, int32_t leaf, float boxd, const double q[3], const float qf[3],
-                                          float bestd, double best, double &cand, int32_t &cf, double cc[3]) {
-  if (leaf_lower_bound(b.leafd, leaf, qf, boxd) > bestd) return false;
+__device__ __forceinline__ void eval_exact(const BvhDev &b, int32_t leaf, const double q[3], double &best, int32_t &bf,
+                                           double bc[3]) {
   const int32_t f = b.leaf_face[leaf];
   double P[3][3];
   face_pts(b, f, P);
   if (MODE == 0) {
     double c[3];
     closest_pt_tri(q, P[0], P[1], P[2], c);
-    const double e0 = q[0] - c[0], e1 = q[1] - c[1], e2 = q[2] - c[2];
-    cand = e0 * e0 + e1 * e1 + e2 * e2;
-    cf = f;
-    cc[0] = c[0]; cc[1] = c[1]; cc[2] = c[2];
+    double e[3];
+    nsub3(q, c, e);
+    const double cand = ndot(e, e);
+    if (cand < best) { best = cand; bf = f; bc[0] = c[0]; bc[1] = c[1]; bc[2] = c[2]; }
   } else {
     EPFace fe;
     ep_setup(P, fe);
-    double dd = best;
-    point_distance_ep(fe, q, dd);
-    cand = dd;
+    point_distance_ep(fe, q, best);
   }
-  return true;
 }
 
 template <int MODE>
 __device__ __forceinline__ float dist_bound(double x) {
   if (isinf(x)) return INFINITY;
   return MODE == 0 ? __double2float_ru(sqrt(x)) : __double2float_ru(x);
+}
+
+// Deferred exact evaluation.  The traversal keeps `ub`, an FP32 upper bound of the minimum
+// (the smallest leaf `hi` seen, or the exact best rounded up), prunes on it, and records the
+// leaves whose `lo` is within it in visiting order.  At the end only the recorded leaves whose
+// `lo` is still within the final `ub` are evaluated in FP64, in the same order, with the same
+// strict-improvement rule: every leaf left out has an exact distance above the minimum, so the
+// result (distance, and face and point for MODE 0) is the one evaluating every visited leaf in
+// FP64 gives.  A full list is first compacted, then evaluated and emptied.
+constexpr int kCand = 8;
+
+template <int MODE>
+__device__ __forceinline__ void flush_cands(const BvhDev &b, const double q[3], int32_t *cl, float *cb, int &nc, float &ub,
+                                            double &best, int32_t &bf, double bc[3]) {
+  for (int k = 0; k < nc; k++)
+    if (cb[k] <= ub) eval_exact<MODE>(b, cl[k], q, best, bf, bc);
+  nc = 0;
+  ub = fminf(ub, dist_bound<MODE>(best));
+}
+
+template <int MODE>
+__device__ __forceinline__ void add_cand(const BvhDev &b, const double q[3], int32_t leaf, float lo, int32_t *cl, float *cb,
+                                         int &nc, float &ub, double &best, int32_t &bf, double bc[3]) {
+  if (nc == kCand) {
+    int w = 0;
+    for (int k = 0; k < nc; k++)
+      if (cb[k] <= ub) { cl[w] = cl[k]; cb[w] = cb[k]; w++; }
+    nc = w;
+    if (nc == kCand) flush_cands<MODE>(b, q, cl, cb, nc, ub, best, bf, bc);
+  }
+  cl[nc] = leaf;
+  cb[nc] = lo;
+  nc++;
 }
 
 // Per-thread depth-first traversal with at most `budget` pops.  Returns 0 when done, 1 on stack
@@ -399,38 +493,37 @@ __device__ int thread_traverse(const BvhDev &b, const double q[3], double &best,
   const int n = b.n;
   const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
   const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
-  float bestd = dist_bound<MODE>(best);
+  float ub = dist_bound<MODE>(best);
   if (n == 1) {
-    double cand = INFINITY, cc[3];
-    int32_t cf = -1;
-    if (eval_leaf<MODE>(b, 0, -INFINITY, q, qf, bestd, best, cand, cf, cc) && cand < best) {
-      best = cand;
-      if (MODE == 0) { bf = cf; bc[0] = cc[0]; bc[1] = cc[1]; bc[2] = cc[2]; }
-    }
+    eval_exact<MODE>(b, 0, q, best, bf, bc);
     return 0;
   }
+  int32_t cl[kCand];
+  float cb[kCand];
+  int nc = 0;
   int32_t sn[kStack];
   float sd[kStack];
   int sp = 0, pops = 0;
   bool ok = true;
   sn[sp] = 0; sd[sp] = 0.f; sp++;
   while (sp > 0) {
-    if (pops >= budget) return 2;
+    if (pops >= budget) {
+      flush_cands<MODE>(b, q, cl, cb, nc, ub, best, bf, bc);
+      return 2;
+    }
     --sp;
     const int32_t node = sn[sp];
     const float d = sd[sp];
     pops++;
-    if (d > bestd) continue;
+    if (d > ub) continue;
     if (node < 0) {
       const int32_t leaf = ~node;
       if (leaf >= n) { ok = false; continue; }
-      double cand = INFINITY, cc[3];
-      int32_t cf = -1;
-      if (eval_leaf<MODE>(b, leaf, d, q, qf, bestd, best, cand, cf, cc) && cand < best) {
-        best = cand;
-        if (MODE == 0) { bf = cf; bc[0] = cc[0]; bc[1] = cc[1]; bc[2] = cc[2]; }
-        bestd = dist_bound<MODE>(best);
-      }
+      float lo, hi;
+      leaf_bounds<MODE>(b.leafd, leaf, qf, d, lo, hi);
+      if (lo > ub) continue;
+      ub = fminf(ub, hi);
+      add_cand<MODE>(b, q, leaf, lo, cl, cb, nc, ub, best, bf, bc);
       continue;
     }
     if (node >= n - 1) { ok = false; continue; }
@@ -441,15 +534,18 @@ __device__ int thread_traverse(const BvhDev &b, const double q[3], double &best,
     const bool lnear = dl <= dr;
     const int32_t nearc = lnear ? r.l : r.r, farc = lnear ? r.r : r.l;
     const float dn = lnear ? dl : dr, df = lnear ? dr : dl;
-    if (df <= bestd) { if (sp < kStack) { sn[sp] = farc; sd[sp] = df; sp++; } else ok = false; }
-    if (dn <= bestd) { if (sp < kStack) { sn[sp] = nearc; sd[sp] = dn; sp++; } else ok = false; }
+    if (df <= ub) { if (sp < kStack) { sn[sp] = farc; sd[sp] = df; sp++; } else ok = false; }
+    if (dn <= ub) { if (sp < kStack) { sn[sp] = nearc; sd[sp] = dn; sp++; } else ok = false; }
   }
+  flush_cands<MODE>(b, q, cl, cb, nc, ub, best, bf, bc);
   return ok ? 0 : 1;
 }
 
 // Warp-cooperative traversal for the queries left over by the per-thread pass: one query per
-// warp, up to 32 frontier entries per step (one per lane), LIFO frontier in shared memory.
+// warp, up to 32 frontier entries per step (one per lane), LIFO frontier in shared memory, and
+// the deferred candidate list (kWarpCand entries, in (step, lane) order) in shared memory too.
 constexpr int kWarpStack = 1024;
+constexpr int kWarpCand = 64;
 
 __device__ __forceinline__ int warp_excl_scan(int v, int &total) {
   const int lane = threadIdx.x & 31;
@@ -463,16 +559,59 @@ __device__ __forceinline__ int warp_excl_scan(int v, int &total) {
   return x - v;
 }
 
+// Evaluates the warp's recorded candidates with lo <= ub: lane k takes entries k, k + 32; the
+// winner is the smallest exact value, ties to the earliest entry, kept only on strict
+// improvement of `best` -- the sequential rule.  MODE 1 evaluates every entry from the best at
+// entry time, as PointDistanceEP takes its bound.
 template <int MODE>
-__device__ bool warp_traverse(const BvhDev &b, const double q[3], int32_t *sn, float *sd, double &best, int32_t &bf,
-                              double bc[3]) {
+__device__ void warp_flush(const BvhDev &b, const double q[3], const int32_t *cl, const float *cb, int nc, float &ub,
+                           double &best, int32_t &bf, double bc[3]) {
+  const int lane = threadIdx.x & 31;
+  double vbest = INFINITY;
+  int kbest = 0x7fffffff;
+  int32_t fbest = -1;
+  double cbest[3] = {0, 0, 0};
+  for (int k = lane; k < nc; k += 32) {
+    if (cb[k] > ub) continue;
+    double v = best;
+    int32_t f = -1;
+    double c[3];
+    eval_exact<MODE>(b, cl[k], q, v, f, c);
+    if (v < best && v < vbest) {
+      vbest = v; kbest = k; fbest = f;
+      cbest[0] = c[0]; cbest[1] = c[1]; cbest[2] = c[2];
+    }
+  }
+  double m = vbest;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (m < best) {
+    int kk = vbest == m ? kbest : 0x7fffffff;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) kk = min(kk, __shfl_xor_sync(0xffffffffu, kk, o));
+    const unsigned who = __ballot_sync(0xffffffffu, vbest == m && kbest == kk);
+    const int src = __ffs(who) - 1;
+    if (MODE == 0) {
+      bf = __shfl_sync(0xffffffffu, fbest, src);
+      bc[0] = __shfl_sync(0xffffffffu, cbest[0], src);
+      bc[1] = __shfl_sync(0xffffffffu, cbest[1], src);
+      bc[2] = __shfl_sync(0xffffffffu, cbest[2], src);
+    }
+    best = m;
+  }
+  ub = fminf(ub, dist_bound<MODE>(best));
+}
+
+template <int MODE>
+__device__ bool warp_traverse(const BvhDev &b, const double q[3], int32_t *sn, float *sd, int32_t *cl, float *cb,
+                              double &best, int32_t &bf, double bc[3]) {
   const int lane = threadIdx.x & 31;
   const int n = b.n;
   const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
   const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
-  float bestd = dist_bound<MODE>(best);
+  float ub = dist_bound<MODE>(best);
   bool ok = true;
-  int sz = 1;
+  int sz = 1, nc = 0;
   if (lane == 0) { sn[0] = n == 1 ? ~0 : 0; sd[0] = -INFINITY; }
   __syncwarp();
   for (int guard = 0; sz > 0 && guard < 4 * (2 * n + 64); guard++) {
@@ -482,17 +621,20 @@ __device__ bool warp_traverse(const BvhDev &b, const double q[3], int32_t *sn, f
     const float d = has ? sd[sz - take + lane] : INFINITY;
     __syncwarp();
     sz -= take;
-    double cand = INFINITY;
-    int32_t cf = -1;
-    double cc[3] = {0, 0, 0};
     int32_t push[2];
     float pd[2];
     int np = 0;
-    if (has && d <= bestd) {
+    bool cand = false;
+    float lo = INFINITY, hi = INFINITY;
+    if (has && d <= ub) {
       if (node < 0) {
         const int32_t leaf = ~node;
-        if (leaf < n) eval_leaf<MODE>(b, leaf, d, q, qf, bestd, best, cand, cf, cc);
-        else ok = false;
+        if (leaf < n) {
+          leaf_bounds<MODE>(b.leafd, leaf, qf, d, lo, hi);
+          cand = true;
+        } else {
+          ok = false;
+        }
       } else if (node < n - 1) {
         const NodeRec r = load_node(b.node, node);
         if (r.l >= n - 1 || r.r >= n - 1 || ~r.l >= n || ~r.r >= n) {
@@ -502,27 +644,51 @@ __device__ bool warp_traverse(const BvhDev &b, const double q[3], int32_t *sn, f
           const float dr = sqrtf(box_d2f(r.rb, qf)) - mbox;
           const bool lnear = dl <= dr;
           const float dn = lnear ? dl : dr, df = lnear ? dr : dl;
-          if (df <= bestd) { push[np] = lnear ? r.r : r.l; pd[np] = df; np++; }
-          if (dn <= bestd) { push[np] = lnear ? r.l : r.r; pd[np] = dn; np++; }
+          if (df <= ub) { push[np] = lnear ? r.r : r.l; pd[np] = df; np++; }
+          if (dn <= ub) { push[np] = lnear ? r.l : r.r; pd[np] = dn; np++; }
         }
       } else {
         ok = false;
       }
     }
-    double m = cand;
+    // tighten ub by this step's leaves, then record those still within it
+    float h = hi;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (m < best) {
-      if (MODE == 0) {
-        const unsigned who = __ballot_sync(0xffffffffu, cand == m);
-        const int src = __ffs(who) - 1;
-        bf = __shfl_sync(0xffffffffu, cf, src);
-        bc[0] = __shfl_sync(0xffffffffu, cc[0], src);
-        bc[1] = __shfl_sync(0xffffffffu, cc[1], src);
-        bc[2] = __shfl_sync(0xffffffffu, cc[2], src);
+    for (int o = 16; o > 0; o >>= 1) h = fminf(h, __shfl_xor_sync(0xffffffffu, h, o));
+    ub = fminf(ub, h);
+    const bool rec = cand && lo <= ub;
+    const unsigned rb = __ballot_sync(0xffffffffu, rec);
+    const int nrec = __popc(rb);
+    if (nrec > 0) {
+      if (nc + nrec > kWarpCand) {
+        // compact in order, then evaluate if still too full
+        int w = 0;
+        for (int k0 = 0; k0 < nc; k0 += 32) {
+          const int k = k0 + lane;
+          const bool keep = k < nc && cb[k] <= ub;
+          const unsigned kb = __ballot_sync(0xffffffffu, keep);
+          int32_t lk = keep ? cl[k] : 0;
+          float bk = keep ? cb[k] : 0.f;
+          __syncwarp();
+          if (keep) {
+            const int pos = w + __popc(kb & ((1u << lane) - 1u));
+            cl[pos] = lk; cb[pos] = bk;
+          }
+          w += __popc(kb);
+          __syncwarp();
+        }
+        nc = w;
+        if (nc + nrec > kWarpCand) {
+          warp_flush<MODE>(b, q, cl, cb, nc, ub, best, bf, bc);
+          nc = 0;
+        }
+        __syncwarp();
       }
-      best = m;
-      bestd = dist_bound<MODE>(best);
+      if (rec) {
+        const int pos = nc + __popc(rb & ((1u << lane) - 1u));
+        cl[pos] = ~node; cb[pos] = lo;
+      }
+      nc += nrec;
     }
     int total;
     const int off = warp_excl_scan(np, total);
@@ -534,6 +700,8 @@ __device__ bool warp_traverse(const BvhDev &b, const double q[3], int32_t *sn, f
     sz += total < room ? total : room;
   }
   if (sz > 0) ok = false;
+  __syncwarp();
+  warp_flush<MODE>(b, q, cl, cb, nc, ub, best, bf, bc);
   return __all_sync(0xffffffffu, ok);
 }
 
@@ -552,21 +720,22 @@ __device__ void pseudonormal(const TargetDev &t, int32_t f, const double c[3], d
   double A[3], B[3], C[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) { A[d] = t.tri[(int64_t)f * 9 + d]; B[d] = t.tri[(int64_t)f * 9 + 3 + d]; C[d] = t.tri[(int64_t)f * 9 + 6 + d]; }
-  const double e1[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]}, e2[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
-  const double x0 = e1[1] * e2[2] - e1[2] * e2[1], x1 = e1[2] * e2[0] - e1[0] * e2[2], x2 = e1[0] * e2[1] - e1[1] * e2[0];
-  const double area = sqrt(x0 * x0 + x1 * x1 + x2 * x2);  // doublearea
+  double e1[3], e2[3], x[3];
+  nsub3(B, A, e1);
+  nsub3(C, A, e2);
+  ncross(e1, e2, x);
+  const double area = sqrt(ndot(x, x));  // doublearea
   const double epsilon = 1e-12;
   int kind = 0, which = 0;  // 0 face, 1 vertex (which corner), 2 edge (opposite which corner)
   if (area > 1e-4) {
-    const double v2[3] = {c[0] - A[0], c[1] - A[1], c[2] - A[2]};
-    const double d00 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2], d01 = e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2];
-    const double d11 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
-    const double d20 = v2[0] * e1[0] + v2[1] * e1[1] + v2[2] * e1[2], d21 = v2[0] * e2[0] + v2[1] * e2[1] + v2[2] * e2[2];
-    const double den = d00 * d11 - d01 * d01;
+    double v2[3];
+    nsub3(c, A, v2);
+    const double d00 = ndot(e1, e1), d01 = ndot(e1, e2), d11 = ndot(e2, e2), d20 = ndot(v2, e1), d21 = ndot(v2, e2);
+    const double den = nsub(nmul(d00, d11), nmul(d01, d01));
     double bb[3];
-    bb[1] = (d11 * d20 - d01 * d21) / den;
-    bb[2] = (d00 * d21 - d01 * d20) / den;
-    bb[0] = 1.0 - (bb[1] + bb[2]);
+    bb[1] = nsub(nmul(d11, d20), nmul(d01, d21)) / den;
+    bb[2] = nsub(nmul(d00, d21), nmul(d01, d20)) / den;
+    bb[0] = nsub(1.0, nadd(bb[1], bb[2]));
     const int type = (bb[0] <= epsilon) + (bb[1] <= epsilon) + (bb[2] <= epsilon);
     if (type == 2) {
       kind = 1;
@@ -579,27 +748,29 @@ __device__ void pseudonormal(const TargetDev &t, int32_t f, const double c[3], d
     const double *P[3] = {A, B, C};
     bool found = false;
     for (int v = 0; v < 3 && !found; v++) {
-      const double dx = c[0] - P[v][0], dy = c[1] - P[v][1], dz = c[2] - P[v][2];
-      if (sqrt(dx * dx + dy * dy + dz * dz) < epsilon) { found = true; kind = 1; which = v; }
+      double dv[3];
+      nsub3(c, P[v], dv);
+      if (sqrt(ndot(dv, dv)) < epsilon) { found = true; kind = 1; which = v; }
     }
     for (int e = 0; e < 3 && !found; e++) {
-      const double *s = P[(e + 1) % 3], *dd = P[(e + 2) % 3];
-      const double dms[3] = {dd[0] - s[0], dd[1] - s[1], dd[2] - s[2]};
-      const double smp[3] = {s[0] - c[0], s[1] - c[1], s[2] - c[2]};
-      const double vl = dms[0] * dms[0] + dms[1] * dms[1] + dms[2] * dms[2];
-      const double tt = -(dms[0] * smp[0] + dms[1] * smp[1] + dms[2] * smp[2]) / vl;
-      double sq;
+      const double *sp = P[(e + 1) % 3], *dp = P[(e + 2) % 3];
+      double dms[3], smp[3];
+      nsub3(dp, sp, dms);
+      nsub3(sp, c, smp);
+      const double vl = ndot(dms, dms);
+      const double tt = -ndot(dms, smp) / vl;
+      double z[3];
       if (tt < 0) {
-        sq = smp[0] * smp[0] + smp[1] * smp[1] + smp[2] * smp[2];
+        nsub3(c, sp, z);
       } else if (tt > 1) {
-        const double z0 = c[0] - dd[0], z1 = c[1] - dd[1], z2 = c[2] - dd[2];
-        sq = z0 * z0 + z1 * z1 + z2 * z2;
+        nsub3(c, dp, z);
       } else {
-        const double pr0 = (1.0 - tt) * s[0] + tt * dd[0], pr1 = (1.0 - tt) * s[1] + tt * dd[1], pr2 = (1.0 - tt) * s[2] + tt * dd[2];
-        const double m0 = c[0] - pr0, m1 = c[1] - pr1, m2 = c[2] - pr2;
-        sq = m0 * m0 + m1 * m1 + m2 * m2;
+        const double pr[3] = {nadd(nmul(nsub(1.0, tt), sp[0]), nmul(tt, dp[0])),
+                              nadd(nmul(nsub(1.0, tt), sp[1]), nmul(tt, dp[1])),
+                              nadd(nmul(nsub(1.0, tt), sp[2]), nmul(tt, dp[2]))};
+        nsub3(c, pr, z);
       }
-      if (sqrt(sq) < epsilon) { found = true; kind = 2; which = e; }
+      if (sqrt(ndot(z, z)) < epsilon) { found = true; kind = 2; which = e; }
     }
   }
   const double *src = kind == 0 ? t.FN + 3 * (int64_t)f : kind == 1 ? t.VNc + 9 * (int64_t)f + 3 * which : t.ENc + 9 * (int64_t)f + 3 * which;
@@ -642,6 +813,8 @@ __global__ void __launch_bounds__(128) k_project(ProjArgs p) {
 __global__ void __launch_bounds__(128) k_project_warp(ProjArgs p) {
   __shared__ int32_t sn[4][kWarpStack];
   __shared__ float sd[4][kWarpStack];
+  __shared__ int32_t scl[4][kWarpCand];
+  __shared__ float scb[4][kWarpCand];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned cnt = *p.ovf.count;
   for (unsigned k = warp_global(); k < cnt; k += warps_total()) {
@@ -654,7 +827,7 @@ __global__ void __launch_bounds__(128) k_project_warp(ProjArgs p) {
     const double q[3] = {p.X[4 * v], p.X[4 * v + 1], p.X[4 * v + 2]};
     double best = p.ovf.best[i], c[3] = {p.ovf.pt[3 * i], p.ovf.pt[3 * i + 1], p.ovf.pt[3 * i + 2]};
     int32_t f = p.ovf.face[i];
-    const bool ok = warp_traverse<0>(t.bvh, q, sn[w], sd[w], best, f, c);
+    const bool ok = warp_traverse<0>(t.bvh, q, sn[w], sd[w], scl[w], scb[w], best, f, c);
     if (lane == 0) {
       if (!ok) atomicOr(&p.sc[m].status, 8);
       write_tangent(p, t, e, f, c);
@@ -675,7 +848,9 @@ __global__ void __launch_bounds__(128) k_signed_distance(TargetDev t, int64_t np
   double s = 1;
   if (f >= 0) {
     pseudonormal(t, f, c, n);
-    s = ((q[0] - c[0]) * n[0] + (q[1] - c[1]) * n[1] + (q[2] - c[2]) * n[2]) >= 0 ? 1. : -1.;
+    double qc[3];
+    nsub3(q, c, qc);
+    s = ndot(qc, n) >= 0 ? 1. : -1.;
   }
   S[i] = s * sqrt(best);
   I[i] = f;
@@ -805,6 +980,8 @@ template <int SIDE>
 __global__ void __launch_bounds__(128) k_haus_warp(HausArgs h) {
   __shared__ int32_t sn[4][kWarpStack];
   __shared__ float sd[4][kWarpStack];
+  __shared__ int32_t scl[4][kWarpCand];
+  __shared__ float scb[4][kWarpCand];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned cnt = *h.ovf.count;
   for (unsigned k = warp_global(); k < cnt; k += warps_total()) {
@@ -816,7 +993,7 @@ __global__ void __launch_bounds__(128) k_haus_warp(HausArgs h) {
     double dist = h.ovf.best[i];
     int32_t fd = -1;
     double cd[3];
-    const bool ok = warp_traverse<1>(*b, q, sn[w], sd[w], dist, fd, cd);
+    const bool ok = warp_traverse<1>(*b, q, sn[w], sd[w], scl[w], scb[w], dist, fd, cd);
     if (lane == 0) {
       if (!ok) atomicOr(&h.sc[m].status, 8);
       h.dist[i] = dist;

@@ -206,7 +206,9 @@ HEXOPT_API int hexopt_timer_stop(hexopt_ctx *ctx, double *ms);
 /* Average device time of one launch of a stage, timed with CUDA events over `reps` back-to-back
  * launches on the current state (after slim_precompute / an iteration):
  *   0 element SpMV of the PCG   1 local step   2 line-search energy pass (ls_candidates steps)
- *   3 scaled Jacobian           4 feature projection   5 one full SLIM iteration
+ *   3 scaled-Jacobian check as the feature-alignment loop runs it (FP64 in plain mode; FP32
+ *     screen with FP64 re-evaluation near the minimum in mixed mode)
+ *   4 feature projection        5 one full SLIM iteration
  * Stages 0-2 leave the solver scratch in an unspecified state; positions are not modified by
  * 0-4 (stage 5 advances them like slim_iterate). */
 HEXOPT_API int hexopt_time_stage(hexopt_ctx *ctx, int stage, int reps, double *ms_per_launch);
