@@ -86,6 +86,9 @@ SIGNATURES = {
     "hexopt_set_surface": (C.c_int, [_vp, C.c_int, C.c_int64, _i32]),
     "hexopt_hausdorff_meshes": (C.c_int, [_vp, _d, _d, _d]),
     "hexopt_point_face_distance": (C.c_int, [_vp, C.c_int64, _d, C.c_int64, _d, C.c_int64, _i32, _d]),
+    "hexopt_point_face_distance_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                                     C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_char_p,
+                                                     C.c_size_t]),
     "hexopt_fa_begin": (C.c_int, [_vp, C.POINTER(SlimParams), C.c_double, C.c_double]),
     "hexopt_feature_alignment_step": (C.c_int, [_vp, C.c_int, C.POINTER(FaReport)]),
     "hexopt_use_graph": (C.c_int, [_vp, C.c_int]),
@@ -129,6 +132,21 @@ def ptr(a, t):
 
 class HexoptError(RuntimeError):
     pass
+
+
+def point_face_distance_noalloc(P_dev: int, np_: int, V_dev: int, nv: int, F_dev: int, nf: int, dist_dev: int,
+                                device: int = 0, stream: int = 0):
+    """hexopt_point_face_distance_noalloc on raw device addresses (P_dev np_ x 3 doubles, V_dev
+    nv x 3 doubles, F_dev nf x 3 int32, dist_dev np_ doubles) on `stream` (a cudaStream_t as an
+    int, 0 = legacy default stream); no device allocation.  Raises HexoptError with the library's
+    message on failure."""
+    L = load()
+    buf = C.create_string_buffer(512)
+    rc = L.hexopt_point_face_distance_noalloc(device, C.c_void_p(stream or None), np_, C.c_void_p(P_dev), nv,
+                                              C.c_void_p(V_dev), nf, C.c_void_p(F_dev), C.c_void_p(dist_dev), buf,
+                                              len(buf))
+    if rc != 0:
+        raise HexoptError(f"point_face_distance_noalloc failed ({rc}): {buf.value.decode(errors='replace')}")
 
 
 class Context:

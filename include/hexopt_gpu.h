@@ -27,6 +27,7 @@
  */
 #ifndef HEXOPT_GPU_H
 #define HEXOPT_GPU_H
+#include <stddef.h>
 #include <stdint.h>
 #ifdef __cplusplus
 extern "C" {
@@ -214,6 +215,30 @@ HEXOPT_API int hexopt_timer_stop(hexopt_ctx *ctx, double *ms);
 HEXOPT_API int hexopt_time_stage(hexopt_ctx *ctx, int stage, int reps, double *ms_per_launch);
 /* Kernel launches issued by this context since creation (for the bench's launch count). */
 HEXOPT_API int64_t hexopt_launch_count(const hexopt_ctx *ctx);
+
+/* ---- no-allocation variant (no counterpart in the reference) ----
+ * hexopt_point_face_distance on caller-owned DEVICE arrays -- P_dev (np x 3), V_dev (nv x 3),
+ * F_dev (nf x 3 vertex ids), dist_dev (np) -- on CUDA device `device` and the caller's `stream`
+ * (a cudaStream_t; NULL = the legacy default stream), with no device allocation: the triangle
+ * soup, the LBVH, the sort workspace and the status word live in one static 80 MiB device array
+ * per device.  For callers that must not allocate or free device memory: cudaFree synchronises
+ * the whole device and stalls work on other streams, and a caller running under a fixed
+ * device-memory budget (a pool that owns the rest of HBM) cannot have a library take memory.
+ * No context is needed (creating one allocates).
+ *   limit:     nf <= 262,144 faces; a larger surface returns HEXOPT_ERR_UNSUPPORTED with both
+ *              sizes in the message (use hexopt_point_face_distance).  np is not limited.
+ *   set-up:    the first call on a device resolves the static array's address, which loads it;
+ *              when that happens lazily it must come before any stream capture on the device,
+ *              so make one small call up front.  The call synchronises `stream` and is not
+ *              itself meant to be captured.
+ *   races:     every call on a device shares that one array: calls overlapping in time (two
+ *              streams, two host threads) race and give wrong results -- serialise them.
+ *   zeroing:   the parts that must start at zero (BVH refit counters, status word) are cleared
+ *              by the call itself on `stream`; nothing is assumed between calls.
+ *   errors:    status as elsewhere; the message goes to err (err_len bytes, may be NULL). */
+HEXOPT_API int hexopt_point_face_distance_noalloc(int device, void *stream, int64_t np, const double *P_dev, int64_t nv,
+                                                  const double *V_dev, int64_t nf, const int32_t *F_dev,
+                                                  double *dist_dev, char *err, size_t err_len);
 
 /* ---- aabb.h value types (Ray / AABB, aabb.h:5-115) on the host ---- */
 typedef struct hexopt_aabb { double min[3], max[3]; } hexopt_aabb;
