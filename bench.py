@@ -137,6 +137,11 @@ def spmv_bytes_per_hex(mixed: bool) -> float:
     return 32 + 8 * 6 * w + 4 * w + 2 * 4 * w
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_spmv<float> launch per hex,
+# from an ncu capture on the 96^3 grid (working set above L2; traffic grows with the hex count).
+SPMV_DRAM_BYTES_PER_HEX_MIXED = (231.138560e6 + 10.954496e6) / 96 ** 3
+
+
 def cpu_baseline(steps=None, budget_s=12.0):
     """The oracle (CPU restatement of the reference's FP64 path) on a 32^3 sample of the
     workload, single-threaded; returns (iters/s scaled to the full workload, details)."""
@@ -291,7 +296,8 @@ def run_ours(args):
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nv * 3 * 8,
                    "d2h_bytes_per_step": nv * 3 * 8 + rep_bytes},
            "roofline": {"bound": "hbm", "kernel": "k_spmv (element SpMV of the PCG)", "achieved": achieved,
-                        "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                        "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "traffic": SPMV_DRAM_BYTES_PER_HEX_MIXED * nh if mixed else None,
                         "peak_kind": peak_kind, "kernel_ms": spmv_ms,
                         "bytes_per_hex": spmv_bytes_per_hex(mixed)},
            "stages": stages}
