@@ -40,7 +40,8 @@ def dist_init():
     if ws > 1:
         import torch.distributed as tdist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        tdist.init_process_group("gloo", rank=rank, world_size=ws)
+        if not tdist.is_initialized():
+            tdist.init_process_group("gloo", rank=rank, world_size=ws)
         return rank, ws, tdist
     return 0, 1, None
 
