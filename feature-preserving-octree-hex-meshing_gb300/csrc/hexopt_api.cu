@@ -128,6 +128,9 @@ struct hexopt_ctx {
   std::vector<SurfaceHost> surf;
   DBuf tgt_d, surf_d, hm_d, tgt_vs_d, surf_vs_d;
   DBuf ovf_item, ovf_mesh, ovf_count, ovf_best, ovf_face, ovf_pt, hdist;
+  // batched exact evaluation of the BVH queries (shared by projection and both Hausdorff sides)
+  DBuf cand_leaf, cand_qi, cand_x, cand_d, cand_count, q_off, q_cnt, qpos, q_mesh, fb_count, fb_item, fb_mesh;
+  int64_t cand_cap = 0;
   std::vector<int64_t> tgt_vs_cnt, surf_vs_cnt;
   bool haus_ready = false;
   // feature alignment
@@ -461,7 +464,41 @@ int ensure_query_buffers(hexopt_ctx *ctx) {
   CK(ctx->ovf_face.ensure(sizeof(int32_t) * n));
   CK(ctx->ovf_pt.ensure(sizeof(double) * 3 * n));
   CK(ctx->hdist.ensure(sizeof(double) * n));
+  // up to kQueryCandidates recorded candidates per query on average (a query over its share goes
+  // to the exact fallback)
+  constexpr int64_t kQueryCandidates = 16;
+  ctx->cand_cap = kQueryCandidates * n;
+  CK(ctx->cand_leaf.ensure(sizeof(int32_t) * ctx->cand_cap));
+  CK(ctx->cand_qi.ensure(sizeof(int32_t) * ctx->cand_cap));
+  CK(ctx->cand_x.ensure(sizeof(double) * ctx->cand_cap));
+  CK(ctx->cand_d.ensure(sizeof(double) * ctx->cand_cap));
+  CK(ctx->cand_count.ensure(sizeof(unsigned)));
+  CK(ctx->q_off.ensure(sizeof(int32_t) * n));
+  CK(ctx->q_cnt.ensure(sizeof(int32_t) * n));
+  CK(ctx->qpos.ensure(sizeof(double) * 3 * n));
+  CK(ctx->q_mesh.ensure(sizeof(int32_t) * n));
+  CK(ctx->fb_count.ensure(sizeof(unsigned)));
+  CK(ctx->fb_item.ensure(sizeof(int64_t) * n));
+  CK(ctx->fb_mesh.ensure(sizeof(int32_t) * n));
   return HEXOPT_OK;
+}
+
+CandBuf make_cand(hexopt_ctx *c) {
+  CandBuf b{};
+  b.leaf = c->cand_leaf.as<int32_t>();
+  b.qi = c->cand_qi.as<int32_t>();
+  b.x = c->cand_x.as<double>();
+  b.d = c->cand_d.as<double>();
+  b.count = c->cand_count.as<unsigned>();
+  b.cap = c->cand_cap;
+  b.q_off = c->q_off.as<int32_t>();
+  b.q_cnt = c->q_cnt.as<int32_t>();
+  b.qpos = c->qpos.as<double>();
+  b.q_mesh = c->q_mesh.as<int32_t>();
+  b.fb_count = c->fb_count.as<unsigned>();
+  b.fb_item = c->fb_item.as<int64_t>();
+  b.fb_mesh = c->fb_mesh.as<int32_t>();
+  return b;
 }
 
 Overflow make_ovf(hexopt_ctx *c) {
@@ -478,6 +515,7 @@ Overflow make_ovf(hexopt_ctx *c) {
 ProjArgs make_proj(hexopt_ctx *c, int kind) {
   ProjArgs p{};
   p.ovf = make_ovf(c);
+  p.cand = make_cand(c);
   p.seg = c->kind[kind].dev.as<Seg>();
   p.mesh = c->md_d.as<MeshDesc>();
   p.sc = c->sc_d.as<MeshScalars>();
@@ -492,6 +530,7 @@ ProjArgs make_proj(hexopt_ctx *c, int kind) {
 HausArgs make_haus(hexopt_ctx *c, int kind) {
   HausArgs h{};
   h.ovf = make_ovf(c);
+  h.cand = make_cand(c);
   h.dist = c->hdist.as<double>();
   h.seg = c->kind[kind].dev.as<Seg>();
   h.mesh = c->md_d.as<MeshDesc>();
@@ -510,7 +549,7 @@ HausArgs make_haus(hexopt_ctx *c, int kind) {
 int run_projection(hexopt_ctx *ctx) {
   if (ctx->NT) {
     launch_project(make_proj(ctx, K_PROJ), ctx->kind[K_PROJ].nblk, ctx->st);
-    ctx->launches += 2;
+    ctx->launches += 5;
   }
   if (ctx->NL) {
     launch_curve_project(make_proj(ctx, K_LINE), ctx->kind[K_LINE].nblk, ctx->st);
@@ -540,7 +579,7 @@ int run_hausdorff(hexopt_ctx *ctx) {
   launch_haus_bbox(make_haus(ctx, K_SURFV), ctx->kind[K_SURFV].nblk, ctx->st);
   launch_haus_side(make_haus(ctx, K_TGTV), 0, ctx->kind[K_TGTV].nblk, ctx->st);
   launch_haus_side(make_haus(ctx, K_SURFV), 1, ctx->kind[K_SURFV].nblk, ctx->st);
-  ctx->launches += 7;
+  ctx->launches += 13;
   CKL();
   return HEXOPT_OK;
 }

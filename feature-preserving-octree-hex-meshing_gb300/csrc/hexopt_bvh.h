@@ -37,6 +37,23 @@ struct Overflow {
   double *pt;        // per query item: closest point (3)
 };
 
+// Batched exact evaluation.  The traversals record, per query, the leaves that FP32 cannot
+// rule out (in visiting order) into one flat list; a dense pass evaluates every entry in FP64
+// (one entry per thread), and a per-query pass applies the sequential improvement rule in
+// recorded order.  Queries whose candidates do not fit go to the exact per-thread fallback.
+struct CandBuf {
+  int32_t *leaf, *qi;     // [cap] leaf (sorted order) and query item of each entry
+  double *x, *d;          // [cap] exact value (squared distance / PointDistanceEP) and plane distance
+  unsigned *count;        // entries used
+  int64_t cap;
+  int32_t *q_off, *q_cnt; // per query item: first entry and entry count (-1: fallback)
+  double *qpos;           // per query item: the query point (3)
+  int32_t *q_mesh;        // per query item: its mesh
+  unsigned *fb_count;     // fallback list: count, items, meshes
+  int64_t *fb_item;
+  int32_t *fb_mesh;
+};
+
 // A mesh's target triangle mesh (mf.tri / tri_tree): geometry, per-face normals of
 // build_aabb_tree, and the feature curves as polylines over its vertices.
 struct TargetDev {
@@ -53,6 +70,7 @@ struct TargetDev {
 
 struct ProjArgs {
   Overflow ovf;
+  CandBuf cand;
   const Seg *seg;
   const MeshDesc *mesh;
   MeshScalars *sc;
@@ -73,6 +91,7 @@ struct HausMesh {
 
 struct HausArgs {
   Overflow ovf;
+  CandBuf cand;
   double *dist;             // per sample item of the side being processed
   const Seg *seg;
   const MeshDesc *mesh;

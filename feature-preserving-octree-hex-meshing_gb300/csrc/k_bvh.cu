@@ -541,11 +541,16 @@ __device__ int thread_traverse(const BvhDev &b, const double q[3], double &best,
   return ok ? 0 : 1;
 }
 
-// Warp-cooperative traversal for the queries left over by the per-thread pass: one query per
-// warp, up to 32 frontier entries per step (one per lane), LIFO frontier in shared memory, and
-// the deferred candidate list (kWarpCand entries, in (step, lane) order) in shared memory too.
+// ---- candidate collection (batched exact evaluation) ----
+// The traversals below run in FP32 only: they prune on ub and record the leaves with lo <= ub
+// in visiting order.  The exact FP64 values are computed afterwards by one dense pass over all
+// queries' candidates (k_cand_eval) and reduced per query in recorded order (the *_finish
+// kernels), which gives the sequential search's result: every leaf left out has an exact
+// distance above the minimum.  A query with more candidates than it may record goes to the
+// exact per-thread search above (the *_fallback kernels).
+constexpr int kQCand = 16;     // candidates a per-thread query may hold
 constexpr int kWarpStack = 1024;
-constexpr int kWarpCand = 64;
+constexpr int kWarpCand = 64;  // candidates a warp-pass query may hold
 
 __device__ __forceinline__ int warp_excl_scan(int v, int &total) {
   const int lane = threadIdx.x & 31;
@@ -559,62 +564,106 @@ __device__ __forceinline__ int warp_excl_scan(int v, int &total) {
   return x - v;
 }
 
-// Evaluates the warp's recorded candidates with lo <= ub: lane k takes entries k, k + 32; the
-// winner is the smallest exact value, ties to the earliest entry, kept only on strict
-// improvement of `best` -- the sequential rule.  MODE 1 evaluates every entry from the best at
-// entry time, as PointDistanceEP takes its bound.
+// Per-thread collection with at most `budget` pops.  Returns 0 when done, 1 on stack overflow
+// (candidates may miss subtrees), 2 when the budget ran out (ub stays a valid bound), 3 when more
+// than kQCand candidates remain after compaction.
 template <int MODE>
-__device__ void warp_flush(const BvhDev &b, const double q[3], const int32_t *cl, const float *cb, int nc, float &ub,
-                           double &best, int32_t &bf, double bc[3]) {
-  const int lane = threadIdx.x & 31;
-  double vbest = INFINITY;
-  int kbest = 0x7fffffff;
-  int32_t fbest = -1;
-  double cbest[3] = {0, 0, 0};
-  for (int k = lane; k < nc; k += 32) {
-    if (cb[k] > ub) continue;
-    double v = best;
-    int32_t f = -1;
-    double c[3];
-    eval_exact<MODE>(b, cl[k], q, v, f, c);
-    if (v < best && v < vbest) {
-      vbest = v; kbest = k; fbest = f;
-      cbest[0] = c[0]; cbest[1] = c[1]; cbest[2] = c[2];
-    }
+__device__ int thread_collect(const BvhDev &b, const double q[3], float &ub, int32_t *cl, float *cb, int &nc,
+                              int budget) {
+  const int n = b.n;
+  nc = 0;
+  if (n == 1) {
+    cl[0] = 0;
+    cb[0] = -INFINITY;
+    nc = 1;
+    return 0;
   }
-  double m = vbest;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if (m < best) {
-    int kk = vbest == m ? kbest : 0x7fffffff;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) kk = min(kk, __shfl_xor_sync(0xffffffffu, kk, o));
-    const unsigned who = __ballot_sync(0xffffffffu, vbest == m && kbest == kk);
-    const int src = __ffs(who) - 1;
-    if (MODE == 0) {
-      bf = __shfl_sync(0xffffffffu, fbest, src);
-      bc[0] = __shfl_sync(0xffffffffu, cbest[0], src);
-      bc[1] = __shfl_sync(0xffffffffu, cbest[1], src);
-      bc[2] = __shfl_sync(0xffffffffu, cbest[2], src);
+  const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
+  const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
+  int32_t sn[kStack];
+  float sd[kStack];
+  int sp = 0, pops = 0;
+  bool ok = true;
+  sn[sp] = 0; sd[sp] = 0.f; sp++;
+  while (sp > 0) {
+    if (pops >= budget) return 2;
+    --sp;
+    const int32_t node = sn[sp];
+    const float d = sd[sp];
+    pops++;
+    if (d > ub) continue;
+    if (node < 0) {
+      const int32_t leaf = ~node;
+      if (leaf >= n) { ok = false; continue; }
+      float lo, hi;
+      leaf_bounds<MODE>(b.leafd, leaf, qf, d, lo, hi);
+      if (lo > ub) continue;
+      ub = fminf(ub, hi);
+      if (nc == kQCand) {
+        int w = 0;
+        for (int k = 0; k < nc; k++)
+          if (cb[k] <= ub) { cl[w] = cl[k]; cb[w] = cb[k]; w++; }
+        nc = w;
+        if (nc == kQCand) return 3;
+      }
+      cl[nc] = leaf;
+      cb[nc] = lo;
+      nc++;
+      continue;
     }
-    best = m;
+    if (node >= n - 1) { ok = false; continue; }
+    const NodeRec r = load_node(b.node, node);
+    if (r.l >= n - 1 || r.r >= n - 1 || ~r.l >= n || ~r.r >= n) { ok = false; continue; }
+    const float dl = sqrtf(box_d2f(r.lb, qf)) - mbox;
+    const float dr = sqrtf(box_d2f(r.rb, qf)) - mbox;
+    const bool lnear = dl <= dr;
+    const int32_t nearc = lnear ? r.l : r.r, farc = lnear ? r.r : r.l;
+    const float dn = lnear ? dl : dr, df = lnear ? dr : dl;
+    if (df <= ub) { if (sp < kStack) { sn[sp] = farc; sd[sp] = df; sp++; } else ok = false; }
+    if (dn <= ub) { if (sp < kStack) { sn[sp] = nearc; sd[sp] = dn; sp++; } else ok = false; }
   }
-  ub = fminf(ub, dist_bound<MODE>(best));
+  return ok ? 0 : 1;
 }
 
+// In-order compaction of a warp's shared candidate list to the entries with lo <= ub.
+__device__ __forceinline__ int warp_compact(int32_t *cl, float *cb, int nc, float ub) {
+  const int lane = threadIdx.x & 31;
+  int w = 0;
+  for (int k0 = 0; k0 < nc; k0 += 32) {
+    const int k = k0 + lane;
+    const bool keep = k < nc && cb[k] <= ub;
+    const unsigned kb = __ballot_sync(0xffffffffu, keep);
+    const int32_t lk = keep ? cl[k] : 0;
+    const float bk = keep ? cb[k] : 0.f;
+    __syncwarp();
+    if (keep) {
+      const int pos = w + __popc(kb & ((1u << lane) - 1u));
+      cl[pos] = lk;
+      cb[pos] = bk;
+    }
+    w += __popc(kb);
+    __syncwarp();
+  }
+  return w;
+}
+
+// Warp-cooperative collection for the queries left over by the per-thread pass: one query per
+// warp, up to 32 frontier entries per step (one per lane), LIFO frontier and candidate list in
+// shared memory, ub shared by the warp.  Returns 0 when done (cl/cb compacted to lo <= ub),
+// 1 on frontier overflow, 3 when more than kWarpCand candidates remain after compaction.
 template <int MODE>
-__device__ bool warp_traverse(const BvhDev &b, const double q[3], int32_t *sn, float *sd, int32_t *cl, float *cb,
-                              double &best, int32_t &bf, double bc[3]) {
+__device__ int warp_collect(const BvhDev &b, const double q[3], int32_t *sn, float *sd, int32_t *cl, float *cb,
+                            float &ub, int &nc) {
   const int lane = threadIdx.x & 31;
   const int n = b.n;
   const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
   const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
-  float ub = dist_bound<MODE>(best);
-  bool ok = true;
-  int sz = 1, nc = 0;
+  bool ok = true, full = false;
+  int sz = 1;
+  nc = 0;
   if (lane == 0) { sn[0] = n == 1 ? ~0 : 0; sd[0] = -INFINITY; }
   __syncwarp();
-  for (int guard = 0; sz > 0 && guard < 4 * (2 * n + 64); guard++) {
+  for (int guard = 0; sz > 0 && !full && guard < 4 * (2 * n + 64); guard++) {
     const int take = sz < 32 ? sz : 32;
     const bool has = lane < take;
     const int32_t node = has ? sn[sz - take + lane] : 0;
@@ -630,7 +679,8 @@ __device__ bool warp_traverse(const BvhDev &b, const double q[3], int32_t *sn, f
       if (node < 0) {
         const int32_t leaf = ~node;
         if (leaf < n) {
-          leaf_bounds<MODE>(b.leafd, leaf, qf, d, lo, hi);
+          if (n == 1) { lo = -INFINITY; hi = INFINITY; }
+          else leaf_bounds<MODE>(b.leafd, leaf, qf, d, lo, hi);
           cand = true;
         } else {
           ok = false;
@@ -652,43 +702,26 @@ __device__ bool warp_traverse(const BvhDev &b, const double q[3], int32_t *sn, f
       }
     }
     // tighten ub by this step's leaves, then record those still within it
-    float h = hi;
+    float hm = hi;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) h = fminf(h, __shfl_xor_sync(0xffffffffu, h, o));
-    ub = fminf(ub, h);
+    for (int o = 16; o > 0; o >>= 1) hm = fminf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
+    ub = fminf(ub, hm);
     const bool rec = cand && lo <= ub;
     const unsigned rb = __ballot_sync(0xffffffffu, rec);
     const int nrec = __popc(rb);
     if (nrec > 0) {
       if (nc + nrec > kWarpCand) {
-        // compact in order, then evaluate if still too full
-        int w = 0;
-        for (int k0 = 0; k0 < nc; k0 += 32) {
-          const int k = k0 + lane;
-          const bool keep = k < nc && cb[k] <= ub;
-          const unsigned kb = __ballot_sync(0xffffffffu, keep);
-          int32_t lk = keep ? cl[k] : 0;
-          float bk = keep ? cb[k] : 0.f;
-          __syncwarp();
-          if (keep) {
-            const int pos = w + __popc(kb & ((1u << lane) - 1u));
-            cl[pos] = lk; cb[pos] = bk;
-          }
-          w += __popc(kb);
-          __syncwarp();
-        }
-        nc = w;
-        if (nc + nrec > kWarpCand) {
-          warp_flush<MODE>(b, q, cl, cb, nc, ub, best, bf, bc);
-          nc = 0;
-        }
-        __syncwarp();
+        nc = warp_compact(cl, cb, nc, ub);
+        if (nc + nrec > kWarpCand) full = true;
       }
-      if (rec) {
-        const int pos = nc + __popc(rb & ((1u << lane) - 1u));
-        cl[pos] = ~node; cb[pos] = lo;
+      if (!full) {
+        if (rec) {
+          const int pos = nc + __popc(rb & ((1u << lane) - 1u));
+          cl[pos] = ~node;
+          cb[pos] = lo;
+        }
+        nc += nrec;
       }
-      nc += nrec;
     }
     int total;
     const int off = warp_excl_scan(np, total);
@@ -699,10 +732,11 @@ __device__ bool warp_traverse(const BvhDev &b, const double q[3], int32_t *sn, f
     __syncwarp();
     sz += total < room ? total : room;
   }
-  if (sz > 0) ok = false;
   __syncwarp();
-  warp_flush<MODE>(b, q, cl, cb, nc, ub, best, bf, bc);
-  return __all_sync(0xffffffffu, ok);
+  if (full) return 3;
+  if (sz > 0) ok = false;
+  nc = warp_compact(cl, cb, nc, ub);
+  return __all_sync(0xffffffffu, ok) ? 0 : 1;
 }
 
 constexpr int kThreadBudget = 64;   // pops per query before handing over to the warp pass
@@ -713,6 +747,87 @@ __device__ __forceinline__ void push_overflow(const Overflow &o, int64_t item, i
   const unsigned k = atomicAdd(o.count, 1u);
   o.item[k] = item;
   o.mesh[k] = mesh;
+}
+
+__device__ __forceinline__ void push_fallback(const CandBuf &c, int64_t item, int32_t mesh) {
+  const unsigned k = atomicAdd(c.fb_count, 1u);
+  c.fb_item[k] = item;
+  c.fb_mesh[k] = mesh;
+  c.q_cnt[item] = -1;
+}
+
+__device__ __forceinline__ void store_query(const CandBuf &c, int64_t i, int32_t mesh, const double q[3], int64_t off,
+                                            int cnt) {
+  c.q_off[i] = (int32_t)off;
+  c.q_cnt[i] = cnt;
+  c.qpos[3 * i] = q[0]; c.qpos[3 * i + 1] = q[1]; c.qpos[3 * i + 2] = q[2];
+  c.q_mesh[i] = mesh;
+}
+
+// Per-thread pass: every lane of the warp calls this (has = false for lanes without candidates
+// to store); one atomic per warp reserves the warp's entries.  Returns false for a lane whose
+// entries do not fit (the caller sends that query to the fallback).
+__device__ bool store_cands_warp(const CandBuf &c, bool has, int64_t i, int32_t mesh, const double q[3],
+                                 const int32_t *cl, const float *cb, int nc, float ub) {
+  int k = 0;
+  if (has)
+    for (int j = 0; j < nc; j++) k += cb[j] <= ub;
+  int total;
+  const int off = warp_excl_scan(k, total);
+  unsigned base = 0;
+  if ((threadIdx.x & 31) == 0 && total > 0) base = atomicAdd(c.count, (unsigned)total);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (!has) return true;
+  const int64_t o = (int64_t)base + off;
+  if (o + k > c.cap) return false;
+  int w = 0;
+  for (int j = 0; j < nc; j++)
+    if (cb[j] <= ub) { c.leaf[o + w] = cl[j]; c.qi[o + w] = (int32_t)i; w++; }
+  store_query(c, i, mesh, q, o, k);
+  return true;
+}
+
+// Warp pass: one query per warp, candidates already compacted in shared memory.
+__device__ bool store_cands_query(const CandBuf &c, int64_t i, int32_t mesh, const double q[3], const int32_t *cl,
+                                  int nc) {
+  const int lane = threadIdx.x & 31;
+  unsigned base = 0;
+  if (lane == 0 && nc > 0) base = atomicAdd(c.count, (unsigned)nc);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if ((int64_t)base + nc > c.cap) return false;
+  for (int j = lane; j < nc; j += 32) { c.leaf[base + j] = cl[j]; c.qi[base + j] = (int32_t)i; }
+  if (lane == 0) store_query(c, i, mesh, q, base, nc);
+  return true;
+}
+
+// The dense exact pass: one candidate per thread.  MODE 0: squared point-triangle distance;
+// MODE 1: PointDistanceEP without a bound, and the plane distance the bound test reads.
+// SRC 0: the BVH of mesh m is tgt[m].bvh; SRC 1: surf[m].
+template <int MODE, int SRC>
+__global__ void __launch_bounds__(128) k_cand_eval(CandBuf c, const TargetDev *tgt, const BvhDev *surf) {
+  const unsigned cnt = *c.count;
+  const int64_t n = cnt < c.cap ? (int64_t)cnt : c.cap;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t qi = c.qi[e];
+    const int32_t m = c.q_mesh[qi];
+    const BvhDev &b = SRC == 0 ? tgt[m].bvh : surf[m];
+    const double q[3] = {c.qpos[3 * (int64_t)qi], c.qpos[3 * (int64_t)qi + 1], c.qpos[3 * (int64_t)qi + 2]};
+    double P[3][3];
+    face_pts(b, b.leaf_face[c.leaf[e]], P);
+    if (MODE == 0) {
+      double cp[3], r[3];
+      closest_pt_tri(q, P[0], P[1], P[2], cp);
+      nsub3(q, cp, r);
+      c.x[e] = ndot(r, r);
+    } else {
+      EPFace fe;
+      ep_setup(P, fe);
+      double x = INFINITY;
+      point_distance_ep(fe, q, x);
+      c.x[e] = x;
+      c.d[e] = nsub(ndot(fe.dir, q), fe.off);
+    }
+  }
 }
 
 // pseudonormal_test: normal at the closest point c of face f (vertex / edge / face normal).
@@ -787,27 +902,41 @@ __device__ __forceinline__ void write_tangent(const ProjArgs &p, const TargetDev
   p.t_dis[e] = n[0] * c[0] + n[1] * c[1] + n[2] * c[2];
 }
 
+// The projection query of item i: tangent entry e and the vertex position.
+__device__ __forceinline__ int64_t proj_entry(const ProjArgs &p, const MeshDesc &md, int64_t i, double q[3]) {
+  const int64_t e = md.t_off + (i - md.kitem0[K_PROJ]);
+  const int64_t v = md.v_off + p.t_ids[e];
+  q[0] = p.X[4 * v]; q[1] = p.X[4 * v + 1]; q[2] = p.X[4 * v + 2];
+  return e;
+}
+
 __global__ void __launch_bounds__(128) k_project(ProjArgs p) {
   const Seg sg = p.seg[blockIdx.x];
   const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
-  const MeshDesc md = p.mesh[sg.mesh];
-  const TargetDev &t = p.tgt[sg.mesh];
-  const int64_t e = md.t_off + (i - md.kitem0[K_PROJ]);
-  const int64_t v = md.v_off + p.t_ids[e];
-  const double q[3] = {p.X[4 * v], p.X[4 * v + 1], p.X[4 * v + 2]};
-  double best = INFINITY, c[3] = {0, 0, 0};
-  int32_t f = -1;
-  int st = 0;
-  if (t.bvh.n > 0) st = thread_traverse<0>(t.bvh, q, best, f, c, kThreadBudget);
-  if (st == 2) {
-    p.ovf.best[i] = best; p.ovf.face[i] = f;
-    p.ovf.pt[3 * i] = c[0]; p.ovf.pt[3 * i + 1] = c[1]; p.ovf.pt[3 * i + 2] = c[2];
-    push_overflow(p.ovf, i, sg.mesh);
-    return;
+  bool has = i < sg.end;
+  double q[3] = {0, 0, 0};
+  int32_t cl[kQCand];
+  float cb[kQCand];
+  int nc = 0;
+  float ub = INFINITY;
+  if (has) {
+    const MeshDesc md = p.mesh[sg.mesh];
+    const TargetDev &t = p.tgt[sg.mesh];
+    proj_entry(p, md, i, q);
+    int st = 0;
+    if (t.bvh.n > 0) st = thread_collect<0>(t.bvh, q, ub, cl, cb, nc, kThreadBudget);
+    if (st == 2) {
+      p.ovf.best[i] = ub;
+      push_overflow(p.ovf, i, sg.mesh);
+      has = false;
+    } else if (st == 3) {
+      push_fallback(p.cand, i, sg.mesh);
+      has = false;
+    } else if (st == 1) {
+      atomicOr(&p.sc[sg.mesh].status, 8);
+    }
   }
-  if (st == 1) atomicOr(&p.sc[sg.mesh].status, 8);
-  write_tangent(p, t, e, f, c);
+  if (!store_cands_warp(p.cand, has, i, sg.mesh, q, cl, cb, nc, ub)) push_fallback(p.cand, i, sg.mesh);
 }
 
 __global__ void __launch_bounds__(128) k_project_warp(ProjArgs p) {
@@ -821,18 +950,66 @@ __global__ void __launch_bounds__(128) k_project_warp(ProjArgs p) {
     const int64_t i = p.ovf.item[k];
     const int32_t m = p.ovf.mesh[k];
     const MeshDesc md = p.mesh[m];
-    const TargetDev &t = p.tgt[m];
-    const int64_t e = md.t_off + (i - md.kitem0[K_PROJ]);
-    const int64_t v = md.v_off + p.t_ids[e];
-    const double q[3] = {p.X[4 * v], p.X[4 * v + 1], p.X[4 * v + 2]};
-    double best = p.ovf.best[i], c[3] = {p.ovf.pt[3 * i], p.ovf.pt[3 * i + 1], p.ovf.pt[3 * i + 2]};
-    int32_t f = p.ovf.face[i];
-    const bool ok = warp_traverse<0>(t.bvh, q, sn[w], sd[w], scl[w], scb[w], best, f, c);
-    if (lane == 0) {
-      if (!ok) atomicOr(&p.sc[m].status, 8);
-      write_tangent(p, t, e, f, c);
+    double q[3];
+    proj_entry(p, md, i, q);
+    float ub = (float)p.ovf.best[i];
+    int nc = 0;
+    const int st = warp_collect<0>(p.tgt[m].bvh, q, sn[w], sd[w], scl[w], scb[w], ub, nc);
+    if (st == 3) {
+      if (lane == 0) push_fallback(p.cand, i, m);
+    } else {
+      if (st == 1 && lane == 0) atomicOr(&p.sc[m].status, 8);
+      if (!store_cands_query(p.cand, i, m, q, scl[w], nc) && lane == 0) push_fallback(p.cand, i, m);
     }
     __syncwarp();
+  }
+}
+
+// Winner of each projection query in recorded order (strict improvement), its closest point and
+// pseudonormal -> tangent plane.
+__global__ void __launch_bounds__(128) k_project_finish(ProjArgs p) {
+  const Seg sg = p.seg[blockIdx.x];
+  const int64_t i = sg.begin + threadIdx.x;
+  if (i >= sg.end) return;
+  const int cnt = p.cand.q_cnt[i];
+  if (cnt < 0) return;
+  const MeshDesc md = p.mesh[sg.mesh];
+  const TargetDev &t = p.tgt[sg.mesh];
+  double q[3];
+  const int64_t e = proj_entry(p, md, i, q);
+  const int64_t o = p.cand.q_off[i];
+  double best = INFINITY;
+  int win = -1;
+  for (int k = 0; k < cnt; k++) {
+    const double x = p.cand.x[o + k];
+    if (x < best) { best = x; win = k; }
+  }
+  int32_t f = -1;
+  double c[3] = {0, 0, 0};
+  if (win >= 0) {
+    f = t.bvh.leaf_face[p.cand.leaf[o + win]];
+    double P[3][3];
+    face_pts(t.bvh, f, P);
+    closest_pt_tri(q, P[0], P[1], P[2], c);
+  }
+  write_tangent(p, t, e, f, c);
+}
+
+// Queries whose candidates did not fit: the exact per-thread search (deferred in-thread
+// evaluation), one thread per query.
+__global__ void __launch_bounds__(128) k_project_fallback(ProjArgs p) {
+  const unsigned cnt = *p.cand.fb_count;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+    const int64_t i = p.cand.fb_item[k];
+    const int32_t m = p.cand.fb_mesh[k];
+    const MeshDesc md = p.mesh[m];
+    const TargetDev &t = p.tgt[m];
+    double q[3];
+    const int64_t e = proj_entry(p, md, i, q);
+    double best = INFINITY, c[3] = {0, 0, 0};
+    int32_t f = -1;
+    if (t.bvh.n > 0 && thread_traverse<0>(t.bvh, q, best, f, c, 1 << 30) != 0) atomicOr(&p.sc[m].status, 8);
+    write_tangent(p, t, e, f, c);
   }
 }
 
@@ -958,22 +1135,30 @@ template <int SIDE>
 __global__ void __launch_bounds__(128) k_haus_side(HausArgs h) {
   const Seg sg = h.seg[blockIdx.x];
   const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
-  double q[3];
-  const BvhDev *b;
-  haus_query<SIDE>(h, i, sg.mesh, q, b);
-  double dist = h.hm[sg.mesh].diag;
-  int32_t fd = -1;
-  double cd[3];
-  int st = 0;
-  if (b->n > 0) st = thread_traverse<1>(*b, q, dist, fd, cd, kThreadBudget);
-  if (st == 2) {
-    h.ovf.best[i] = dist;
-    push_overflow(h.ovf, i, sg.mesh);
-    return;
+  bool has = i < sg.end;
+  double q[3] = {0, 0, 0};
+  int32_t cl[kQCand];
+  float cb[kQCand];
+  int nc = 0;
+  float ub = INFINITY;
+  if (has) {
+    const BvhDev *b;
+    haus_query<SIDE>(h, i, sg.mesh, q, b);
+    ub = dist_bound<1>(h.hm[sg.mesh].diag);
+    int st = 0;
+    if (b->n > 0) st = thread_collect<1>(*b, q, ub, cl, cb, nc, kThreadBudget);
+    if (st == 2) {
+      h.ovf.best[i] = ub;
+      push_overflow(h.ovf, i, sg.mesh);
+      has = false;
+    } else if (st == 3) {
+      push_fallback(h.cand, i, sg.mesh);
+      has = false;
+    } else if (st == 1) {
+      atomicOr(&h.sc[sg.mesh].status, 8);
+    }
   }
-  if (st == 1) atomicOr(&h.sc[sg.mesh].status, 8);
-  h.dist[i] = dist;
+  if (!store_cands_warp(h.cand, has, i, sg.mesh, q, cl, cb, nc, ub)) push_fallback(h.cand, i, sg.mesh);
 }
 
 template <int SIDE>
@@ -990,15 +1175,54 @@ __global__ void __launch_bounds__(128) k_haus_warp(HausArgs h) {
     double q[3];
     const BvhDev *b;
     haus_query<SIDE>(h, i, m, q, b);
-    double dist = h.ovf.best[i];
-    int32_t fd = -1;
-    double cd[3];
-    const bool ok = warp_traverse<1>(*b, q, sn[w], sd[w], scl[w], scb[w], dist, fd, cd);
-    if (lane == 0) {
-      if (!ok) atomicOr(&h.sc[m].status, 8);
-      h.dist[i] = dist;
+    float ub = (float)h.ovf.best[i];
+    int nc = 0;
+    const int st = warp_collect<1>(*b, q, sn[w], sd[w], scl[w], scb[w], ub, nc);
+    if (st == 3) {
+      if (lane == 0) push_fallback(h.cand, i, m);
+    } else {
+      if (st == 1 && lane == 0) atomicOr(&h.sc[m].status, 8);
+      if (!store_cands_query(h.cand, i, m, q, scl[w], nc) && lane == 0) push_fallback(h.cand, i, m);
     }
     __syncwarp();
+  }
+}
+
+// Per-sample distance from the recorded candidates: PointDistanceEP's bound test against the
+// running distance (from the inflated diagonal), then the minimum -- the sequential rule, replayed
+// with the plane distance of each candidate.
+template <int SIDE>
+__global__ void __launch_bounds__(128) k_haus_finish(HausArgs h) {
+  const Seg sg = h.seg[blockIdx.x];
+  const int64_t i = sg.begin + threadIdx.x;
+  if (i >= sg.end) return;
+  const int cnt = h.cand.q_cnt[i];
+  if (cnt < 0) return;
+  const int64_t o = h.cand.q_off[i];
+  double dist = h.hm[sg.mesh].diag;
+  for (int k = 0; k < cnt; k++) {
+    const double d = h.cand.d[o + k];
+    if (d > dist || d < -dist) continue;
+    const double x = h.cand.x[o + k];
+    if (dist > x) dist = x;
+  }
+  h.dist[i] = dist;
+}
+
+template <int SIDE>
+__global__ void __launch_bounds__(128) k_haus_fallback(HausArgs h) {
+  const unsigned cnt = *h.cand.fb_count;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+    const int64_t i = h.cand.fb_item[k];
+    const int32_t m = h.cand.fb_mesh[k];
+    double q[3];
+    const BvhDev *b;
+    haus_query<SIDE>(h, i, m, q, b);
+    double dist = h.hm[m].diag;
+    int32_t fd = -1;
+    double cd[3];
+    if (b->n > 0 && thread_traverse<1>(*b, q, dist, fd, cd, 1 << 30) != 0) atomicOr(&h.sc[m].status, 8);
+    h.dist[i] = dist;
   }
 }
 
@@ -1115,11 +1339,17 @@ void bvh_refit(const BvhDev &b, float *box, const int32_t *parent, unsigned *cou
   if (b.n > 1) k_pack<<<(b.n + 254) / 256, 256, 0, st>>>(b.n, b.child, box, node);
 }
 static const unsigned kWarpGrid = 912;  // persistent warp-pass grid (152 SMs x 6 blocks of 4 warps)
+static const unsigned kEvalGrid = 152 * 8;  // dense exact pass: grid-stride over the candidates
 void launch_project(const ProjArgs &p, int64_t nblk, cudaStream_t st) {
   if (nblk <= 0) return;
   cudaMemsetAsync(p.ovf.count, 0, sizeof(unsigned), st);
+  cudaMemsetAsync(p.cand.count, 0, sizeof(unsigned), st);
+  cudaMemsetAsync(p.cand.fb_count, 0, sizeof(unsigned), st);
   k_project<<<(unsigned)nblk, 128, 0, st>>>(p);
   k_project_warp<<<kWarpGrid, 128, 0, st>>>(p);
+  k_cand_eval<0, 0><<<kEvalGrid, 128, 0, st>>>(p.cand, p.tgt, nullptr);
+  k_project_finish<<<(unsigned)nblk, 128, 0, st>>>(p);
+  k_project_fallback<<<kWarpGrid, 128, 0, st>>>(p);
 }
 void launch_curve_project(const ProjArgs &p, int64_t nblk, cudaStream_t st) {
   if (nblk > 0) k_curve_project<<<(unsigned)nblk, 128, 0, st>>>(p);
@@ -1133,13 +1363,21 @@ void launch_haus_bbox(const HausArgs &h, int64_t nblk, cudaStream_t st) {
 }
 void launch_haus_side(const HausArgs &h, int side, int64_t nblk, cudaStream_t st) {
   cudaMemsetAsync(h.ovf.count, 0, sizeof(unsigned), st);
-  if (side == 0) {
+  cudaMemsetAsync(h.cand.count, 0, sizeof(unsigned), st);
+  cudaMemsetAsync(h.cand.fb_count, 0, sizeof(unsigned), st);
+  if (side == 0) {  // target samples against the boundary surface
     k_haus_side<0><<<(unsigned)nblk, 128, 0, st>>>(h);
     k_haus_warp<0><<<kWarpGrid, 128, 0, st>>>(h);
+    k_cand_eval<1, 1><<<kEvalGrid, 128, 0, st>>>(h.cand, h.tgt, h.surf);
+    k_haus_finish<0><<<(unsigned)nblk, 128, 0, st>>>(h);
+    k_haus_fallback<0><<<kWarpGrid, 128, 0, st>>>(h);
     k_haus_reduce<0><<<(unsigned)nblk, 128, 0, st>>>(h);
-  } else {
+  } else {  // surface samples against the target
     k_haus_side<1><<<(unsigned)nblk, 128, 0, st>>>(h);
     k_haus_warp<1><<<kWarpGrid, 128, 0, st>>>(h);
+    k_cand_eval<1, 0><<<kEvalGrid, 128, 0, st>>>(h.cand, h.tgt, h.surf);
+    k_haus_finish<1><<<(unsigned)nblk, 128, 0, st>>>(h);
+    k_haus_fallback<1><<<kWarpGrid, 128, 0, st>>>(h);
     k_haus_reduce<1><<<(unsigned)nblk, 128, 0, st>>>(h);
   }
 }
