@@ -259,6 +259,35 @@ __device__ T tet_energy_density(int energy, T exp_f, const T J[3][3]) {
 }
 
 // ------------------------------------------------------------------------------- reductions
+// Per-thread accumulators.  SumAcc<double> is a plain FP64 sum.  SumAcc<float> is a compensated
+// FP32 sum (Ogita, Rump & Oishi 2005, "Accurate sum and dot product": TwoSum and the FMA-based
+// TwoProduct error-free transformations), carrying about twice FP32's precision on the FP32
+// pipes -- GB300's FP64 rate is a small fraction of its FP32 rate, so per-item FP64 adds would
+// bound the vector kernels.  value() hands the thread's total to the FP64 block reduction.
+template <typename T> struct SumAcc;
+template <> struct SumAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ void add_prod(double a, double b) { s += a * b; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct SumAcc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = __fadd_rn(s, x);
+    const float z = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z)));
+    s = t;
+  }
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
+    add(p);
+    c = __fadd_rn(c, e);
+  }
+  __device__ __forceinline__ double value() const { return double(s) + double(c); }
+};
+
 // Block-level sum of NV doubles (all threads get nothing back; thread 0 gets the total).
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double (*smem)[32]) {

@@ -358,9 +358,24 @@ __global__ void __launch_bounds__(256) k_cg_start(KArgs a) {
   VT *r = reinterpret_cast<VT *>(a.r), *p = reinterpret_cast<VT *>(a.p), *d = reinterpret_cast<VT *>(a.d);
   VT *q = reinterpret_cast<VT *>(a.q), *invd = reinterpret_cast<VT *>(a.invd);
   const VT *b = reinterpret_cast<const VT *>(a.b), *dg = reinterpret_cast<const VT *>(a.diag);
+  SumAcc<VT> s_bb, s_rr, s_rp;  // mixed mode: FP32 arithmetic, compensated sums
   for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
     const ItemRef it = item_ref(md, i);
-    if (!it.curve) {
+    if (!it.curve && sizeof(VT) == 4) {
+      const int64_t v = it.idx;
+      const V3<VT> bb = ld3(b, v), rr = ld3(r, v), gg = ld3(dg, v);
+      const VT pr = VT(prox);
+      const VT b0 = bb.x + pr * VT(a.X[4 * v]), b1 = bb.y + pr * VT(a.X[4 * v + 1]), b2 = bb.z + pr * VT(a.X[4 * v + 2]);
+      const VT i0 = VT(1) / (gg.x + pr), i1 = VT(1) / (gg.y + pr), i2 = VT(1) / (gg.z + pr);
+      const VT p0 = i0 * rr.x, p1 = i1 * rr.y, p2 = i2 * rr.z;
+      st3(p, v, V3<VT>{p0, p1, p2});
+      st3(d, v, V3<VT>{VT(0), VT(0), VT(0)});
+      st3(invd, v, V3<VT>{i0, i1, i2});
+      st3(q, v, V3<VT>{pr * p0, pr * p1, pr * p2});
+      s_bb.add_prod(b0, b0); s_bb.add_prod(b1, b1); s_bb.add_prod(b2, b2);
+      s_rr.add_prod(rr.x, rr.x); s_rr.add_prod(rr.y, rr.y); s_rr.add_prod(rr.z, rr.z);
+      s_rp.add_prod(rr.x, p0); s_rp.add_prod(rr.y, p1); s_rp.add_prod(rr.z, p2);
+    } else if (!it.curve) {
       const int64_t v = it.idx;
       const V3<VT> bb = ld3(b, v), rr = ld3(r, v), gg = ld3(dg, v);
       const double x0 = a.X[4 * v], x1 = a.X[4 * v + 1], x2 = a.X[4 * v + 2];
@@ -386,6 +401,11 @@ __global__ void __launch_bounds__(256) k_cg_start(KArgs a) {
       pa[e] = VT(pp); da[e] = VT(0); invda[e] = VT(id); qa[e] = VT(0);
       acc[0] += bb * bb; acc[1] += rr * rr; acc[2] += rr * pp;
     }
+  }
+  if (sizeof(VT) == 4) {
+    acc[0] += s_bb.value();
+    acc[1] += s_rr.value();
+    acc[2] += s_rp.value();
   }
   __shared__ double smem[3][32];
   block_sum<3>(acc, smem);
@@ -417,16 +437,22 @@ __global__ void __launch_bounds__(256) k_cg_alpha(KArgs a) {
   const MeshDesc md = a.mesh[sg.mesh];
   const VT *p = reinterpret_cast<const VT *>(a.p), *q = reinterpret_cast<const VT *>(a.q);
   double acc[1] = {0};
+  SumAcc<VT> pq;  // mixed mode: compensated FP32 dot product
   for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
     const ItemRef it = item_ref(md, i);
     if (!it.curve) {
       const V3<VT> pp = ld3(p, it.idx), qq = ld3(q, it.idx);
-      acc[0] += double(pp.x) * double(qq.x) + double(pp.y) * double(qq.y) + double(pp.z) * double(qq.z);
+      if (sizeof(VT) == 4) {
+        pq.add_prod(pp.x, qq.x); pq.add_prod(pp.y, qq.y); pq.add_prod(pp.z, qq.z);
+      } else {
+        acc[0] += double(pp.x) * double(qq.x) + double(pp.y) * double(qq.y) + double(pp.z) * double(qq.z);
+      }
     } else {
       const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
       acc[0] += double(pa[it.idx]) * double(qa[it.idx]);
     }
   }
+  if (sizeof(VT) == 4) acc[0] += pq.value();
   __shared__ double smem[1][32];
   block_sum<1>(acc, smem);
   if (publish_partials<1>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
@@ -448,6 +474,7 @@ __global__ void __launch_bounds__(256) k_cg_update(KArgs a) {
   const MeshDesc md = a.mesh[sg.mesh];
   const VT alpha = VT(S.alpha);
   double acc[2] = {0, 0};
+  SumAcc<VT> s_rr, s_rz;  // mixed mode: compensated FP32 dot products
   for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
     const ItemRef it = item_ref(md, i);
     if (!it.curve) {
@@ -461,8 +488,13 @@ __global__ void __launch_bounds__(256) k_cg_update(KArgs a) {
       rr.x -= alpha * qq.x; rr.y -= alpha * qq.y; rr.z -= alpha * qq.z;
       st3(d, v, dd);
       st3(r, v, rr);
-      acc[0] += double(rr.x) * double(rr.x) + double(rr.y) * double(rr.y) + double(rr.z) * double(rr.z);
-      acc[1] += double(rr.x) * double(id.x * rr.x) + double(rr.y) * double(id.y * rr.y) + double(rr.z) * double(id.z * rr.z);
+      if (sizeof(VT) == 4) {
+        s_rr.add_prod(rr.x, rr.x); s_rr.add_prod(rr.y, rr.y); s_rr.add_prod(rr.z, rr.z);
+        s_rz.add_prod(rr.x, id.x * rr.x); s_rz.add_prod(rr.y, id.y * rr.y); s_rz.add_prod(rr.z, id.z * rr.z);
+      } else {
+        acc[0] += double(rr.x) * double(rr.x) + double(rr.y) * double(rr.y) + double(rr.z) * double(rr.z);
+        acc[1] += double(rr.x) * double(id.x * rr.x) + double(rr.y) * double(id.y * rr.y) + double(rr.z) * double(id.z * rr.z);
+      }
     } else {
       VT *ra = reinterpret_cast<VT *>(a.ra), *da = reinterpret_cast<VT *>(a.da);
       const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
@@ -474,6 +506,10 @@ __global__ void __launch_bounds__(256) k_cg_update(KArgs a) {
       acc[0] += double(rr) * double(rr);
       acc[1] += double(rr) * double(invda[e] * rr);
     }
+  }
+  if (sizeof(VT) == 4) {
+    acc[0] += s_rr.value();
+    acc[1] += s_rz.value();
   }
   __shared__ double smem[2][32];
   block_sum<2>(acc, smem);
@@ -635,8 +671,8 @@ __device__ __forceinline__ void tet_dir(const VT *d, const uint32_t hv[8], doubl
 // Energy density of corner tet K at edges E (ET); tets with |det J| below 1e-3 are re-evaluated
 // in FP64 from the FP64 positions (mixed mode only).
 template <typename ET, typename VT, int K>
-__device__ __forceinline__ double tet_energy_e(const KArgs &a, int64_t h, const uint32_t hv[8], int32_t gs,
-                                               const ET E[3][3], double alpha) {
+__device__ __forceinline__ void tet_energy_acc(const KArgs &a, int64_t h, const uint32_t hv[8], int32_t gs,
+                                               const ET E[3][3], double alpha, SumAcc<ET> &fast, double &slow) {
   const ET *Sinv = reinterpret_cast<const ET *>(a.Sinv);
   const double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
   const ET is = Sinv[tet_idx<1>(h, K, 0)];
@@ -654,10 +690,11 @@ __device__ __forceinline__ double tet_energy_e(const KArgs &a, int64_t h, const 
 #pragma unroll
         for (int c = 0; c < 3; c++) Ed[r][c] = E0[r][c] + alpha * Dd[r][c];
       apply_B<K>(Ed, gs, B, double(is), Jd);
-      return tet_energy_density<double>(a.energy, a.sc_exp_f, Jd);
+      slow += tet_energy_density<double>(a.energy, a.sc_exp_f, Jd);
+      return;
     }
   }
-  return double(e);
+  fast.add(e);
 }
 
 // Flip-avoiding step bound of corner tet K.  Only a root of det(E + t D) in [0, 1.25] can lower
@@ -732,18 +769,19 @@ __global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
 #pragma unroll
         for (int r = 0; r < 3; r++) D12[e][r] = ET(Dv[e][r]);
     }
-    double esum = 0;
+    SumAcc<ET> efast;
+    double eslow = 0;
 #define HX_LS(K)                                                  \
     {                                                             \
       ET E[3][3], D[3][3];                                        \
       tet_E12<K>(E12, E);                                         \
       tet_E12<K>(D12, D);                                         \
       tet_bound<ET, VT, K>(a, hv, E, D, mn[0]);                   \
-      esum += tet_energy_e<ET, VT, K>(a, h, hv, gs, E, 0.0);      \
+      tet_energy_acc<ET, VT, K>(a, h, hv, gs, E, 0.0, efast, eslow); \
     }
     HX_LS(0) HX_LS(1) HX_LS(2) HX_LS(3) HX_LS(4) HX_LS(5) HX_LS(6) HX_LS(7)
 #undef HX_LS
-    eq[0] = S.M * esum;
+    eq[0] = S.M * (efast.value() + eslow);
   }
   __shared__ double smem[1][32];
   block_min<1>(mn, smem);
@@ -800,6 +838,10 @@ __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t n
       double al[NC];
 #pragma unroll
       for (int j = 0; j < NC; j++) al[j] = cand_alpha(S, round * NC + j);
+      SumAcc<ET> efast[NC];
+      double eslow[NC];
+#pragma unroll
+      for (int j = 0; j < NC; j++) eslow[j] = 0;
 #define HX_LE(K)                                                             \
       {                                                                      \
         ET E0[3][3], D[3][3];                                                \
@@ -810,13 +852,13 @@ __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t n
           const ET aj = ET(al[j]);                                           \
           _Pragma("unroll") for (int r = 0; r < 3; r++)                      \
           _Pragma("unroll") for (int c = 0; c < 3; c++) E[r][c] = E0[r][c] + aj * D[r][c]; \
-          acc[j] += tet_energy_e<ET, VT, K>(a, h, hv, gs, E, al[j]);         \
+          tet_energy_acc<ET, VT, K>(a, h, hv, gs, E, al[j], efast[j], eslow[j]); \
         }                                                                    \
       }
       HX_LE(0) HX_LE(1) HX_LE(2) HX_LE(3) HX_LE(4) HX_LE(5) HX_LE(6) HX_LE(7)
 #undef HX_LE
 #pragma unroll
-      for (int j = 0; j < NC; j++) acc[j] *= S.M;
+      for (int j = 0; j < NC; j++) acc[j] = S.M * (efast[j].value() + eslow[j]);
     }
     block_sum<NC>(acc, smem);
     if (publish_partials<NC>(acc, a.partials, sb, a.counters + sg.mesh, md.nhblk)) {
