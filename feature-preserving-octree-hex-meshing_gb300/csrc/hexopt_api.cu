@@ -110,6 +110,7 @@ struct hexopt_ctx {
   DBuf b, diag, ba, diaga;
   DBuf d, r, p, q, invd, da, ra, pa, qa, invda;
   DBuf stage, stage2, HJs, VJs, Xa, grad, Xbak;
+  DBuf root_list, root_mesh, root_count, root_min;  // flip-avoid bound: tets needing the exact root
   bool adj_ready = false;
   DBuf partials, counters;
   DBuf c_ids, c_pos, t_ids, t_nrm, t_dis, l_ids, l_axis, l_orig, l_curve;
@@ -288,6 +289,11 @@ KArgs make_args(hexopt_ctx *c) {
   a.vthreads = c->block[K_VERT];
   a.Xa = c->Xa.as<double>();
   a.grad = c->grad.as<double>();
+  a.root_list = c->root_list.as<uint32_t>();
+  a.root_mesh = c->root_mesh.as<int32_t>();
+  a.root_count = c->root_count.as<unsigned>();
+  a.root_min = c->root_min.as<unsigned long long>();
+  a.n_meshes = c->n_meshes;
   return a;
 }
 
@@ -302,6 +308,18 @@ int alloc_vectors(hexopt_ctx *ctx) {
   CK(ctx->Sinv.ensure(nt * vt));
   CK(ctx->Ccoef.ensure(nt * 6 * vt));
   CK(ctx->Bgen.ensure((size_t)std::max<int64_t>(ctx->NG, 1) * 8 * 9 * sizeof(double)));
+  // every corner tet may need the exact root: the list holds all of them
+  const size_t nroot = (size_t)ctx->NH * 8;
+  CK(ctx->root_list.ensure(nroot * sizeof(uint32_t)));
+  CK(ctx->root_mesh.ensure(nroot * sizeof(int32_t)));
+  CK(ctx->root_count.ensure(sizeof(unsigned)));
+  CK(ctx->root_min.ensure(sizeof(unsigned long long) * ctx->n_meshes));
+  {
+    CK(cudaMemsetAsync(ctx->root_count.p, 0, sizeof(unsigned), ctx->st));
+    std::vector<double> inf(ctx->n_meshes, INFINITY);
+    CK(cudaMemcpyAsync(ctx->root_min.p, inf.data(), sizeof(double) * ctx->n_meshes, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
   return HEXOPT_OK;
 }
 
@@ -342,7 +360,7 @@ int run_iteration(hexopt_ctx *ctx, bool pre) {
   ctx->launches += (int64_t)kLaunchesCgIter * ctx->params.cg_max_iter;
   launch_line_search<ET, VT>(a, hb, vb, cb, st);
   const int rounds = (kHalvings + 1 + ctx->params.ls_candidates - 1) / ctx->params.ls_candidates;
-  ctx->launches += 3 + 2 * rounds;
+  ctx->launches += 5 + 2 * rounds;
   CKL();
   return HEXOPT_OK;
 }
@@ -658,6 +676,7 @@ int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const
     NH += nh[m];
   }
   if (NV >= (int64_t)UINT32_MAX) return fail(ctx, HEXOPT_ERR_ARG, "too many vertices in one batch");
+  if (NH >= ((int64_t)1 << 29)) return fail(ctx, HEXOPT_ERR_ARG, "too many hexes in one batch (limit 2^29)");
   // validate hex ids (host, integer pass over the input)
   {
     int64_t ho = 0;

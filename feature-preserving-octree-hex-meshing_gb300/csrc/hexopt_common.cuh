@@ -288,6 +288,19 @@ template <> struct SumAcc<float> {
   __device__ __forceinline__ double value() const { return double(s) + double(c); }
 };
 
+// Exclusive prefix sum of v over the 32 lanes of a warp (all lanes must call it); total = sum.
+__device__ __forceinline__ int warp_exclusive_sum(int v, int &total) {
+  const int lane = threadIdx.x & 31;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  total = __shfl_sync(0xffffffffu, x, 31);
+  return x - v;
+}
+
 // Block-level sum of NV doubles (all threads get nothing back; thread 0 gets the total).
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double (*smem)[32]) {

@@ -36,7 +36,7 @@ struct KArgs {
   int energy;
   int cg_max_iter;
   int ls_cand;
-  int pad_;
+  int n_meshes;
   double cg_tol;
   double sc_exp_f;
   int hthreads;   // block size of hex-kind launches (<= 128)
@@ -44,6 +44,12 @@ struct KArgs {
   // adjoint
   double *Xa;     // evaluation point (AoS4 FP64)
   double *grad;   // dE/dX (AoS4 FP64)
+  // flip-avoiding step bound: corner tets whose cubic may have a root in [0, 1.25] (8 h + K),
+  // their meshes, the count, and the per-mesh minimum root (bits of a non-negative double)
+  uint32_t *root_list;
+  int32_t *root_mesh;
+  unsigned *root_count;
+  unsigned long long *root_min;
 };
 
 template <typename ET, typename VT> void launch_precompute(const KArgs &a, int64_t nblk, cudaStream_t st);

@@ -703,9 +703,8 @@ __device__ __forceinline__ void tet_energy_acc(const KArgs &a, int64_t h, const 
 // margin that covers the ET rounding (bounded through Hadamard's inequality), there is no root in
 // the interval and the tet is skipped.  Otherwise the smallest positive root is solved in FP64
 // exactly as the reference does.
-template <typename ET, typename VT, int K>
-__device__ __forceinline__ void tet_bound(const KArgs &a, const uint32_t hv[8], const ET E[3][3], const ET D[3][3],
-                                          double &mn) {
+template <typename ET, int K>
+__device__ __forceinline__ bool tet_bound(const ET E[3][3], const ET D[3][3]) {
   ET ne[3], nd[3];
 #pragma unroll
   for (int j = 0; j < 3; j++) {
@@ -740,12 +739,56 @@ __device__ __forceinline__ void tet_bound(const KArgs &a, const uint32_t hv[8], 
   const ET err = rel * (M0 + M1 * T + M2 * T * T + M3 * T * T * T);
   const bool pos = b0 > err && b1 > err && b2 > err && b3 > err;
   const bool neg = b0 < -err && b1 < -err && b2 < -err && b3 < -err;
-  if (pos || neg) return;
-  double E64[3][3], D64[3][3];
-  tet_edges<K>(a.X, hv, E64);
-  tet_dir<VT, K>(reinterpret_cast<const VT *>(a.d), hv, D64);
-  mn = fmin(mn, min_pos_root(E64, D64));
+  return !(pos || neg);
 }
+
+// Corner tet K of hex h (K at run time) -> its FP64 edges and direction edges.
+template <typename VT>
+__device__ __forceinline__ void tet_edges_dir(const KArgs &a, const uint32_t hv[8], int K, double E[3][3],
+                                              double D[3][3]) {
+  const VT *d = reinterpret_cast<const VT *>(a.d);
+  switch (K) {
+    case 0: tet_edges<0>(a.X, hv, E); tet_dir<VT, 0>(d, hv, D); break;
+    case 1: tet_edges<1>(a.X, hv, E); tet_dir<VT, 1>(d, hv, D); break;
+    case 2: tet_edges<2>(a.X, hv, E); tet_dir<VT, 2>(d, hv, D); break;
+    case 3: tet_edges<3>(a.X, hv, E); tet_dir<VT, 3>(d, hv, D); break;
+    case 4: tet_edges<4>(a.X, hv, E); tet_dir<VT, 4>(d, hv, D); break;
+    case 5: tet_edges<5>(a.X, hv, E); tet_dir<VT, 5>(d, hv, D); break;
+    case 6: tet_edges<6>(a.X, hv, E); tet_dir<VT, 6>(d, hv, D); break;
+    default: tet_edges<7>(a.X, hv, E); tet_dir<VT, 7>(d, hv, D); break;
+  }
+}
+
+// Dense exact pass over the recorded tets: the reference's smallest positive root in FP64, one
+// tet per thread, reduced per mesh by atomicMin on the bits of the (non-negative) root.
+template <typename VT>
+__global__ void __launch_bounds__(128) k_ls_roots(KArgs a) {
+  const unsigned n = *a.root_count;
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const uint32_t code = a.root_list[e];
+    const int64_t h = code >> 3;
+    uint32_t hv[8];
+    load_hex(a.hexv, h, hv);
+    double E[3][3], D[3][3];
+    tet_edges_dir<VT>(a, hv, (int)(code & 7), E, D);
+    const double r = min_pos_root(E, D);
+    atomicMin(a.root_min + a.root_mesh[e], (unsigned long long)__double_as_longlong(r));
+  }
+}
+
+// max_step = min(1, 0.8 min_root) per mesh; re-arms the minimum and the list for the next call.
+__global__ void k_ls_bound_finish(KArgs a, int n_meshes) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m == 0) *a.root_count = 0;
+  if (m >= n_meshes) return;
+  MeshScalars &S = a.sc[m];
+  const double r = __longlong_as_double((long long)a.root_min[m]);
+  S.min_root = r;
+  S.max_step = fmin(1.0, r * 0.8);
+  a.root_min[m] = (unsigned long long)__double_as_longlong(INFINITY);
+}
+
+
 
 // Pass 1: step bound over the tets and the quality energy at the current X.
 template <typename ET, typename VT>
@@ -754,7 +797,8 @@ __global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
   const int64_t h = sg.begin + threadIdx.x;
   const MeshDesc md = a.mesh[sg.mesh];
   MeshScalars &S = a.sc[sg.mesh];
-  double mn[1] = {INFINITY}, eq[1] = {0};
+  double eq[1] = {0};
+  unsigned need = 0;  // bit K: corner tet K needs the exact root
   if (h < sg.end) {
     uint32_t hv[8];
     load_hex(a.hexv, h, hv);
@@ -776,25 +820,36 @@ __global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
       ET E[3][3], D[3][3];                                        \
       tet_E12<K>(E12, E);                                         \
       tet_E12<K>(D12, D);                                         \
-      tet_bound<ET, VT, K>(a, hv, E, D, mn[0]);                   \
+      if (tet_bound<ET, K>(E, D)) need |= 1u << K;              \
       tet_energy_acc<ET, VT, K>(a, h, hv, gs, E, 0.0, efast, eslow); \
     }
     HX_LS(0) HX_LS(1) HX_LS(2) HX_LS(3) HX_LS(4) HX_LS(5) HX_LS(6) HX_LS(7)
 #undef HX_LS
     eq[0] = S.M * (efast.value() + eslow);
   }
+  {
+    // record the tets that need the exact root (one reservation per warp)
+    const int k = __popc(need);
+    int total;
+    const int off = warp_exclusive_sum(k, total);
+    unsigned base = 0;
+    if ((threadIdx.x & 31) == 0 && total > 0) base = atomicAdd(a.root_count, (unsigned)total);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    int w = 0;
+    for (int K = 0; K < 8; K++)
+      if ((need >> K) & 1u) {
+        a.root_list[base + off + w] = (uint32_t)(h * 8 + K);
+        a.root_mesh[base + off + w] = sg.mesh;
+        w++;
+      }
+  }
   __shared__ double smem[1][32];
-  block_min<1>(mn, smem);
-  double acc[2] = {0, 0};
-  if (threadIdx.x == 0) acc[0] = mn[0];
+  double acc[1] = {0};
   block_sum<1>(eq, smem);
-  if (threadIdx.x == 0) acc[1] = eq[0];
-  if (publish_partials<2>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
-    double m = gather_partials_min(a.partials, md.hblk0, md.nhblk, 2, 0, smem);
-    double e = gather_partials_sum(a.partials, md.hblk0, md.nhblk, 2, 1, smem);
+  if (threadIdx.x == 0) acc[0] = eq[0];
+  if (publish_partials<1>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
+    double e = gather_partials_sum(a.partials, md.hblk0, md.nhblk, 1, 0, smem);
     if (threadIdx.x == 0) {
-      S.min_root = m;
-      S.max_step = fmin(1.0, m * 0.8);
       S.old_eq = e;
       S.ls_done = 0;
       a.counters[sg.mesh] = 0;
@@ -1028,6 +1083,8 @@ void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cu
 template <typename ET, typename VT>
 void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st) {
   k_ls_bound<ET, VT><<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
+  k_ls_roots<VT><<<152 * 4, 128, 0, st>>>(a);
+  k_ls_bound_finish<<<(a.n_meshes + 127) / 128, 128, 0, st>>>(a, a.n_meshes);
   k_ls_soft<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a, -1);
   const int rounds = (kHalvings + 1 + a.ls_cand - 1) / a.ls_cand;
   for (int r = 0; r < rounds; r++) {
