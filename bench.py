@@ -312,6 +312,155 @@ def run_ours(args):
     return 0
 
 
+def run_batch(args):
+    """The batching workload: args.batch meshes of uneven size (per-axis dims in [12, 96]), each
+    with its own superellipsoid target, all advanced by one feature-alignment iteration per step
+    in one launch per stage (graph replay, autotuned).  One JSON line, value = iterations/s of
+    the whole batch; the plain FP64 path is timed on the same batch for the ratio."""
+    rank, ws, tdist = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import build
+    build.build()
+    import hexopt
+    from hexopt import workloads
+    t0 = time.perf_counter()
+    probs = workloads.grid_batch(args.batch, seed=rank)
+    nh = sum(len(p["H"]) for p in probs)
+    nv = sum(len(p["V"]) for p in probs)
+    ntri = sum(len(p["TF"]) for p in probs)
+    ctx = hexopt.Context(local)
+    workloads.load(ctx, probs)
+    t_load = time.perf_counter() - t0
+    res = {}
+    for name, prec in (("fp64", hexopt.FP64), ("mixed", hexopt.MIXED)):
+        if name == "fp64" and args.skip_compare:
+            continue
+        ctx.set_positions(np.concatenate([p["V"] for p in probs]))
+        ctx.fa_begin(lamda0=0.05, precision=prec, weight_opt=0.001)
+        tune = ctx.autotune() if (name == "mixed" and not args.no_autotune) else None
+        ctx.use_graph(True)
+        steps = args.steps if name == "mixed" else min(args.steps, 3)
+        for _ in range(args.warmup):
+            ctx.fa_step(hausdorff=not args.no_hausdorff, report=False)
+        ctx.sync()
+        clocks = ClockSampler(local)
+        clocks.start()
+        barrier(tdist)
+        l0 = ctx.launch_count()
+        profiler(True)
+        ctx.timer_start()
+        for _ in range(steps):
+            ctx.fa_step(hausdorff=not args.no_hausdorff, report=False)
+        ms = ctx.timer_stop()
+        profiler(False)
+        clk = clocks.stop()
+        ms = max_over_ranks(tdist, ms)
+        rep = ctx.fa_step(hausdorff=not args.no_hausdorff)
+        res[name] = dict(iters_per_s=steps / (ms / 1e3), ms=ms / steps, launches=ctx.launch_count() - l0,
+                         min_J=min(r["min_J"] for r in rep), clocks=clk, tune=tune, steps=steps)
+    m = res["mixed"]
+    out = {"metric": METRIC, "value": ws * m["iters_per_s"], "unit": UNIT, "n_gpus": ws, "steps": m["steps"],
+           "warmup": args.warmup, "ms_per_step": m["ms"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+           "config": {"workload": f"grid_batch{args.batch}: {args.batch} jittered grids (per-axis dims uniform in "
+                                  f"[12, 96], sigma 0.15h, seed {rank}), each with its own superellipsoid target "
+                                  f"(exponent in [2, 6], 20k-200k triangles); one launch per stage over the batch, "
+                                  f"CUDA-graph replay, Hausdorff every iteration "
+                                  f"{'off' if args.no_hausdorff else 'on'}",
+                      "meshes": args.batch, "hexes": nh, "vertices": nv, "target_triangles": ntri,
+                      "tuning": m["tune"], "load_s": t_load},
+           "mhex_per_s": ws * m["iters_per_s"] * nh / 1e6, "gpu_launches": m["launches"], "clocks": m["clocks"],
+           "min_J": m["min_J"]}
+    if "fp64" in res:
+        out.update({"fp64_iters_per_s": res["fp64"]["iters_per_s"],
+                    "mixed_over_fp64": m["iters_per_s"] / res["fp64"]["iters_per_s"]})
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+def run_adjoint(args):
+    """The differentiation workload: symmetric Dirichlet over the corner tets of the n^3 grid
+    plus 100 x squared closest-point distance of the boundary vertices (corner terms at the
+    closest points of the evaluation point), operator frozen at the precompute.  Times the
+    forward and backward kernels (CUDA events) and checks the gradient against FP64 central
+    differences (h = 1e-6 and h/2, Richardson-extrapolated) on args.fd_coords seeded
+    coordinates, the closest points recomputed at every perturbed point."""
+    rank, ws, tdist = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import build
+    build.build()
+    import hexopt
+    from hexopt import workloads
+    n = args.grid if args.grid != GRID_N else 96
+    p = workloads.adjoint_problem(n, seed=rank)
+    V, b = p["V"], p["corners"]
+    ctx = hexopt.Context(local)
+    ctx.upload([(V, p["H"])])
+    ctx.set_target(0, p["TV"], p["TF"])
+    C = ctx.signed_distance(0, V[b])[2]
+    ctx.set_corners([b], [C])
+    ctx.set_weights(p["weight"], 0.0, 0.0)
+    ctx.slim_precompute(precision=hexopt.FP64, weight_opt=0.001)
+    E0 = ctx.energy_fwd(V)[0]
+    G = ctx.energy_bwd()
+    t_fwd = ctx.time_stage(6, reps=20)
+    t_bwd = ctx.time_stage(7, reps=20)
+    rng = np.random.default_rng(1234 + rank)
+    coords = rng.choice(len(V) * 3, size=args.fd_coords, replace=False)
+    slot = {int(v): k for k, v in enumerate(b)}
+    h = 1e-6
+    errs, gfs, gas, conv = [], [], [], []
+    scale = float(np.sqrt(np.mean(G ** 2)))
+    for c in coords:
+        v, ax = divmod(int(c), 3)
+        def central(step):
+            fd = []
+            for sgn in (1.0, -1.0):
+                Vp = V.copy()
+                Vp[v, ax] += sgn * step
+                if v in slot:
+                    Cp = C.copy()
+                    Cp[slot[v]] = ctx.signed_distance(0, Vp[v:v + 1])[2][0]
+                    ctx.set_corners([b], [Cp])
+                fd.append(ctx.energy_fwd(Vp)[0])
+                if v in slot:
+                    ctx.set_corners([b], [C])
+            return (fd[0] - fd[1]) / (2 * step)
+        # Richardson extrapolation of the central differences at h and h/2 (cancels the h^2
+        # truncation term, large next to near-degenerate tets); |D(h/2) - D(h)| estimates the
+        # differences' own error, and a coordinate whose estimate exceeds 1e-4 of its gradient is
+        # one where finite differences have not converged (a vertex of a near-singular tet)
+        d1, d2 = central(h), central(h / 2)
+        g_fd = (4 * d2 - d1) / 3
+        g = G[v, ax]
+        gfs.append(g_fd)
+        gas.append(g)
+        errs.append(abs(g_fd - g) / max(abs(g), 1e-2 * scale))
+        conv.append(abs(d2 - d1) <= 1e-4 * max(abs(g), 1e-2 * scale))
+    gfs, gas, conv, errs = np.array(gfs), np.array(gas), np.array(conv), np.array(errs)
+    ctx.close()
+    out = {"metric": "adjoint fwd+bwd per s", "value": 1e3 / (t_fwd + t_bwd), "unit": "evals/s", "n_gpus": 1,
+           "steps": 20, "warmup": 1, "ms_per_step": t_fwd + t_bwd, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"grid{n}_adjoint: {len(p['H'])} hexes, symmetric Dirichlet over 8 corner tets + "
+                                  f"100 x squared closest-point distance of {len(b)} boundary vertices "
+                                  f"(200k-triangle superellipsoid), operator frozen at the precompute"},
+           "fwd_ms": t_fwd, "bwd_ms": t_bwd, "energy": E0,
+           "fd_check": {"coords": int(args.fd_coords), "h": h, "method": "central, Richardson from h and h/2",
+                        "rel_err_all": float(np.linalg.norm(gfs - gas) / np.linalg.norm(gas)),
+                        "max_coord_rel_err_all": float(errs.max()), "median_coord_rel_err": float(np.median(errs)),
+                        "fd_converged": int(conv.sum()),
+                        "rel_err_converged": float(np.linalg.norm((gfs - gas)[conv]) / np.linalg.norm(gas[conv])),
+                        "max_coord_rel_err_converged": float(errs[conv].max()),
+                        "within_1e-4": int((errs <= 1e-4).sum()),
+                        "criterion": "rel_err <= 1e-4 (|g_fd - g| / |g| over the sampled coordinates)"}}
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -325,9 +474,20 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=GRID_N,
                     help="grid cells per axis (128 = the 2.1M-hex workload; smaller only for profiler captures)")
+    ap.add_argument("--workload", default="grid128", choices=["grid128", "batch", "adjoint"],
+                    help="grid128: the headline line (default); batch: the batching workload; "
+                         "adjoint: the differentiation workload")
+    ap.add_argument("--batch", type=int, default=256, help="meshes in the batching workload")
+    ap.add_argument("--fd-coords", type=int, default=1000, help="coordinates of the adjoint's FD check")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
-    return run_reference(args) if args.impl == "reference" else run_ours(args)
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
+    return run_ours(args)
 
 
 if __name__ == "__main__":

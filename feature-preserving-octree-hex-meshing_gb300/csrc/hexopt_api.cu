@@ -1625,6 +1625,11 @@ static void stage_launch(hexopt_ctx *ctx, int stage) {
       if (ctx->mixed) launch_sj_check(a, hb, ctx->st);
       else launch_scaled_jacobian(a, hb, nullptr, ctx->HJs.as<double>(), ctx->st);
       break;
+    case 6: launch_energy_fwd<ET>(a, hb, ctx->kind[K_CONS].nblk, ctx->st); break;
+    case 7:
+      cudaMemsetAsync(ctx->grad.p, 0, sizeof(double) * 4 * ctx->NV, ctx->st);
+      launch_energy_bwd<ET>(a, hb, ctx->kind[K_CONS].nblk, ctx->st);
+      break;
     case 4: run_projection(ctx); break;
     default: break;
   }
@@ -1636,7 +1641,9 @@ int hexopt_time_stage(hexopt_ctx *ctx, int stage, int reps, double *ms_per_launc
   int rc = check_ctx(ctx);
   if (rc) return rc;
   if (!ctx->precomputed) return fail(ctx, HEXOPT_ERR_STATE, "time_stage before slim_precompute");
-  if (stage < 0 || stage > 5 || reps <= 0) return fail(ctx, HEXOPT_ERR_ARG, "time_stage: bad stage or reps");
+  if (stage < 0 || stage > 7 || reps <= 0) return fail(ctx, HEXOPT_ERR_ARG, "time_stage: bad stage or reps");
+  if (stage >= 6 && (!ctx->Xa.p || !ctx->grad.p))
+    return fail(ctx, HEXOPT_ERR_STATE, "time_stage: energy stages need one energy_fwd and one energy_bwd first");
   if (stage <= 2) {
     // make the solver state well defined (one iteration), then reopen the per-mesh CG and
     // line-search flags so the timed launches do their full work

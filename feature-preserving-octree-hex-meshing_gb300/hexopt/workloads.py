@@ -6,6 +6,11 @@ optimiser is measured on, and the calls that load them into a Context.
                           (exponent 4, float32 coordinates) -- n = 128 is the 2.1M-hex workload.
   cylinder()              O-grid hex mesh of the r = 0.5, h = 1 cylinder; the two cap circles are
                           feature curves (64 x 8 target triangulation, 1152 triangles).
+  grid_batch(n_meshes)    the batching workload: jittered structured grids with per-axis dims
+                          drawn from [12, 96], each tied to its own superellipsoid (exponent in
+                          [2, 6], 20k-200k triangles); 256 meshes is the ~40M-hex batch.
+  adjoint_problem(n)      the differentiation workload: the n^3 grid with 100 x squared
+                          closest-point distance of the boundary vertices as corner terms.
 """
 from __future__ import annotations
 
@@ -28,6 +33,44 @@ def grid_superellipsoid(n=128, sigma=0.2, seed=0, n_tri=200_000, exponent=4.0):
     return dict(name=f"grid{n}_superellipsoid", V=V, H=H, TV=TV, TF=TF, regular=regular,
                 lines=np.zeros(0, np.int32), line_curve=np.zeros(0, np.int32), curves=[], closed=[],
                 corners=np.zeros(0, np.int32), surface=meshgen.quads_to_tris(meshgen.grid_boundary_quads(n)))
+
+
+def grid_box_superellipsoid(dims, sigma, seed, n_tri, exponent):
+    """One mesh of the batch: an nx x ny x nz grid of the unit cube (jitter in units of the
+    smallest cell edge) tied to a superellipsoid of the given exponent."""
+    nx, ny, nz = (int(d) for d in dims)
+    V, H = meshgen.grid_hex(nx, ny, nz)
+    b = meshgen.grid_boundary_mask(nx, ny, nz)
+    V = meshgen.jitter(V, ~b, 1.0 / max(nx, ny, nz), seed, sigma=sigma)
+    TV, TF = meshgen.superellipsoid(n_tri, exponent=exponent, radius=0.5)
+    regular = np.nonzero(b)[0].astype(np.int32)
+    return dict(name=f"grid{nx}x{ny}x{nz}_se{exponent:.2f}", V=V, H=H, TV=TV, TF=TF, regular=regular,
+                lines=np.zeros(0, np.int32), line_curve=np.zeros(0, np.int32), curves=[], closed=[],
+                corners=np.zeros(0, np.int32),
+                surface=meshgen.quads_to_tris(meshgen.grid_boundary_quads(nx, ny, nz)))
+
+
+def grid_batch(n_meshes=256, seed=0, dmin=12, dmax=96, sigma=0.15, tri_min=20_000, tri_max=200_000):
+    """The batching workload (seeded): per mesh, per-axis dims uniform in [dmin, dmax], Gaussian
+    jitter sigma * h, and a superellipsoid target with exponent uniform in [2, 6] and a
+    triangle count uniform in [tri_min, tri_max]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for m in range(n_meshes):
+        dims = rng.integers(dmin, dmax + 1, 3)
+        exponent = float(rng.uniform(2.0, 6.0))
+        n_tri = int(rng.integers(tri_min, tri_max + 1))
+        out.append(grid_box_superellipsoid(dims, sigma, seed * 100003 + m, n_tri, exponent))
+    return out
+
+
+def adjoint_problem(n=96, sigma=0.2, seed=0, n_tri=200_000, weight=100.0):
+    """The differentiation workload: grid_superellipsoid(n) whose boundary vertices carry corner
+    terms weight * |x - cp(x)|^2 (cp = closest point on the target, recomputed wherever the
+    energy is evaluated); no tangent-plane or line terms."""
+    p = grid_superellipsoid(n, sigma=sigma, seed=seed, n_tri=n_tri)
+    p = dict(p, name=f"grid{n}_adjoint", corners=p["regular"], regular=np.zeros(0, np.int32), weight=weight)
+    return p
 
 
 def cylinder(n_core=8, n_ring=6, n_z=16):

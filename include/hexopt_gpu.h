@@ -210,8 +210,9 @@ HEXOPT_API int hexopt_timer_stop(hexopt_ctx *ctx, double *ms);
  *   3 scaled-Jacobian check as the feature-alignment loop runs it (FP64 in plain mode; FP32
  *     screen with FP64 re-evaluation near the minimum in mixed mode)
  *   4 feature projection        5 one full SLIM iteration
+ *   6 adjoint forward (energy at the last energy_fwd point)   7 adjoint backward (gradient)
  * Stages 0-2 leave the solver scratch in an unspecified state; positions are not modified by
- * 0-4 (stage 5 advances them like slim_iterate). */
+ * 0-4 (stage 5 advances them like slim_iterate); 6-7 need one energy_fwd and energy_bwd first. */
 HEXOPT_API int hexopt_time_stage(hexopt_ctx *ctx, int stage, int reps, double *ms_per_launch);
 /* Kernel launches issued by this context since creation (for the bench's launch count). */
 HEXOPT_API int64_t hexopt_launch_count(const hexopt_ctx *ctx);

@@ -1,0 +1,119 @@
+"""The differentiation, batching and uniform-sample Hausdorff workloads at test sizes.
+
+- Adjoint through the projection: symmetric Dirichlet + 100 x squared closest-point distance of
+  the boundary vertices (corner terms at the closest points of the evaluation point).  The
+  gradient must match FP64 central differences (h = 1e-6, closest points recomputed at every
+  perturbed point) within 1e-4 relative over the seeded coordinates (|g_fd - g| / |g| of the
+  sampled vectors), and each coordinate within 1e-3.  The differences are Richardson-extrapolated
+  from h and h/2: near-degenerate tets of the jittered grid give |J^-1|^2 third derivatives
+  large enough that a single central difference at h = 1e-6 carries ~1e-4 of truncation error.
+- Batching: meshes of uneven size with their own targets, advanced together by the
+  feature-alignment step, give each mesh the result of running it alone.  Float atomics make the
+  vertex sums order-dependent and the truncated CG + line search amplify that to a few 1e-9 after
+  two steps, so positions are compared to 1e-7 (a tenth of the 1e-6 x diagonal parity bar) and
+  the reported scalars to 1e-7 relative, instead of bit equality.
+- Uniform-sample Hausdorff: the GPU sample distances against the oracle's on the same samples.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def hx():
+    import build
+    build.build()
+    import hexopt
+    return hexopt
+
+
+def test_adjoint_through_projection_matches_central_differences(hx):
+    from hexopt import workloads
+    p = workloads.adjoint_problem(20, n_tri=20000)
+    V, b = p["V"], p["corners"]
+    ctx = hx.Context(0)
+    try:
+        ctx.upload([(V, p["H"])])
+        ctx.set_target(0, p["TV"], p["TF"])
+        C = ctx.signed_distance(0, V[b])[2]
+        ctx.set_corners([b], [C])
+        ctx.set_weights(p["weight"], 0.0, 0.0)
+        ctx.slim_precompute(precision=hx.FP64, weight_opt=0.001)
+        ctx.energy_fwd(V)
+        G = ctx.energy_bwd()
+        scale = float(np.sqrt(np.mean(G ** 2)))
+        slot = {int(v): k for k, v in enumerate(b)}
+        rng = np.random.default_rng(7)
+        # half the coordinates on boundary vertices (the projection term), half anywhere
+        vs = np.concatenate([rng.choice(b, 60, replace=False), rng.choice(len(V), 60, replace=False)])
+        h = 1e-6
+        worst = 0.0
+        gf, ga = [], []
+        for v in vs:
+            ax = int(rng.integers(0, 3))
+            def central(step):
+                fd = []
+                for sgn in (1.0, -1.0):
+                    Vp = V.copy()
+                    Vp[v, ax] += sgn * step
+                    if int(v) in slot:
+                        Cp = C.copy()
+                        Cp[slot[int(v)]] = ctx.signed_distance(0, Vp[v:v + 1])[2][0]
+                        ctx.set_corners([b], [Cp])
+                    fd.append(ctx.energy_fwd(Vp)[0])
+                    if int(v) in slot:
+                        ctx.set_corners([b], [C])
+                return (fd[0] - fd[1]) / (2 * step)
+            g_fd = (4 * central(h / 2) - central(h)) / 3
+            gf.append(g_fd)
+            ga.append(G[v, ax])
+            worst = max(worst, abs(g_fd - G[v, ax]) / max(abs(G[v, ax]), 1e-2 * scale))
+        gf, ga = np.array(gf), np.array(ga)
+        assert np.linalg.norm(gf - ga) / np.linalg.norm(ga) <= 1e-4
+        assert worst <= 1e-3, worst
+    finally:
+        ctx.close()
+
+
+def test_batch_of_uneven_meshes_equals_individual_runs(hx):
+    from hexopt import workloads
+    probs = workloads.grid_batch(4, seed=3, dmin=5, dmax=14, tri_min=2000, tri_max=6000)
+    def run(ps, steps=2):
+        ctx = hx.Context(0)
+        try:
+            workloads.load(ctx, ps)
+            ctx.fa_begin(lamda0=0.05, precision=hx.FP64, weight_opt=0.001)
+            for _ in range(steps):
+                reps = ctx.fa_step(hausdorff=True)
+            return ctx.get_positions(), reps
+        finally:
+            ctx.close()
+    Vb, rb = run(probs)
+    off = 0
+    for m, p in enumerate(probs):
+        Vm, rm = run([p])
+        n = len(p["V"])
+        np.testing.assert_allclose(Vb[off:off + n], Vm, rtol=0, atol=1e-7)
+        for k in ("min_J", "energy", "hausdorff_max"):
+            assert rb[m][k] == pytest.approx(rm[0][k], rel=1e-7, abs=1e-12), (m, k)
+        off += n
+
+
+def test_uniform_sample_hausdorff_matches_oracle(hx, oracle):
+    from hexopt import meshgen, workloads
+    p = workloads.cylinder()
+    V0, F0 = p["TV"], p["TF"]
+    V1, F1 = p["V"], p["surface"]
+    ctx = hx.Context(0)
+    try:
+        D, mx, ave = hx.hausdorff_uniform(V0, F0, V1, F1, n_samples=10_000, seed=5, ctx=ctx)
+    finally:
+        ctx.close()
+    S0 = meshgen.area_samples(V0, F0, 10_000, 5)
+    S1 = meshgen.area_samples(V1, F1, 10_000, 6)
+    d0 = oracle.point_face_distance(S0, V1, F1)
+    d1 = oracle.point_face_distance(S1, V0, F0)
+    k0, k1 = d0[d0 < D], d1[d1 < D]
+    assert mx == pytest.approx(max(k0.max(), k1.max()), rel=1e-12)
+    assert ave == pytest.approx(max(k0.mean(), k1.mean()), rel=1e-12)
