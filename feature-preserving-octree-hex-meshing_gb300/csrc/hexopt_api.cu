@@ -127,7 +127,8 @@ struct hexopt_ctx {
   // targets / surfaces
   std::vector<TargetHost> tgt;
   std::vector<SurfaceHost> surf;
-  DBuf tgt_d, surf_d, hm_d, tgt_vs_d, surf_vs_d;
+  DBuf tgt_d, surf_d, refit_d, hm_d, tgt_vs_d, surf_vs_d;
+  int64_t n_surf_faces = 0;  // surface faces of the batch (items of K_SURFF)
   DBuf ovf_item, ovf_mesh, ovf_count, ovf_best, ovf_face, ovf_pt, hdist;
   // batched exact evaluation of the BVH queries (shared by projection and both Hausdorff sides)
   DBuf cand_leaf, cand_qi, cand_x, cand_d, cand_count, q_off, q_cnt, qpos, q_mesh, fb_count, fb_item, fb_mesh;
@@ -240,8 +241,16 @@ int rebuild_tables(hexopt_ctx *ctx) {
     for (int m = 0; m < M; m++) { cnt[m] = m < (int)ctx->surf_vs_cnt.size() ? ctx->surf_vs_cnt[m] : 0; it0[m] = o; o += cnt[m]; }
     build_kind(ctx, K_SURFV, cnt, it0);
   }
-  for (int m = 0; m < M; m++) { cnt[m] = 0; it0[m] = 0; }
-  build_kind(ctx, K_SURFF, cnt, it0);
+  {
+    int64_t o = 0;
+    for (int m = 0; m < M; m++) {
+      cnt[m] = (m < (int)ctx->surf.size() && ctx->surf[m].set) ? ctx->surf[m].nf : 0;
+      it0[m] = o;
+      o += cnt[m];
+    }
+    ctx->n_surf_faces = o;
+    build_kind(ctx, K_SURFF, cnt, it0);
+  }
   for (int m = 0; m < M; m++) {
     MeshDesc &d = ctx->md[m];
     d.hblk0 = d.kblk0[K_HEX]; d.nhblk = d.knblk[K_HEX];
@@ -464,6 +473,21 @@ int upload_targets_table(hexopt_ctx *ctx) {
     sd[m] = b;
   }
   CK(upload(ctx->surf_d, sd.data(), sd.size(), ctx->st));
+  std::vector<RefitDev> rd(ctx->n_meshes);
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    RefitDev r{};
+    SurfaceHost &s = ctx->surf[m];
+    r.b = sd[m];
+    if (s.set) {
+      r.box = s.box.as<float>();
+      r.parent = s.parent.as<int32_t>();
+      r.counters = s.counters.as<unsigned>();
+      r.node = s.node.as<float4>();
+      r.leafd = s.leafd.as<float4>();
+    }
+    rd[m] = r;
+  }
+  CK(upload(ctx->refit_d, rd.data(), rd.size(), ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
   return HEXOPT_OK;
 }
@@ -578,21 +602,11 @@ int run_projection(hexopt_ctx *ctx) {
 }
 
 int run_hausdorff(hexopt_ctx *ctx) {
-  // refit the dynamic surface trees at the current positions
-  for (int m = 0; m < ctx->n_meshes; m++) {
-    SurfaceHost &s = ctx->surf[m];
-    if (!s.set || s.nf == 0) continue;
-    BvhDev b{};
-    b.n = (int32_t)s.nf;
-    b.child = s.child.as<int32_t>();
-    b.leaf_face = s.leaf_face.as<int32_t>();
-    b.F = s.F.as<int32_t>();
-    b.X = ctx->X.as<double>();
-    b.node = s.node.as<float4>();
-    b.leafd = s.leafd.as<float4>();
-    bvh_refit(b, s.box.as<float>(), s.parent.as<int32_t>(), s.counters.as<unsigned>(), s.node.as<float4>(),
-              s.leafd.as<float4>(), ctx->st);
-    ctx->launches += 2;
+  // refit every mesh's surface tree at the current positions, one launch for the batch
+  if (ctx->n_surf_faces > 0) {
+    bvh_refit_batch(ctx->refit_d.as<RefitDev>(), ctx->kind[K_SURFF].dev.as<Seg>(), ctx->md_d.as<MeshDesc>(),
+                    ctx->kind[K_SURFF].nblk, ctx->block[K_SURFF] * ctx->ipt[K_SURFF], ctx->st);
+    ctx->launches += 1;
   }
   launch_haus_bbox(make_haus(ctx, K_SURFV), ctx->kind[K_SURFV].nblk, ctx->st);
   launch_haus_side(make_haus(ctx, K_TGTV), 0, ctx->kind[K_TGTV].nblk, ctx->st);

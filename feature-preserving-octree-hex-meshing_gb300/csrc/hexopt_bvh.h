@@ -27,6 +27,17 @@ struct BvhDev {
   const float4 *leafd;
 };
 
+// Per-mesh refit view of a dynamic (hex-boundary) surface tree: the tree and the buffers the
+// refit writes.
+struct RefitDev {
+  BvhDev b;
+  float *box;
+  const int32_t *parent;
+  unsigned *counters;
+  float4 *node;
+  float4 *leafd;
+};
+
 // Queries that exceed the per-thread traversal budget are finished by a warp-cooperative pass.
 struct Overflow {
   int64_t *item;     // query item ids
@@ -112,6 +123,10 @@ void bvh_karras(int n, const unsigned long long *keys, int32_t *child, int32_t *
 // refit boxes bottom-up and rewrite the packed node records
 void bvh_refit(const BvhDev &b, float *box, const int32_t *parent, unsigned *counters, float4 *node, float4 *leafd,
                cudaStream_t st);
+// every mesh's surface tree in one launch (segment table over the surface faces, kind K_SURFF);
+// node records written as each internal node's box is finalised
+void bvh_refit_batch(const RefitDev *R, const Seg *seg, const MeshDesc *md, int64_t nblk, int threads,
+                     cudaStream_t st);
 // both passes of the tangent-plane projection
 void launch_project(const ProjArgs &p, int64_t nblk, cudaStream_t st);
 void launch_curve_project(const ProjArgs &p, int64_t nblk, cudaStream_t st);

@@ -106,9 +106,11 @@ __device__ __forceinline__ float up(double x) { float f = __double2float_ru(x); 
 
 // Leaf boxes, leaf screening frames and bottom-up union.  counters: n - 1 zeros on entry, zeros
 // again on exit.
-__global__ void k_refit(BvhDev b, float *box, const int32_t *parent, unsigned *counters, float4 *leafd) {
-  const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= b.n) return;
+// Refit of leaf k: its screening frame and box, then the bottom-up walk; the second child to
+// arrive at an internal node forms that node's box (and, when `node` is given, its packed
+// record from the two now-final child boxes).
+__device__ __forceinline__ void refit_leaf(const BvhDev &b, float *box, const int32_t *parent, unsigned *counters,
+                                           float4 *leafd, float4 *node_rec, int32_t k) {
   const int n = b.n;
   double p[3][3];
   face_pts(b, b.leaf_face[k], p);
@@ -141,16 +143,44 @@ __global__ void k_refit(BvhDev b, float *box, const int32_t *parent, unsigned *c
     const int32_t l = b.child[2 * node], r = b.child[2 * node + 1];
     const float *bl = box + 6 * (int64_t)(l >= 0 ? l : n - 1 + ~l);
     const float *br = box + 6 * (int64_t)(r >= 0 ? r : n - 1 + ~r);
+    float L[6], R[6];
+#pragma unroll
+    for (int d = 0; d < 6; d++) { L[d] = __ldcg(bl + d); R[d] = __ldcg(br + d); }
     float *bn = box + 6 * (int64_t)node;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      bn[d] = fminf(__ldcg(bl + d), __ldcg(br + d));
-      bn[3 + d] = fmaxf(__ldcg(bl + 3 + d), __ldcg(br + 3 + d));
+      bn[d] = fminf(L[d], R[d]);
+      bn[3 + d] = fmaxf(L[3 + d], R[3 + d]);
+    }
+    if (node_rec) {
+      node_rec[4 * (int64_t)node] = make_float4(L[0], L[1], L[2], L[3]);
+      node_rec[4 * (int64_t)node + 1] = make_float4(L[4], L[5], R[0], R[1]);
+      node_rec[4 * (int64_t)node + 2] = make_float4(R[2], R[3], R[4], R[5]);
+      node_rec[4 * (int64_t)node + 3] = make_float4(__int_as_float(l), __int_as_float(r), 0.f, 0.f);
     }
     counters[node] = 0;
     __threadfence();
     node = parent[node];
   }
+}
+
+// Leaf boxes, leaf screening frames and bottom-up union.  counters: n - 1 zeros on entry, zeros
+// again on exit.
+__global__ void k_refit(BvhDev b, float *box, const int32_t *parent, unsigned *counters, float4 *leafd) {
+  const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= b.n) return;
+  refit_leaf(b, box, parent, counters, leafd, nullptr, k);
+}
+
+// All meshes' surface trees at once: one thread per surface face of the batch.
+__global__ void k_refit_batch(const RefitDev *R, const Seg *seg, const MeshDesc *md) {
+  const Seg sg = seg[blockIdx.x];
+  const int64_t i = sg.begin + threadIdx.x;
+  if (i >= sg.end) return;
+  const RefitDev &r = R[sg.mesh];
+  const int32_t k = (int32_t)(i - md[sg.mesh].kitem0[K_SURFF]);
+  if (k >= r.b.n) return;
+  refit_leaf(r.b, r.box, r.parent, r.counters, r.leafd, r.node, k);
 }
 
 // ------------------------------------------------------------------------------- queries
@@ -1331,6 +1361,10 @@ void bvh_morton(const BvhDev &b, const double lo[3], const double hi[3], unsigne
 void bvh_karras(int n, const unsigned long long *keys, int32_t *child, int32_t *parent, int32_t *leaf_face,
                 cudaStream_t st) {
   if (n > 0) k_karras<<<(n + 255) / 256, 256, 0, st>>>(n, keys, child, parent, leaf_face);
+}
+void bvh_refit_batch(const RefitDev *R, const Seg *seg, const MeshDesc *md, int64_t nblk, int threads,
+                     cudaStream_t st) {
+  if (nblk > 0) k_refit_batch<<<(unsigned)nblk, threads, 0, st>>>(R, seg, md);
 }
 void bvh_refit(const BvhDev &b, float *box, const int32_t *parent, unsigned *counters, float4 *node, float4 *leafd,
                cudaStream_t st) {
