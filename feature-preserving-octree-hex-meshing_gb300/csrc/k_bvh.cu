@@ -769,7 +769,7 @@ __device__ int warp_collect(const BvhDev &b, const double q[3], int32_t *sn, flo
   return __all_sync(0xffffffffu, ok) ? 0 : 1;
 }
 
-constexpr int kThreadBudget = 64;   // pops per query before handing over to the warp pass
+constexpr int kThreadBudget = 128;  // pops per query before handing over to the warp pass
 __device__ __forceinline__ unsigned warps_total() { return gridDim.x * (blockDim.x >> 5); }
 __device__ __forceinline__ unsigned warp_global() { return blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); }
 

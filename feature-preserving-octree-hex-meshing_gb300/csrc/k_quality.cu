@@ -103,16 +103,19 @@ __global__ void __launch_bounds__(128) k_sj_dev(KArgs a, const double *H_Js) {
 // frame; a corner whose FP32 value is within 1e-4 of zero (its sign, i.e. the inversion flag, is
 // in doubt) or whose edges are near the Precision guard is re-evaluated bit-exactly in FP64.
 // Per mesh: min, sum and inverted count (the deviation pass is not part of the check).
+// The FP32 minimum (fast corners) and the FP64 minimum (re-evaluated corners) are kept apart so
+// the per-corner minimum stays on the FP32 pipes; a corner re-evaluated in FP64 is rare.
 template <int K>
-__device__ __forceinline__ double corner_sj_fast(const float E12[12][3], const double *X, const uint32_t hv[8]) {
+__device__ __forceinline__ void corner_sj_fast(const float E12[12][3], const double *X, const uint32_t hv[8],
+                                               float &m32, double &m64) {
   float E[3][3];
   tet_E12<K>(E12, E);
   const float n1 = sqrtf(E[0][0] * E[0][0] + E[1][0] * E[1][0] + E[2][0] * E[2][0]);
   const float n2 = sqrtf(E[0][1] * E[0][1] + E[1][1] * E[1][1] + E[2][1] * E[2][1]);
   const float n3 = sqrtf(E[0][2] * E[0][2] + E[1][2] * E[1][2] + E[2][2] * E[2][2]);
   const float sj = det3(E) / (n1 * n2 * n3);
-  if (fabsf(sj) < 1e-4f || fminf(n1, fminf(n2, n3)) < 1e-5f || !(fabsf(sj) <= 2.f)) return corner_sj<K>(X, hv);
-  return double(sj);
+  if (fabsf(sj) < 1e-4f || fminf(n1, fminf(n2, n3)) < 1e-5f || !(fabsf(sj) <= 2.f)) m64 = fmin(m64, corner_sj<K>(X, hv));
+  else m32 = fminf(m32, sj);
 }
 
 __global__ void __launch_bounds__(128) k_sj_fast(KArgs a) {
@@ -126,11 +129,13 @@ __global__ void __launch_bounds__(128) k_sj_fast(KArgs a) {
     for (int c = 0; c < 8; c++) hv[c] = __ldg(a.hexv + hex_idx(h, c));
     float E12[12][3];
     hex_edges_pos(a.X, hv, E12);
-    double hm = 1.0;
-    hm = fmin(hm, corner_sj_fast<0>(E12, a.X, hv)); hm = fmin(hm, corner_sj_fast<1>(E12, a.X, hv));
-    hm = fmin(hm, corner_sj_fast<2>(E12, a.X, hv)); hm = fmin(hm, corner_sj_fast<3>(E12, a.X, hv));
-    hm = fmin(hm, corner_sj_fast<4>(E12, a.X, hv)); hm = fmin(hm, corner_sj_fast<5>(E12, a.X, hv));
-    hm = fmin(hm, corner_sj_fast<6>(E12, a.X, hv)); hm = fmin(hm, corner_sj_fast<7>(E12, a.X, hv));
+    float m32 = 1.f;
+    double m64 = 1.0;
+    corner_sj_fast<0>(E12, a.X, hv, m32, m64); corner_sj_fast<1>(E12, a.X, hv, m32, m64);
+    corner_sj_fast<2>(E12, a.X, hv, m32, m64); corner_sj_fast<3>(E12, a.X, hv, m32, m64);
+    corner_sj_fast<4>(E12, a.X, hv, m32, m64); corner_sj_fast<5>(E12, a.X, hv, m32, m64);
+    corner_sj_fast<6>(E12, a.X, hv, m32, m64); corner_sj_fast<7>(E12, a.X, hv, m32, m64);
+    const double hm = fmin(double(m32), m64);
     mn[0] = hm;
     acc[0] = hm;
     acc[1] = hm < 0 ? 1.0 : 0.0;

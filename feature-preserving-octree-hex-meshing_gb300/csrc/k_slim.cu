@@ -192,8 +192,9 @@ __device__ __forceinline__ void spmv_tet(const KArgs &a, int64_t h, int32_t gs, 
   scatter_cols<K>(G, F);
 }
 
+// 64 registers (8 blocks of 128 per SM): more gathers in flight outweigh the few spills
 template <typename ET>
-__global__ void __launch_bounds__(128) k_spmv(KArgs a) {
+__global__ void __launch_bounds__(128, 8) k_spmv(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
   if (a.sc[sg.mesh].cg_done) return;
   const int64_t h = sg.begin + threadIdx.x;
