@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(128) k_precompute(KArgs a) {
 // and to diag(L).
 template <typename ET, int K, bool PRE>
 __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs, const ET E12[12][3], ET M, ET exp_f,
-                                          int energy, ET Fb[8][3], ET Fr[8][3], ET Dg[8][3], bool &degenerate) {
+                                          int energy, const uint32_t hv[8], bool &degenerate) {
+  ET *gb = reinterpret_cast<ET *>(a.b), *gr = reinterpret_cast<ET *>(a.r), *gd = reinterpret_cast<ET *>(a.diag);
   ET E[3][3];
   tet_E12<K>(E12, E);
   ET *Sinv = reinterpret_cast<ET *>(a.Sinv);
@@ -106,14 +107,30 @@ __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs,
   ET Q[3][3], G[3][3];
   sym_mul(c, R, Q);
   apply_BT<K>(Q, gs, B, is, G);
-  scatter_cols<K>(G, Fb);
+  {
+    ET s0 = 0, s1 = 0, s2 = 0;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      atomic_add3(gb, hv[tet_v(K, j + 1)], G[0][j], G[1][j], G[2][j]);
+      s0 += G[0][j]; s1 += G[1][j]; s2 += G[2][j];
+    }
+    atomic_add3(gb, hv[tet_v(K, 0)], -s0, -s1, -s2);
+  }
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) R[i][j] -= J[i][j];
   sym_mul(c, R, Q);
   apply_BT<K>(Q, gs, B, is, G);
-  scatter_cols<K>(G, Fr);
+  {
+    ET s0 = 0, s1 = 0, s2 = 0;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      atomic_add3(gr, hv[tet_v(K, j + 1)], G[0][j], G[1][j], G[2][j]);
+      s0 += G[0][j]; s1 += G[1][j]; s2 += G[2][j];
+    }
+    atomic_add3(gr, hv[tet_v(K, 0)], -s0, -s1, -s2);
+  }
   ET *C = reinterpret_cast<ET *>(a.Ccoef);
   ET w[4];
   if (gs < 0) {
@@ -132,12 +149,12 @@ __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs,
     w[0] = g0[0] * g0[0] + g0[1] * g0[1] + g0[2] * g0[2];
   }
 #pragma unroll
-  for (int j = 0; j < 4; j++) {
-    const int cc = tet_v(K, j);
-    Dg[cc][0] += w[j] * c[0]; Dg[cc][1] += w[j] * c[1]; Dg[cc][2] += w[j] * c[2];
-  }
+  for (int j = 0; j < 4; j++) atomic_add3(gd, hv[tet_v(K, j)], w[j] * c[0], w[j] * c[1], w[j] * c[2]);
 }
 
+// Each corner tet scatters its right-hand-side, residual and diagonal contributions straight to
+// the vertex vectors (float atomics): holding 8 corners x 3 vectors per hex in registers would
+// halve the occupancy of this latency-bound kernel.
 template <typename ET, bool PRE>
 __global__ void __launch_bounds__(128) k_local(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
@@ -150,27 +167,15 @@ __global__ void __launch_bounds__(128) k_local(KArgs a) {
   const int32_t gs = a.gslot[h];
   ET E12[12][3];
   hex_edges_pos(a.X, hv, E12);
-  ET Fb[8][3], Fr[8][3], Dg[8][3];
-#pragma unroll
-  for (int c = 0; c < 8; c++)
-#pragma unroll
-    for (int r = 0; r < 3; r++) Fb[c][r] = Fr[c][r] = Dg[c][r] = ET(0);
   bool degenerate = false;
-  local_tet<ET, 0, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
-  local_tet<ET, 1, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
-  local_tet<ET, 2, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
-  local_tet<ET, 3, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
-  local_tet<ET, 4, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
-  local_tet<ET, 5, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
-  local_tet<ET, 6, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
-  local_tet<ET, 7, PRE>(a, h, gs, E12, M, exp_f, a.energy, Fb, Fr, Dg, degenerate);
-  ET *b = reinterpret_cast<ET *>(a.b), *r = reinterpret_cast<ET *>(a.r), *dg = reinterpret_cast<ET *>(a.diag);
-#pragma unroll
-  for (int c = 0; c < 8; c++) {
-    atomic_add3(b, hv[c], Fb[c][0], Fb[c][1], Fb[c][2]);
-    atomic_add3(r, hv[c], Fr[c][0], Fr[c][1], Fr[c][2]);
-    atomic_add3(dg, hv[c], Dg[c][0], Dg[c][1], Dg[c][2]);
-  }
+  local_tet<ET, 0, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
+  local_tet<ET, 1, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
+  local_tet<ET, 2, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
+  local_tet<ET, 3, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
+  local_tet<ET, 4, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
+  local_tet<ET, 5, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
+  local_tet<ET, 6, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
+  local_tet<ET, 7, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
   if (PRE && degenerate) atomicOr(&a.sc[sg.mesh].status, 2);
 }
 
