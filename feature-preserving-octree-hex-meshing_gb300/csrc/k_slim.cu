@@ -1,1058 +1,36 @@
-// k_slim.cu -- SLIM local/global iteration on sm_103a, one thread per hex (8 corner tets).
+// k_slim.cu -- launchers of the SLIM local/global iteration (kernels in k_slim.cuh).
 //
-// Stages (slim_m.cpp:1269-1288, one iteration of slim_solve2's fixed-N branch):
-//   k_precompute     slim_precompute: per-tet inverse rest scale 1/cbrt(6 vol) (cube targets) or
-//                    rest-edge inverse (own-shape targets)      grad.cpp:372-478 closed form
-//   k_local          update_weights_and_closest_rotations + buildRhs: per-tet SVD, SD weights,
-//                    stores C_t = M W^T W (6 values) and scatters A^T M f   slim_m.cpp:108-381, 1044-1092
-//   k_spmv           matrix-free  y += sum_t K_t x  with K_t = (D_t^T D_t) (x) C_t  (buildA + L = A^T M A,
-//                    slim_m.cpp:568-595, 918-1042, never assembled)
-//   k_soft_*         add_soft_constraints / compute_soft_const_energy   slim_m.cpp:597-714, 735-790
-//   k_cg_*           Eigen ConjugateGradient<Lower|Upper> + Jacobi, solved for the update
-//                    delta = x - x0 with an FP64 initial residual      ConjugateGradient.h:39-80
-//   k_ls_*           flip_avoiding_line_search + igl::line_search      flip_avoiding_line_search.cpp,
-//                                                                       line_search.cpp:10-53
-// Precision: ET = element coefficient / arithmetic type, VT = CG vector type.  FP64 mode uses
-// <double,double>.  MIXED uses <float,float>: edges are formed from FP64 positions in FP64 and
-// rounded once; the PCG solves for the update delta from an initial residual formed per element
-// as M W^T W (R - J) B^T (no cancellation against A x0); positions are updated in FP64; every
-// reduction accumulates in FP64; the step bound's root solve is FP64.
-#include "hexopt_common.cuh"
-#include "hexopt_kernels.h"
-#include "hexopt_elem.cuh"
+// Stages (slim_m.cpp:1269-1288, one iteration of slim_solve2's fixed-N branch): precompute, local
+// step, matrix-free PCG, flip-avoiding line search.  The line-search energy passes are compiled in
+// the k_ls_energy_*.cu units; this unit only declares them.
+#include "k_slim.cuh"
 
 namespace hexopt {
 
-// ------------------------------------------------------------------------------- precompute
-// slim_precompute alone (hexopt_slim_precompute): per-tet 1/cbrt(6 vol) of cube-target tets,
-// rest-edge inverse of own-shape tets, from the FP64 positions.
-template <typename ET>
-__global__ void __launch_bounds__(128) k_precompute(KArgs a) {
-  const Seg sg = a.hseg[blockIdx.x];
-  const int64_t h = sg.begin + threadIdx.x;
-  if (h >= sg.end) return;
-  uint32_t hv[8];
-  load_hex(a.hexv, h, hv);
-  const int32_t gs = a.gslot[h];
-  ET *Sinv = reinterpret_cast<ET *>(a.Sinv);
-  bool degenerate = false;
-#define HX_PRE(K)                                                                              \
-  {                                                                                            \
-    double E[3][3];                                                                            \
-    tet_edges<K>(a.X, hv, E);                                                                  \
-    const double d = det3(E);                                                                  \
-    degenerate |= (d == 0.0);                                                                  \
-    if (gs < 0) {                                                                              \
-      Sinv[tet_idx<1>(h, K, 0)] = ET(1.0 / cbrt(d));                                            \
-    } else {                                                                                   \
-      double A[3][3];                                                                          \
-      adj3(E, A);                                                                              \
-      double *B = a.Bgen + ((int64_t)gs * 8 + K) * 9;                                          \
-      _Pragma("unroll") for (int i = 0; i < 3; i++)                                            \
-      _Pragma("unroll") for (int j = 0; j < 3; j++) B[i * 3 + j] = A[i][j] / d;                 \
-      Sinv[tet_idx<1>(h, K, 0)] = ET(1);                                                       \
-    }                                                                                          \
-  }
-  HX_PRE(0) HX_PRE(1) HX_PRE(2) HX_PRE(3) HX_PRE(4) HX_PRE(5) HX_PRE(6) HX_PRE(7)
-#undef HX_PRE
-  if (degenerate) atomicOr(&a.sc[sg.mesh].status, 2);
-}
-
-// ------------------------------------------------------------------------------- local step
-// One corner tet of the fused local step: (optional) volume snapshot, J, SVD, SLIM weights, the
-// stored coefficients C' and the tet's contributions to b = A^T M f, to the initial residual
-// r0 = b - A x0 = sum_t M W^T W (R - J) B^T (formed per element, so it carries no cancellation)
-// and to diag(L).
-template <typename ET, int K, bool PRE>
-__device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs, const ET E12[12][3], ET M, ET exp_f,
-                                          int energy, const uint32_t hv[8], bool &degenerate) {
-  ET *gb = reinterpret_cast<ET *>(a.b), *gr = reinterpret_cast<ET *>(a.r), *gd = reinterpret_cast<ET *>(a.diag);
-  ET E[3][3];
-  tet_E12<K>(E12, E);
-  ET *Sinv = reinterpret_cast<ET *>(a.Sinv);
-  double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
-  ET is;
-  if (PRE) {
-    const ET d = det3(E);
-    degenerate |= (d == ET(0));
-    if (gs < 0) {
-      is = ET(1) / cbrt(d);
-    } else {
-      ET A[3][3];
-      adj3(E, A);
-#pragma unroll
-      for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) B[i * 3 + j] = double(A[i][j] / d);
-      is = ET(1);
-    }
-    Sinv[tet_idx<1>(h, K, 0)] = is;
-  } else {
-    is = Sinv[tet_idx<1>(h, K, 0)];
-  }
-  ET J[3][3];
-  apply_B<K>(E, gs, B, is, J);
-  ET R[3][3], U[3][3], s[3], Vm[3][3], m[3];
-  polar_svd3(J, R, U, s, Vm);
-  slim_weights(energy, exp_f, s, U, Vm, m, R);
-  // W = U diag(m) U^T is symmetric, so M W^T W = M U diag(m^2) U^T
-  ET c[6];
-  const ET m0 = M * m[0] * m[0], m1 = M * m[1] * m[1], m2 = M * m[2] * m[2];
-  c[0] = U[0][0] * U[0][0] * m0 + U[0][1] * U[0][1] * m1 + U[0][2] * U[0][2] * m2;
-  c[1] = U[1][0] * U[1][0] * m0 + U[1][1] * U[1][1] * m1 + U[1][2] * U[1][2] * m2;
-  c[2] = U[2][0] * U[2][0] * m0 + U[2][1] * U[2][1] * m1 + U[2][2] * U[2][2] * m2;
-  c[3] = U[0][0] * U[1][0] * m0 + U[0][1] * U[1][1] * m1 + U[0][2] * U[1][2] * m2;
-  c[4] = U[0][0] * U[2][0] * m0 + U[0][1] * U[2][1] * m1 + U[0][2] * U[2][2] * m2;
-  c[5] = U[1][0] * U[2][0] * m0 + U[1][1] * U[2][1] * m1 + U[1][2] * U[2][2] * m2;
-  ET Q[3][3], G[3][3];
-  sym_mul(c, R, Q);
-  apply_BT<K>(Q, gs, B, is, G);
-  {
-    ET s0 = 0, s1 = 0, s2 = 0;
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      atomic_add3(gb, hv[tet_v(K, j + 1)], G[0][j], G[1][j], G[2][j]);
-      s0 += G[0][j]; s1 += G[1][j]; s2 += G[2][j];
-    }
-    atomic_add3(gb, hv[tet_v(K, 0)], -s0, -s1, -s2);
-  }
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) R[i][j] -= J[i][j];
-  sym_mul(c, R, Q);
-  apply_BT<K>(Q, gs, B, is, G);
-  {
-    ET s0 = 0, s1 = 0, s2 = 0;
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      atomic_add3(gr, hv[tet_v(K, j + 1)], G[0][j], G[1][j], G[2][j]);
-      s0 += G[0][j]; s1 += G[1][j]; s2 += G[2][j];
-    }
-    atomic_add3(gr, hv[tet_v(K, 0)], -s0, -s1, -s2);
-  }
-  ET *C = reinterpret_cast<ET *>(a.Ccoef);
-  ET w[4];
-  if (gs < 0) {
-    const ET s2 = is * is;  // fold 1 / cbrt(6 vol)^2 into the stored coefficients
-#pragma unroll
-    for (int i = 0; i < 6; i++) C[tet_idx<6>(h, K, i)] = c[i] * s2;
-    w[0] = ET(3) * s2; w[1] = w[2] = w[3] = s2;  // |g_j|^2 of the cube-corner gradient rows
-  } else {
-#pragma unroll
-    for (int i = 0; i < 6; i++) C[tet_idx<6>(h, K, i)] = c[i];
-#pragma unroll
-    for (int j = 0; j < 3; j++) w[j + 1] = ET(B[j * 3] * B[j * 3] + B[j * 3 + 1] * B[j * 3 + 1] + B[j * 3 + 2] * B[j * 3 + 2]);
-    ET g0[3];
-#pragma unroll
-    for (int r = 0; r < 3; r++) g0[r] = ET(B[r] + B[3 + r] + B[6 + r]);
-    w[0] = g0[0] * g0[0] + g0[1] * g0[1] + g0[2] * g0[2];
-  }
-#pragma unroll
-  for (int j = 0; j < 4; j++) atomic_add3(gd, hv[tet_v(K, j)], w[j] * c[0], w[j] * c[1], w[j] * c[2]);
-}
-
-// Each corner tet scatters its right-hand-side, residual and diagonal contributions straight to
-// the vertex vectors (float atomics): holding 8 corners x 3 vectors per hex in registers would
-// halve the occupancy of this latency-bound kernel.
-template <typename ET, bool PRE>
-__global__ void __launch_bounds__(128) k_local(KArgs a) {
-  const Seg sg = a.hseg[blockIdx.x];
-  const int64_t h = sg.begin + threadIdx.x;
-  if (h >= sg.end) return;
-  const MeshScalars &S = a.sc[sg.mesh];
-  const ET M = ET(S.M), exp_f = ET(S.exp_f);
-  uint32_t hv[8];
-  load_hex(a.hexv, h, hv);
-  const int32_t gs = a.gslot[h];
-  ET E12[12][3];
-  hex_edges_pos(a.X, hv, E12);
-  bool degenerate = false;
-  local_tet<ET, 0, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 1, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 2, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 3, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 4, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 5, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 6, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 7, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  if (PRE && degenerate) atomicOr(&a.sc[sg.mesh].status, 2);
-}
-
-// ------------------------------------------------------------------------------- SpMV
-// q += K p over the element terms: J' = E(p) B', Q = C' J', forces G = Q B'^T (the cube scale
-// is folded into C').
-template <typename ET, int K>
-__device__ __forceinline__ void spmv_tet(const KArgs &a, int64_t h, int32_t gs, const ET E12[12][3], ET F[8][3]) {
-  ET E[3][3], J[3][3], Q[3][3], G[3][3];
-  tet_E12<K>(E12, E);
-  const double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
-  apply_B<K>(E, gs, B, ET(1), J);
-  const ET *C = reinterpret_cast<const ET *>(a.Ccoef);
-  ET c[6];
-#pragma unroll
-  for (int i = 0; i < 6; i++) c[i] = C[tet_idx<6>(h, K, i)];
-  sym_mul(c, J, Q);
-  apply_BT<K>(Q, gs, B, ET(1), G);
-  scatter_cols<K>(G, F);
-}
-
-// 64 registers (8 blocks of 128 per SM): more gathers in flight outweigh the few spills
-template <typename ET>
-__global__ void __launch_bounds__(128, 8) k_spmv(KArgs a) {
-  const Seg sg = a.hseg[blockIdx.x];
-  if (a.sc[sg.mesh].cg_done) return;
-  const int64_t h = sg.begin + threadIdx.x;
-  if (h >= sg.end) return;
-  uint32_t hv[8];
-  load_hex(a.hexv, h, hv);
-  const int32_t gs = a.gslot[h];
-  ET E12[12][3];
-  hex_edges_vec(reinterpret_cast<const ET *>(a.p), hv, E12);
-  ET F[8][3];
-#pragma unroll
-  for (int c = 0; c < 8; c++) F[c][0] = F[c][1] = F[c][2] = ET(0);
-  spmv_tet<ET, 0>(a, h, gs, E12, F);
-  spmv_tet<ET, 1>(a, h, gs, E12, F);
-  spmv_tet<ET, 2>(a, h, gs, E12, F);
-  spmv_tet<ET, 3>(a, h, gs, E12, F);
-  spmv_tet<ET, 4>(a, h, gs, E12, F);
-  spmv_tet<ET, 5>(a, h, gs, E12, F);
-  spmv_tet<ET, 6>(a, h, gs, E12, F);
-  spmv_tet<ET, 7>(a, h, gs, E12, F);
-  ET *q = reinterpret_cast<ET *>(a.q);
-#pragma unroll
-  for (int c = 0; c < 8; c++) atomic_add3(q, hv[c], F[c][0], F[c][1], F[c][2]);
-}
-
-// ------------------------------------------------------------------------------- soft terms
-// Constraint items of a mesh: [0, nc) corners, [nc, nc+nt) tangent planes, [nc+nt, +nl) lines.
-// add_soft_constraints (slim_m.cpp:647-711): rhs, diagonal and the residual at x0 (curve
-// unknowns start at 0).
-template <typename VT>
-__global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
-  const Seg sg = a.cseg[blockIdx.x];
-  const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
-  const MeshDesc md = a.mesh[sg.mesh];
-  const MeshScalars &S = a.sc[sg.mesh];
-  VT *b = reinterpret_cast<VT *>(a.b), *r = reinterpret_cast<VT *>(a.r), *dg = reinterpret_cast<VT *>(a.diag);
-  int64_t li = i - md.c_off - md.t_off - md.l_off;
-  if (li < md.nc) {
-    const int64_t e = md.c_off + li;
-    const uint32_t v = (uint32_t)(md.v_off + a.c_ids[e]);
-    const double lc = S.lamda_C;
-    const double *x = a.X + 4 * (int64_t)v;
-    const double c0 = a.c_pos[3 * e], c1 = a.c_pos[3 * e + 1], c2 = a.c_pos[3 * e + 2];
-    atomic_add3(b, v, VT(lc * c0), VT(lc * c1), VT(lc * c2));
-    atomic_add3(r, v, VT(lc * (c0 - x[0])), VT(lc * (c1 - x[1])), VT(lc * (c2 - x[2])));
-    atomic_add3(dg, v, VT(lc), VT(lc), VT(lc));
-    return;
-  }
-  li -= md.nc;
-  if (li < md.nt) {
-    const int64_t e = md.t_off + li;
-    const uint32_t v = (uint32_t)(md.v_off + a.t_ids[e]);
-    const double lt = S.lamda_T;
-    const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2], d = a.t_dis[e];
-    const double *x = a.X + 4 * (int64_t)v;
-    const double res = lt * (d - (n0 * x[0] + n1 * x[1] + n2 * x[2]));
-    atomic_add3(b, v, VT(lt * n0 * d), VT(lt * n1 * d), VT(lt * n2 * d));
-    atomic_add3(r, v, VT(res * n0), VT(res * n1), VT(res * n2));
-    atomic_add3(dg, v, VT(lt * n0 * n0), VT(lt * n1 * n1), VT(lt * n2 * n2));
-    return;
-  }
-  li -= md.nt;
-  {
-    const int64_t e = md.l_off + li;
-    const uint32_t v = (uint32_t)(md.v_off + a.l_ids[e]);
-    const double ll = S.lamda_L;
-    const double x0 = a.l_axis[3 * e], x1 = a.l_axis[3 * e + 1], x2 = a.l_axis[3 * e + 2];
-    const double o0 = a.l_orig[3 * e], o1 = a.l_orig[3 * e + 1], o2 = a.l_orig[3 * e + 2];
-    const double *x = a.X + 4 * (int64_t)v;
-    atomic_add3(b, v, VT(ll * o0), VT(ll * o1), VT(ll * o2));
-    atomic_add3(r, v, VT(ll * (o0 - x[0])), VT(ll * (o1 - x[1])), VT(ll * (o2 - x[2])));
-    atomic_add3(dg, v, VT(ll), VT(ll), VT(ll));
-    VT *ba = reinterpret_cast<VT *>(a.ba), *ra = reinterpret_cast<VT *>(a.ra), *dga = reinterpret_cast<VT *>(a.diaga);
-    ba[e] = VT(ll * (-x0 * o0 - x1 * o1 - x2 * o2));
-    ra[e] = VT(ll * (x0 * (x[0] - o0) + x1 * (x[1] - o1) + x2 * (x[2] - o2)));
-    dga[e] = VT(ll * (x0 * x0 + x1 * x1 + x2 * x2));
-  }
-}
-
-// q += S p for the soft-constraint block of L
-template <typename VT>
-__global__ void __launch_bounds__(256) k_soft_mv(KArgs a) {
-  const Seg sg = a.cseg[blockIdx.x];
-  if (a.sc[sg.mesh].cg_done) return;
-  const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
-  const MeshDesc md = a.mesh[sg.mesh];
-  const MeshScalars &S = a.sc[sg.mesh];
-  const VT *in = reinterpret_cast<const VT *>(a.p), *in_a = reinterpret_cast<const VT *>(a.pa);
-  VT *out = reinterpret_cast<VT *>(a.q), *out_a = reinterpret_cast<VT *>(a.qa);
-  int64_t li = i - md.c_off - md.t_off - md.l_off;
-  if (li < md.nc) {
-    const uint32_t v = (uint32_t)(md.v_off + a.c_ids[md.c_off + li]);
-    const VT lc = VT(S.lamda_C);
-    const VT *p = in + 4 * (int64_t)v;
-    atomic_add3(out, v, lc * p[0], lc * p[1], lc * p[2]);
-    return;
-  }
-  li -= md.nc;
-  if (li < md.nt) {
-    const int64_t e = md.t_off + li;
-    const uint32_t v = (uint32_t)(md.v_off + a.t_ids[e]);
-    const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2];
-    const VT *p = in + 4 * (int64_t)v;
-    const double s = S.lamda_T * (n0 * double(p[0]) + n1 * double(p[1]) + n2 * double(p[2]));
-    atomic_add3(out, v, VT(s * n0), VT(s * n1), VT(s * n2));
-    return;
-  }
-  li -= md.nt;
-  {
-    const int64_t e = md.l_off + li;
-    const uint32_t v = (uint32_t)(md.v_off + a.l_ids[e]);
-    const double ll = S.lamda_L;
-    const double x0 = a.l_axis[3 * e], x1 = a.l_axis[3 * e + 1], x2 = a.l_axis[3 * e + 2];
-    const VT *p = in + 4 * (int64_t)v;
-    const double pa = double(in_a[e]);
-    atomic_add3(out, v, VT(ll * (double(p[0]) - x0 * pa)), VT(ll * (double(p[1]) - x1 * pa)),
-                VT(ll * (double(p[2]) - x2 * pa)));
-    out_a[e] += VT(ll * (-(x0 * double(p[0]) + x1 * double(p[1]) + x2 * double(p[2])) + (x0 * x0 + x1 * x1 + x2 * x2) * pa));
-  }
-}
-
-// ------------------------------------------------------------------------------- CG vectors
-// Unknown items of a mesh: [0, nv) vertices (3 coordinates), [nv, nv + nl) curve unknowns.
-struct ItemRef {
-  bool curve;
-  int64_t idx;  // global vertex id or global curve entry
-};
-__device__ __forceinline__ ItemRef item_ref(const MeshDesc &md, int64_t i) {
-  const int64_t li = i - md.v_off - md.l_off;
-  if (li < md.nv) return {false, md.v_off + li};
-  return {true, md.l_off + (li - md.nv)};
-}
-
-template <typename T> struct V3 { T x, y, z; };
-__device__ __forceinline__ V3<float> ld3(const float *Y, int64_t v) {
-  const float4 t = *reinterpret_cast<const float4 *>(Y + 4 * v);
-  return {t.x, t.y, t.z};
-}
-__device__ __forceinline__ V3<double> ld3(const double *Y, int64_t v) {
-  const double2 t = *reinterpret_cast<const double2 *>(Y + 4 * v);
-  return {t.x, t.y, Y[4 * v + 2]};
-}
-__device__ __forceinline__ void st3(float *Y, int64_t v, V3<float> a) {
-  *reinterpret_cast<float4 *>(Y + 4 * v) = make_float4(a.x, a.y, a.z, 0.f);
-}
-__device__ __forceinline__ void st3(double *Y, int64_t v, V3<double> a) {
-  *reinterpret_cast<double2 *>(Y + 4 * v) = make_double2(a.x, a.y);
-  Y[4 * v + 2] = a.z;
-  Y[4 * v + 3] = 0.0;
-}
-
-// r0 is already formed (local step + soft terms): p = invd r0, delta = 0, q = prox p, norms.
-template <typename VT>
-__global__ void __launch_bounds__(256) k_cg_start(KArgs a) {
-  const Seg sg = a.vseg[blockIdx.x];
-  const MeshDesc md = a.mesh[sg.mesh];
-  MeshScalars &S = a.sc[sg.mesh];
-  const double prox = S.prox;
-  double acc[3] = {0, 0, 0};  // |b|^2, |r|^2, r.p
-  VT *r = reinterpret_cast<VT *>(a.r), *p = reinterpret_cast<VT *>(a.p), *d = reinterpret_cast<VT *>(a.d);
-  VT *q = reinterpret_cast<VT *>(a.q), *invd = reinterpret_cast<VT *>(a.invd);
-  const VT *b = reinterpret_cast<const VT *>(a.b), *dg = reinterpret_cast<const VT *>(a.diag);
-  SumAcc<VT> s_bb, s_rr, s_rp;  // mixed mode: FP32 arithmetic, compensated sums
-  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
-    const ItemRef it = item_ref(md, i);
-    if (!it.curve && sizeof(VT) == 4) {
-      const int64_t v = it.idx;
-      const V3<VT> bb = ld3(b, v), rr = ld3(r, v), gg = ld3(dg, v);
-      const VT pr = VT(prox);
-      const VT b0 = bb.x + pr * VT(a.X[4 * v]), b1 = bb.y + pr * VT(a.X[4 * v + 1]), b2 = bb.z + pr * VT(a.X[4 * v + 2]);
-      const VT i0 = VT(1) / (gg.x + pr), i1 = VT(1) / (gg.y + pr), i2 = VT(1) / (gg.z + pr);
-      const VT p0 = i0 * rr.x, p1 = i1 * rr.y, p2 = i2 * rr.z;
-      st3(p, v, V3<VT>{p0, p1, p2});
-      st3(d, v, V3<VT>{VT(0), VT(0), VT(0)});
-      st3(invd, v, V3<VT>{i0, i1, i2});
-      st3(q, v, V3<VT>{pr * p0, pr * p1, pr * p2});
-      s_bb.add_prod(b0, b0); s_bb.add_prod(b1, b1); s_bb.add_prod(b2, b2);
-      s_rr.add_prod(rr.x, rr.x); s_rr.add_prod(rr.y, rr.y); s_rr.add_prod(rr.z, rr.z);
-      s_rp.add_prod(rr.x, p0); s_rp.add_prod(rr.y, p1); s_rp.add_prod(rr.z, p2);
-    } else if (!it.curve) {
-      const int64_t v = it.idx;
-      const V3<VT> bb = ld3(b, v), rr = ld3(r, v), gg = ld3(dg, v);
-      const double x0 = a.X[4 * v], x1 = a.X[4 * v + 1], x2 = a.X[4 * v + 2];
-      const double b0 = double(bb.x) + prox * x0, b1 = double(bb.y) + prox * x1, b2 = double(bb.z) + prox * x2;
-      const double i0 = 1.0 / (double(gg.x) + prox), i1 = 1.0 / (double(gg.y) + prox), i2 = 1.0 / (double(gg.z) + prox);
-      const double p0 = i0 * double(rr.x), p1 = i1 * double(rr.y), p2 = i2 * double(rr.z);
-      st3(p, v, V3<VT>{VT(p0), VT(p1), VT(p2)});
-      st3(d, v, V3<VT>{VT(0), VT(0), VT(0)});
-      st3(invd, v, V3<VT>{VT(i0), VT(i1), VT(i2)});
-      st3(q, v, V3<VT>{VT(prox * p0), VT(prox * p1), VT(prox * p2)});
-      acc[0] += b0 * b0 + b1 * b1 + b2 * b2;
-      acc[1] += double(rr.x) * double(rr.x) + double(rr.y) * double(rr.y) + double(rr.z) * double(rr.z);
-      acc[2] += double(rr.x) * p0 + double(rr.y) * p1 + double(rr.z) * p2;
-    } else {
-      const int64_t e = it.idx;
-      VT *ra = reinterpret_cast<VT *>(a.ra), *pa = reinterpret_cast<VT *>(a.pa), *da = reinterpret_cast<VT *>(a.da);
-      VT *qa = reinterpret_cast<VT *>(a.qa), *invda = reinterpret_cast<VT *>(a.invda);
-      const double bb = double(reinterpret_cast<const VT *>(a.ba)[e]);
-      const double rr = double(ra[e]);
-      const double g = double(reinterpret_cast<const VT *>(a.diaga)[e]);
-      const double id = g != 0.0 ? 1.0 / g : 0.0;  // DiagonalPreconditioner: 0 without a diagonal
-      const double pp = id * rr;
-      pa[e] = VT(pp); da[e] = VT(0); invda[e] = VT(id); qa[e] = VT(0);
-      acc[0] += bb * bb; acc[1] += rr * rr; acc[2] += rr * pp;
-    }
-  }
-  if (sizeof(VT) == 4) {
-    acc[0] += s_bb.value();
-    acc[1] += s_rr.value();
-    acc[2] += s_rp.value();
-  }
-  __shared__ double smem[3][32];
-  block_sum<3>(acc, smem);
-  if (publish_partials<3>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
-    double v0 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 3, 0, smem);
-    double v1 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 3, 1, smem);
-    double v2 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 3, 2, smem);
-    if (threadIdx.x == 0) {
-      S.rhs_norm2 = v0;
-      S.threshold = a.cg_tol * a.cg_tol * v0;
-      S.rn2 = v1;
-      S.abs_new = v2;
-      S.cg_iters = 0;
-      S.cg_done = 0;
-      if (v0 == 0.0) { S.cg_done = 1; S.cg_error = 0; }
-      else if (v1 < S.threshold) { S.cg_done = 1; S.cg_error = sqrt(v1 / v0); }
-      else if (a.cg_max_iter <= 0) { S.cg_done = 1; S.cg_error = sqrt(v1 / v0); }
-      a.counters[sg.mesh] = 0;
-    }
-  }
-}
-
-// alpha = abs_new / (p . q)
-template <typename VT>
-__global__ void __launch_bounds__(256) k_cg_alpha(KArgs a) {
-  const Seg sg = a.vseg[blockIdx.x];
-  MeshScalars &S = a.sc[sg.mesh];
-  if (S.cg_done) return;
-  const MeshDesc md = a.mesh[sg.mesh];
-  const VT *p = reinterpret_cast<const VT *>(a.p), *q = reinterpret_cast<const VT *>(a.q);
-  double acc[1] = {0};
-  SumAcc<VT> pq;  // mixed mode: compensated FP32 dot product
-  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
-    const ItemRef it = item_ref(md, i);
-    if (!it.curve) {
-      const V3<VT> pp = ld3(p, it.idx), qq = ld3(q, it.idx);
-      if (sizeof(VT) == 4) {
-        pq.add_prod(pp.x, qq.x); pq.add_prod(pp.y, qq.y); pq.add_prod(pp.z, qq.z);
-      } else {
-        acc[0] += double(pp.x) * double(qq.x) + double(pp.y) * double(qq.y) + double(pp.z) * double(qq.z);
-      }
-    } else {
-      const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
-      acc[0] += double(pa[it.idx]) * double(qa[it.idx]);
-    }
-  }
-  if (sizeof(VT) == 4) acc[0] += pq.value();
-  __shared__ double smem[1][32];
-  block_sum<1>(acc, smem);
-  if (publish_partials<1>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
-    double pAp = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 1, 0, smem);
-    if (threadIdx.x == 0) {
-      S.alpha = S.abs_new / pAp;
-      if (!(pAp > 0.0)) S.status |= 4;
-      a.counters[sg.mesh] = 0;
-    }
-  }
-}
-
-// delta += alpha p; r -= alpha q; rn2 = r.r; rz = r.(invd r); convergence / beta
-template <typename VT>
-__global__ void __launch_bounds__(256) k_cg_update(KArgs a) {
-  const Seg sg = a.vseg[blockIdx.x];
-  MeshScalars &S = a.sc[sg.mesh];
-  if (S.cg_done) return;
-  const MeshDesc md = a.mesh[sg.mesh];
-  const VT alpha = VT(S.alpha);
-  double acc[2] = {0, 0};
-  SumAcc<VT> s_rr, s_rz;  // mixed mode: compensated FP32 dot products
-  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
-    const ItemRef it = item_ref(md, i);
-    if (!it.curve) {
-      VT *r = reinterpret_cast<VT *>(a.r), *d = reinterpret_cast<VT *>(a.d);
-      const VT *p = reinterpret_cast<const VT *>(a.p), *q = reinterpret_cast<const VT *>(a.q);
-      const VT *invd = reinterpret_cast<const VT *>(a.invd);
-      const int64_t v = it.idx;
-      const V3<VT> pp = ld3(p, v), qq = ld3(q, v), id = ld3(invd, v);
-      V3<VT> dd = ld3(d, v), rr = ld3(r, v);
-      dd.x += alpha * pp.x; dd.y += alpha * pp.y; dd.z += alpha * pp.z;
-      rr.x -= alpha * qq.x; rr.y -= alpha * qq.y; rr.z -= alpha * qq.z;
-      st3(d, v, dd);
-      st3(r, v, rr);
-      if (sizeof(VT) == 4) {
-        s_rr.add_prod(rr.x, rr.x); s_rr.add_prod(rr.y, rr.y); s_rr.add_prod(rr.z, rr.z);
-        s_rz.add_prod(rr.x, id.x * rr.x); s_rz.add_prod(rr.y, id.y * rr.y); s_rz.add_prod(rr.z, id.z * rr.z);
-      } else {
-        acc[0] += double(rr.x) * double(rr.x) + double(rr.y) * double(rr.y) + double(rr.z) * double(rr.z);
-        acc[1] += double(rr.x) * double(id.x * rr.x) + double(rr.y) * double(id.y * rr.y) + double(rr.z) * double(id.z * rr.z);
-      }
-    } else {
-      VT *ra = reinterpret_cast<VT *>(a.ra), *da = reinterpret_cast<VT *>(a.da);
-      const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
-      const VT *invda = reinterpret_cast<const VT *>(a.invda);
-      const int64_t e = it.idx;
-      da[e] += alpha * pa[e];
-      const VT rr = ra[e] - alpha * qa[e];
-      ra[e] = rr;
-      acc[0] += double(rr) * double(rr);
-      acc[1] += double(rr) * double(invda[e] * rr);
-    }
-  }
-  if (sizeof(VT) == 4) {
-    acc[0] += s_rr.value();
-    acc[1] += s_rz.value();
-  }
-  __shared__ double smem[2][32];
-  block_sum<2>(acc, smem);
-  if (publish_partials<2>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
-    double rn2 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 2, 0, smem);
-    double rz = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 2, 1, smem);
-    if (threadIdx.x == 0) {
-      S.rn2 = rn2;
-      S.cg_error = sqrt(rn2 / S.rhs_norm2);
-      if (rn2 < S.threshold) {
-        S.cg_done = 1;
-      } else {
-        S.beta = rz / S.abs_new;
-        S.abs_new = rz;
-        S.cg_iters += 1;
-        if (S.cg_iters >= a.cg_max_iter) S.cg_done = 1;
-      }
-      a.counters[sg.mesh] = 0;
-    }
-  }
-}
-
-// p = invd r + beta p; q = prox p (vertex) / 0 (curve), ready for the next SpMV
-template <typename VT>
-__global__ void __launch_bounds__(256) k_cg_dir(KArgs a) {
-  const Seg sg = a.vseg[blockIdx.x];
-  const MeshScalars &S = a.sc[sg.mesh];
-  if (S.cg_done) return;
-  const MeshDesc md = a.mesh[sg.mesh];
-  const VT beta = VT(S.beta), prox = VT(S.prox);
-  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
-  const ItemRef it = item_ref(md, i);
-  if (!it.curve) {
-    const VT *r = reinterpret_cast<const VT *>(a.r), *invd = reinterpret_cast<const VT *>(a.invd);
-    VT *p = reinterpret_cast<VT *>(a.p), *q = reinterpret_cast<VT *>(a.q);
-    const int64_t v = it.idx;
-    const V3<VT> rr = ld3(r, v), id = ld3(invd, v);
-    V3<VT> pp = ld3(p, v);
-    pp.x = id.x * rr.x + beta * pp.x;
-    pp.y = id.y * rr.y + beta * pp.y;
-    pp.z = id.z * rr.z + beta * pp.z;
-    st3(p, v, pp);
-    st3(q, v, V3<VT>{prox * pp.x, prox * pp.y, prox * pp.z});
-  } else {
-    const VT *ra = reinterpret_cast<const VT *>(a.ra), *invda = reinterpret_cast<const VT *>(a.invda);
-    VT *pa = reinterpret_cast<VT *>(a.pa), *qa = reinterpret_cast<VT *>(a.qa);
-    const int64_t e = it.idx;
-    pa[e] = invda[e] * ra[e] + beta * pa[e];
-    qa[e] = VT(0);
-  }
-  }
-}
-
-// ------------------------------------------------------------------------------- line search
-// Smallest positive root of det(E + t D) = 0 (get_min_pos_root_3D, flip_avoiding_line_search.cpp:
-// 177-271), FP64.  The cubic is solved by the trigonometric / Cardano method of SolveP3 (:24-61).
-__device__ double smallest_pos_quad_zero(double a, double b, double c) {
-  double t1, t2;
-  if (fabs(a) > 1.0e-10) {
-    const double delta_in = b * b - 4 * a * c;
-    if (delta_in <= 0) return INFINITY;
-    const double delta = sqrt(delta_in);
-    if (b >= 0) {
-      const double bd = -b - delta;
-      t1 = 2 * c / bd;
-      t2 = bd / (2 * a);
-    } else {
-      const double bd = -b + delta;
-      t1 = bd / (2 * a);
-      t2 = (2 * c) / bd;
-    }
-    if (a < 0) { const double tt = t1; t1 = t2; t2 = tt; }
-    if (t1 > 0) return t2 > 0 ? t2 : t1;
-    return INFINITY;
-  }
-  if (b == 0) return INFINITY;
-  t1 = -c / b;
-  return t1 > 0 ? t1 : INFINITY;
-}
-
-__device__ double min_pos_root(const double E[3][3], const double D[3][3]) {
-  double M[3][3];
-  const double c3 = det3(D), c0 = det3(E);
-  double c1 = 0, c2 = 0;
-#pragma unroll
-  for (int col = 0; col < 3; col++) {
-#pragma unroll
-    for (int r = 0; r < 3; r++)
-#pragma unroll
-      for (int cc = 0; cc < 3; cc++) M[r][cc] = (cc == col) ? D[r][cc] : E[r][cc];
-    c1 += det3(M);
-#pragma unroll
-    for (int r = 0; r < 3; r++)
-#pragma unroll
-      for (int cc = 0; cc < 3; cc++) M[r][cc] = (cc == col) ? E[r][cc] : D[r][cc];
-    c2 += det3(M);
-  }
-  double a = -c3, b = -c2, c = -c1, d = -c0;
-  if (fabs(a) <= 1.e-10) return smallest_pos_quad_zero(b, c, d);
-  b /= a; c /= a; d /= a;
-  // cubic x^3 + b x^2 + c x + d
-  const double a2 = b * b;
-  double q = (a2 - 3 * c) / 9;
-  const double r = (b * (2 * a2 - 9 * c) + 27 * d) / 54;
-  const double r2 = r * r, q3 = q * q * q;
-  double x0, x1, x2;
-  int nr;
-  if (r2 < q3) {
-    double t = r / sqrt(q3);
-    t = fmin(1.0, fmax(-1.0, t));
-    t = acos(t);
-    const double a3 = b / 3;
-    q = -2 * sqrt(q);
-    x0 = q * cos(t / 3) - a3;
-    x1 = q * cos((t + (2 * M_PI)) / 3) - a3;
-    x2 = q * cos((t - (2 * M_PI)) / 3) - a3;
-    nr = 3;
-  } else {
-    double A = -pow(fabs(r) + sqrt(r2 - q3), 1. / 3);
-    if (r < 0) A = -A;
-    const double Bc = (A == 0) ? 0 : q / A;
-    const double a3 = b / 3;
-    x0 = (A + Bc) - a3;
-    x1 = -0.5 * (A + Bc) - a3;
-    x2 = 0.5 * sqrt(3.) * (A - Bc);
-    nr = 1;
-    if (fabs(x2) < 1e-14) { x2 = x1; nr = 2; }
-  }
-  if (nr == 1) return (x0 >= 0) ? x0 : INFINITY;
-  if (nr == 2) {
-    const double mx = fmax(x0, x1), mn = fmin(x0, x1);
-    if (mn > 0) return mn;
-    if (mx > 0) return mx;
-    return INFINITY;
-  }
-  // sort three
-  double lo = fmin(x0, fmin(x1, x2)), hi = fmax(x0, fmax(x1, x2));
-  double mid = x0 + x1 + x2 - lo - hi;
-  if (lo > 0) return lo;
-  if (mid > 0) return mid;
-  if (hi > 0) return hi;
-  return INFINITY;
-}
-
-template <typename VT, int K>
-__device__ __forceinline__ void tet_dir(const VT *d, const uint32_t hv[8], double Dd[3][3]) {
-  VT p0[3];
-  load_vec(d, hv[tet_v(K, 0)], p0);
-#pragma unroll
-  for (int j = 0; j < 3; j++) {
-    VT q[3];
-    load_vec(d, hv[tet_v(K, j + 1)], q);
-    Dd[0][j] = double(q[0]) - double(p0[0]);
-    Dd[1][j] = double(q[1]) - double(p0[1]);
-    Dd[2][j] = double(q[2]) - double(p0[2]);
-  }
-}
-
-// Energy density of corner tet K at edges E (ET); tets with |det J| below 1e-3 are re-evaluated
-// in FP64 from the FP64 positions (mixed mode only).
-template <typename ET, typename VT, int K>
-__device__ __forceinline__ void tet_energy_acc(const KArgs &a, int64_t h, const uint32_t hv[8], int32_t gs,
-                                               const ET E[3][3], double alpha, SumAcc<ET> &fast, double &slow) {
-  const ET *Sinv = reinterpret_cast<const ET *>(a.Sinv);
-  const double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
-  const ET is = Sinv[tet_idx<1>(h, K, 0)];
-  ET J[3][3];
-  apply_B<K>(E, gs, B, is, J);
-  const ET e = tet_energy_density<ET>(a.energy, ET(a.sc_exp_f), J);
-  if (sizeof(ET) == 4) {
-    const ET d = det3(J);
-    if (!(fabs(d) > ET(1e-3))) {
-      double E0[3][3], Dd[3][3], Ed[3][3], Jd[3][3];
-      tet_edges<K>(a.X, hv, E0);
-      tet_dir<VT, K>(reinterpret_cast<const VT *>(a.d), hv, Dd);
-#pragma unroll
-      for (int r = 0; r < 3; r++)
-#pragma unroll
-        for (int c = 0; c < 3; c++) Ed[r][c] = E0[r][c] + alpha * Dd[r][c];
-      apply_B<K>(Ed, gs, B, double(is), Jd);
-      slow += tet_energy_density<double>(a.energy, a.sc_exp_f, Jd);
-      return;
-    }
-  }
-  fast.add(e);
-}
-
-// Flip-avoiding step bound of corner tet K.  Only a root of det(E + t D) in [0, 1.25] can lower
-// max_step = min(1, 0.8 min_root).  The cubic's coefficients are formed in ET and converted to the
-// Bernstein basis on [0, 1.25]; when all four Bernstein coefficients keep the sign of det E with a
-// margin that covers the ET rounding (bounded through Hadamard's inequality), there is no root in
-// the interval and the tet is skipped.  Otherwise the smallest positive root is solved in FP64
-// exactly as the reference does.
-template <typename ET, int K>
-__device__ __forceinline__ bool tet_bound(const ET E[3][3], const ET D[3][3]) {
-  ET ne[3], nd[3];
-#pragma unroll
-  for (int j = 0; j < 3; j++) {
-    ne[j] = sqrt(E[0][j] * E[0][j] + E[1][j] * E[1][j] + E[2][j] * E[2][j]);
-    nd[j] = sqrt(D[0][j] * D[0][j] + D[1][j] * D[1][j] + D[2][j] * D[2][j]);
-  }
-  const ET T = ET(1.25);
-  const ET M0 = ne[0] * ne[1] * ne[2];
-  const ET M1 = nd[0] * ne[1] * ne[2] + ne[0] * nd[1] * ne[2] + ne[0] * ne[1] * nd[2];
-  const ET M2 = nd[0] * nd[1] * ne[2] + nd[0] * ne[1] * nd[2] + ne[0] * nd[1] * nd[2];
-  const ET M3 = nd[0] * nd[1] * nd[2];
-  // det(E + tD) = c0 + c1 t + c2 t^2 + c3 t^3
-  ET Mx[3][3];
-  const ET c0 = det3(E), c3 = det3(D);
-  ET c1 = 0, c2 = 0;
-#pragma unroll
-  for (int col = 0; col < 3; col++) {
-#pragma unroll
-    for (int r = 0; r < 3; r++)
-#pragma unroll
-      for (int cc = 0; cc < 3; cc++) Mx[r][cc] = (cc == col) ? D[r][cc] : E[r][cc];
-    c1 += det3(Mx);
-#pragma unroll
-    for (int r = 0; r < 3; r++)
-#pragma unroll
-      for (int cc = 0; cc < 3; cc++) Mx[r][cc] = (cc == col) ? E[r][cc] : D[r][cc];
-    c2 += det3(Mx);
-  }
-  const ET a1 = c1 * T, a2 = c2 * T * T, a3 = c3 * T * T * T;
-  const ET b0 = c0, b1 = c0 + a1 / ET(3), b2 = c0 + ET(2) * a1 / ET(3) + a2 / ET(3), b3 = c0 + a1 + a2 + a3;
-  const ET rel = sizeof(ET) == 4 ? ET(2e-5) : ET(1e-13);
-  const ET err = rel * (M0 + M1 * T + M2 * T * T + M3 * T * T * T);
-  const bool pos = b0 > err && b1 > err && b2 > err && b3 > err;
-  const bool neg = b0 < -err && b1 < -err && b2 < -err && b3 < -err;
-  return !(pos || neg);
-}
-
-// Corner tet K of hex h (K at run time) -> its FP64 edges and direction edges.
-template <typename VT>
-__device__ __forceinline__ void tet_edges_dir(const KArgs &a, const uint32_t hv[8], int K, double E[3][3],
-                                              double D[3][3]) {
-  const VT *d = reinterpret_cast<const VT *>(a.d);
-  switch (K) {
-    case 0: tet_edges<0>(a.X, hv, E); tet_dir<VT, 0>(d, hv, D); break;
-    case 1: tet_edges<1>(a.X, hv, E); tet_dir<VT, 1>(d, hv, D); break;
-    case 2: tet_edges<2>(a.X, hv, E); tet_dir<VT, 2>(d, hv, D); break;
-    case 3: tet_edges<3>(a.X, hv, E); tet_dir<VT, 3>(d, hv, D); break;
-    case 4: tet_edges<4>(a.X, hv, E); tet_dir<VT, 4>(d, hv, D); break;
-    case 5: tet_edges<5>(a.X, hv, E); tet_dir<VT, 5>(d, hv, D); break;
-    case 6: tet_edges<6>(a.X, hv, E); tet_dir<VT, 6>(d, hv, D); break;
-    default: tet_edges<7>(a.X, hv, E); tet_dir<VT, 7>(d, hv, D); break;
-  }
-}
-
-// Dense exact pass over the recorded tets: the reference's smallest positive root in FP64, one
-// tet per thread, reduced per mesh by atomicMin on the bits of the (non-negative) root.
-template <typename VT>
-__global__ void __launch_bounds__(128) k_ls_roots(KArgs a) {
-  const unsigned n = *a.root_count;
-  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-    const uint32_t code = a.root_list[e];
-    const int64_t h = code >> 3;
-    uint32_t hv[8];
-    load_hex(a.hexv, h, hv);
-    double E[3][3], D[3][3];
-    tet_edges_dir<VT>(a, hv, (int)(code & 7), E, D);
-    const double r = min_pos_root(E, D);
-    atomicMin(a.root_min + a.root_mesh[e], (unsigned long long)__double_as_longlong(r));
-  }
-}
-
-// max_step = min(1, 0.8 min_root) per mesh; re-arms the minimum and the list for the next call.
-__global__ void k_ls_bound_finish(KArgs a, int n_meshes) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m == 0) *a.root_count = 0;
-  if (m >= n_meshes) return;
-  MeshScalars &S = a.sc[m];
-  const double r = __longlong_as_double((long long)a.root_min[m]);
-  S.min_root = r;
-  S.max_step = fmin(1.0, r * 0.8);
-  a.root_min[m] = (unsigned long long)__double_as_longlong(INFINITY);
-}
-
-
-
-// Pass 1: step bound over the tets and the quality energy at the current X.
-template <typename ET, typename VT>
-__global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
-  const Seg sg = a.hseg[blockIdx.x];
-  const int64_t h = sg.begin + threadIdx.x;
-  const MeshDesc md = a.mesh[sg.mesh];
-  MeshScalars &S = a.sc[sg.mesh];
-  double eq[1] = {0};
-  unsigned need = 0;  // bit K: corner tet K needs the exact root
-  if (h < sg.end) {
-    uint32_t hv[8];
-    load_hex(a.hexv, h, hv);
-    const int32_t gs = a.gslot[h];
-    ET E12[12][3], D12[12][3];
-    hex_edges_pos(a.X, hv, E12);
-    {
-      VT Dv[12][3];
-      hex_edges_vec(reinterpret_cast<const VT *>(a.d), hv, Dv);
-#pragma unroll
-      for (int e = 0; e < 12; e++)
-#pragma unroll
-        for (int r = 0; r < 3; r++) D12[e][r] = ET(Dv[e][r]);
-    }
-    SumAcc<ET> efast;
-    double eslow = 0;
-#define HX_LS(K)                                                  \
-    {                                                             \
-      ET E[3][3], D[3][3];                                        \
-      tet_E12<K>(E12, E);                                         \
-      tet_E12<K>(D12, D);                                         \
-      if (tet_bound<ET, K>(E, D)) need |= 1u << K;              \
-      tet_energy_acc<ET, VT, K>(a, h, hv, gs, E, 0.0, efast, eslow); \
-    }
-    HX_LS(0) HX_LS(1) HX_LS(2) HX_LS(3) HX_LS(4) HX_LS(5) HX_LS(6) HX_LS(7)
-#undef HX_LS
-    eq[0] = S.M * (efast.value() + eslow);
-  }
-  {
-    // record the tets that need the exact root (one reservation per warp)
-    const int k = __popc(need);
-    int total;
-    const int off = warp_exclusive_sum(k, total);
-    unsigned base = 0;
-    if ((threadIdx.x & 31) == 0 && total > 0) base = atomicAdd(a.root_count, (unsigned)total);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    int w = 0;
-    for (int K = 0; K < 8; K++)
-      if ((need >> K) & 1u) {
-        a.root_list[base + off + w] = (uint32_t)(h * 8 + K);
-        a.root_mesh[base + off + w] = sg.mesh;
-        w++;
-      }
-  }
-  __shared__ double smem[1][32];
-  double acc[1] = {0};
-  block_sum<1>(eq, smem);
-  if (threadIdx.x == 0) acc[0] = eq[0];
-  if (publish_partials<1>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
-    double e = gather_partials_sum(a.partials, md.hblk0, md.nhblk, 1, 0, smem);
-    if (threadIdx.x == 0) {
-      S.old_eq = e;
-      S.ls_done = 0;
-      a.counters[sg.mesh] = 0;
-    }
-  }
-}
-
-__device__ __forceinline__ double cand_alpha(const MeshScalars &S, int j) {
-  return j > kHalvings - 1 ? 0.0 : ldexp(S.max_step, -j);
-}
-
-// Quality energy at the NC candidates j = round*NC .. round*NC + NC - 1 (E = E0 + alpha D).
-// Persistent launch: a fixed grid walks the hex segments, so the rounds after the line search
-// has accepted a step cost one scalar read per segment.
-template <typename ET, typename VT, int NC>
-__global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t nseg) {
-  __shared__ double smem[NC][32];
-  for (int64_t sb = blockIdx.x; sb < nseg; sb += gridDim.x) {
-    const Seg sg = a.hseg[sb];
-    MeshScalars &S = a.sc[sg.mesh];
-    if (S.ls_done) continue;
-    const int64_t h = sg.begin + threadIdx.x;
-    const MeshDesc md = a.mesh[sg.mesh];
-    double acc[NC];
-#pragma unroll
-    for (int j = 0; j < NC; j++) acc[j] = 0;
-    if (h < sg.end) {
-      uint32_t hv[8];
-      load_hex(a.hexv, h, hv);
-      const int32_t gs = a.gslot[h];
-      ET E12[12][3], D12[12][3];
-      hex_edges_pos(a.X, hv, E12);
-      {
-        VT Dv[12][3];
-        hex_edges_vec(reinterpret_cast<const VT *>(a.d), hv, Dv);
-#pragma unroll
-        for (int e = 0; e < 12; e++)
-#pragma unroll
-          for (int r = 0; r < 3; r++) D12[e][r] = ET(Dv[e][r]);
-      }
-      double al[NC];
-#pragma unroll
-      for (int j = 0; j < NC; j++) al[j] = cand_alpha(S, round * NC + j);
-      SumAcc<ET> efast[NC];
-      double eslow[NC];
-#pragma unroll
-      for (int j = 0; j < NC; j++) eslow[j] = 0;
-#define HX_LE(K)                                                             \
-      {                                                                      \
-        ET E0[3][3], D[3][3];                                                \
-        tet_E12<K>(E12, E0);                                                 \
-        tet_E12<K>(D12, D);                                                  \
-        _Pragma("unroll") for (int j = 0; j < NC; j++) {                     \
-          ET E[3][3];                                                        \
-          const ET aj = ET(al[j]);                                           \
-          _Pragma("unroll") for (int r = 0; r < 3; r++)                      \
-          _Pragma("unroll") for (int c = 0; c < 3; c++) E[r][c] = E0[r][c] + aj * D[r][c]; \
-          tet_energy_acc<ET, VT, K>(a, h, hv, gs, E, al[j], efast[j], eslow[j]); \
-        }                                                                    \
-      }
-      HX_LE(0) HX_LE(1) HX_LE(2) HX_LE(3) HX_LE(4) HX_LE(5) HX_LE(6) HX_LE(7)
-#undef HX_LE
-#pragma unroll
-      for (int j = 0; j < NC; j++) acc[j] = S.M * (efast[j].value() + eslow[j]);
-    }
-    block_sum<NC>(acc, smem);
-    if (publish_partials<NC>(acc, a.partials, sb, a.counters + sg.mesh, md.nhblk)) {
-      for (int j = 0; j < NC; j++) {
-        double e = gather_partials_sum(a.partials, md.hblk0, md.nhblk, NC, j, smem);
-        if (threadIdx.x == 0) S.cand_eq[j] = e;
-      }
-      if (threadIdx.x == 0) a.counters[sg.mesh] = 0;
-    }
-    __syncthreads();
-  }
-}
-
-// Soft energy at the current X (round < 0) or at the candidates of `round`; its last block
-// takes the line-search decision for the round (accept the first finite E <= E_old,
-// line_search.cpp:26-47).
-template <typename VT>
-__global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
-  const Seg sg = a.cseg[blockIdx.x];
-  MeshScalars &S = a.sc[sg.mesh];
-  if (round >= 0 && S.ls_done) return;
-  const int nc = round < 0 ? 1 : a.ls_cand;
-  const int64_t i = sg.begin + threadIdx.x;
-  const MeshDesc md = a.mesh[sg.mesh];
-  const VT *d = reinterpret_cast<const VT *>(a.d);
-  const VT *da = reinterpret_cast<const VT *>(a.da);
-  double acc[kMaxCand];
-#pragma unroll
-  for (int j = 0; j < kMaxCand; j++) acc[j] = 0;
-  if (i < sg.end) {
-    int64_t li = i - md.c_off - md.t_off - md.l_off;
-    int kind = 0;
-    int64_t e;
-    if (li < md.nc) { e = md.c_off + li; }
-    else if ((li -= md.nc) < md.nt) { kind = 1; e = md.t_off + li; }
-    else { li -= md.nt; kind = 2; e = md.l_off + li; }
-    const int32_t lv = kind == 0 ? a.c_ids[e] : kind == 1 ? a.t_ids[e] : a.l_ids[e];
-    const int64_t v = md.v_off + lv;
-    const double x0 = a.X[4 * v], x1 = a.X[4 * v + 1], x2 = a.X[4 * v + 2];
-    const double d0 = double(d[4 * v]), d1 = double(d[4 * v + 1]), d2 = double(d[4 * v + 2]);
-#pragma unroll
-    for (int j = 0; j < kMaxCand; j++) {
-      if (j >= nc) break;
-      const double al = round < 0 ? 0.0 : cand_alpha(S, round * nc + j);
-      const double y0 = x0 + al * d0, y1 = x1 + al * d1, y2 = x2 + al * d2;
-      double en;
-      if (kind == 0) {
-        const double e0 = a.c_pos[3 * e] - y0, e1 = a.c_pos[3 * e + 1] - y1, e2 = a.c_pos[3 * e + 2] - y2;
-        en = S.lamda_C * (e0 * e0 + e1 * e1 + e2 * e2);
-      } else if (kind == 1) {
-        const double ad = a.t_nrm[3 * e] * y0 + a.t_nrm[3 * e + 1] * y1 + a.t_nrm[3 * e + 2] * y2 - a.t_dis[e];
-        en = S.lamda_T * ad * ad;
-      } else {
-        const double al_ = double(da[e]);  // a_L = CG solution (curve unknowns start at 0)
-        const double r0 = y0 - al_ * a.l_axis[3 * e] - a.l_orig[3 * e];
-        const double r1 = y1 - al_ * a.l_axis[3 * e + 1] - a.l_orig[3 * e + 1];
-        const double r2 = y2 - al_ * a.l_axis[3 * e + 2] - a.l_orig[3 * e + 2];
-        en = S.lamda_L * (r0 * r0 + r1 * r1 + r2 * r2);
-      }
-      acc[j] += en;
-    }
-  }
-  __shared__ double smem[kMaxCand][32];
-  block_sum<kMaxCand>(acc, smem);
-  if (publish_partials<kMaxCand>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.ncblk)) {
-    double es[kMaxCand];
-    for (int j = 0; j < nc; j++) es[j] = gather_partials_sum(a.partials, md.cblk0, md.ncblk, kMaxCand, j, smem);
-    if (threadIdx.x == 0) {
-      if (round < 0) {
-        S.old_es = es[0];
-        S.old_e = S.old_eq + es[0];
-      } else {
-        for (int j = 0; j < nc; j++) {
-          const int jj = round * nc + j;
-          if (jj > kHalvings) break;
-          const double e = S.cand_eq[j] + es[j];
-          const bool bad = isnan(e) || isinf(e) || e > S.old_e;
-          if (!bad) {
-            S.ls_done = 1;
-            S.step = cand_alpha(S, jj);
-            S.energy = e;
-            S.eq = S.cand_eq[j];
-            S.es = es[j];
-            S.halvings = jj;
-            break;
-          }
-        }
-        if (!S.ls_done && (round + 1) * nc > kHalvings) {  // only NaN/Inf energies, even at step 0
-          S.ls_done = 1; S.step = 0; S.energy = S.old_e; S.eq = S.old_eq; S.es = S.old_es;
-          S.halvings = kHalvings; S.status |= 1;
-        }
-      }
-      a.counters[sg.mesh] = 0;
-    }
-  }
-}
-
-// X += step d; a_L = delta_a
-template <typename VT>
-__global__ void __launch_bounds__(256) k_ls_apply(KArgs a) {
-  const Seg sg = a.vseg[blockIdx.x];
-  const MeshDesc md = a.mesh[sg.mesh];
-  const MeshScalars &S = a.sc[sg.mesh];
-  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
-  const ItemRef it = item_ref(md, i);
-  if (!it.curve) {
-    const VT *d = reinterpret_cast<const VT *>(a.d);
-    const int64_t o = 4 * it.idx;
-    const double st = S.step;
-#pragma unroll
-    for (int c = 0; c < 3; c++) a.X[o + c] = a.X[o + c] + st * double(d[o + c]);
-  } else {
-    const VT *da = reinterpret_cast<const VT *>(a.da);
-    a.aL[it.idx] = double(da[it.idx]);
-  }
-  }
-}
-
-// Persistent grid size: enough blocks to fill the GPU (152 SMs x 6), never more than segments.
-static inline unsigned pgrid(int64_t nseg) { return (unsigned)(nseg < 912 ? nseg : 912); }
-
+#define HX_LS_ENERGY_EXTERN(ET, VT)                                                                 \
+  extern template void launch_ls_energy_nc<ET, VT, 1>(const KArgs &, int, int64_t, cudaStream_t);   \
+  extern template void launch_ls_energy_nc<ET, VT, 2>(const KArgs &, int, int64_t, cudaStream_t);   \
+  extern template void launch_ls_energy_nc<ET, VT, 3>(const KArgs &, int, int64_t, cudaStream_t);   \
+  extern template void launch_ls_energy_nc<ET, VT, 4>(const KArgs &, int, int64_t, cudaStream_t);   \
+  extern template void launch_ls_energy_nc<ET, VT, 5>(const KArgs &, int, int64_t, cudaStream_t);   \
+  extern template void launch_ls_energy_nc<ET, VT, 6>(const KArgs &, int, int64_t, cudaStream_t);   \
+  extern template void launch_ls_energy_nc<ET, VT, 7>(const KArgs &, int, int64_t, cudaStream_t);   \
+  extern template void launch_ls_energy_nc<ET, VT, 8>(const KArgs &, int, int64_t, cudaStream_t);
+HX_LS_ENERGY_EXTERN(double, double)
+HX_LS_ENERGY_EXTERN(float, float)
+#undef HX_LS_ENERGY_EXTERN
 // One candidate-energy pass alone (timing): the pass of round 0.
 template <typename ET, typename VT>
 void launch_ls_energy_pass(const KArgs &a, int64_t hblk, cudaStream_t st) {
   switch (a.ls_cand) {
-    case 1: k_ls_energy<ET, VT, 1><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
-    case 2: k_ls_energy<ET, VT, 2><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
-    case 3: k_ls_energy<ET, VT, 3><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
-    case 4: k_ls_energy<ET, VT, 4><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
-    case 5: k_ls_energy<ET, VT, 5><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
-    case 6: k_ls_energy<ET, VT, 6><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
-    case 7: k_ls_energy<ET, VT, 7><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
-    default: k_ls_energy<ET, VT, 8><<<pgrid(hblk), a.hthreads, 0, st>>>(a, 0, hblk); break;
+    case 1: launch_ls_energy_nc<ET, VT, 1>(a, 0, hblk, st); break;
+    case 2: launch_ls_energy_nc<ET, VT, 2>(a, 0, hblk, st); break;
+    case 3: launch_ls_energy_nc<ET, VT, 3>(a, 0, hblk, st); break;
+    case 4: launch_ls_energy_nc<ET, VT, 4>(a, 0, hblk, st); break;
+    case 5: launch_ls_energy_nc<ET, VT, 5>(a, 0, hblk, st); break;
+    case 6: launch_ls_energy_nc<ET, VT, 6>(a, 0, hblk, st); break;
+    case 7: launch_ls_energy_nc<ET, VT, 7>(a, 0, hblk, st); break;
+    default: launch_ls_energy_nc<ET, VT, 8>(a, 0, hblk, st); break;
   }
 }
 
@@ -1095,14 +73,14 @@ void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk
   const int rounds = (kHalvings + 1 + a.ls_cand - 1) / a.ls_cand;
   for (int r = 0; r < rounds; r++) {
     switch (a.ls_cand) {
-      case 1: k_ls_energy<ET, VT, 1><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
-      case 2: k_ls_energy<ET, VT, 2><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
-      case 3: k_ls_energy<ET, VT, 3><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
-      case 4: k_ls_energy<ET, VT, 4><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
-      case 5: k_ls_energy<ET, VT, 5><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
-      case 6: k_ls_energy<ET, VT, 6><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
-      case 7: k_ls_energy<ET, VT, 7><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
-      default: k_ls_energy<ET, VT, 8><<<pgrid(hblk), a.hthreads, 0, st>>>(a, r, hblk); break;
+      case 1: launch_ls_energy_nc<ET, VT, 1>(a, r, hblk, st); break;
+      case 2: launch_ls_energy_nc<ET, VT, 2>(a, r, hblk, st); break;
+      case 3: launch_ls_energy_nc<ET, VT, 3>(a, r, hblk, st); break;
+      case 4: launch_ls_energy_nc<ET, VT, 4>(a, r, hblk, st); break;
+      case 5: launch_ls_energy_nc<ET, VT, 5>(a, r, hblk, st); break;
+      case 6: launch_ls_energy_nc<ET, VT, 6>(a, r, hblk, st); break;
+      case 7: launch_ls_energy_nc<ET, VT, 7>(a, r, hblk, st); break;
+      default: launch_ls_energy_nc<ET, VT, 8>(a, r, hblk, st); break;
     }
     k_ls_soft<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a, r);
   }
