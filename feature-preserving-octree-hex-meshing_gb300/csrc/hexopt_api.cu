@@ -302,6 +302,7 @@ KArgs make_args(hexopt_ctx *c) {
   a.root_mesh = c->root_mesh.as<int32_t>();
   a.root_count = c->root_count.as<unsigned>();
   a.root_min = c->root_min.as<unsigned long long>();
+  a.ls_active = c->root_count.as<unsigned>() + 1;
   a.n_meshes = c->n_meshes;
   return a;
 }
@@ -321,10 +322,10 @@ int alloc_vectors(hexopt_ctx *ctx) {
   const size_t nroot = (size_t)ctx->NH * 8;
   CK(ctx->root_list.ensure(nroot * sizeof(uint32_t)));
   CK(ctx->root_mesh.ensure(nroot * sizeof(int32_t)));
-  CK(ctx->root_count.ensure(sizeof(unsigned)));
+  CK(ctx->root_count.ensure(2 * sizeof(unsigned)));  // [0] root-list length, [1] line searches open
   CK(ctx->root_min.ensure(sizeof(unsigned long long) * ctx->n_meshes));
   {
-    CK(cudaMemsetAsync(ctx->root_count.p, 0, sizeof(unsigned), ctx->st));
+    CK(cudaMemsetAsync(ctx->root_count.p, 0, 2 * sizeof(unsigned), ctx->st));
     std::vector<double> inf(ctx->n_meshes, INFINITY);
     CK(cudaMemcpyAsync(ctx->root_min.p, inf.data(), sizeof(double) * ctx->n_meshes, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
@@ -1668,6 +1669,9 @@ int hexopt_time_stage(hexopt_ctx *ctx, int stage, int reps, double *ms_per_launc
     for (auto &S : ctx->sc) { S.cg_done = 0; S.ls_done = 0; }
     rc = push_scalars(ctx);
     if (rc) return rc;
+    const unsigned open = (unsigned)ctx->n_meshes;
+    CK(cudaMemcpyAsync(ctx->root_count.as<unsigned>() + 1, &open, sizeof(unsigned), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
   }
   rc = hexopt_timer_start(ctx);
   if (rc) return rc;

@@ -236,16 +236,13 @@ __device__ void slim_weights(int energy, T exp_f, const T s[3], const T U[3][3],
 }
 
 // Per-tet energy density (compute_energy_with_jacobians 3-D branch, slim_m.cpp:850-912).
-// Symmetric Dirichlet needs no SVD: sum s^2 = |J|_F^2 and sum s^-2 = |adj J|_F^2 / det^2.
+// The SVD-based energies (ARAP, LOG_ARAP, CONFORMAL, EXP_CONFORMAL) are out of line: the optimiser
+// runs symmetric Dirichlet, and inlining a 3x3 SVD into every corner tet of the energy kernels
+// would size their register allocation for code that does not run.
 template <typename T>
-__device__ T tet_energy_density(int energy, T exp_f, const T J[3][3]) {
-  if (energy == SYMMETRIC_DIRICHLET || energy == EXP_SYMMETRIC_DIRICHLET) {
-    T A[3][3];
-    adj3(J, A);
-    T d = det3(J);
-    T e = frob2(J) + frob2(A) / (d * d);
-    return energy == SYMMETRIC_DIRICHLET ? e : exp(exp_f * e);
-  }
+__device__ __noinline__ T tet_energy_density_svd(int energy, T J00, T J01, T J02, T J10, T J11, T J12, T J20,
+                                                 T J21, T J22) {
+  const T J[3][3] = {{J00, J01, J02}, {J10, J11, J12}, {J20, J21, J22}};
   T R[3][3], U[3][3], s[3], Vm[3][3];
   polar_svd3(J, R, U, s, Vm);
   const T s1 = s[0], s2 = s[1], s3 = s[2];
@@ -256,6 +253,19 @@ __device__ T tet_energy_density(int energy, T exp_f, const T J[3][3]) {
     case EXP_CONFORMAL: return exp((s1 * s1 + s2 * s2 + s3 * s3) / (T(3) * pow(s1 * s2 * s3, T(2.0 / 3.0))));
   }
   return T(NAN);
+}
+// Symmetric Dirichlet needs no SVD: sum s^2 = |J|_F^2 and sum s^-2 = |adj J|_F^2 / det^2.
+template <typename T>
+__device__ __forceinline__ T tet_energy_density(int energy, T exp_f, const T J[3][3]) {
+  if (energy == SYMMETRIC_DIRICHLET || energy == EXP_SYMMETRIC_DIRICHLET) {
+    T A[3][3];
+    adj3(J, A);
+    T d = det3(J);
+    T e = frob2(J) + frob2(A) / (d * d);
+    return energy == SYMMETRIC_DIRICHLET ? e : exp(exp_f * e);
+  }
+  return tet_energy_density_svd<T>(energy, J[0][0], J[0][1], J[0][2], J[1][0], J[1][1], J[1][2], J[2][0], J[2][1],
+                                   J[2][2]);
 }
 
 // ------------------------------------------------------------------------------- reductions
@@ -377,6 +387,37 @@ __device__ __forceinline__ double gather_partials_sum(const double *partials, in
   double v[1] = {x};
   block_sum<1>(v, smem);
   return v[0];
+}
+// The same fixed-order sums for components 0..NV-1 at once.  Each thread adds its blocks
+// b = tid, tid + blockDim, ... in that order, exactly as above, but with the loads of U blocks in
+// flight together, so the last block's tail costs a few L2 round trips instead of one per block.
+template <int NV>
+__device__ __forceinline__ void gather_partials_sums(const double *partials, int64_t first_blk, int nblk, int stride,
+                                                     double (&out)[NV], double (*smem)[32]) {
+  constexpr int U = NV == 1 ? 16 : NV == 2 ? 8 : NV <= 4 ? 4 : 2;
+  double x[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) x[k] = 0;
+  const double *base = partials + first_blk * stride;
+  const int bd = blockDim.x;
+  int b = threadIdx.x;
+  for (; b + (U - 1) * bd < nblk; b += U * bd) {
+    double t[U][NV];
+#pragma unroll
+    for (int u = 0; u < U; u++)
+#pragma unroll
+      for (int k = 0; k < NV; k++) t[u][k] = __ldcg(base + (int64_t)(b + u * bd) * stride + k);
+#pragma unroll
+    for (int u = 0; u < U; u++)
+#pragma unroll
+      for (int k = 0; k < NV; k++) x[k] += t[u][k];
+  }
+  for (; b < nblk; b += bd)
+#pragma unroll
+    for (int k = 0; k < NV; k++) x[k] += __ldcg(base + (int64_t)b * stride + k);
+  block_sum<NV>(x, smem);
+#pragma unroll
+  for (int k = 0; k < NV; k++) out[k] = x[k];
 }
 __device__ __forceinline__ double gather_partials_min(const double *partials, int64_t first_blk, int nblk, int NV,
                                                       int k, double (*smem)[32]) {

@@ -50,6 +50,8 @@ struct KArgs {
   int32_t *root_mesh;
   unsigned *root_count;
   unsigned long long *root_min;
+  // meshes whose line search has not accepted a step yet (later candidate passes exit when 0)
+  unsigned *ls_active;
 };
 
 template <typename ET, typename VT> void launch_precompute(const KArgs &a, int64_t nblk, cudaStream_t st);

@@ -1276,8 +1276,9 @@ __global__ void __launch_bounds__(256) k_haus_reduce(HausArgs h) {
   const int kind = SIDE == 0 ? K_TGTV : K_SURFV;
   if (publish_partials<3>(out, h.partials, blockIdx.x, h.counters + sg.mesh, md.knblk[kind])) {
     double m = gather_partials_min(h.partials, md.kblk0[kind], md.knblk[kind], 3, 0, smem);
-    double s = gather_partials_sum(h.partials, md.kblk0[kind], md.knblk[kind], 3, 1, smem);
-    double c = gather_partials_sum(h.partials, md.kblk0[kind], md.knblk[kind], 3, 2, smem);
+    double g[2];  // components 1 and 2 of 3
+    gather_partials_sums<2>(h.partials + 1, md.kblk0[kind], md.knblk[kind], 3, g, smem);
+    const double s = g[0], c = g[1];
     if (threadIdx.x == 0) {
       hm.side_max[SIDE] = -m;
       hm.side_mean[SIDE] = s / c;

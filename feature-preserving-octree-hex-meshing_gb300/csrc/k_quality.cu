@@ -64,8 +64,9 @@ __global__ void __launch_bounds__(128) k_sj(KArgs a, double *V_Js, double *H_Js)
   double out[3] = {m0, acc[0], acc[1]};
   if (publish_partials<3>(out, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
     double m = gather_partials_min(a.partials, md.hblk0, md.nhblk, 3, 0, smem);
-    double s = gather_partials_sum(a.partials, md.hblk0, md.nhblk, 3, 1, smem);
-    double c = gather_partials_sum(a.partials, md.hblk0, md.nhblk, 3, 2, smem);
+    double g[2];  // components 1 and 2 of 3
+    gather_partials_sums<2>(a.partials + 1, md.hblk0, md.nhblk, 3, g, smem);
+    const double s = g[0], c = g[1];
     if (threadIdx.x == 0) {
       MeshScalars &S = a.sc[sg.mesh];
       S.sj_min = fmin(m, 1.0);
@@ -147,8 +148,9 @@ __global__ void __launch_bounds__(128) k_sj_fast(KArgs a) {
   double out[3] = {m0, acc[0], acc[1]};
   if (publish_partials<3>(out, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
     double m = gather_partials_min(a.partials, md.hblk0, md.nhblk, 3, 0, smem);
-    double s = gather_partials_sum(a.partials, md.hblk0, md.nhblk, 3, 1, smem);
-    double c = gather_partials_sum(a.partials, md.hblk0, md.nhblk, 3, 2, smem);
+    double g[2];  // components 1 and 2 of 3
+    gather_partials_sums<2>(a.partials + 1, md.hblk0, md.nhblk, 3, g, smem);
+    const double s = g[0], c = g[1];
     if (threadIdx.x == 0) {
       MeshScalars &S = a.sc[sg.mesh];
       S.sj_min = fmin(m, 1.0);

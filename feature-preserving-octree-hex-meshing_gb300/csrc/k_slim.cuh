@@ -417,9 +417,9 @@ __global__ void __launch_bounds__(256) k_cg_start(KArgs a) {
   __shared__ double smem[3][32];
   block_sum<3>(acc, smem);
   if (publish_partials<3>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
-    double v0 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 3, 0, smem);
-    double v1 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 3, 1, smem);
-    double v2 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 3, 2, smem);
+    double v[3];
+    gather_partials_sums<3>(a.partials, md.vblk0, md.nvblk, 3, v, smem);
+    const double v0 = v[0], v1 = v[1], v2 = v[2];
     if (threadIdx.x == 0) {
       S.rhs_norm2 = v0;
       S.threshold = a.cg_tol * a.cg_tol * v0;
@@ -463,7 +463,9 @@ __global__ void __launch_bounds__(256) k_cg_alpha(KArgs a) {
   __shared__ double smem[1][32];
   block_sum<1>(acc, smem);
   if (publish_partials<1>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
-    double pAp = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 1, 0, smem);
+    double g[1];
+    gather_partials_sums<1>(a.partials, md.vblk0, md.nvblk, 1, g, smem);
+    const double pAp = g[0];
     if (threadIdx.x == 0) {
       S.alpha = S.abs_new / pAp;
       if (!(pAp > 0.0)) S.status |= 4;
@@ -521,8 +523,9 @@ __global__ void __launch_bounds__(256) k_cg_update(KArgs a) {
   __shared__ double smem[2][32];
   block_sum<2>(acc, smem);
   if (publish_partials<2>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
-    double rn2 = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 2, 0, smem);
-    double rz = gather_partials_sum(a.partials, md.vblk0, md.nvblk, 2, 1, smem);
+    double g[2];
+    gather_partials_sums<2>(a.partials, md.vblk0, md.nvblk, 2, g, smem);
+    const double rn2 = g[0], rz = g[1];
     if (threadIdx.x == 0) {
       S.rn2 = rn2;
       S.cg_error = sqrt(rn2 / S.rhs_norm2);
@@ -806,7 +809,7 @@ __global__ void __launch_bounds__(128) k_ls_roots(KArgs a) {
 // max_step = min(1, 0.8 min_root) per mesh; re-arms the minimum and the list for the next call.
 static __global__ void k_ls_bound_finish(KArgs a, int n_meshes) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m == 0) *a.root_count = 0;
+  if (m == 0) { *a.root_count = 0; *a.ls_active = (unsigned)n_meshes; }
   if (m >= n_meshes) return;
   MeshScalars &S = a.sc[m];
   const double r = __longlong_as_double((long long)a.root_min[m]);
@@ -875,7 +878,9 @@ __global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
   block_sum<1>(eq, smem);
   if (threadIdx.x == 0) acc[0] = eq[0];
   if (publish_partials<1>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
-    double e = gather_partials_sum(a.partials, md.hblk0, md.nhblk, 1, 0, smem);
+    double g[1];
+    gather_partials_sums<1>(a.partials, md.hblk0, md.nhblk, 1, g, smem);
+    const double e = g[0];
     if (threadIdx.x == 0) {
       S.old_eq = e;
       S.ls_done = 0;
@@ -894,6 +899,7 @@ __device__ __forceinline__ double cand_alpha(const MeshScalars &S, int j) {
 template <typename ET, typename VT, int NC>
 __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t nseg) {
   __shared__ double smem[NC][32];
+  if (*a.ls_active == 0) return;  // every mesh has accepted its step
   for (int64_t sb = blockIdx.x; sb < nseg; sb += gridDim.x) {
     const Seg sg = a.hseg[sb];
     MeshScalars &S = a.sc[sg.mesh];
@@ -944,10 +950,10 @@ __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t n
     }
     block_sum<NC>(acc, smem);
     if (publish_partials<NC>(acc, a.partials, sb, a.counters + sg.mesh, md.nhblk)) {
-      for (int j = 0; j < NC; j++) {
-        double e = gather_partials_sum(a.partials, md.hblk0, md.nhblk, NC, j, smem);
-        if (threadIdx.x == 0) S.cand_eq[j] = e;
-      }
+      double g[NC];
+      gather_partials_sums<NC>(a.partials, md.hblk0, md.nhblk, NC, g, smem);
+      if (threadIdx.x == 0)
+        for (int j = 0; j < NC; j++) S.cand_eq[j] = g[j];
       if (threadIdx.x == 0) a.counters[sg.mesh] = 0;
     }
     __syncthreads();
@@ -960,6 +966,7 @@ __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t n
 template <typename VT>
 __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
   const Seg sg = a.cseg[blockIdx.x];
+  if (round >= 0 && *a.ls_active == 0) return;  // every mesh has accepted its step
   MeshScalars &S = a.sc[sg.mesh];
   if (round >= 0 && S.ls_done) return;
   const int nc = round < 0 ? 1 : a.ls_cand;
@@ -1007,7 +1014,7 @@ __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
   block_sum<kMaxCand>(acc, smem);
   if (publish_partials<kMaxCand>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.ncblk)) {
     double es[kMaxCand];
-    for (int j = 0; j < nc; j++) es[j] = gather_partials_sum(a.partials, md.cblk0, md.ncblk, kMaxCand, j, smem);
+    gather_partials_sums<kMaxCand>(a.partials, md.cblk0, md.ncblk, kMaxCand, es, smem);
     if (threadIdx.x == 0) {
       if (round < 0) {
         S.old_es = es[0];
@@ -1020,6 +1027,7 @@ __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
           const bool bad = isnan(e) || isinf(e) || e > S.old_e;
           if (!bad) {
             S.ls_done = 1;
+            atomicSub(a.ls_active, 1u);
             S.step = cand_alpha(S, jj);
             S.energy = e;
             S.eq = S.cand_eq[j];
@@ -1030,6 +1038,7 @@ __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
         }
         if (!S.ls_done && (round + 1) * nc > kHalvings) {  // only NaN/Inf energies, even at step 0
           S.ls_done = 1; S.step = 0; S.energy = S.old_e; S.eq = S.old_eq; S.es = S.old_es;
+          atomicSub(a.ls_active, 1u);
           S.halvings = kHalvings; S.status |= 1;
         }
       }
