@@ -106,7 +106,7 @@ struct hexopt_ctx {
   std::vector<MeshDesc> md;
   DBuf md_d, sc_d;
   std::vector<MeshScalars> sc;
-  DBuf X, hexv, gslot, Sinv, Ccoef, Bgen, aL;
+  DBuf X, X32, hexv, gslot, Sinv, Ccoef, Bgen, aL;
   DBuf b, diag, ba, diaga;
   DBuf d, r, p, q, invd, da, ra, pa, qa, invda;
   DBuf stage, stage2, HJs, VJs, Xa, grad, Xbak;
@@ -279,6 +279,7 @@ KArgs make_args(hexopt_ctx *c) {
   a.hexv = c->hexv.as<uint32_t>();
   a.gslot = c->gslot.as<int32_t>();
   a.X = c->X.as<double>();
+  a.X32 = c->X32.as<float>();
   a.aL = c->aL.as<double>();
   a.Sinv = c->Sinv.p;
   a.Ccoef = c->Ccoef.p;
@@ -732,7 +733,10 @@ int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const
   // positions
   CK(upload(ctx->stage, V, (size_t)NV * 3, ctx->st));
   CK(ctx->X.ensure(sizeof(double) * 4 * NV));
+  CK(ctx->X32.ensure(sizeof(float) * 8 * NV));
   launch_rows_to_aos4(ctx->stage.as<double>(), ctx->X.as<double>(), NV, ctx->st);
+  launch_split_pos(ctx->X.as<double>(), ctx->X32.as<float>(), NV, ctx->st);
+  ctx->launches += 1;
   // hexes -> AoSoA with global ids
   const int64_t NHp = (NH + 31) / 32 * 32;
   CK(upload(ctx->stage2, H, (size_t)NH * 8, ctx->st));
@@ -760,7 +764,8 @@ int hexopt_set_positions(hexopt_ctx *ctx, const double *V) {
   if (!V) return fail(ctx, HEXOPT_ERR_ARG, "set_positions: NULL");
   CK(upload(ctx->stage, V, (size_t)ctx->NV * 3, ctx->st));
   launch_rows_to_aos4(ctx->stage.as<double>(), ctx->X.as<double>(), ctx->NV, ctx->st);
-  ctx->launches++;
+  launch_split_pos(ctx->X.as<double>(), ctx->X32.as<float>(), ctx->NV, ctx->st);
+  ctx->launches += 2;
   CKL();
   return HEXOPT_OK;
 }
@@ -1522,7 +1527,7 @@ int hexopt_autotune(hexopt_ctx *ctx) {
         if (rc) return rc;
         float ms = 0;
         for (int rep = 0; rep < 2; rep++) {
-          CK(cudaMemcpyAsync(ctx->X.p, ctx->Xbak.p, sizeof(double) * 4 * ctx->NV, cudaMemcpyDeviceToDevice, ctx->st));
+          CK(cudaMemcpyAsync(ctx->X.p, ctx->Xbak.p, sizeof(double) * 4 * ctx->NV, cudaMemcpyDeviceToDevice, ctx->st)); launch_split_pos(ctx->X.as<double>(), ctx->X32.as<float>(), ctx->NV, ctx->st);
           ctx->sc = sc0;
           rc = push_scalars(ctx);
           if (rc) return rc;
@@ -1542,7 +1547,7 @@ int hexopt_autotune(hexopt_ctx *ctx) {
   ctx->params.ls_candidates = bl;
   rc = rebuild_tables(ctx);
   if (rc) return rc;
-  CK(cudaMemcpyAsync(ctx->X.p, ctx->Xbak.p, sizeof(double) * 4 * ctx->NV, cudaMemcpyDeviceToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->X.p, ctx->Xbak.p, sizeof(double) * 4 * ctx->NV, cudaMemcpyDeviceToDevice, ctx->st)); launch_split_pos(ctx->X.as<double>(), ctx->X32.as<float>(), ctx->NV, ctx->st);
   ctx->sc = sc0;
   rc = push_scalars(ctx);
   if (rc) return rc;

@@ -156,6 +156,40 @@ __device__ __forceinline__ void hex_edges_pos(const double *X, const uint32_t hv
 #pragma unroll
     for (int r = 0; r < 3; r++) E12[e][r] = T(P[hex_edge_hi(e)][r] - P[hex_edge_lo(e)][r]);
 }
+// FP32 hi/lo split of one position: hi = fl32(x), lo = fl32(x - hi), so hi + lo carries x to
+// about 48 bits.  Layout per vertex: hi.x hi.y hi.z 0 lo.x lo.y lo.z 0 (two float4).
+__device__ __forceinline__ void store_split(float *X32, int64_t v, double x, double y, double z) {
+  const float hx = float(x), hy = float(y), hz = float(z);
+  reinterpret_cast<float4 *>(X32)[2 * v] = make_float4(hx, hy, hz, 0.f);
+  reinterpret_cast<float4 *>(X32)[2 * v + 1] =
+      make_float4(float(x - double(hx)), float(y - double(hy)), float(z - double(hz)), 0.f);
+}
+// Hex edges from the split positions, all in FP32: e = (hi_b - hi_a) + (lo_b - lo_a).  The
+// hi difference is exact for nearby points (Sterbenz) and otherwise rounds once, so each edge is
+// within ~1.5 FP32 ulps of the FP64 edge, with no FP64 instruction (GB300's FP64 pipe is a small
+// fraction of its FP32 rate).
+__device__ __forceinline__ void hex_edges_split(const float *X32, const uint32_t hv[8], float E12[12][3]) {
+  float H[8][3], L[8][3];
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const float4 h = __ldg(reinterpret_cast<const float4 *>(X32) + 2 * (int64_t)hv[c]);
+    const float4 l = __ldg(reinterpret_cast<const float4 *>(X32) + 2 * (int64_t)hv[c] + 1);
+    H[c][0] = h.x; H[c][1] = h.y; H[c][2] = h.z;
+    L[c][0] = l.x; L[c][1] = l.y; L[c][2] = l.z;
+  }
+#pragma unroll
+  for (int e = 0; e < 12; e++)
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+      E12[e][r] = __fadd_rn(__fsub_rn(H[hex_edge_hi(e)][r], H[hex_edge_lo(e)][r]),
+                            __fsub_rn(L[hex_edge_hi(e)][r], L[hex_edge_lo(e)][r]));
+}
+// Edge frame in the arithmetic type of the mode: FP32 from the split, FP64 from X.
+template <typename ET>
+__device__ __forceinline__ void hex_edges_mode(const KArgs &a, const uint32_t hv[8], ET E12[12][3]) {
+  if constexpr (sizeof(ET) == 4) hex_edges_split(a.X32, hv, E12);
+  else hex_edges_pos(a.X, hv, E12);
+}
 template <typename T>
 __device__ __forceinline__ void hex_edges_vec(const T *Y, const uint32_t hv[8], T E12[12][3]) {
   T P[8][3];

@@ -19,6 +19,7 @@ struct KArgs {
   const uint32_t *hexv;  // AoSoA corners
   const int32_t *gslot;  // per hex: -1 cube target, else own-shape slot
   double *X;             // positions AoS4 FP64
+  float *X32;            // FP32 hi/lo split of X per vertex: hi.xyz, 0, lo.xyz, 0 (x = hi + lo to ~48 bits)
   double *aL;            // curve parameters (FP64)
   void *Sinv;            // per tet 1/cbrt(6 vol) (ET, AoSoA NC=1)
   void *Ccoef;           // per tet C_t (ET, AoSoA NC=6)
@@ -81,6 +82,8 @@ void launch_fa_schedule(MeshScalars *sc, int n_meshes, double lamda0, double bou
 // ---- layout helpers (k_layout.cu) ----
 void launch_rows_to_aos4(const double *src, double *dst, int64_t n, cudaStream_t st);
 void launch_aos4_to_rows(const double *src, double *dst, int64_t n, cudaStream_t st);
+// X32 <- hi/lo split of the FP64 positions (after every host-side write of X)
+void launch_split_pos(const double *X, float *X32, int64_t n, cudaStream_t st);
 void launch_hex_to_aosoa_mesh(const uint32_t *src, int64_t h0, int64_t nh, uint32_t voff, uint32_t *dst,
                               cudaStream_t st);
 

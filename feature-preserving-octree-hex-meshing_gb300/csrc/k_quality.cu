@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(128) k_sj_dev(KArgs a, const double *H_Js) {
   }
 }
 
-// In-loop quality check of the mixed mode: corner scaled Jacobians in FP32 from the FP64 edge
+// In-loop quality check of the mixed mode: corner scaled Jacobians in FP32 from the FP32 hi/lo edge
 // frame; a corner whose FP32 value is within 1e-4 of zero (its sign, i.e. the inversion flag, is
 // in doubt) or whose edges are near the Precision guard is re-evaluated bit-exactly in FP64.
 // Per mesh: min, sum and inverted count (the deviation pass is not part of the check).
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(128) k_sj_fast(KArgs a) {
 #pragma unroll
     for (int c = 0; c < 8; c++) hv[c] = __ldg(a.hexv + hex_idx(h, c));
     float E12[12][3];
-    hex_edges_pos(a.X, hv, E12);
+    hex_edges_split(a.X32, hv, E12);
     float m32 = 1.f;
     double m64 = 1.0;
     corner_sj_fast<0>(E12, a.X, hv, m32, m64); corner_sj_fast<1>(E12, a.X, hv, m32, m64);
@@ -208,6 +208,14 @@ __global__ void k_hex_to_aosoa(const uint32_t *src, int64_t h0, int64_t nh, uint
 
 void launch_rows_to_aos4(const double *src, double *dst, int64_t n, cudaStream_t st) {
   if (n > 0) k_rows_to_aos4<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, dst, n);
+}
+__global__ void k_split_pos(const double *X, float *X32, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  store_split(X32, i, X[4 * i], X[4 * i + 1], X[4 * i + 2]);
+}
+void launch_split_pos(const double *X, float *X32, int64_t n, cudaStream_t st) {
+  if (n > 0) k_split_pos<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(X, X32, n);
 }
 void launch_aos4_to_rows(const double *src, double *dst, int64_t n, cudaStream_t st) {
   if (n > 0) k_aos4_to_rows<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, dst, n);

@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(128) k_local(KArgs a) {
   load_hex(a.hexv, h, hv);
   const int32_t gs = a.gslot[h];
   ET E12[12][3];
-  hex_edges_pos(a.X, hv, E12);
+  hex_edges_mode<ET>(a, hv, E12);
   bool degenerate = false;
   local_tet<ET, 0, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
   local_tet<ET, 1, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
@@ -834,7 +834,7 @@ __global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
     load_hex(a.hexv, h, hv);
     const int32_t gs = a.gslot[h];
     ET E12[12][3], D12[12][3];
-    hex_edges_pos(a.X, hv, E12);
+    hex_edges_mode<ET>(a, hv, E12);
     {
       VT Dv[12][3];
       hex_edges_vec(reinterpret_cast<const VT *>(a.d), hv, Dv);
@@ -913,25 +913,35 @@ __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t n
       uint32_t hv[8];
       load_hex(a.hexv, h, hv);
       const int32_t gs = a.gslot[h];
-      ET E12[12][3], D12[12][3];
-      hex_edges_pos(a.X, hv, E12);
-      {
-        VT Dv[12][3];
-        hex_edges_vec(reinterpret_cast<const VT *>(a.d), hv, Dv);
-#pragma unroll
-        for (int e = 0; e < 12; e++)
-#pragma unroll
-          for (int r = 0; r < 3; r++) D12[e][r] = ET(Dv[e][r]);
-      }
       double al[NC];
 #pragma unroll
       for (int j = 0; j < NC; j++) al[j] = cand_alpha(S, round * NC + j);
+      ET E12[12][3], D12[NC == 1 ? 1 : 12][3];
+      hex_edges_mode<ET>(a, hv, E12);
+      {
+        VT Dv[12][3];
+        hex_edges_vec(reinterpret_cast<const VT *>(a.d), hv, Dv);
+        // One candidate: fold the step into the edge frame, E + a D per edge.  A corner tet's
+        // edges are these with a sign, and sg (E + a D) rounds exactly like sg E + a (sg D).
+        const ET a0 = ET(al[0]);
+#pragma unroll
+        for (int e = 0; e < 12; e++)
+#pragma unroll
+          for (int r = 0; r < 3; r++) {
+            if constexpr (NC == 1) E12[e][r] = E12[e][r] + a0 * ET(Dv[e][r]);
+            else D12[e][r] = ET(Dv[e][r]);
+          }
+      }
       SumAcc<ET> efast[NC];
       double eslow[NC];
 #pragma unroll
       for (int j = 0; j < NC; j++) eslow[j] = 0;
 #define HX_LE(K)                                                             \
-      {                                                                      \
+      if constexpr (NC == 1) {                                               \
+        ET E[3][3];                                                          \
+        tet_E12<K>(E12, E);                                                  \
+        tet_energy_acc<ET, VT, K>(a, h, hv, gs, E, al[0], efast[0], eslow[0]); \
+      } else {                                                               \
         ET E0[3][3], D[3][3];                                                \
         tet_E12<K>(E12, E0);                                                 \
         tet_E12<K>(D12, D);                                                  \
@@ -1059,8 +1069,10 @@ __global__ void __launch_bounds__(256) k_ls_apply(KArgs a) {
     const VT *d = reinterpret_cast<const VT *>(a.d);
     const int64_t o = 4 * it.idx;
     const double st = S.step;
+    double x[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) a.X[o + c] = a.X[o + c] + st * double(d[o + c]);
+    for (int c = 0; c < 3; c++) { x[c] = a.X[o + c] + st * double(d[o + c]); a.X[o + c] = x[c]; }
+    store_split(a.X32, it.idx, x[0], x[1], x[2]);
   } else {
     const VT *da = reinterpret_cast<const VT *>(a.da);
     a.aL[it.idx] = double(da[it.idx]);
@@ -1068,15 +1080,28 @@ __global__ void __launch_bounds__(256) k_ls_apply(KArgs a) {
   }
 }
 
-// Persistent grid size: enough blocks to fill the GPU (152 SMs x 6), never more than segments.
-static inline unsigned pgrid(int64_t nseg) { return (unsigned)(nseg < 912 ? nseg : 912); }
 
 
 // One line-search energy pass over NC candidate steps.  Each (ET, VT, NC) is instantiated in a
 // k_ls_energy_*.cu unit of its own, so the unrolled candidate loops compile in parallel.
+// The persistent grid is the number of blocks resident at once (from this kernel's registers and
+// the device's SM count, looked up once per block size), never more than the segments.
 template <typename ET, typename VT, int NC>
 void launch_ls_energy_nc(const KArgs &a, int round, int64_t hblk, cudaStream_t st) {
-  k_ls_energy<ET, VT, NC><<<pgrid(hblk), a.hthreads, 0, st>>>(a, round, hblk);
+  static int grid_threads = 0, grid = 0;
+  if (grid_threads != a.hthreads) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ls_energy<ET, VT, NC>, a.hthreads, 0) != cudaSuccess ||
+        sms <= 0 || per_sm <= 0) {
+      sms = 152; per_sm = 6;
+    }
+    grid = sms * per_sm;
+    grid_threads = a.hthreads;
+  }
+  const int64_t g = hblk < grid ? hblk : grid;
+  k_ls_energy<ET, VT, NC><<<(unsigned)g, a.hthreads, 0, st>>>(a, round, hblk);
 }
 #define HX_LS_ENERGY_INST(ET, VT, NC) \
   template void launch_ls_energy_nc<ET, VT, NC>(const KArgs &, int, int64_t, cudaStream_t);
