@@ -182,45 +182,79 @@ __global__ void __launch_bounds__(128) k_local(KArgs a) {
 
 // ------------------------------------------------------------------------------- SpMV
 // q += K p over the element terms: J' = E(p) B', Q = C' J', forces G = Q B'^T (the cube scale
-// is folded into C').
+// is folded into C').  crow points at the hex's coefficient of row 0 (tet 0, component 0); the
+// row (K, i) is crow[(K * 6 + i) * 32], in global memory or in the block's shared-memory copy.
 template <typename ET, int K>
-__device__ __forceinline__ void spmv_tet(const KArgs &a, int64_t h, int32_t gs, const ET E12[12][3], ET F[8][3]) {
+__device__ __forceinline__ void spmv_tet(const KArgs &a, int32_t gs, const ET E12[12][3], const ET *crow,
+                                         ET F[8][3]) {
   ET E[3][3], J[3][3], Q[3][3], G[3][3];
   tet_E12<K>(E12, E);
   const double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
   apply_B<K>(E, gs, B, ET(1), J);
-  const ET *C = reinterpret_cast<const ET *>(a.Ccoef);
   ET c[6];
 #pragma unroll
-  for (int i = 0; i < 6; i++) c[i] = C[tet_idx<6>(h, K, i)];
+  for (int i = 0; i < 6; i++) c[i] = crow[(K * 6 + i) * 32];
   sym_mul(c, J, Q);
   apply_BT<K>(Q, gs, B, ET(1), G);
   scatter_cols<K>(G, F);
 }
 
-// 64 registers (8 blocks of 128 per SM): more gathers in flight outweigh the few spills
+// 16-byte asynchronous global -> shared copy (cp.async, cached in L2 only); completion is awaited
+// with cp.async.wait_all by the issuing thread, a hardware wait on its own copies.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Mixed mode: 64 registers (8 blocks of 128 per SM), more gathers in flight outweigh the few
+// spills; FP64 mode: 128 registers (4 blocks), as its 64-register build spills 1.6 KB a thread.
+// Mixed mode: a warp whose 32 hexes fill one AoSoA tile copies the tile's 8 x 6 FP32
+// coefficients (6 KB, contiguous) into shared memory with cp.async before it gathers the corner
+// ids and directions, so the coefficient stream (70% of the bytes) is in flight while the
+// dependent gathers wait; other warps (a mesh tail, or a batch mesh not starting on a multiple
+// of 32 hexes) read the coefficients from global memory.
 template <typename ET>
-__global__ void __launch_bounds__(128, 8) k_spmv(KArgs a) {
+__global__ void __launch_bounds__(128, sizeof(ET) == 4 ? 8 : 4) k_spmv(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
   if (a.sc[sg.mesh].cg_done) return;
   const int64_t h = sg.begin + threadIdx.x;
+  const ET *C = reinterpret_cast<const ET *>(a.Ccoef);
+  const ET *crow = C + tet_idx<6>(h, 0, 0);
+  bool staged = false;  // every lane of a staged warp is active
+  if constexpr (sizeof(ET) == 4) {
+    __shared__ __align__(16) float cs[4][48 * 32];  // blockDim.x <= 128
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t hw = sg.begin + 32 * w;  // the warp's first hex
+    if ((hw & 31) == 0 && hw + 32 <= sg.end && w < 4) {
+      const float *src = C + tet_idx<6>(hw, 0, 0);  // 1536 floats, 16-byte aligned
+#pragma unroll
+      for (int i = 0; i < 12; i++) cp_async16(&cs[w][(i * 32 + lane) * 4], src + (i * 32 + lane) * 4);
+      crow = &cs[w][lane];
+      staged = true;
+    }
+  }
   if (h >= sg.end) return;
   uint32_t hv[8];
   load_hex(a.hexv, h, hv);
   const int32_t gs = a.gslot[h];
   ET E12[12][3];
   hex_edges_vec(reinterpret_cast<const ET *>(a.p), hv, E12);
+  if (staged) {
+    cp_async_wait_all();
+    __syncwarp();
+  }
   ET F[8][3];
 #pragma unroll
   for (int c = 0; c < 8; c++) F[c][0] = F[c][1] = F[c][2] = ET(0);
-  spmv_tet<ET, 0>(a, h, gs, E12, F);
-  spmv_tet<ET, 1>(a, h, gs, E12, F);
-  spmv_tet<ET, 2>(a, h, gs, E12, F);
-  spmv_tet<ET, 3>(a, h, gs, E12, F);
-  spmv_tet<ET, 4>(a, h, gs, E12, F);
-  spmv_tet<ET, 5>(a, h, gs, E12, F);
-  spmv_tet<ET, 6>(a, h, gs, E12, F);
-  spmv_tet<ET, 7>(a, h, gs, E12, F);
+  spmv_tet<ET, 0>(a, gs, E12, crow, F);
+  spmv_tet<ET, 1>(a, gs, E12, crow, F);
+  spmv_tet<ET, 2>(a, gs, E12, crow, F);
+  spmv_tet<ET, 3>(a, gs, E12, crow, F);
+  spmv_tet<ET, 4>(a, gs, E12, crow, F);
+  spmv_tet<ET, 5>(a, gs, E12, crow, F);
+  spmv_tet<ET, 6>(a, gs, E12, crow, F);
+  spmv_tet<ET, 7>(a, gs, E12, crow, F);
   ET *q = reinterpret_cast<ET *>(a.q);
 #pragma unroll
   for (int c = 0; c < 8; c++) atomic_add3(q, hv[c], F[c][0], F[c][1], F[c][2]);
@@ -822,7 +856,7 @@ static __global__ void k_ls_bound_finish(KArgs a, int n_meshes) {
 
 // Pass 1: step bound over the tets and the quality energy at the current X.
 template <typename ET, typename VT>
-__global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
+__global__ void __launch_bounds__(128, sizeof(ET) == 4 ? 4 : 1) k_ls_bound(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
   const int64_t h = sg.begin + threadIdx.x;
   const MeshDesc md = a.mesh[sg.mesh];
@@ -833,8 +867,21 @@ __global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
     uint32_t hv[8];
     load_hex(a.hexv, h, hv);
     const int32_t gs = a.gslot[h];
-    ET E12[12][3], D12[12][3];
+    ET E12[12][3];
     hex_edges_mode<ET>(a, hv, E12);
+    // the energy at the current positions first, then the direction frame and the root screens,
+    // so the two sets of temporaries are never live together
+    SumAcc<ET> efast;
+    double eslow = 0;
+#define HX_LS_E(K)                                                \
+    {                                                             \
+      ET E[3][3];                                                 \
+      tet_E12<K>(E12, E);                                         \
+      tet_energy_acc<ET, VT, K>(a, h, hv, gs, E, 0.0, efast, eslow); \
+    }
+    HX_LS_E(0) HX_LS_E(1) HX_LS_E(2) HX_LS_E(3) HX_LS_E(4) HX_LS_E(5) HX_LS_E(6) HX_LS_E(7)
+#undef HX_LS_E
+    ET D12[12][3];
     {
       VT Dv[12][3];
       hex_edges_vec(reinterpret_cast<const VT *>(a.d), hv, Dv);
@@ -843,18 +890,15 @@ __global__ void __launch_bounds__(128) k_ls_bound(KArgs a) {
 #pragma unroll
         for (int r = 0; r < 3; r++) D12[e][r] = ET(Dv[e][r]);
     }
-    SumAcc<ET> efast;
-    double eslow = 0;
-#define HX_LS(K)                                                  \
+#define HX_LS_B(K)                                                \
     {                                                             \
       ET E[3][3], D[3][3];                                        \
       tet_E12<K>(E12, E);                                         \
       tet_E12<K>(D12, D);                                         \
       if (tet_bound<ET, K>(E, D)) need |= 1u << K;              \
-      tet_energy_acc<ET, VT, K>(a, h, hv, gs, E, 0.0, efast, eslow); \
     }
-    HX_LS(0) HX_LS(1) HX_LS(2) HX_LS(3) HX_LS(4) HX_LS(5) HX_LS(6) HX_LS(7)
-#undef HX_LS
+    HX_LS_B(0) HX_LS_B(1) HX_LS_B(2) HX_LS_B(3) HX_LS_B(4) HX_LS_B(5) HX_LS_B(6) HX_LS_B(7)
+#undef HX_LS_B
     eq[0] = S.M * (efast.value() + eslow);
   }
   {
