@@ -295,6 +295,11 @@ template <> struct SumAcc<float> {
     add(p);
     c = __fadd_rn(c, e);
   }
+  // fold in another accumulator's (sum, carry): TwoSum of the sums, carries added
+  __device__ __forceinline__ void merge(float s2, float c2) {
+    add(s2);
+    c = __fadd_rn(c, c2);
+  }
   __device__ __forceinline__ double value() const { return double(s) + double(c); }
 };
 
@@ -377,6 +382,43 @@ __device__ __forceinline__ bool publish_partials(const double (&v)[NV], double *
   }
   __syncthreads();
   return am_last;
+}
+
+// Block sum of compensated FP32 accumulators: the (sum, carry) pairs are reduced through the
+// warps and the block with FP32 TwoSum merges, and only thread 0 converts the block total to
+// FP64 (out[k] is valid in thread 0).  Vertex kernels do a few FP32 operations per item, so
+// per-thread FP64 shuffles and conversions would keep GB300's slow FP64 pipe busy.
+template <int NV>
+__device__ __forceinline__ void block_sum_acc(SumAcc<float> (&v)[NV], double (&out)[NV], float (*smem)[2][32]) {
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float s2 = __shfl_down_sync(0xffffffffu, v[k].s, o), c2 = __shfl_down_sync(0xffffffffu, v[k].c, o);
+      v[k].merge(s2, c2);
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; k++) { smem[k][0][wid] = v[k].s; smem[k][1][wid] = v[k].c; }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      SumAcc<float> x;
+      x.s = lane < nw ? smem[k][0][lane] : 0.f;
+      x.c = lane < nw ? smem[k][1][lane] : 0.f;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_down_sync(0xffffffffu, x.s, o), c2 = __shfl_down_sync(0xffffffffu, x.c, o);
+        x.merge(s2, c2);
+      }
+      out[k] = x.value();
+    }
+  }
 }
 
 // Fixed-order sum (by the last block) of a mesh's partials, k-th component.

@@ -492,12 +492,18 @@ __global__ void __launch_bounds__(256) k_cg_alpha(KArgs a) {
       }
     } else {
       const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
-      acc[0] += double(pa[it.idx]) * double(qa[it.idx]);
+      if constexpr (sizeof(VT) == 4) pq.add_prod(pa[it.idx], qa[it.idx]);
+      else acc[0] += double(pa[it.idx]) * double(qa[it.idx]);
     }
   }
-  if (sizeof(VT) == 4) acc[0] += pq.value();
   __shared__ double smem[1][32];
-  block_sum<1>(acc, smem);
+  if constexpr (sizeof(VT) == 4) {
+    __shared__ float fsm[1][2][32];
+    SumAcc<float> v[1] = {pq};
+    block_sum_acc<1>(v, acc, fsm);
+  } else {
+    block_sum<1>(acc, smem);
+  }
   if (publish_partials<1>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
     double g[1];
     gather_partials_sums<1>(a.partials, md.vblk0, md.nvblk, 1, g, smem);
@@ -548,16 +554,23 @@ __global__ void __launch_bounds__(256) k_cg_update(KArgs a) {
       da[e] += alpha * pa[e];
       const VT rr = ra[e] - alpha * qa[e];
       ra[e] = rr;
-      acc[0] += double(rr) * double(rr);
-      acc[1] += double(rr) * double(invda[e] * rr);
+      if constexpr (sizeof(VT) == 4) {
+        s_rr.add_prod(rr, rr);
+        s_rz.add_prod(rr, invda[e] * rr);
+      } else {
+        acc[0] += double(rr) * double(rr);
+        acc[1] += double(rr) * double(invda[e] * rr);
+      }
     }
   }
-  if (sizeof(VT) == 4) {
-    acc[0] += s_rr.value();
-    acc[1] += s_rz.value();
-  }
   __shared__ double smem[2][32];
-  block_sum<2>(acc, smem);
+  if constexpr (sizeof(VT) == 4) {
+    __shared__ float fsm[2][2][32];
+    SumAcc<float> v[2] = {s_rr, s_rz};
+    block_sum_acc<2>(v, acc, fsm);
+  } else {
+    block_sum<2>(acc, smem);
+  }
   if (publish_partials<2>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
     double g[2];
     gather_partials_sums<2>(a.partials, md.vblk0, md.nvblk, 2, g, smem);
