@@ -133,6 +133,8 @@ struct hexopt_ctx {
   // batched exact evaluation of the BVH queries (shared by projection and both Hausdorff sides)
   DBuf cand_leaf, cand_qi, cand_x, cand_d, cand_count, q_off, q_cnt, qpos, q_mesh, fb_count, fb_item, fb_mesh;
   int64_t cand_cap = 0;
+  DBuf qseed;           // previous winning leaf per query: projection, Hausdorff side 0, side 1
+  int64_t qseed_n = 0;  // items per region of qseed
   std::vector<int64_t> tgt_vs_cnt, surf_vs_cnt;
   bool haus_ready = false;
   // feature alignment
@@ -508,6 +510,9 @@ int ensure_query_buffers(hexopt_ctx *ctx) {
   CK(ctx->ovf_face.ensure(sizeof(int32_t) * n));
   CK(ctx->ovf_pt.ensure(sizeof(double) * 3 * n));
   CK(ctx->hdist.ensure(sizeof(double) * n));
+  CK(ctx->qseed.ensure(sizeof(int32_t) * 3 * n));
+  CK(cudaMemsetAsync(ctx->qseed.p, 0xFF, sizeof(int32_t) * 3 * n, ctx->st));  // -1: no seed yet
+  ctx->qseed_n = n;
   // up to kQueryCandidates recorded candidates per query on average (a query over its share goes
   // to the exact fallback)
   constexpr int64_t kQueryCandidates = 16;
@@ -568,6 +573,7 @@ ProjArgs make_proj(hexopt_ctx *c, int kind) {
   p.t_ids = c->t_ids.as<int32_t>(); p.t_nrm = c->t_nrm.as<double>(); p.t_dis = c->t_dis.as<double>();
   p.l_ids = c->l_ids.as<int32_t>(); p.l_curve = c->l_curve.as<int32_t>();
   p.l_axis = c->l_axis.as<double>(); p.l_orig = c->l_orig.as<double>();
+  p.seed = c->qseed.as<int32_t>();
   return p;
 }
 
@@ -587,6 +593,7 @@ HausArgs make_haus(hexopt_ctx *c, int kind) {
   h.surf_vs = c->surf_vs_d.as<int64_t>();
   h.partials = c->partials.as<double>();
   h.counters = c->counters.as<unsigned>();
+  h.seed = c->qseed.as<int32_t>() + (kind == K_SURFV ? 2 : 1) * c->qseed_n;
   return h;
 }
 

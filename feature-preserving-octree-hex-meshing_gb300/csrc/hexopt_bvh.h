@@ -91,6 +91,9 @@ struct ProjArgs {
   double *t_nrm, *t_dis;
   const int32_t *l_ids, *l_curve;
   double *l_axis, *l_orig;
+  // per projection item: the leaf that won its previous query (-1: none), whose FP32 upper
+  // bound at the new position seeds the traversal's pruning bound
+  int32_t *seed;
 };
 
 struct HausMesh {
@@ -115,6 +118,7 @@ struct HausArgs {
   const int64_t *surf_vs;   // K_SURFV items: referenced surface vertices (global ids)
   double *partials;
   unsigned *counters;
+  int32_t *seed;            // per sample item of this side: the previous winning leaf (-1: none)
 };
 
 void bvh_morton(const BvhDev &b, const double lo[3], const double hi[3], unsigned long long *keys, cudaStream_t st);

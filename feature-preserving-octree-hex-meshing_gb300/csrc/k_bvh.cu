@@ -594,6 +594,22 @@ __device__ __forceinline__ int warp_excl_scan(int v, int &total) {
   return x - v;
 }
 
+// Pruning bound from the leaf that won this query's previous search: its FP32 upper bound at q.
+// Any leaf's upper bound bounds the minimum, so a seed never changes which leaves can attain the
+// minimum nor their traversal order (hence not the winner); a stale seed only prunes less, and
+// one outside the tree (an earlier target) is ignored.
+template <int MODE>
+__device__ __forceinline__ void seed_bound(const BvhDev &b, const int32_t *seed, int64_t i, const double q[3],
+                                           float &ub) {
+  if (!seed || b.n < 2) return;
+  const int32_t s = seed[i];
+  if (s < 0 || s >= b.n) return;
+  const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
+  float lo, hi;
+  leaf_bounds<MODE>(b.leafd, s, qf, 0.f, lo, hi);
+  ub = fminf(ub, hi);
+}
+
 // Per-thread collection with at most `budget` pops.  Returns 0 when done, 1 on stack overflow
 // (candidates may miss subtrees), 2 when the budget ran out (ub stays a valid bound), 3 when more
 // than kQCand candidates remain after compaction.
@@ -954,6 +970,7 @@ __global__ void __launch_bounds__(128) k_project(ProjArgs p) {
     const TargetDev &t = p.tgt[sg.mesh];
     proj_entry(p, md, i, q);
     int st = 0;
+    seed_bound<0>(t.bvh, p.seed, i, q, ub);
     if (t.bvh.n > 0) st = thread_collect<0>(t.bvh, q, ub, cl, cb, nc, kThreadBudget);
     if (st == 2) {
       p.ovf.best[i] = ub;
@@ -1017,6 +1034,7 @@ __global__ void __launch_bounds__(128) k_project_finish(ProjArgs p) {
   int32_t f = -1;
   double c[3] = {0, 0, 0};
   if (win >= 0) {
+    if (p.seed) p.seed[i] = p.cand.leaf[o + win];
     f = t.bvh.leaf_face[p.cand.leaf[o + win]];
     double P[3][3];
     face_pts(t.bvh, f, P);
@@ -1175,6 +1193,7 @@ __global__ void __launch_bounds__(128) k_haus_side(HausArgs h) {
     const BvhDev *b;
     haus_query<SIDE>(h, i, sg.mesh, q, b);
     ub = dist_bound<1>(h.hm[sg.mesh].diag);
+    seed_bound<1>(*b, h.seed, i, q, ub);
     int st = 0;
     if (b->n > 0) st = thread_collect<1>(*b, q, ub, cl, cb, nc, kThreadBudget);
     if (st == 2) {
@@ -1230,13 +1249,15 @@ __global__ void __launch_bounds__(128) k_haus_finish(HausArgs h) {
   if (cnt < 0) return;
   const int64_t o = h.cand.q_off[i];
   double dist = h.hm[sg.mesh].diag;
+  int wk = -1;
   for (int k = 0; k < cnt; k++) {
     const double d = h.cand.d[o + k];
     if (d > dist || d < -dist) continue;
     const double x = h.cand.x[o + k];
-    if (dist > x) dist = x;
+    if (dist > x) { dist = x; wk = k; }
   }
   h.dist[i] = dist;
+  if (wk >= 0 && h.seed) h.seed[i] = h.cand.leaf[o + wk];
 }
 
 template <int SIDE>

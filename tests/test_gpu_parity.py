@@ -199,6 +199,28 @@ def test_hausdorff_meshes_matches_oracle(ctx, hx, oracle):
     assert abs(mx[0] - ref[1]) <= 1e-5 * ref[0] and abs(av[0] - ref[2]) <= 1e-5 * ref[0]
 
 
+def test_seeded_queries_match_oracle(ctx, hx, oracle):
+    """Projection and Hausdorff queries start their pruning bound from the leaf that won the
+    query's previous search.  After the points move (a little, then far, so seeds go stale), the
+    tangent planes and the two-sided Hausdorff still equal the oracle's exact search."""
+    from hexopt import workloads
+    p = workloads.cylinder()
+    workloads.load(ctx, [p])
+    reg = np.asarray(p["regular"], np.int64)
+    rng = np.random.default_rng(12)
+    for step, amp in enumerate([0.0, 1e-3, 2e-3, 5e-2]):
+        V = p["V"] + amp * rng.standard_normal(p["V"].shape)
+        ctx.set_positions(V)
+        ctx.project_features()
+        nrm, dis = ctx.get_tangents(len(reg))
+        S, I, Cc, N = oracle.signed_distance(p["TV"], p["TF"], V[reg])
+        np.testing.assert_allclose(nrm, N, rtol=0, atol=1e-12, err_msg=f"normals, round {step}")
+        np.testing.assert_allclose(dis, (N * Cc).sum(1), rtol=0, atol=1e-12, err_msg=f"dis, round {step}")
+        dg, mx, av = ctx.hausdorff_meshes()
+        ref = oracle.hausdorff(p["TV"], p["TF"], V, p["surface"])
+        assert abs(mx[0] - ref[1]) <= 1e-9 * ref[0] and abs(av[0] - ref[2]) <= 1e-9 * ref[0], step
+
+
 # ------------------------------------------------------------------ feature alignment
 @pytest.mark.parametrize("graph", [False, True])
 def test_feature_alignment_cylinder_vs_oracle(ctx, hx, graph):
