@@ -1362,7 +1362,7 @@ static int fa_enqueue(hexopt_ctx *ctx, int do_hausdorff) {
   KArgs a = make_args(ctx);
   if (ctx->mixed) {
     launch_sj_check(a, ctx->kind[K_HEX].nblk, ctx->st);
-    ctx->launches += 2;
+    ctx->launches += 3;
   } else {
     launch_scaled_jacobian(a, ctx->kind[K_HEX].nblk, nullptr, ctx->HJs.as<double>(), ctx->st);
     ctx->launches += 3;

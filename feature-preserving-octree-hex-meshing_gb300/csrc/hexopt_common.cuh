@@ -463,8 +463,20 @@ __device__ __forceinline__ void gather_partials_sums(const double *partials, int
 }
 __device__ __forceinline__ double gather_partials_min(const double *partials, int64_t first_blk, int nblk, int NV,
                                                       int k, double (*smem)[32]) {
+  // 16 loads in flight per thread (the minimum does not depend on the order)
+  constexpr int U = 16;
   double x = INFINITY;
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x) x = fmin(x, __ldcg(&partials[(first_blk + b) * NV + k]));
+  const double *base = partials + first_blk * NV + k;
+  const int bd = blockDim.x;
+  int b = threadIdx.x;
+  for (; b + (U - 1) * bd < nblk; b += U * bd) {
+    double t[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) t[u] = __ldcg(base + (int64_t)(b + u * bd) * NV);
+#pragma unroll
+    for (int u = 0; u < U; u++) x = fmin(x, t[u]);
+  }
+  for (; b < nblk; b += bd) x = fmin(x, __ldcg(base + (int64_t)b * NV));
   double v[1] = {x};
   block_min<1>(v, smem);
   return v[0];

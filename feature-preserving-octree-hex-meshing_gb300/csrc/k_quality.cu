@@ -122,7 +122,6 @@ __device__ __forceinline__ void corner_sj_fast(const float E12[12][3], const dou
 __global__ void __launch_bounds__(128) k_sj_fast(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
   const int64_t h = sg.begin + threadIdx.x;
-  const MeshDesc md = a.mesh[sg.mesh];
   double mn[1] = {1.0}, acc[2] = {0, 0};
   if (h < sg.end) {
     uint32_t hv[8];
@@ -145,24 +144,34 @@ __global__ void __launch_bounds__(128) k_sj_fast(KArgs a) {
   block_min<1>(mn, smem);
   double m0 = mn[0];
   block_sum<2>(acc, smem);
-  double out[3] = {m0, acc[0], acc[1]};
-  if (publish_partials<3>(out, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
-    double m = gather_partials_min(a.partials, md.hblk0, md.nhblk, 3, 0, smem);
-    double g[2];  // components 1 and 2 of 3
-    gather_partials_sums<2>(a.partials + 1, md.hblk0, md.nhblk, 3, g, smem);
-    const double s = g[0], c = g[1];
-    if (threadIdx.x == 0) {
-      MeshScalars &S = a.sc[sg.mesh];
-      S.sj_min = fmin(m, 1.0);
-      S.sj_sum = s;
-      S.n_inv = (int64_t)c;
-      a.counters[sg.mesh] = 0;
-    }
+  // plain store of the block's partials: the per-mesh reduction is a separate launch, which
+  // spares each of the many short blocks a fence and an atomic
+  if (threadIdx.x == 0) {
+    a.partials[3 * (int64_t)blockIdx.x] = m0;
+    a.partials[3 * (int64_t)blockIdx.x + 1] = acc[0];
+    a.partials[3 * (int64_t)blockIdx.x + 2] = acc[1];
+  }
+}
+
+// One block of 128 per mesh: fixed-order reduction of the mesh's k_sj_fast partials.
+__global__ void __launch_bounds__(128) k_sj_fast_finish(KArgs a) {
+  const int m = blockIdx.x;
+  const MeshDesc md = a.mesh[m];
+  __shared__ double smem[2][32];
+  const double mn = gather_partials_min(a.partials, md.hblk0, md.nhblk, 3, 0, smem);
+  double g[2];  // components 1 and 2 of 3
+  gather_partials_sums<2>(a.partials + 1, md.hblk0, md.nhblk, 3, g, smem);
+  if (threadIdx.x == 0) {
+    MeshScalars &S = a.sc[m];
+    S.sj_min = fmin(mn, 1.0);
+    S.sj_sum = g[0];
+    S.n_inv = (int64_t)g[1];
   }
 }
 
 void launch_sj_check(const KArgs &a, int64_t hblk, cudaStream_t st) {
   k_sj_fast<<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
+  k_sj_fast_finish<<<(unsigned)a.n_meshes, 128, 0, st>>>(a);
 }
 
 void launch_scaled_jacobian(const KArgs &a, int64_t hblk, double *V_Js, double *H_Js, cudaStream_t st) {

@@ -68,7 +68,7 @@ template <typename ET, typename VT>
 void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st) {
   k_ls_bound<ET, VT><<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
   k_ls_roots<VT><<<152 * 4, 128, 0, st>>>(a);
-  k_ls_bound_finish<<<(a.n_meshes + 127) / 128, 128, 0, st>>>(a, a.n_meshes);
+  k_ls_bound_finish<<<(unsigned)a.n_meshes, 128, 0, st>>>(a, a.n_meshes);
   k_ls_soft<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a, -1);
   const int rounds = (kHalvings + 1 + a.ls_cand - 1) / a.ls_cand;
   for (int r = 0; r < rounds; r++) {

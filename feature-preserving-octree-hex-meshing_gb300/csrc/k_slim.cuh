@@ -856,15 +856,25 @@ __global__ void __launch_bounds__(128) k_ls_roots(KArgs a) {
 }
 
 // max_step = min(1, 0.8 min_root) per mesh; re-arms the minimum and the list for the next call.
-static __global__ void k_ls_bound_finish(KArgs a, int n_meshes) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m == 0) { *a.root_count = 0; *a.ls_active = (unsigned)n_meshes; }
-  if (m >= n_meshes) return;
-  MeshScalars &S = a.sc[m];
-  const double r = __longlong_as_double((long long)a.root_min[m]);
-  S.min_root = r;
-  S.max_step = fmin(1.0, r * 0.8);
-  a.root_min[m] = (unsigned long long)__double_as_longlong(INFINITY);
+// One block of 128 per mesh (after k_ls_roots): the mesh's energy at the current positions from
+// k_ls_bound's partials (fixed order), the step bound from the minimum root, and the line-search
+// state reset.
+static __global__ void __launch_bounds__(128) k_ls_bound_finish(KArgs a, int n_meshes) {
+  const int m = blockIdx.x;
+  const MeshDesc md = a.mesh[m];
+  __shared__ double smem[1][32];
+  double g[1];
+  gather_partials_sums<1>(a.partials, md.hblk0, md.nhblk, 1, g, smem);
+  if (threadIdx.x == 0) {
+    if (m == 0) { *a.root_count = 0; *a.ls_active = (unsigned)n_meshes; }
+    MeshScalars &S = a.sc[m];
+    S.old_eq = g[0];
+    S.ls_done = 0;
+    const double r = __longlong_as_double((long long)a.root_min[m]);
+    S.min_root = r;
+    S.max_step = fmin(1.0, r * 0.8);
+    a.root_min[m] = (unsigned long long)__double_as_longlong(INFINITY);
+  }
 }
 
 
@@ -933,19 +943,9 @@ __global__ void __launch_bounds__(128, sizeof(ET) == 4 ? 4 : 1) k_ls_bound(KArgs
       }
   }
   __shared__ double smem[1][32];
-  double acc[1] = {0};
   block_sum<1>(eq, smem);
-  if (threadIdx.x == 0) acc[0] = eq[0];
-  if (publish_partials<1>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nhblk)) {
-    double g[1];
-    gather_partials_sums<1>(a.partials, md.hblk0, md.nhblk, 1, g, smem);
-    const double e = g[0];
-    if (threadIdx.x == 0) {
-      S.old_eq = e;
-      S.ls_done = 0;
-      a.counters[sg.mesh] = 0;
-    }
-  }
+  // plain store of the block's partial; k_ls_bound_finish reduces them per mesh
+  if (threadIdx.x == 0) a.partials[blockIdx.x] = eq[0];
 }
 
 __device__ __forceinline__ double cand_alpha(const MeshScalars &S, int j) {
