@@ -248,7 +248,7 @@ def run_ours(args):
     e2e_ms = max_over_ranks(tdist, ctx.timer_stop())
     e2e = ws * args.steps / (e2e_ms / 1e3)
     rep_bytes = 128  # per-mesh report read back (hexopt_fa_report)
-    # ---------------- FP64 plain path on the same input (the benchmark spec comparison), same steps
+    # ---------------- FP64 plain path on the same input (the mixed vs FP64 comparison), same steps
     out_extra = {}
     if not args.skip_compare:
         cmp_steps = min(args.steps, 5)
