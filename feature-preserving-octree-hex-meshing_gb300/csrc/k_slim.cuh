@@ -1080,10 +1080,23 @@ __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
     }
   }
   __shared__ double smem[kMaxCand][32];
-  block_sum<kMaxCand>(acc, smem);
+  // reduce only the live candidates (FP64 shuffles are slow on GB300); the sums are the same
+  if (nc == 1) {
+    double a1[1] = {acc[0]};
+    block_sum<1>(a1, smem);
+    acc[0] = a1[0];
+  } else {
+    block_sum<kMaxCand>(acc, smem);
+  }
   if (publish_partials<kMaxCand>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.ncblk)) {
     double es[kMaxCand];
-    gather_partials_sums<kMaxCand>(a.partials, md.cblk0, md.ncblk, kMaxCand, es, smem);
+    if (nc == 1) {
+      double g[1];
+      gather_partials_sums<1>(a.partials, md.cblk0, md.ncblk, kMaxCand, g, smem);
+      es[0] = g[0];
+    } else {
+      gather_partials_sums<kMaxCand>(a.partials, md.cblk0, md.ncblk, kMaxCand, es, smem);
+    }
     if (threadIdx.x == 0) {
       if (round < 0) {
         S.old_es = es[0];
