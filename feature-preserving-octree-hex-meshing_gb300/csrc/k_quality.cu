@@ -153,8 +153,8 @@ __global__ void __launch_bounds__(128) k_sj_fast(KArgs a) {
   }
 }
 
-// One block of 128 per mesh: fixed-order reduction of the mesh's k_sj_fast partials.
-__global__ void __launch_bounds__(128) k_sj_fast_finish(KArgs a) {
+// One block of 512 per mesh: fixed-order reduction of the mesh's k_sj_fast partials.
+__global__ void __launch_bounds__(512) k_sj_fast_finish(KArgs a) {
   const int m = blockIdx.x;
   const MeshDesc md = a.mesh[m];
   __shared__ double smem[2][32];
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(128) k_sj_fast_finish(KArgs a) {
 
 void launch_sj_check(const KArgs &a, int64_t hblk, cudaStream_t st) {
   k_sj_fast<<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
-  k_sj_fast_finish<<<(unsigned)a.n_meshes, 128, 0, st>>>(a);
+  k_sj_fast_finish<<<(unsigned)a.n_meshes, 512, 0, st>>>(a);
 }
 
 void launch_scaled_jacobian(const KArgs &a, int64_t hblk, double *V_Js, double *H_Js, cudaStream_t st) {
