@@ -8,6 +8,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -22,6 +23,10 @@
 using namespace hexopt;
 
 namespace {
+
+// Device allocations made by any context; a captured step graph holds raw buffer addresses, so a
+// graph captured before the count changed is re-captured before its next replay.
+std::atomic<uint64_t> g_device_allocs{0};
 
 // ------------------------------------------------------------------ device buffer
 struct DBuf {
@@ -48,6 +53,7 @@ struct DBuf {
     cudaError_t e = cudaMalloc(&p, n);
     if (e == cudaSuccess) bytes = n;
     else p = nullptr;
+    g_device_allocs.fetch_add(1, std::memory_order_relaxed);
     return e;
   }
   template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
@@ -144,6 +150,10 @@ struct hexopt_ctx {
   cudaGraphExec_t graph_exec = nullptr;
   bool graph_hausdorff = false;
   int64_t graph_launches = 0;
+  // what the captured graph baked in: launch tables, buffer addresses, parameters
+  uint64_t tables_epoch = 0, graph_tables = 0, graph_allocs = 0;
+  hexopt_slim_params graph_params{};
+  double graph_lamda0 = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -211,6 +221,7 @@ int ensure_query_buffers(hexopt_ctx *ctx);
 
 int rebuild_tables(hexopt_ctx *ctx) {
   const int M = ctx->n_meshes;
+  ctx->tables_epoch++;  // grid sizes of a captured graph are stale
   ctx->block[K_CONS] = ctx->block[K_VERT];  // constraint launches use the vertex block size
   std::vector<int64_t> cnt(M), it0(M);
   int64_t off_c = 0, off_t = 0, off_l = 0;
@@ -1348,9 +1359,14 @@ int hexopt_fa_begin(hexopt_ctx *ctx, const hexopt_slim_params *p, double lamda0,
   }
   rc = push_scalars(ctx);
   if (rc) return rc;
-  if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
-  ctx->fa_ready = true;
+  ctx->fa_ready = true;  // a captured step stays valid while nothing it baked in has changed
   return HEXOPT_OK;
+}
+
+static bool same_params(const hexopt_slim_params &a, const hexopt_slim_params &b) {
+  return a.energy == b.energy && a.precision == b.precision && a.weight_opt == b.weight_opt &&
+         a.exp_factor == b.exp_factor && a.cg_max_iter == b.cg_max_iter && a.cg_tol == b.cg_tol &&
+         a.ls_candidates == b.ls_candidates && a.cube == b.cube;
 }
 
 static int fa_enqueue(hexopt_ctx *ctx, int do_hausdorff) {
@@ -1386,7 +1402,10 @@ int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_r
     if (rc) return rc;
   }
   if (ctx->use_graph) {
-    if (ctx->graph_exec && ctx->graph_hausdorff != (do_hausdorff != 0)) {
+    if (ctx->graph_exec &&
+        (ctx->graph_hausdorff != (do_hausdorff != 0) || ctx->graph_tables != ctx->tables_epoch ||
+         ctx->graph_allocs != g_device_allocs.load(std::memory_order_relaxed) || ctx->graph_lamda0 != ctx->lamda0 ||
+         !same_params(ctx->graph_params, ctx->params))) {
       cudaGraphExecDestroy(ctx->graph_exec);
       ctx->graph_exec = nullptr;
     }
@@ -1403,6 +1422,10 @@ int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_r
       CK(cudaGraphInstantiate(&ctx->graph_exec, g, 0));
       cudaGraphDestroy(g);
       ctx->graph_hausdorff = do_hausdorff != 0;
+      ctx->graph_tables = ctx->tables_epoch;
+      ctx->graph_allocs = g_device_allocs.load(std::memory_order_relaxed);
+      ctx->graph_params = ctx->params;
+      ctx->graph_lamda0 = ctx->lamda0;
       ctx->graph_launches = ctx->launches - l0;  // kernels in one replay
       ctx->launches = l0;                        // capture executed nothing
     }

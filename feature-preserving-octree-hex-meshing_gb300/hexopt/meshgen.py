@@ -246,3 +246,109 @@ def grid_boundary_quads(nx: int, ny: int | None = None, nz: int | None = None) -
 def quads_to_tris(Q: np.ndarray) -> np.ndarray:
     """Split boundary quads into (0,1,2), (2,3,0) (grid_hex_meshing.cpp:4290-4313)."""
     return np.concatenate([Q[:, [0, 1, 2]], Q[:, [2, 3, 0]]]).astype(np.int32)
+
+
+def _ogrid_square_minus_disc(n: int, n_r: int, radius: float, center=(0.5, 0.5)):
+    """2-D O-grid of the unit square minus a centred disc: 4n columns around the hole (n per
+    square side, uniform in angle on the circle and in arc length on the square), n_r rings from
+    the circle (ring 0) to the square (ring n_r), each column a straight blend of the two.
+    Vertex (t, j) has id j * 4n + t.  Returns P (4n (n_r+1), 2) and Q (4n n_r, 4), counter-
+    clockwise."""
+    cx, cy = center
+    t = np.arange(4 * n)
+    side, u = t // n, (t % n) / n
+    outer = np.empty((4 * n, 2))
+    outer[side == 0] = np.stack([np.ones((side == 0).sum()), u[side == 0]], 1)
+    outer[side == 1] = np.stack([1 - u[side == 1], np.ones((side == 1).sum())], 1)
+    outer[side == 2] = np.stack([np.zeros((side == 2).sum()), 1 - u[side == 2]], 1)
+    outer[side == 3] = np.stack([u[side == 3], np.zeros((side == 3).sum())], 1)
+    th = -np.pi / 4 + (np.pi / 2) * (t / n)
+    inner = np.stack([cx + radius * np.cos(th), cy + radius * np.sin(th)], 1)
+    w = (np.arange(n_r + 1) / n_r)[:, None, None]
+    P = ((1 - w) * inner[None] + w * outer[None]).reshape(-1, 2)  # ring n_r is the square exactly
+    j, tt = np.meshgrid(np.arange(n_r), t, indexing="ij")
+    j, tt = j.ravel(), tt.ravel()
+    t1 = (tt + 1) % (4 * n)
+    Q = np.stack([j * 4 * n + tt, (j + 1) * 4 * n + tt, (j + 1) * 4 * n + t1, j * 4 * n + t1], 1)
+    e1 = P[Q[:, 1]] - P[Q[:, 0]]
+    e2 = P[Q[:, 3]] - P[Q[:, 0]]
+    cr = e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]
+    Q[cr < 0] = Q[cr < 0][:, [0, 3, 2, 1]]
+    return P, Q.astype(np.int64)
+
+
+def cube_minus_cylinder_hex(n: int = 64, n_r: int = 16, n_z: int = 64, radius: float = 0.25):
+    """Structured multi-block hex mesh of the unit cube minus the centred z-axis through-cylinder
+    of the given radius: the 2-D O-grid of _ogrid_square_minus_disc (4n columns, n_r rings)
+    extruded in n_z layers, 4 n n_r n_z hexes (n = 64, n_r = 16, n_z = 64: 262,144).
+
+    Returns V, H and a dict of vertex sets: 'boundary' (mask), 'corners' (8 ids: square corner
+    columns at z = 0 and 1), 'lines' with 'line_curve' (vertices on the 12 cube edges and the
+    2 hole circles, corners excluded; curve ids follow cube_minus_cylinder_surface's curves)."""
+    P2, Q = _ogrid_square_minus_disc(n, n_r, radius)
+    n2 = len(P2)
+    zs = np.linspace(0.0, 1.0, n_z + 1)
+    V = np.concatenate([np.column_stack([P2, np.full(n2, z)]) for z in zs])
+    H = np.empty((len(Q) * n_z, 8), dtype=np.uint32)
+    for k in range(n_z):
+        blk = slice(k * len(Q), (k + 1) * len(Q))
+        H[blk, :4] = Q + k * n2
+        H[blk, 4:] = Q + (k + 1) * n2
+    T = 4 * n
+
+    def vid(t, j, k):
+        return k * n2 + j * T + (np.asarray(t) % T)
+
+    bmask = np.zeros(len(V), bool)
+    for k in range(n_z + 1):
+        bmask[vid(np.arange(T), 0, k)] = True
+        bmask[vid(np.arange(T), n_r, k)] = True
+    bmask[:n2] = True
+    bmask[n_z * n2:] = True
+    corners = np.array([vid(s * n, n_r, k) for k in (0, n_z) for s in range(4)], np.int64)
+    lines, lcurve = [], []
+    # curves 0-3: vertical cube edges at the square corners s * n
+    for s in range(4):
+        lines.append(vid(s * n, n_r, np.arange(1, n_z)))
+        lcurve.append(np.full(n_z - 1, s))
+    # curves 4-11: horizontal cube edges, side s at z = 0 (4 + s) and z = 1 (8 + s)
+    for zi, k in enumerate((0, n_z)):
+        for s in range(4):
+            lines.append(vid(s * n + np.arange(1, n), n_r, k))
+            lcurve.append(np.full(n - 1, 4 + 4 * zi + s))
+    # curves 12, 13: the hole circles at z = 0 and z = 1 (closed)
+    for zi, k in enumerate((0, n_z)):
+        lines.append(vid(np.arange(T), 0, k))
+        lcurve.append(np.full(T, 12 + zi))
+    return V, H, dict(boundary=bmask, corners=corners, lines=np.concatenate(lines).astype(np.int32),
+                      line_curve=np.concatenate(lcurve).astype(np.int32))
+
+
+def cube_minus_cylinder_surface(n: int = 24, n_r: int = 12, n_z: int = 48, radius: float = 0.25):
+    """Triangulated surface of the unit cube minus the centred z-axis cylinder: the boundary of
+    cube_minus_cylinder_hex(n, n_r, n_z) (24 / 12 / 48: 23,040 triangles), quads split 0-1-2 /
+    2-3-0, vertices compacted.  Returns TV, TF, the 14 feature curves as target-vertex chains
+    (0-3 vertical cube edges, 4-11 horizontal cube edges, 12-13 hole circles), their closed
+    flags, and the 8 cube corners' target-vertex ids."""
+    V, H, sets = cube_minus_cylinder_hex(n, n_r, n_z, radius)
+    F = quads_to_tris(hex_boundary_quads(H))
+    used = np.unique(F)
+    remap = -np.ones(len(V), np.int64)
+    remap[used] = np.arange(len(used))
+    TV = V[used]
+    TF = remap[F].astype(np.int32)
+    n2 = 4 * n * (n_r + 1)
+    T = 4 * n
+
+    def vid(t, j, k):
+        return remap[k * n2 + j * T + (np.asarray(t) % T)]
+
+    curves = [vid(s * n, n_r, np.arange(n_z + 1)) for s in range(4)]
+    for k in (0, n_z):
+        for s in range(4):
+            curves.append(vid(s * n + np.arange(n + 1), n_r, k))
+    for k in (0, n_z):
+        curves.append(vid(np.arange(T), 0, k))
+    closed = [False] * 12 + [True, True]
+    corners = np.array([vid(s * n, n_r, k) for k in (0, n_z) for s in range(4)], np.int64)
+    return TV, TF, [np.asarray(c, np.int32) for c in curves], closed, corners

@@ -11,6 +11,10 @@ optimiser is measured on, and the calls that load them into a Context.
                           [2, 6], 20k-200k triangles); 256 meshes is the ~40M-hex batch.
   adjoint_problem(n)      the differentiation workload: the n^3 grid with 100 x squared
                           closest-point distance of the boundary vertices as corner terms.
+  cube_minus_cylinder()   the mid-size feature workload: the unit cube minus the centred r = 0.25
+                          z-axis through-hole, 262,144 hexes, 12 cube edges + 2 hole circles as
+                          feature curves with the 8 cube corners, uniform +/-0.1h jitter of the
+                          interior vertices, a 23k-triangle target of the same solid.
 """
 from __future__ import annotations
 
@@ -86,10 +90,33 @@ def cylinder(n_core=8, n_ring=6, n_z=16):
                 corners=np.zeros(0, np.int32), surface=boundary_surface(H))
 
 
+def cube_minus_cylinder(n=64, n_r=16, n_z=64, jitter=0.1, seed=0, target=(24, 12, 48)):
+    """The unit cube minus the centred z-axis through-cylinder of radius 0.25 as a structured
+    O-grid hex mesh (4 n n_r n_z hexes; 262,144 at the defaults), interior vertices jittered
+    uniformly in [-jitter h, +jitter h] per coordinate (h = 1/n, seeded).  Feature curves: the 12
+    cube edges and the 2 hole circles of the target (a 23,040-triangle triangulation of the same
+    solid at another resolution); the hex vertices on them are line vertices, the 8 cube corners
+    are corner vertices tied to the target's corners, every other boundary vertex gets a tangent
+    plane."""
+    V, H, sets = meshgen.cube_minus_cylinder_hex(n, n_r, n_z)
+    b = sets["boundary"]
+    V = meshgen.jitter(V, ~b, 1.0 / n, seed, uniform=jitter)
+    TV, TF, curves, closed, tcorners = meshgen.cube_minus_cylinder_surface(*target)
+    special = np.zeros(len(V), bool)
+    special[sets["lines"]] = True
+    special[sets["corners"]] = True
+    regular = np.nonzero(b & ~special)[0].astype(np.int32)
+    return dict(name=f"cube_minus_cylinder_{len(H)}", V=V, H=H, TV=TV, TF=TF, regular=regular,
+                lines=sets["lines"], line_curve=sets["line_curve"], curves=curves, closed=closed,
+                corners=sets["corners"].astype(np.int32), corner_pos=TV[tcorners],
+                surface=boundary_surface(H))
+
+
 def load(ctx, problems, with_surface=True):
     """Upload a batch of problems and their targets / feature sets into ctx."""
     ctx.upload([(p["V"], p["H"]) for p in problems])
-    ctx.set_corners([p["corners"] for p in problems], [p["TV"][:0] if len(p["corners"]) == 0 else None for p in problems])
+    ctx.set_corners([p["corners"] for p in problems],
+                    [p["corner_pos"] if len(p["corners"]) else np.zeros((0, 3)) for p in problems])
     for m, p in enumerate(problems):
         ctx.set_target(m, p["TV"], p["TF"])
     ctx.set_feature_sets([p["regular"] for p in problems], [p["lines"] for p in problems],

@@ -1314,6 +1314,41 @@ void orc_point_line_projection(const double *v1, const double *v2, const double 
   else if (*t > 1.0) memcpy(pv, v2, 24);
 }
 
+/* LINE branch of dirty_graph_projection (grid_hex_meshing.cpp:3963-4025): for each line vertex,
+ * the closest point over the segments of its curve (a closed curve also has the segment from
+ * its last vertex back to the first), the first such segment on ties, and that segment's unit
+ * tangent.  A curve with no segment gives its single vertex and the tangent (1, 0, 0). */
+void orc_curve_targets(int64_t nl, const double *X, const int32_t *lines, const int32_t *line_curve,
+                       const double *TV, const int64_t *curve_ptr, const int32_t *curve_vs,
+                       const uint8_t *closed, double *origin, double *axis) {
+  for (int64_t i = 0; i < nl; i++) {
+    const double *v = X + 3 * (int64_t)lines[i];
+    const int32_t cu = line_curve[i];
+    const int64_t c0 = curve_ptr[cu], size = curve_ptr[cu + 1] - c0;
+    const int64_t len = closed[cu] ? size : size - 1;
+    double best = INFINITY, pv[3] = {0, 0, 0}, tg[3] = {1, 0, 0};
+    for (int64_t j = 0; j < len; j++) {
+      const double *a = TV + 3 * (int64_t)curve_vs[c0 + j];
+      const double *b = TV + 3 * (int64_t)curve_vs[c0 + (j + 1) % size];
+      double pp[3], t, d[3];
+      orc_point_line_projection(a, b, v, pp, &t);
+      sub3(v, pp, d);
+      const double dist = norm3(d);
+      if (dist < best) {
+        double e[3];
+        sub3(b, a, e);
+        const double ln = norm3(e);
+        best = dist;
+        memcpy(pv, pp, 24);
+        for (int k = 0; k < 3; k++) tg[k] = e[k] / ln;
+      }
+    }
+    if (len <= 0 && size > 0) memcpy(pv, TV + 3 * (int64_t)curve_vs[c0], 24);
+    memcpy(origin + 3 * i, pv, 24);
+    memcpy(axis + 3 * i, tg, 24);
+  }
+}
+
 /* ------------------------------------------------------------------ Hausdorff */
 /* vcg edge-plane face data (vcg/complex/algorithms/update/component_ep.h:45-75) */
 typedef struct ep_face { double p[3][3]; double edge[3][3]; double dir[3]; double off; int axis; double darea; } ep_face;

@@ -105,6 +105,14 @@ void orc_signed_distance(const orc_tree *t, int64_t np, const double *P, double 
 void orc_point_line_projection(const double *v1, const double *v2, const double *v, double *pv,
                                double *t);
 
+/* LINE branch of dirty_graph_projection (grid_hex_meshing.cpp:3963-4025): per line vertex
+ * lines[i] of X (nv x 3), the closest point on its curve line_curve[i] (curves as chains of TV
+ * vertices, curve_ptr / curve_vs, closed flags) -> origin (nl x 3) and the segment's unit
+ * tangent -> axis (nl x 3). */
+void orc_curve_targets(int64_t nl, const double *X, const int32_t *lines, const int32_t *line_curve,
+                       const double *TV, const int64_t *curve_ptr, const int32_t *curve_vs,
+                       const uint8_t *closed, double *origin, double *axis);
+
 /* --- Hausdorff (metro_hausdorff.cpp:358-506, vcg sampling.h:224-289, 547-603) --- */
 void orc_hausdorff(int64_t nv0, const double *V0, int64_t nf0, const int32_t *F0,
                    int64_t nv1, const double *V1, int64_t nf1, const int32_t *F1,

@@ -77,6 +77,7 @@ def lib():
         L.orc_tree_free.argtypes = [C.c_void_p]
         L.orc_signed_distance.argtypes = [C.c_void_p, C.c_int64, _d, _d, _i32, _d, _d]
         L.orc_point_line_projection.argtypes = [_d, _d, _d, _d, _d]
+        L.orc_curve_targets.argtypes = [C.c_int64, _d, _i32, _i32, _d, _i64, _i32, _u8, _d, _d]
         L.orc_hausdorff.argtypes = [C.c_int64, _d, C.c_int64, _i32, C.c_int64, _d, C.c_int64, _i32, _d, _d, _d]
         L.orc_point_face_distance.argtypes = [C.c_int64, _d, C.c_int64, _d, C.c_int64, _i32, _d]
         _lib = L
@@ -195,6 +196,23 @@ def point_line_projection(v1, v2, v):
     pv = np.empty(3); t = C.c_double()
     lib().orc_point_line_projection(_p(v1, _d), _p(v2, _d), _p(v, _d), _p(pv, _d), C.byref(t))
     return pv, t.value
+
+
+def curve_targets(X, lines, line_curve, TV, curves, closed):
+    """LINE branch of dirty_graph_projection: (origin, axis) of each line vertex on its curve."""
+    X, TV = _f64(X), _f64(TV)
+    lines = np.ascontiguousarray(lines, dtype=np.int32)
+    line_curve = np.ascontiguousarray(line_curve, dtype=np.int32)
+    ptr = np.ascontiguousarray(np.concatenate([[0], np.cumsum([len(c) for c in curves])]), dtype=np.int64)
+    vs = np.ascontiguousarray(np.concatenate([np.asarray(c, np.int32) for c in curves]) if len(curves)
+                              else np.zeros(1, np.int32), dtype=np.int32)
+    cl = np.ascontiguousarray(np.asarray(closed, np.uint8).reshape(-1) if len(closed) else np.zeros(1, np.uint8))
+    n = len(lines)
+    org = np.zeros((n, 3)); ax = np.zeros((n, 3))
+    if n:
+        lib().orc_curve_targets(n, _p(X, _d), _p(lines, _i32), _p(line_curve, _i32), _p(TV, _d), _p(ptr, _i64),
+                                _p(vs, _i32), _p(cl, _u8), _p(org, _d), _p(ax, _d))
+    return org, ax
 
 
 def hausdorff(V0, F0, V1, F1):

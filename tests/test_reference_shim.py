@@ -17,12 +17,22 @@ import pytest
 
 from conftest import PKG, ROOT
 
-REF = os.environ.get("HEXOPT_REFERENCE_TREE", "/root/reference")
+def _ref_tree():
+    """The reference tree oracle/Makefile reads (its REF: $HEXOPT_REFERENCE_TREE or its default)."""
+    try:
+        r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "print-ref"], capture_output=True,
+                           text=True, timeout=60)
+        return r.stdout.strip()
+    except (OSError, subprocess.SubprocessError):
+        return ""
+
+
+REF = _ref_tree()
 OBJ = os.path.join(ROOT, "oracle", "_ref")
 SHIM = os.path.join(PKG, "shim", "hexopt_reference_shim.cpp")
 CPU_SJ = "_Z15scaled_jacobianR4MeshR12Mesh_Quality"
 
-pytestmark = pytest.mark.skipif(not os.path.isdir(REF) or shutil.which("g++") is None
+pytestmark = pytest.mark.skipif(not REF or not os.path.isdir(REF) or shutil.which("g++") is None
                                 or shutil.which("objcopy") is None,
                                 reason="reference tree or host toolchain absent")
 
