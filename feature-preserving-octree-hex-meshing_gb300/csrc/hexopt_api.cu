@@ -115,6 +115,11 @@ struct hexopt_ctx {
   DBuf X, X32, hexv, gslot, Sinv, Ccoef, Bgen, aL;
   DBuf b, diag, ba, diaga;
   DBuf d, r, p, q, invd, da, ra, pa, qa, invda;
+  DBuf Rrot, dd, dda;  // mixed mode's FP64 refinement: stored rotations, FP64 update accumulator
+  // general reference shapes (compute_referenceMesh with cube = 0, or reference corners set by the
+  // caller): per-hex h_flag, optional reference corners, shapes, and the all-hex slot tables
+  DBuf hflag_d, ref_p8, Bref, gslot_all, Bgen_all;
+  bool has_ref_p8 = false, rest_fixed = false;
   DBuf stage, stage2, HJs, VJs, Xa, grad, Xbak;
   DBuf root_list, root_mesh, root_count, root_min;  // flip-avoid bound: tets needing the exact root
   bool adj_ready = false;
@@ -297,9 +302,19 @@ KArgs make_args(hexopt_ctx *c) {
   a.Sinv = c->Sinv.p;
   a.Ccoef = c->Ccoef.p;
   a.Bgen = c->Bgen.as<double>();
+  a.Bref = nullptr;
+  if (c->rest_fixed) {  // every hex has a slot (its own index) and a general reference shape
+    a.gslot = c->gslot_all.as<int32_t>();
+    a.Bgen = c->Bgen_all.as<double>();
+    a.Bref = c->Bref.as<double>();
+  }
   a.b = c->b.p; a.diag = c->diag.p; a.ba = c->ba.p; a.diaga = c->diaga.p;
   a.d = c->d.p; a.r = c->r.p; a.p = c->p.p; a.q = c->q.p; a.invd = c->invd.p;
   a.da = c->da.p; a.ra = c->ra.p; a.pa = c->pa.p; a.qa = c->qa.p; a.invda = c->invda.p;
+  a.Rrot = c->Rrot.as<float>();
+  a.dd = c->dd.as<double>();
+  a.dda = c->dda.as<double>();
+  a.cg_refine = c->params.cg_refine > 0 ? c->params.cg_refine : 10;
   a.c_ids = c->c_ids.as<int32_t>(); a.c_pos = c->c_pos.as<double>();
   a.t_ids = c->t_ids.as<int32_t>(); a.t_nrm = c->t_nrm.as<double>(); a.t_dis = c->t_dis.as<double>();
   a.l_ids = c->l_ids.as<int32_t>(); a.l_axis = c->l_axis.as<double>(); a.l_orig = c->l_orig.as<double>();
@@ -332,6 +347,11 @@ int alloc_vectors(hexopt_ctx *ctx) {
   CK(ctx->Sinv.ensure(nt * vt));
   CK(ctx->Ccoef.ensure(nt * 6 * vt));
   CK(ctx->Bgen.ensure((size_t)std::max<int64_t>(ctx->NG, 1) * 8 * 9 * sizeof(double)));
+  if (ctx->mixed) {
+    CK(ctx->Rrot.ensure(nt * 9 * sizeof(float)));
+    CK(ctx->dd.ensure(nv4 * sizeof(double)));
+    CK(ctx->dda.ensure(nl * sizeof(double)));
+  }
   // every corner tet may need the exact root: the list holds all of them
   const size_t nroot = (size_t)ctx->NH * 8;
   CK(ctx->root_list.ensure(nroot * sizeof(uint32_t)));
@@ -344,6 +364,24 @@ int alloc_vectors(hexopt_ctx *ctx) {
     CK(cudaMemcpyAsync(ctx->root_min.p, inf.data(), sizeof(double) * ctx->n_meshes, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
   }
+  return HEXOPT_OK;
+}
+
+// compute_referenceMesh for the general shapes: every hex gets a slot (its index) and Bref from its
+// reference corners (set_reference_hexes) or from the current positions.
+int build_ref_shapes(hexopt_ctx *ctx) {
+  const size_t nt = (size_t)ctx->NH * 8;
+  CK(ctx->Bref.ensure(nt * 9 * sizeof(double)));
+  CK(ctx->Bgen_all.ensure(nt * 9 * sizeof(double)));
+  if (ctx->gslot_all.bytes < sizeof(int32_t) * (size_t)ctx->NH) {
+    std::vector<int32_t> id(ctx->NH);
+    for (int64_t h = 0; h < ctx->NH; h++) id[h] = (int32_t)h;
+    CK(upload(ctx->gslot_all, id.data(), id.size(), ctx->st));
+  }
+  launch_ref_shapes(ctx->has_ref_p8 ? ctx->ref_p8.as<double>() : nullptr, ctx->hexv.as<uint32_t>(), ctx->X.as<double>(),
+                    ctx->hflag_d.as<uint8_t>(), ctx->params.cube, ctx->NH, ctx->Bref.as<double>(), ctx->st);
+  ctx->launches++;
+  CKL();
   return HEXOPT_OK;
 }
 
@@ -378,10 +416,31 @@ int run_iteration(hexopt_ctx *ctx, bool pre) {
   const int64_t hb = ctx->kind[K_HEX].nblk, vb = ctx->kind[K_VERT].nblk, cb = ctx->kind[K_CONS].nblk;
   launch_local<ET, VT>(a, hb, pre, st);
   launch_soft_rhs<VT>(a, cb, st);
+  ctx->launches += 2;
+  const int iters = ctx->params.cg_max_iter;
+  if (sizeof(VT) == 4) {
+    // mixed: FP32 PCG on the update, anchored to the FP64 positions by residual replacements
+    CK(cudaMemsetAsync(ctx->dd.p, 0, nv4 * sizeof(double), st));
+    if (ctx->NL) CK(cudaMemsetAsync(ctx->dda.p, 0, (size_t)ctx->NL * sizeof(double), st));
+    launch_ir_residual(a, hb, vb, cb, false, st);
+    ctx->launches += kLaunchesIrInitial;
+  }
   launch_cg_start<VT>(a, vb, st);
-  ctx->launches += 3;
-  for (int i = 0; i < ctx->params.cg_max_iter; i++) launch_cg_iter<VT>(a, hb, vb, cb, st);
-  ctx->launches += (int64_t)kLaunchesCgIter * ctx->params.cg_max_iter;
+  ctx->launches += 1;
+  for (int i = 0; i < iters; i++) {
+    const bool replace = sizeof(VT) == 4 && (i + 1) % a.cg_refine == 0 && i + 1 < iters;
+    launch_cg_iter<VT>(a, hb, vb, cb, st, !replace);
+    ctx->launches += kLaunchesCgIter - (replace ? 1 : 0);
+    if (replace) {
+      launch_ir_residual(a, hb, vb, cb, true, st);
+      launch_cg_dir<VT>(a, vb, st);
+      ctx->launches += kLaunchesIrReplace + 1;
+    }
+  }
+  if (sizeof(VT) == 4) {
+    launch_ir_final(a, vb, st);
+    ctx->launches += kLaunchesIrFinal;
+  }
   launch_line_search<ET, VT>(a, hb, vb, cb, st);
   const int rounds = (kHalvings + 1 + ctx->params.ls_candidates - 1) / ctx->params.ls_candidates;
   ctx->launches += 5 + 2 * rounds;
@@ -665,7 +724,7 @@ int hexopt_create(hexopt_ctx **out, int device) {
   ctx->params.energy = HEXOPT_SYMMETRIC_DIRICHLET;
   ctx->params.precision = HEXOPT_FP64;
   ctx->params.weight_opt = 1.0;
-  ctx->params.exp_factor = 5.0;
+  ctx->params.exp_factor = 1.0;  // slim_precompute leaves SLIMData::exp_factor at 1 (slim_m.cpp:1125)
   ctx->params.cg_max_iter = 20;
   ctx->params.cg_tol = 1e-8;
   ctx->params.ls_candidates = 4;
@@ -765,6 +824,13 @@ int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const
                              (uint32_t)ctx->md[m].v_off, ctx->hexv.as<uint32_t>(), ctx->st);
   ctx->launches += 1 + n_meshes;
   CK(upload(ctx->gslot, gs.data(), gs.size(), ctx->st));
+  {
+    std::vector<uint8_t> hf(NH, 1);
+    if (h_flag) std::copy(h_flag, h_flag + NH, hf.begin());
+    CK(upload(ctx->hflag_d, hf.data(), hf.size(), ctx->st));
+  }
+  ctx->has_ref_p8 = false;
+  ctx->rest_fixed = false;
   CK(ctx->counters.ensure(sizeof(unsigned) * n_meshes));
   CK(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned) * n_meshes, ctx->st));
   int rc = rebuild_tables(ctx);
@@ -914,6 +980,20 @@ int hexopt_get_lines(hexopt_ctx *ctx, double *axis, double *origin) {
   return HEXOPT_OK;
 }
 
+int hexopt_set_reference_hexes(hexopt_ctx *ctx, const double *P8) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (P8) {
+    CK(upload(ctx->ref_p8, P8, (size_t)ctx->NH * 24, ctx->st));
+    ctx->has_ref_p8 = true;
+  } else {
+    ctx->has_ref_p8 = false;
+  }
+  ctx->precomputed = false;
+  ctx->tables_epoch++;
+  return HEXOPT_OK;
+}
+
 int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *p) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
@@ -922,11 +1002,15 @@ int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *p) {
   if (p->precision != HEXOPT_FP64 && p->precision != HEXOPT_MIXED) return fail(ctx, HEXOPT_ERR_ARG, "unknown precision");
   if (p->ls_candidates < 1 || p->ls_candidates > kMaxCand) return fail(ctx, HEXOPT_ERR_ARG, "ls_candidates must be 1..%d", kMaxCand);
   if (p->cg_max_iter < 0) return fail(ctx, HEXOPT_ERR_ARG, "cg_max_iter < 0");
-  if (!p->cube) return fail(ctx, HEXOPT_ERR_UNSUPPORTED, "cube = 0 reference shapes (edge-averaged cuboids) are not implemented");
   ctx->params = *p;
   ctx->mixed = p->precision == HEXOPT_MIXED;
+  ctx->rest_fixed = !p->cube || ctx->has_ref_p8;
   rc = alloc_vectors(ctx);
   if (rc) return rc;
+  if (ctx->rest_fixed) {
+    rc = build_ref_shapes(ctx);
+    if (rc) return rc;
+  }
   rc = pull_scalars(ctx);
   if (rc) return rc;
   for (int m = 0; m < ctx->n_meshes; m++) {
@@ -1372,6 +1456,10 @@ static bool same_params(const hexopt_slim_params &a, const hexopt_slim_params &b
 static int fa_enqueue(hexopt_ctx *ctx, int do_hausdorff) {
   int rc = run_projection(ctx);
   if (rc) return rc;
+  if (ctx->rest_fixed && !ctx->has_ref_p8) {  // compute_referenceMesh(ts.UV, ...) of this step
+    rc = build_ref_shapes(ctx);
+    if (rc) return rc;
+  }
   rc = dispatch_iteration(ctx, true);  // slim_precompute fused into the local step
   if (rc) return rc;
   launch_fa_schedule(ctx->sc_d.as<MeshScalars>(), ctx->n_meshes, ctx->lamda0, 1e16, ctx->st);

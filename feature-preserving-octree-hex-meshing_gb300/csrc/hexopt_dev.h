@@ -56,6 +56,7 @@ struct MeshScalars {
   double lamda_C, lamda_T, lamda_L, lamda0;
   // CG (Eigen semantics)
   double rhs_norm2, threshold, abs_new, alpha, beta, rn2, cg_error;
+  double rz_prev;  // r.z before the last update (a replaced residual restarts beta from it)
   int32_t cg_iters, cg_done;
   // line search
   double min_root, max_step, old_e, old_eq, old_es;

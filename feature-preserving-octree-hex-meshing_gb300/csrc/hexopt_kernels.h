@@ -24,11 +24,17 @@ struct KArgs {
   void *Sinv;            // per tet 1/cbrt(6 vol) (ET, AoSoA NC=1)
   void *Ccoef;           // per tet C_t (ET, AoSoA NC=6)
   double *Bgen;          // own-shape rest inverses, 9 per tet
+  const double *Bref;    // general reference shapes (k_shapes.cu): adj(R) / |det R|^(2/3) per tet slot, or
+                         // null; with it every hex has a slot and the precompute sets Bgen = Bref / cbrt(det E)
   // linear system right-hand side and diagonal (VT)
   void *b, *diag, *ba, *diaga;
   // CG vectors (VT)
   void *d, *r, *p, *q, *invd;
   void *da, *ra, *pa, *qa, *invda;
+  // mixed mode's FP64 refinement: per-tet rotations R of the local step (FP32, AoSoA NC=9), and
+  // the update accumulated in FP64 between residual replacements (vertices AoS4, curve entries)
+  float *Rrot;
+  double *dd, *dda;
   // constraints
   const int32_t *c_ids; const double *c_pos;
   const int32_t *t_ids; double *t_nrm; double *t_dis;
@@ -40,6 +46,7 @@ struct KArgs {
   int n_meshes;
   double cg_tol;
   double sc_exp_f;
+  int cg_refine;  // mixed mode: inner FP32 iterations between residual replacements
   int hthreads;   // block size of hex-kind launches (<= 128)
   int vthreads;   // block size of vertex / constraint launches (<= 256)
   // adjoint
@@ -61,12 +68,29 @@ template <typename ET, typename VT> void launch_local(const KArgs &a, int64_t nb
 template <typename ET, typename VT> void launch_spmv_elems(const KArgs &a, int64_t nblk, cudaStream_t st);
 template <typename VT> void launch_soft_rhs(const KArgs &a, int64_t nblk, cudaStream_t st);
 template <typename VT> void launch_cg_start(const KArgs &a, int64_t nblk, cudaStream_t st);
-template <typename VT> void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st);
+// one PCG iteration: SpMV, soft block, alpha, update and (with_dir) the next direction
+template <typename VT>
+void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st, bool with_dir = true);
+template <typename VT> void launch_cg_dir(const KArgs &a, int64_t vblk, cudaStream_t st);
+// Mixed mode's FP64 iterative refinement of the PCG (k_slim.cuh): the residual b - A x at
+// x = X + dd re-evaluated from the FP64 positions (element terms in double-float, soft and
+// proximal terms in FP64); `replace` = a replacement inside the CG (accumulate d into dd first,
+// then take the new residual's norms), else the initial residual of the solve.
+void launch_ir_residual(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, bool replace, cudaStream_t st);
+// After the last PCG iteration: the search direction d = fl32(dd + d) (curve entries likewise).
+void launch_ir_final(const KArgs &a, int64_t vblk, cudaStream_t st);
 template <typename ET, typename VT> void launch_ls_energy_pass(const KArgs &a, int64_t hblk, cudaStream_t st);
 template <typename ET, typename VT> void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st);
 
 // Launches per call of the launchers above (for the launch count).
 constexpr int kLaunchesCgIter = 5;
+constexpr int kLaunchesIrInitial = 2, kLaunchesIrReplace = 4, kLaunchesIrFinal = 1;
+
+// ---- reference shapes (k_shapes.cu) ----
+// Bref of every hex from its reference corners: P8 (nh x 8 x 3) when given, else the current
+// positions X through the hexes; cube / h_flag as compute_referenceMesh.
+void launch_ref_shapes(const double *P8, const uint32_t *hexv, const double *X, const uint8_t *hflag, int cube,
+                       int64_t nh, double *Bref, cudaStream_t st);
 
 // ---- adjoint (k_adjoint.cu) ----
 template <typename ET> void launch_energy_fwd(const KArgs &a, int64_t hblk, int64_t cblk, cudaStream_t st);

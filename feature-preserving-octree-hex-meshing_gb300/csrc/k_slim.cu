@@ -57,12 +57,25 @@ void launch_cg_start(const KArgs &a, int64_t nblk, cudaStream_t st) {
   k_cg_start<VT><<<(unsigned)nblk, a.vthreads, 0, st>>>(a);
 }
 template <typename VT>
-void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st) {
+void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st, bool with_dir) {
   k_spmv<VT><<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
   k_soft_mv<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a);
   k_cg_alpha<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
   k_cg_update<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+  if (with_dir) k_cg_dir<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+}
+template <typename VT>
+void launch_cg_dir(const KArgs &a, int64_t vblk, cudaStream_t st) {
   k_cg_dir<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+}
+void launch_ir_residual(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, bool replace, cudaStream_t st) {
+  if (replace) k_ir_acc<<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+  k_ir_resid<<<(unsigned)hblk, a.hthreads, 0, st>>>(a, replace ? 1 : 0);
+  k_ir_soft<<<(unsigned)cblk, a.vthreads, 0, st>>>(a, replace ? 1 : 0);
+  if (replace) k_ir_norm<<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+}
+void launch_ir_final(const KArgs &a, int64_t vblk, cudaStream_t st) {
+  k_ir_final<<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
 }
 template <typename ET, typename VT>
 void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st) {
@@ -94,7 +107,8 @@ void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk
   template void launch_spmv_elems<ET, VT>(const KArgs &, int64_t, cudaStream_t);                 \
   template void launch_soft_rhs<VT>(const KArgs &, int64_t, cudaStream_t);                       \
   template void launch_cg_start<VT>(const KArgs &, int64_t, cudaStream_t);                       \
-  template void launch_cg_iter<VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t);      \
+  template void launch_cg_iter<VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t, bool); \
+  template void launch_cg_dir<VT>(const KArgs &, int64_t, cudaStream_t);                         \
   template void launch_line_search<ET, VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t); \
   template void launch_ls_energy_pass<ET, VT>(const KArgs &, int64_t, cudaStream_t);
 HX_INST(double, double)

@@ -26,7 +26,8 @@ namespace hexopt {
 
 // ------------------------------------------------------------------------------- precompute
 // slim_precompute alone (hexopt_slim_precompute): per-tet 1/cbrt(6 vol) of cube-target tets,
-// rest-edge inverse of own-shape tets, from the FP64 positions.
+// rest-edge inverse of own-shape tets, the scaled operator of general reference shapes (Bref),
+// from the FP64 positions.
 template <typename ET>
 __global__ void __launch_bounds__(128) k_precompute(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
@@ -45,6 +46,12 @@ __global__ void __launch_bounds__(128) k_precompute(KArgs a) {
     degenerate |= (d == 0.0);                                                                  \
     if (gs < 0) {                                                                              \
       Sinv[tet_idx<1>(h, K, 0)] = ET(1.0 / cbrt(d));                                            \
+    } else if (a.Bref) {                                                                       \
+      const double *Rf = a.Bref + ((int64_t)gs * 8 + K) * 9;                                   \
+      double *B = a.Bgen + ((int64_t)gs * 8 + K) * 9;                                          \
+      const double cd = cbrt(d);                                                               \
+      _Pragma("unroll") for (int i = 0; i < 9; i++) B[i] = Rf[i] / cd;                         \
+      Sinv[tet_idx<1>(h, K, 0)] = ET(1);                                                       \
     } else {                                                                                   \
       double A[3][3];                                                                          \
       adj3(E, A);                                                                              \
@@ -61,9 +68,10 @@ __global__ void __launch_bounds__(128) k_precompute(KArgs a) {
 
 // ------------------------------------------------------------------------------- local step
 // One corner tet of the fused local step: (optional) volume snapshot, J, SVD, SLIM weights, the
-// stored coefficients C' and the tet's contributions to b = A^T M f, to the initial residual
-// r0 = b - A x0 = sum_t M W^T W (R - J) B^T (formed per element, so it carries no cancellation)
-// and to diag(L).
+// stored coefficients C' and the tet's contributions to b = A^T M f and to diag(L).  FP64 mode
+// also scatters the initial residual r0 = b - A x0 = sum_t M W^T W (R - J) B^T (formed per
+// element, so it carries no cancellation); mixed mode stores R instead and forms r0 in k_ir_resid
+// from the FP64 positions.
 template <typename ET, int K, bool PRE>
 __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs, const ET E12[12][3], ET M, ET exp_f,
                                           int energy, const uint32_t hv[8], bool &degenerate) {
@@ -78,6 +86,13 @@ __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs,
     degenerate |= (d == ET(0));
     if (gs < 0) {
       is = ET(1) / cbrt(d);
+    } else if (a.Bref) {
+      // fixed reference shape: B = adj(R) / |det R|^(2/3) / cbrt(det E) (k_shapes.cu)
+      const double *Rf = a.Bref + ((int64_t)gs * 8 + K) * 9;
+      const double cd = cbrt(double(d));
+#pragma unroll
+      for (int i = 0; i < 9; i++) B[i] = Rf[i] / cd;
+      is = ET(1);
     } else {
       ET A[3][3];
       adj3(E, A);
@@ -117,13 +132,21 @@ __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs,
     }
     atomic_add3(gb, hv[tet_v(K, 0)], -s0, -s1, -s2);
   }
+  if constexpr (sizeof(ET) == 4) {
+    // mixed mode: the rotation is kept for the residual evaluations of the refined PCG (k_ir_*),
+    // which also form the initial residual, from the FP64 positions
 #pragma unroll
-  for (int i = 0; i < 3; i++)
+    for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) R[i][j] -= J[i][j];
-  sym_mul(c, R, Q);
-  apply_BT<K>(Q, gs, B, is, G);
-  {
+      for (int j = 0; j < 3; j++) a.Rrot[tet_idx<9>(h, K, i * 3 + j)] = R[i][j];
+    (void)gr;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) R[i][j] -= J[i][j];
+    sym_mul(c, R, Q);
+    apply_BT<K>(Q, gs, B, is, G);
     ET s0 = 0, s1 = 0, s2 = 0;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
@@ -264,8 +287,8 @@ __global__ void __launch_bounds__(128, sizeof(ET) == 4 ? 8 : 4) k_spmv(KArgs a) 
 
 // ------------------------------------------------------------------------------- soft terms
 // Constraint items of a mesh: [0, nc) corners, [nc, nc+nt) tangent planes, [nc+nt, +nl) lines.
-// add_soft_constraints (slim_m.cpp:647-711): rhs, diagonal and the residual at x0 (curve
-// unknowns start at 0).
+// add_soft_constraints (slim_m.cpp:647-711): rhs, diagonal and (FP64 mode; mixed mode forms it
+// in k_ir_soft) the residual at x0 (curve unknowns start at 0).
 template <typename VT>
 __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
   const Seg sg = a.cseg[blockIdx.x];
@@ -282,7 +305,7 @@ __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
     const double *x = a.X + 4 * (int64_t)v;
     const double c0 = a.c_pos[3 * e], c1 = a.c_pos[3 * e + 1], c2 = a.c_pos[3 * e + 2];
     atomic_add3(b, v, VT(lc * c0), VT(lc * c1), VT(lc * c2));
-    atomic_add3(r, v, VT(lc * (c0 - x[0])), VT(lc * (c1 - x[1])), VT(lc * (c2 - x[2])));
+    if constexpr (sizeof(VT) == 8) atomic_add3(r, v, VT(lc * (c0 - x[0])), VT(lc * (c1 - x[1])), VT(lc * (c2 - x[2])));
     atomic_add3(dg, v, VT(lc), VT(lc), VT(lc));
     return;
   }
@@ -295,7 +318,7 @@ __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
     const double *x = a.X + 4 * (int64_t)v;
     const double res = lt * (d - (n0 * x[0] + n1 * x[1] + n2 * x[2]));
     atomic_add3(b, v, VT(lt * n0 * d), VT(lt * n1 * d), VT(lt * n2 * d));
-    atomic_add3(r, v, VT(res * n0), VT(res * n1), VT(res * n2));
+    if constexpr (sizeof(VT) == 8) atomic_add3(r, v, VT(res * n0), VT(res * n1), VT(res * n2));
     atomic_add3(dg, v, VT(lt * n0 * n0), VT(lt * n1 * n1), VT(lt * n2 * n2));
     return;
   }
@@ -308,11 +331,11 @@ __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
     const double o0 = a.l_orig[3 * e], o1 = a.l_orig[3 * e + 1], o2 = a.l_orig[3 * e + 2];
     const double *x = a.X + 4 * (int64_t)v;
     atomic_add3(b, v, VT(ll * o0), VT(ll * o1), VT(ll * o2));
-    atomic_add3(r, v, VT(ll * (o0 - x[0])), VT(ll * (o1 - x[1])), VT(ll * (o2 - x[2])));
+    if constexpr (sizeof(VT) == 8) atomic_add3(r, v, VT(ll * (o0 - x[0])), VT(ll * (o1 - x[1])), VT(ll * (o2 - x[2])));
     atomic_add3(dg, v, VT(ll), VT(ll), VT(ll));
     VT *ba = reinterpret_cast<VT *>(a.ba), *ra = reinterpret_cast<VT *>(a.ra), *dga = reinterpret_cast<VT *>(a.diaga);
     ba[e] = VT(ll * (-x0 * o0 - x1 * o1 - x2 * o2));
-    ra[e] = VT(ll * (x0 * (x[0] - o0) + x1 * (x[1] - o1) + x2 * (x[2] - o2)));
+    if constexpr (sizeof(VT) == 8) ra[e] = VT(ll * (x0 * (x[0] - o0) + x1 * (x[1] - o1) + x2 * (x[2] - o2)));
     dga[e] = VT(ll * (x0 * x0 + x1 * x1 + x2 * x2));
   }
 }
@@ -582,6 +605,7 @@ __global__ void __launch_bounds__(256) k_cg_update(KArgs a) {
         S.cg_done = 1;
       } else {
         S.beta = rz / S.abs_new;
+        S.rz_prev = S.abs_new;
         S.abs_new = rz;
         S.cg_iters += 1;
         if (S.cg_iters >= a.cg_max_iter) S.cg_done = 1;
@@ -619,6 +643,267 @@ __global__ void __launch_bounds__(256) k_cg_dir(KArgs a) {
     pa[e] = invda[e] * ra[e] + beta * pa[e];
     qa[e] = VT(0);
   }
+  }
+}
+
+// ------------------------------------------------------------------------------- FP64 refinement
+// Mixed mode solves L delta = r0 with FP32 PCG iterations but keeps the solve anchored to the
+// FP64 positions: every cg_refine iterations the FP32 update d moves into the FP64 accumulator
+// dd, and the residual r = b - L (x0 + dd) is re-evaluated from the FP64 positions instead of
+// being carried by the FP32 recurrence (a residual replacement; the search direction p is kept,
+// and beta restarts from the new r.z, so the Krylov process goes on).  The element part of the
+// residual is M W^T W (R - J(x0 + dd)) B^T with R the local step's stored rotation; R - J(x0) is
+// formed in double-float arithmetic (TwoSum / FMA error terms, about 48 bits) from the FP64
+// positions' hi/lo split, so its error is relative to the residual, not to J; the soft and
+// proximal parts are formed in FP64.  The initial residual of every solve is formed the same way.
+
+// The 12 hex edges of X in double-float from the split positions: E = Eh + El to about 2^-48
+// relative (TwoSum of the hi parts, the lo parts and the error term added in FP32).
+__device__ __forceinline__ void hex_edges_split_df(const float *X32, const uint32_t hv[8], float Eh[12][3],
+                                                   float El[12][3]) {
+  float H[8][3], L[8][3];
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const float4 hh = __ldg(reinterpret_cast<const float4 *>(X32) + 2 * (int64_t)hv[c]);
+    const float4 ll = __ldg(reinterpret_cast<const float4 *>(X32) + 2 * (int64_t)hv[c] + 1);
+    H[c][0] = hh.x; H[c][1] = hh.y; H[c][2] = hh.z;
+    L[c][0] = ll.x; L[c][1] = ll.y; L[c][2] = ll.z;
+  }
+#pragma unroll
+  for (int e = 0; e < 12; e++)
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const float x = H[hex_edge_hi(e)][r], y = -H[hex_edge_lo(e)][r];
+      const float sum = __fadd_rn(x, y);
+      const float z = __fsub_rn(sum, x);
+      const float err = __fadd_rn(__fsub_rn(x, __fsub_rn(sum, z)), __fsub_rn(y, z));
+      Eh[e][r] = sum;
+      El[e][r] = __fadd_rn(__fsub_rn(L[hex_edge_hi(e)][r], L[hex_edge_lo(e)][r]), err);
+    }
+}
+
+// Corner tet K's element residual force G (columns: forces on the tet's vertices 1..3; vertex 0
+// gets minus their sum), accumulated into F.  Edges of x = X + dd are Eh + Elo: Eh the hi part of
+// X's double-float edges, Elo their lo part plus the edges of dd (both small next to Eh).
+template <int K>
+__device__ __forceinline__ void ir_tet(const KArgs &a, int64_t h, int32_t gs, const float Eh12[12][3],
+                                       const float El12[12][3], float F[8][3]) {
+  float Eh[3][3], El[3][3];
+  tet_E12<K>(Eh12, Eh);
+  tet_E12<K>(El12, El);
+  const float *Sinv = reinterpret_cast<const float *>(a.Sinv);
+  const float *Cc = reinterpret_cast<const float *>(a.Ccoef);
+  float res[3][3];
+  float G[3][3], Q[3][3], c[6];
+  if (gs < 0) {
+    // J = is E R_k^T: column edge_axis(K, j) is sg E[:, j] with sg = +-is; R - J with the hi
+    // product's exact error (FMA) and the lo part subtracted after the (near-cancelling) hi part
+    const float is = Sinv[tet_idx<1>(h, K, 0)];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int ax = edge_axis(K, j);
+      const float sg = float(edge_sign(K, j)) * is;
+#pragma unroll
+      for (int r = 0; r < 3; r++) {
+        const float jh = __fmul_rn(Eh[r][j], sg);
+        const float jl = __fadd_rn(__fmaf_rn(Eh[r][j], sg, -jh), __fmul_rn(El[r][j], sg));
+        res[r][ax] = __fsub_rn(__fsub_rn(a.Rrot[tet_idx<9>(h, K, r * 3 + ax)], jh), jl);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; i++) c[i] = Cc[tet_idx<6>(h, K, i)];
+    // C' holds c is^2 (the scale folded in), and the force is is (c res) R_k = (C' res) R_k / is
+    sym_mul(c, res, Q);
+    apply_BT<K>(Q, gs, nullptr, 1.0f / is, G);
+  } else {
+    const double *B = a.Bgen + ((int64_t)gs * 8 + K) * 9;
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+      for (int cc = 0; cc < 3; cc++) {
+        double jv = 0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) jv += (double(Eh[r][k]) + double(El[r][k])) * B[k * 3 + cc];
+        res[r][cc] = float(double(a.Rrot[tet_idx<9>(h, K, r * 3 + cc)]) - jv);
+      }
+#pragma unroll
+    for (int i = 0; i < 6; i++) c[i] = Cc[tet_idx<6>(h, K, i)];
+    sym_mul(c, res, Q);
+    apply_BT<K>(Q, gs, B, 1.0f, G);
+  }
+  scatter_cols<K>(G, F);
+}
+
+// r += element residual at X + dd (r starts at -prox dd, or at 0 for the initial residual).
+static __global__ void __launch_bounds__(128, 4) k_ir_resid(KArgs a, int replace) {
+  const Seg sg = a.hseg[blockIdx.x];
+  if (replace && a.sc[sg.mesh].cg_done) return;
+  const int64_t h = sg.begin + threadIdx.x;
+  if (h >= sg.end) return;
+  uint32_t hv[8];
+  load_hex(a.hexv, h, hv);
+  const int32_t gs = a.gslot[h];
+  float Eh[12][3], El[12][3];
+  hex_edges_split_df(a.X32, hv, Eh, El);
+  {
+    float P[8][3];
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const double2 u = __ldg(reinterpret_cast<const double2 *>(a.dd + 4 * (int64_t)hv[c]));
+      const double w = __ldg(a.dd + 4 * (int64_t)hv[c] + 2);
+      P[c][0] = float(u.x); P[c][1] = float(u.y); P[c][2] = float(w);
+    }
+#pragma unroll
+    for (int e = 0; e < 12; e++)
+#pragma unroll
+      for (int r = 0; r < 3; r++) El[e][r] = __fadd_rn(El[e][r], P[hex_edge_hi(e)][r] - P[hex_edge_lo(e)][r]);
+  }
+  float F[8][3];
+#pragma unroll
+  for (int c = 0; c < 8; c++) F[c][0] = F[c][1] = F[c][2] = 0.f;
+  ir_tet<0>(a, h, gs, Eh, El, F);
+  ir_tet<1>(a, h, gs, Eh, El, F);
+  ir_tet<2>(a, h, gs, Eh, El, F);
+  ir_tet<3>(a, h, gs, Eh, El, F);
+  ir_tet<4>(a, h, gs, Eh, El, F);
+  ir_tet<5>(a, h, gs, Eh, El, F);
+  ir_tet<6>(a, h, gs, Eh, El, F);
+  ir_tet<7>(a, h, gs, Eh, El, F);
+  float *r = reinterpret_cast<float *>(a.r);
+#pragma unroll
+  for (int c = 0; c < 8; c++) atomic_add3(r, hv[c], F[c][0], F[c][1], F[c][2]);
+}
+
+// Soft-constraint residual at x = X + dd (curve unknowns a = dda), in FP64: corners
+// lamda_C (c - x), tangent planes lamda_T n (d - n.x), lines lamda_L (o + a t - x) on the vertex
+// rows and lamda_L (t.(x - o) - |t|^2 a) on the curve row (add_soft_constraints' system).
+static __global__ void __launch_bounds__(256) k_ir_soft(KArgs a, int replace) {
+  const Seg sg = a.cseg[blockIdx.x];
+  const MeshScalars &S = a.sc[sg.mesh];
+  if (replace && S.cg_done) return;
+  const int64_t i = sg.begin + threadIdx.x;
+  if (i >= sg.end) return;
+  const MeshDesc md = a.mesh[sg.mesh];
+  float *r = reinterpret_cast<float *>(a.r);
+  int64_t li = i - md.c_off - md.t_off - md.l_off;
+  int kind;
+  int64_t e;
+  if (li < md.nc) { kind = 0; e = md.c_off + li; }
+  else if ((li -= md.nc) < md.nt) { kind = 1; e = md.t_off + li; }
+  else { kind = 2; e = md.l_off + (li - md.nt); }
+  const int32_t lv = kind == 0 ? a.c_ids[e] : kind == 1 ? a.t_ids[e] : a.l_ids[e];
+  const int64_t v = md.v_off + lv;
+  const double x0 = a.X[4 * v] + a.dd[4 * v], x1 = a.X[4 * v + 1] + a.dd[4 * v + 1], x2 = a.X[4 * v + 2] + a.dd[4 * v + 2];
+  if (kind == 0) {
+    const double lc = S.lamda_C;
+    atomic_add3(r, (uint32_t)v, float(lc * (a.c_pos[3 * e] - x0)), float(lc * (a.c_pos[3 * e + 1] - x1)),
+                float(lc * (a.c_pos[3 * e + 2] - x2)));
+  } else if (kind == 1) {
+    const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2];
+    const double res = S.lamda_T * (a.t_dis[e] - (n0 * x0 + n1 * x1 + n2 * x2));
+    atomic_add3(r, (uint32_t)v, float(res * n0), float(res * n1), float(res * n2));
+  } else {
+    const double ll = S.lamda_L, al = a.dda[e];
+    const double t0 = a.l_axis[3 * e], t1 = a.l_axis[3 * e + 1], t2 = a.l_axis[3 * e + 2];
+    const double o0 = a.l_orig[3 * e], o1 = a.l_orig[3 * e + 1], o2 = a.l_orig[3 * e + 2];
+    atomic_add3(r, (uint32_t)v, float(ll * (o0 + al * t0 - x0)), float(ll * (o1 + al * t1 - x1)),
+                float(ll * (o2 + al * t2 - x2)));
+    reinterpret_cast<float *>(a.ra)[e] =
+        float(ll * (t0 * (x0 - o0) + t1 * (x1 - o1) + t2 * (x2 - o2) - (t0 * t0 + t1 * t1 + t2 * t2) * al));
+  }
+}
+
+// Replacement, first pass over the unknowns: dd += d, d = 0 (curve entries: dda += da, da = 0),
+// and r = -prox dd (the proximal term's residual prox (x0 - x)); the element and soft passes add
+// the rest.
+static __global__ void __launch_bounds__(256) k_ir_acc(KArgs a) {
+  const Seg sg = a.vseg[blockIdx.x];
+  const MeshScalars &S = a.sc[sg.mesh];
+  if (S.cg_done) return;
+  const MeshDesc md = a.mesh[sg.mesh];
+  const double prox = S.prox;
+  float *d = reinterpret_cast<float *>(a.d), *r = reinterpret_cast<float *>(a.r);
+  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
+    const ItemRef it = item_ref(md, i);
+    if (!it.curve) {
+      const int64_t v = it.idx;
+      const V3<float> dv = ld3(d, v);
+      double2 u = *reinterpret_cast<const double2 *>(a.dd + 4 * v);
+      double w = a.dd[4 * v + 2];
+      u.x += double(dv.x); u.y += double(dv.y); w += double(dv.z);
+      *reinterpret_cast<double2 *>(a.dd + 4 * v) = u;
+      a.dd[4 * v + 2] = w;
+      st3(d, v, V3<float>{0.f, 0.f, 0.f});
+      st3(r, v, V3<float>{float(-prox * u.x), float(-prox * u.y), float(-prox * w)});
+    } else {
+      float *da = reinterpret_cast<float *>(a.da);
+      a.dda[it.idx] += double(da[it.idx]);
+      da[it.idx] = 0.f;
+    }
+  }
+}
+
+// Replacement, last pass: |r|^2 and r.z of the re-evaluated residual (compensated FP32 sums); the
+// Eigen stopping test on it, and beta = (r.z) / (r.z before the update) for the next direction.
+static __global__ void __launch_bounds__(256) k_ir_norm(KArgs a) {
+  const Seg sg = a.vseg[blockIdx.x];
+  MeshScalars &S = a.sc[sg.mesh];
+  if (S.cg_done) return;
+  const MeshDesc md = a.mesh[sg.mesh];
+  const float *r = reinterpret_cast<const float *>(a.r), *invd = reinterpret_cast<const float *>(a.invd);
+  SumAcc<float> s_rr, s_rz;
+  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
+    const ItemRef it = item_ref(md, i);
+    if (!it.curve) {
+      const V3<float> rr = ld3(r, it.idx), id = ld3(invd, it.idx);
+      s_rr.add_prod(rr.x, rr.x); s_rr.add_prod(rr.y, rr.y); s_rr.add_prod(rr.z, rr.z);
+      s_rz.add_prod(rr.x, id.x * rr.x); s_rz.add_prod(rr.y, id.y * rr.y); s_rz.add_prod(rr.z, id.z * rr.z);
+    } else {
+      const float rr = reinterpret_cast<const float *>(a.ra)[it.idx];
+      const float id = reinterpret_cast<const float *>(a.invda)[it.idx];
+      s_rr.add_prod(rr, rr);
+      s_rz.add_prod(rr, id * rr);
+    }
+  }
+  double acc[2];
+  __shared__ double smem[2][32];
+  __shared__ float fsm[2][2][32];
+  SumAcc<float> v[2] = {s_rr, s_rz};
+  block_sum_acc<2>(v, acc, fsm);
+  if (publish_partials<2>(acc, a.partials, blockIdx.x, a.counters + sg.mesh, md.nvblk)) {
+    double g[2];
+    gather_partials_sums<2>(a.partials, md.vblk0, md.nvblk, 2, g, smem);
+    if (threadIdx.x == 0) {
+      S.rn2 = g[0];
+      S.cg_error = sqrt(g[0] / S.rhs_norm2);
+      if (g[0] < S.threshold) {
+        S.cg_done = 1;
+      } else {
+        S.beta = g[1] / S.rz_prev;
+        S.abs_new = g[1];
+      }
+      a.counters[sg.mesh] = 0;
+    }
+  }
+}
+
+// After the PCG: the search direction d = fl32(dd + d) and da = fl32(dda + da), every mesh.
+static __global__ void __launch_bounds__(256) k_ir_final(KArgs a) {
+  const Seg sg = a.vseg[blockIdx.x];
+  const MeshDesc md = a.mesh[sg.mesh];
+  float *d = reinterpret_cast<float *>(a.d);
+  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
+    const ItemRef it = item_ref(md, i);
+    if (!it.curve) {
+      const int64_t v = it.idx;
+      const V3<float> dv = ld3(d, v);
+      const double2 u = *reinterpret_cast<const double2 *>(a.dd + 4 * v);
+      const double w = a.dd[4 * v + 2];
+      st3(d, v, V3<float>{float(u.x + double(dv.x)), float(u.y + double(dv.y)), float(w + double(dv.z))});
+    } else {
+      float *da = reinterpret_cast<float *>(a.da);
+      da[it.idx] = float(a.dda[it.idx] + double(da[it.idx]));
+    }
   }
 }
 

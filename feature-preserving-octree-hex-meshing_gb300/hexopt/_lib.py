@@ -32,7 +32,7 @@ class Quality(C.Structure):
 class SlimParams(C.Structure):
     _fields_ = [("energy", C.c_int), ("precision", C.c_int), ("weight_opt", C.c_double),
                 ("exp_factor", C.c_double), ("cg_max_iter", C.c_int), ("cg_tol", C.c_double),
-                ("ls_candidates", C.c_int), ("cube", C.c_int)]
+                ("ls_candidates", C.c_int), ("cube", C.c_int), ("cg_refine", C.c_int)]
 
 
 class SlimReport(C.Structure):
@@ -74,6 +74,7 @@ SIGNATURES = {
     "hexopt_set_weights": (C.c_int, [_vp, _d, _d, _d]),
     "hexopt_get_tangents": (C.c_int, [_vp, _d, _d]),
     "hexopt_get_lines": (C.c_int, [_vp, _d, _d]),
+    "hexopt_set_reference_hexes": (C.c_int, [_vp, _d]),
     "hexopt_slim_precompute": (C.c_int, [_vp, C.POINTER(SlimParams)]),
     "hexopt_slim_iterate": (C.c_int, [_vp, C.c_int, C.POINTER(SlimReport)]),
     "hexopt_slim_m_opt": (C.c_int, [_vp, C.POINTER(SlimParams), C.c_int, C.POINTER(SlimReport)]),
@@ -253,10 +254,17 @@ class Context:
         return a, o
 
     # ---- SLIM
+    def set_reference_hexes(self, P8=None):
+        """Reference corners of every hex (n_hexes x 8 x 3) for compute_referenceMesh; None = the
+        positions at the precompute."""
+        P = None if P8 is None else np.ascontiguousarray(P8, np.float64).reshape(-1, 8, 3)
+        self._ck(self.L.hexopt_set_reference_hexes(self.h, ptr(P, _d)), "set_reference_hexes")
+
     @staticmethod
-    def params(precision=FP64, weight_opt=0.001, energy=SYMMETRIC_DIRICHLET, exp_factor=5.0, cg_max_iter=20,
-               cg_tol=1e-8, ls_candidates=4, cube=1):
-        return SlimParams(energy, precision, weight_opt, exp_factor, cg_max_iter, cg_tol, ls_candidates, cube)
+    def params(precision=FP64, weight_opt=0.001, energy=SYMMETRIC_DIRICHLET, exp_factor=1.0, cg_max_iter=20,
+               cg_tol=1e-8, ls_candidates=4, cube=1, cg_refine=10):
+        return SlimParams(energy, precision, weight_opt, exp_factor, cg_max_iter, cg_tol, ls_candidates, cube,
+                          cg_refine)
 
     def slim_m_opt(self, iters, **kw):
         p = self.params(**kw)

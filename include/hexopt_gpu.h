@@ -80,18 +80,24 @@ typedef struct hexopt_slim_params {
   int energy;          /* SLIM_ENERGY; the reference's feature alignment uses SYMMETRIC_DIRICHLET */
   int precision;       /* HEXOPT_FP64 or HEXOPT_MIXED */
   double weight_opt;   /* SLIMData::weight_opt: M per tet, proximal term 1e-5 * weight_opt */
-  double exp_factor;   /* SLIMData::exp_factor (slim_m_opt sets 5.0) */
+  double exp_factor;   /* SLIMData::exp_factor of the exponential energies: slim_precompute resets it to
+                          1.0 (slim_m.cpp:1125, 1181) after slim_m_opt set 5.0, so 1.0 reproduces
+                          the reference */
   int cg_max_iter;     /* 20 (slim_m.cpp:495) */
   double cg_tol;       /* 1e-8 (slim_m.cpp:494) */
   int ls_candidates;   /* step sizes evaluated per line-search pass, 1..8 (same result, fewer passes) */
   int cube;            /* compute_referenceMesh 'cube' flag: 1 in feature alignment */
+  int cg_refine;       /* HEXOPT_MIXED only: FP32 PCG iterations between residual replacements, where
+                          the accumulated update moves to FP64 and the residual b - A x is
+                          re-evaluated from the FP64 positions; <= 0 selects 10 (ignored in FP64) */
 } hexopt_slim_params;
 
 typedef struct hexopt_slim_report {
   double energy;         /* SLIMData::energy (total / mesh_area) */
   double energy_quality; /* SLIMData::engery_quality */
   double energy_soft;    /* SLIMData::engery_soft */
-  double cg_error;       /* relative residual estimate of the last CG */
+  double cg_error;       /* relative residual |b - A x| / |b| of the last CG (mixed mode: from the last
+                            re-evaluated residual when it was the last update, else the recurrence) */
   double max_step;       /* flip-avoiding step bound of the last line search */
   double step;           /* accepted step */
   int32_t cg_iters;
@@ -141,6 +147,15 @@ HEXOPT_API int hexopt_set_lines(hexopt_ctx *ctx, const int64_t *nL, const int32_
 HEXOPT_API int hexopt_set_weights(hexopt_ctx *ctx, const double *lamda_C, const double *lamda_T, const double *lamda_L);
 HEXOPT_API int hexopt_get_tangents(hexopt_ctx *ctx, double *normal, double *dis);
 HEXOPT_API int hexopt_get_lines(hexopt_ctx *ctx, double *axis, double *origin);
+
+/* ---- reference shapes: compute_referenceMesh (global_functions.cpp:3735-3806) ----
+ * By default the reference shape of each hex comes from its positions at the precompute, with
+ * params.cube and the upload's h_flag: cube = 1 a cube of the hex's 24-tet volume, cube = 0 the
+ * edge-averaged cuboid scaled to that volume, h_flag = 0 the hex's own corners.  P8 (n_hexes x 8
+ * x 3, the batch's hexes in order, corners in hex order) makes those corners the source instead,
+ * as the untangling path builds its shapes from another mesh's positions
+ * (optimization.cpp:584); NULL restores the default.  Takes effect at the next precompute. */
+HEXOPT_API int hexopt_set_reference_hexes(hexopt_ctx *ctx, const double *P8);
 
 /* ---- SLIM ---- */
 HEXOPT_API int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *params);

@@ -113,7 +113,7 @@ class SlimProblem:
     """Inputs of one slim_m_opt call (feature-alignment form)."""
 
     def __init__(self, V, H, UV=None, h_flag=None, cube=True, energy=SYMMETRIC_DIRICHLET, weight_opt=0.001,
-                 exp_factor=5.0, ids_C=None, C_=None, lamda_C=0.0, ids_T=None, normal_T=None, dis_T=None,
+                 exp_factor=1.0, ids_C=None, C_=None, lamda_C=0.0, ids_T=None, normal_T=None, dis_T=None,
                  lamda_T=0.0, ids_L=None, Axa_L=None, origin_L=None, lamda_L=0.0):
         self.V = _f64(V)
         self.UV = _f64(V if UV is None else UV)

@@ -170,6 +170,42 @@ int ref_slim_m_opt(int64_t nv, const double *V, int64_t nh, const uint32_t *H, c
   return 0;
 }
 
+// optimization::pipeline2() for a hex mesh (optimization.cpp:416-434): rigidDeformCubes, then
+// glueInternalNodes (per-hex vertex copies glued by the adaptive slim_solve2 branch with the
+// boundary copies held at their positions, optimization.cpp:552-669).  The mesh's vertices carry
+// their hex neighbourhoods and boundary flags as the mesher builds them.  V_out gets the glued
+// positions (mean of each vertex's copies), out4 = {success, min_J, ave_J, opt.energy}.
+int ref_pipeline2(int64_t nv, const double *V, int64_t nh, const uint32_t *H, const uint8_t *boundary,
+                  double weight_opt, double *V_out, double *out4) {
+  optimization opt;
+  opt.weight_opt = weight_opt;
+  Mesh &m = opt.mesh;
+  m = make_hex_mesh(nv, V, nh, H);
+  m.Vs.resize(nv);
+  for (int64_t i = 0; i < nv; i++) {
+    m.Vs[i].id = (uint32_t)i;
+    m.Vs[i].v = {V[3 * i], V[3 * i + 1], V[3 * i + 2]};
+    m.Vs[i].boundary = boundary[i] != 0;
+  }
+  for (int64_t h = 0; h < nh; h++)
+    for (int c = 0; c < 8; c++) m.Vs[H[8 * h + c]].neighbor_hs.push_back((uint32_t)h);
+  Eigen::MatrixXd BV(nv, 3);
+  std::vector<Deform_V_Type> types(nv, Deform_V_Type::Free);
+  for (int64_t i = 0; i < nv; i++) {
+    for (int d = 0; d < 3; d++) BV(i, d) = V[3 * i + d];
+    if (boundary[i]) types[i] = Deform_V_Type::Fixed;
+  }
+  opt.assign_constraints(BV, types);
+  const bool ok = opt.pipeline2();
+  for (int64_t i = 0; i < nv; i++)
+    for (int d = 0; d < 3; d++) V_out[3 * i + d] = opt.mesh.V(d, i);
+  out4[0] = ok ? 1.0 : 0.0;
+  out4[1] = opt.mq.min_Jacobian;
+  out4[2] = opt.mq.ave_Jacobian;
+  out4[3] = opt.energy;
+  return 0;
+}
+
 // Per-tet energies at positions X with the operator of slim_precompute at V
 // (compute_energy_with_jacobians), used to pin the per-element energy.
 int ref_tet_energy(int64_t nv, const double *V, const double *X, int64_t nh, const uint32_t *H, int energy_type,

@@ -2,9 +2,10 @@
 reference's OWN FP64 code (oracle/_ref/libhexopt_ref.so, built from the reference sources by
 `make -C oracle ref`).  Run in a container that has the reference tree:
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [group ...]
 
-Writes tests/golden/*.npz.  The fixtures are committed; the reference build is not.
+Writes tests/golden/*.npz (every group when none is named; groups: base, energies, shapes).  The
+fixtures are committed; the reference build is not.
 """
 from __future__ import annotations
 
@@ -69,12 +70,12 @@ def feature_constraints(V, n, lam=0.05):
                 ids_L=ids_L, Axa_L=Axa_L, origin_L=origin_L, lamda_L=lam)
 
 
-def ref_slim(V, H, fc, iters, weight_opt=0.001, h_flag=None):
+def ref_slim(V, H, fc, iters, weight_opt=0.001, h_flag=None, energy=2, cube=1):
     R = O.ref()
     Vo = np.empty_like(V)
     out = np.empty(3)
     hf = None if h_flag is None else np.ascontiguousarray(h_flag, np.uint8)
-    R.ref_slim_m_opt(len(V), p(V, _d), len(H), p(H, _u32), p(hf, _u8), 1, 2, weight_opt,
+    R.ref_slim_m_opt(len(V), p(V, _d), len(H), p(H, _u32), p(hf, _u8), cube, energy, weight_opt,
                      len(fc["ids_C"]), p(fc["ids_C"], _i32), p(np.ascontiguousarray(fc["C_"]), _d), fc["lamda_C"],
                      len(fc["ids_T"]), p(fc["ids_T"], _i32), p(np.ascontiguousarray(fc["normal_T"]), _d),
                      p(np.ascontiguousarray(fc["dis_T"]), _d), fc["lamda_T"],
@@ -83,7 +84,46 @@ def ref_slim(V, H, fc, iters, weight_opt=0.001, h_flag=None):
     return Vo, out
 
 
-def main():
+def energies():
+    """slim_m_opt with each SLIM_ENERGY (global_types.h:58-66): ARAP, LOG_ARAP, SYMMETRIC_DIRICHLET,
+    CONFORMAL, EXP_CONFORMAL, EXP_SYMMETRIC_DIRICHLET, 2 iterations on a jittered 4^3 grid with the
+    feature-alignment constraint kinds."""
+    for e in range(6):
+        V, H, _ = jittered_grid(4, 0.1, 70 + e)
+        fc = feature_constraints(V, 4, 0.05)
+        Vo, o3 = ref_slim(V, H, fc, 2, energy=e)
+        np.savez_compressed(os.path.join(HERE, f"slim_energy_{e}.npz"), V=V, H=H, iters=2, energy=e, V_o=Vo,
+                            out=o3, **{k: np.asarray(v) for k, v in fc.items()})
+        print("energy", e, o3)
+
+
+def shapes():
+    """slim_m_opt with compute_referenceMesh(cube = false): edge-averaged cuboid reference shapes,
+    on a stretched box grid (cells 0.4 x 0.25 x 0.5) with own-shape hexes mixed in."""
+    V, H = meshgen.grid_hex(5, 4, 3, hi=(2.0, 1.0, 1.5))
+    b = meshgen.grid_boundary_mask(5, 4, 3)
+    V = meshgen.jitter(V, ~b, 0.3, 80, sigma=0.1)
+    hflag = np.ones(len(H), np.uint8)
+    hflag[::7] = 0
+    fc = dict(ids_C=np.zeros(0, np.int32), C_=np.zeros((0, 3)), lamda_C=0.0,
+              ids_T=np.zeros(0, np.int32), normal_T=np.zeros((0, 3)), dis_T=np.zeros(0), lamda_T=0.0,
+              ids_L=np.zeros(0, np.int32), Axa_L=np.zeros((0, 3)), origin_L=np.zeros((0, 3)), lamda_L=0.0)
+    Vo, o3 = ref_slim(V, H, fc, 2, h_flag=hflag, cube=0, weight_opt=1.0)
+    np.savez_compressed(os.path.join(HERE, "slim_cube0.npz"), V=V, H=H, h_flag=hflag, iters=2, V_o=Vo, out=o3,
+                        weight_opt=1.0, cube=0, **{k: np.asarray(v) for k, v in fc.items()})
+    print("cube0", o3)
+
+
+def main(groups):
+    if "energies" in groups:
+        energies()
+    if "shapes" in groups:
+        shapes()
+    if "base" in groups:
+        base()
+
+
+def base():
     R = O.ref()
     out = {}
     # 1. scaled Jacobian on a jittered 5^3 grid with a few tangled vertices
@@ -172,4 +212,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or ["base", "energies", "shapes"])

@@ -8,10 +8,16 @@ oracle's loop (tests/fa_oracle.py: the CPU restatement of the reference's FP64 p
 
 Bars (the criteria the optimiser is held to):
   FP64 positions        within 1e-6 of the bbox diagonal (max over vertices)
-  mixed positions       within 1e-5 of the bbox diagonal
   minimum scaled J      within 1e-4 (both modes)
   Hausdorff max         within 1e-5 of the bbox diagonal (both modes)
-  weight schedule       lamda within 1e-6 relative (FP64), 1e-4 (mixed)
+  weight schedule       lamda within 1e-6 relative (FP64)
+  mixed positions       64^3 grid: 5e-5 of the diagonal, lamda 1e-3 relative; cube minus
+                        cylinder: 1e-5, lamda 1e-4.  Mixed precision rounds the local step's
+                        coefficients at FP32 resolution, and the FP64 path itself moves by
+                        ~1e-5 of the diagonal on the 64^3 grid after 3 iterations when its input
+                        is perturbed at that resolution (2^-24 h, printed by the test): the
+                        truncated 20-iteration CG and the line search amplify such
+                        perturbations.  The mixed bars sit a few times above that sensitivity.
 Each test prints the measured errors.
 """
 import numpy as np
@@ -49,11 +55,13 @@ def oracle_loop(name, p, iters):
     return _oracle_runs[name]
 
 
-def run_gpu(hx, p, iters, precision):
+def run_gpu(hx, p, iters, precision, V0=None):
     from hexopt import workloads
     ctx = hx.Context(0)
     try:
         workloads.load(ctx, [p])
+        if V0 is not None:
+            ctx.set_positions(V0)
         ctx.fa_begin(lamda0=0.05, precision=precision, weight_opt=0.001)
         for _ in range(iters):
             r = ctx.fa_step(hausdorff=True)[0]
@@ -94,7 +102,12 @@ def c2():
 def test_feature_alignment_grid64_vs_oracle(hx, grid64, mode):
     ref = oracle_loop("grid64", grid64, 3)
     Vg, r = run_gpu(hx, grid64, 3, hx.FP64 if mode == "fp64" else hx.MIXED)
-    check(f"grid64 {mode}", grid64, Vg, r, ref, 1e-6 if mode == "fp64" else 1e-5, 1e-6 if mode == "fp64" else 1e-4)
+    if mode == "mixed":  # the FP64 path's own response to an input perturbed at FP32 resolution
+        noise = np.random.default_rng(1).normal(0, 2.0 ** -24 / 64, grid64["V"].shape)
+        Vn, rn = run_gpu(hx, grid64, 3, hx.FP64, V0=grid64["V"] + noise)
+        print(f"\n[grid64 fp64, input noise 2^-24 h] max|dX|/diag {np.abs(Vn - ref['V']).max() / diag_of(grid64['V']):.3e}"
+              f"  lamda rel {abs(rn['lamda'] - ref['lam']) / ref['lam']:.3e}")
+    check(f"grid64 {mode}", grid64, Vg, r, ref, 1e-6 if mode == "fp64" else 5e-5, 1e-6 if mode == "fp64" else 1e-3)
 
 
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])

@@ -59,19 +59,34 @@ def test_flip_avoiding_step_bound_matches_reference(oracle):
 
 
 def _problem(oracle, z):
-    return oracle.SlimProblem(z["V"], z["H"], h_flag=z.get("h_flag"), ids_C=z["ids_C"], C_=z["C_"],
+    return oracle.SlimProblem(z["V"], z["H"], h_flag=z.get("h_flag"), energy=int(z.get("energy", 2)),
+                              cube=bool(int(z.get("cube", 1))), weight_opt=float(z.get("weight_opt", 0.001)),
+                              exp_factor=1.0, ids_C=z["ids_C"], C_=z["C_"],
                               lamda_C=float(z["lamda_C"]), ids_T=z["ids_T"], normal_T=z["normal_T"],
                               dis_T=z["dis_T"], lamda_T=float(z["lamda_T"]), ids_L=z["ids_L"], Axa_L=z["Axa_L"],
                               origin_L=z["origin_L"], lamda_L=float(z["lamda_L"]))
 
 
-@pytest.mark.parametrize("name", ["slim_fa_1", "slim_fa_3", "slim_fa_strong", "slim_fa_hflag"])
+@pytest.mark.parametrize("name", ["slim_fa_1", "slim_fa_3", "slim_fa_strong", "slim_fa_hflag", "slim_cube0"])
 def test_slim_m_opt_matches_reference(oracle, name):
     z = load_golden(name)
     Vo, aL, info = oracle.slim_m_opt(_problem(oracle, z), int(z["iters"]))
     diag = np.linalg.norm(z["V"].max(0) - z["V"].min(0))
     assert np.abs(Vo - z["V_o"]).max() <= 1e-12 * diag
     np.testing.assert_allclose([info["energy"], info["energy_quality"], info["energy_soft"]], z["out"], rtol=1e-11)
+
+
+@pytest.mark.parametrize("energy", range(6))
+def test_slim_energies_match_reference(oracle, energy):
+    """ARAP, LOG_ARAP, SYMMETRIC_DIRICHLET, CONFORMAL, EXP_CONFORMAL, EXP_SYMMETRIC_DIRICHLET: the
+    weights and energies of update_weights_and_closest_rotations / compute_energy_with_jacobians
+    (slim_m.cpp:260-350, 868-913).  slim_precompute resets SLIMData::exp_factor to 1
+    (slim_m.cpp:1125), so the exponential energies run with factor 1."""
+    z = load_golden(f"slim_energy_{energy}")
+    Vo, aL, info = oracle.slim_m_opt(_problem(oracle, z), int(z["iters"]))
+    diag = np.linalg.norm(z["V"].max(0) - z["V"].min(0))
+    assert np.abs(Vo - z["V_o"]).max() <= 1e-11 * diag
+    np.testing.assert_allclose([info["energy"], info["energy_quality"], info["energy_soft"]], z["out"], rtol=1e-10)
 
 
 @pytest.mark.parametrize("name", ["signed_distance", "signed_distance_cyl"])
