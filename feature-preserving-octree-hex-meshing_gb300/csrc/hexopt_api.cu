@@ -127,6 +127,13 @@ struct hexopt_ctx {
   DBuf c_ids, c_pos, t_ids, t_nrm, t_dis, l_ids, l_axis, l_orig, l_curve;
   std::vector<int64_t> nC, nT, nL;
   std::vector<double> lamC, lamT, lamL;
+  // untangling / glue path: projection points, glue groups, held vertices
+  std::vector<int64_t> nB, nG;
+  int64_t NB = 0, NGR = 0;
+  DBuf b_ids, b_pos, g_ptr, g_vs, vfix, Xm;
+  std::vector<uint8_t> fixed_h;  // host copy of the held-vertex flags (for argument checks)
+  std::vector<uint32_t> H_h;     // host copy of the hexes (mesh-local corner ids), for untangling
+  bool has_fixed = false, has_glue = false;
   KindTable kind[8];
   // items per block: hex 128, unknowns 256 x ipt, constraints 256, queries 128
   int block[8] = {128, 256, 256, 128, 128, 128, 128, 128};  // K_CONS follows K_VERT's size
@@ -229,13 +236,15 @@ int rebuild_tables(hexopt_ctx *ctx) {
   ctx->tables_epoch++;  // grid sizes of a captured graph are stale
   ctx->block[K_CONS] = ctx->block[K_VERT];  // constraint launches use the vertex block size
   std::vector<int64_t> cnt(M), it0(M);
-  int64_t off_c = 0, off_t = 0, off_l = 0;
+  int64_t off_c = 0, off_t = 0, off_l = 0, off_b = 0, off_g = 0;
   for (int m = 0; m < M; m++) {
     MeshDesc &d = ctx->md[m];
     d.c_off = off_c; d.nc = ctx->nC[m];
     d.t_off = off_t; d.nt = ctx->nT[m];
     d.l_off = off_l; d.nl = ctx->nL[m];
-    off_c += d.nc; off_t += d.nt; off_l += d.nl;
+    d.b_off = off_b; d.nb = ctx->nB[m];
+    d.grp_off = off_g; d.ngrp = ctx->nG[m];
+    off_c += d.nc; off_t += d.nt; off_l += d.nl; off_b += d.nb; off_g += d.ngrp;
   }
   ctx->NC = off_c; ctx->NT = off_t; ctx->NL = off_l;
   for (int m = 0; m < M; m++) { cnt[m] = ctx->md[m].nh; it0[m] = ctx->md[m].h_off; }
@@ -243,8 +252,9 @@ int rebuild_tables(hexopt_ctx *ctx) {
   for (int m = 0; m < M; m++) { cnt[m] = ctx->md[m].nv + ctx->md[m].nl; it0[m] = ctx->md[m].v_off + ctx->md[m].l_off; }
   build_kind(ctx, K_VERT, cnt, it0);
   for (int m = 0; m < M; m++) {
-    cnt[m] = ctx->md[m].nc + ctx->md[m].nt + ctx->md[m].nl;
-    it0[m] = ctx->md[m].c_off + ctx->md[m].t_off + ctx->md[m].l_off;
+    const MeshDesc &d = ctx->md[m];
+    cnt[m] = d.nc + d.nt + d.nl + d.nb + d.ngrp;
+    it0[m] = d.c_off + d.t_off + d.l_off + d.b_off + d.grp_off;
   }
   build_kind(ctx, K_CONS, cnt, it0);
   for (int m = 0; m < M; m++) { cnt[m] = ctx->md[m].nt; it0[m] = ctx->md[m].t_off; }
@@ -318,6 +328,10 @@ KArgs make_args(hexopt_ctx *c) {
   a.c_ids = c->c_ids.as<int32_t>(); a.c_pos = c->c_pos.as<double>();
   a.t_ids = c->t_ids.as<int32_t>(); a.t_nrm = c->t_nrm.as<double>(); a.t_dis = c->t_dis.as<double>();
   a.l_ids = c->l_ids.as<int32_t>(); a.l_axis = c->l_axis.as<double>(); a.l_orig = c->l_orig.as<double>();
+  a.b_ids = c->b_ids.as<int32_t>(); a.b_pos = c->b_pos.as<double>();
+  a.g_ptr = c->g_ptr.as<int64_t>(); a.g_vs = c->g_vs.as<int32_t>();
+  a.vfix = c->vfix.as<uint8_t>();
+  a.has_fixed = c->has_fixed ? 1 : 0;
   a.energy = c->params.energy;
   a.cg_max_iter = c->params.cg_max_iter;
   a.ls_cand = c->params.ls_candidates;
@@ -417,6 +431,10 @@ int run_iteration(hexopt_ctx *ctx, bool pre) {
   launch_local<ET, VT>(a, hb, pre, st);
   launch_soft_rhs<VT>(a, cb, st);
   ctx->launches += 2;
+  if (ctx->has_fixed) {  // q = L_ib x_b for the known-value solve's rhs norm
+    launch_fixed_pre<VT>(a, hb, vb, st);
+    ctx->launches += 2;
+  }
   const int iters = ctx->params.cg_max_iter;
   if (sizeof(VT) == 4) {
     // mixed: FP32 PCG on the update, anchored to the FP64 positions by residual replacements
@@ -785,6 +803,10 @@ int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const
   ctx->md.assign(n_meshes, MeshDesc{});
   ctx->sc.assign(n_meshes, MeshScalars{});
   ctx->nC.assign(n_meshes, 0); ctx->nT.assign(n_meshes, 0); ctx->nL.assign(n_meshes, 0);
+  ctx->nB.assign(n_meshes, 0); ctx->nG.assign(n_meshes, 0);
+  ctx->NB = ctx->NGR = 0;
+  ctx->fixed_h.assign(NV, 0);
+  ctx->has_fixed = ctx->has_glue = false;
   ctx->lamC.assign(n_meshes, 0); ctx->lamT.assign(n_meshes, 0); ctx->lamL.assign(n_meshes, 0);
   ctx->tgt.clear(); ctx->tgt.resize(n_meshes);
   ctx->surf.clear(); ctx->surf.resize(n_meshes);
@@ -816,6 +838,7 @@ int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const
   ctx->launches += 1;
   // hexes -> AoSoA with global ids
   const int64_t NHp = (NH + 31) / 32 * 32;
+  ctx->H_h.assign(H, H + (size_t)NH * 8);
   CK(upload(ctx->stage2, H, (size_t)NH * 8, ctx->st));
   CK(ctx->hexv.ensure(sizeof(uint32_t) * 8 * NHp));
   CK(cudaMemsetAsync(ctx->hexv.p, 0, sizeof(uint32_t) * 8 * NHp, ctx->st));
@@ -945,6 +968,95 @@ int hexopt_set_lines(hexopt_ctx *ctx, const int64_t *nL, const int32_t *ids, con
   return rebuild_tables(ctx);
 }
 
+int hexopt_set_projection(hexopt_ctx *ctx, const int64_t *nB, const int32_t *ids, const double *bc,
+                          const double *lamda_projection) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!nB) return fail(ctx, HEXOPT_ERR_ARG, "set_projection: NULL counts");
+  rc = set_list(ctx, nB, ctx->nB, ids, ctx->b_ids, "set_projection");
+  if (rc) return rc;
+  int64_t tot = 0;
+  for (int m = 0; m < ctx->n_meshes; m++) tot += nB[m];
+  CK(upload(ctx->b_pos, bc, (size_t)tot * 3, ctx->st));
+  ctx->NB = tot;
+  if (lamda_projection) {
+    rc = pull_scalars(ctx);
+    if (rc) return rc;
+    for (int m = 0; m < ctx->n_meshes; m++) ctx->sc[m].lamda_P = lamda_projection[m];
+    rc = push_scalars(ctx);
+    if (rc) return rc;
+  }
+  return rebuild_tables(ctx);
+}
+
+int hexopt_set_glue(hexopt_ctx *ctx, const int64_t *n_groups, const int64_t *group_ptr, const int32_t *group_vs,
+                    const double *lamda_glue) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!n_groups) return fail(ctx, HEXOPT_ERR_ARG, "set_glue: NULL counts");
+  std::vector<int64_t> gp(1, 0);
+  std::vector<int32_t> gv;
+  int64_t po = 0, vo = 0;
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    if (n_groups[m] < 0) return fail(ctx, HEXOPT_ERR_ARG, "set_glue: negative group count");
+    if (n_groups[m] > 0 && ctx->nL[m] > 0)
+      return fail(ctx, HEXOPT_ERR_UNSUPPORTED, "mesh %d: glue groups replace the feature terms; clear its feature lines first", m);
+    if (n_groups[m] > 0 && (!group_ptr || !group_vs)) return fail(ctx, HEXOPT_ERR_ARG, "set_glue: NULL groups");
+    const int64_t *pm = group_ptr + po + m;  // n_groups[m] + 1 entries per mesh
+    std::vector<uint8_t> seen(ctx->md[m].nv, 0);
+    for (int64_t g = 0; g < n_groups[m]; g++) {
+      if (pm[g + 1] <= pm[g]) return fail(ctx, HEXOPT_ERR_ARG, "mesh %d: empty or unordered glue group %lld", m, (long long)g);
+      for (int64_t k = pm[g]; k < pm[g + 1]; k++) {
+        const int32_t v = group_vs[vo + (k - pm[0])];
+        if (v < 0 || v >= ctx->md[m].nv) return fail(ctx, HEXOPT_ERR_ARG, "mesh %d: glue vertex id out of range", m);
+        if (seen[v]++) return fail(ctx, HEXOPT_ERR_ARG, "mesh %d: vertex %d in two glue groups", m, v);
+        gv.push_back((int32_t)(ctx->md[m].v_off + v));
+      }
+      gp.push_back((int64_t)gv.size());
+    }
+    po += n_groups[m];
+    vo += n_groups[m] > 0 ? pm[n_groups[m]] - pm[0] : 0;
+  }
+  ctx->nG.assign(n_groups, n_groups + ctx->n_meshes);
+  ctx->NGR = (int64_t)gp.size() - 1;
+  ctx->has_glue = ctx->NGR > 0;
+  CK(upload(ctx->g_ptr, gp.data(), gp.size(), ctx->st));
+  CK(upload(ctx->g_vs, gv.data(), std::max<size_t>(gv.size(), 1), ctx->st));
+  rc = pull_scalars(ctx);
+  if (rc) return rc;
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    ctx->sc[m].glue = n_groups[m] > 0 ? 1 : 0;
+    if (lamda_glue) ctx->sc[m].lamda_G = lamda_glue[m];
+  }
+  rc = push_scalars(ctx);
+  if (rc) return rc;
+  ctx->precomputed = false;
+  return rebuild_tables(ctx);
+}
+
+int hexopt_set_fixed(hexopt_ctx *ctx, const int64_t *nF, const int32_t *ids) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!nF) return fail(ctx, HEXOPT_ERR_ARG, "set_fixed: NULL counts");
+  std::fill(ctx->fixed_h.begin(), ctx->fixed_h.end(), 0);
+  int64_t tot = 0;
+  for (int m = 0; m < ctx->n_meshes; m++) {
+    if (nF[m] < 0) return fail(ctx, HEXOPT_ERR_ARG, "set_fixed: negative count");
+    for (int64_t i = 0; i < nF[m]; i++) {
+      const int32_t v = ids[tot + i];
+      if (v < 0 || v >= ctx->md[m].nv) return fail(ctx, HEXOPT_ERR_ARG, "set_fixed: vertex id out of range");
+      ctx->fixed_h[ctx->md[m].v_off + v] = 1;
+    }
+    tot += nF[m];
+  }
+  ctx->has_fixed = tot > 0;
+  CK(upload(ctx->vfix, ctx->fixed_h.data(), ctx->fixed_h.size(), ctx->st));
+  ctx->precomputed = false;
+  ctx->tables_epoch++;
+  CK(cudaStreamSynchronize(ctx->st));
+  return HEXOPT_OK;
+}
+
 int hexopt_set_weights(hexopt_ctx *ctx, const double *lC, const double *lT, const double *lL) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
@@ -1002,6 +1114,8 @@ int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *p) {
   if (p->precision != HEXOPT_FP64 && p->precision != HEXOPT_MIXED) return fail(ctx, HEXOPT_ERR_ARG, "unknown precision");
   if (p->ls_candidates < 1 || p->ls_candidates > kMaxCand) return fail(ctx, HEXOPT_ERR_ARG, "ls_candidates must be 1..%d", kMaxCand);
   if (p->cg_max_iter < 0) return fail(ctx, HEXOPT_ERR_ARG, "cg_max_iter < 0");
+  if (p->precision == HEXOPT_MIXED && (ctx->has_glue || ctx->has_fixed))
+    return fail(ctx, HEXOPT_ERR_UNSUPPORTED, "glue groups and held vertices run in HEXOPT_FP64 only");
   ctx->params = *p;
   ctx->mixed = p->precision == HEXOPT_MIXED;
   ctx->rest_fixed = !p->cube || ctx->has_ref_p8;
@@ -1019,6 +1133,7 @@ int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *p) {
     S.prox = 0.00001 * p->weight_opt;  // slim_m.cpp:1118
     S.exp_f = p->exp_factor;
     S.status = 0;
+    S.frozen = 0;
   }
   rc = push_scalars(ctx);
   if (rc) return rc;
@@ -1549,6 +1664,194 @@ int hexopt_use_graph(hexopt_ctx *ctx, int on) {
     cudaGraphExecDestroy(ctx->graph_exec);
     ctx->graph_exec = nullptr;
   }
+  return HEXOPT_OK;
+}
+
+// ---------------------------------------------------------------- adaptive loop / untangling
+int hexopt_slim_solve_adaptive(hexopt_ctx *ctx, int type, int schedule, int max_iter, hexopt_adaptive_report *rep) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!ctx->precomputed) return fail(ctx, HEXOPT_ERR_STATE, "slim_solve_adaptive before slim_precompute");
+  if (type != 0 && type != 1) return fail(ctx, HEXOPT_ERR_ARG, "slim_solve_adaptive: type must be 0 (projection) or 1 (gluing)");
+  if (schedule != 1 && schedule != 2) return fail(ctx, HEXOPT_ERR_ARG, "slim_solve_adaptive: schedule must be 1 or 2");
+  if (max_iter < 1) return fail(ctx, HEXOPT_ERR_ARG, "slim_solve_adaptive: max_iter < 1");
+  const int M = ctx->n_meshes;
+  rc = pull_scalars(ctx);
+  if (rc) return rc;
+  for (int m = 0; m < M; m++) {
+    ctx->sc[m].frozen = 0;
+    if (schedule == 2) ctx->sc[m].lamda_G = 1e4;  // LAMDA_GLUE_MIN_BOUND (slim_m.cpp:1197)
+  }
+  rc = push_scalars(ctx);
+  if (rc) return rc;
+  CK(ctx->Xm.ensure(sizeof(double) * 4 * ctx->NV));
+  std::vector<hexopt_adaptive_report> out(M);
+  std::vector<char> done(M, 0);
+  for (int m = 0; m < M; m++) { std::memset(&out[m], 0, sizeof out[m]); }
+  for (int it = 0; it < max_iter; it++) {
+    if (schedule == 1) {
+      launch_glue_schedule(ctx->sc_d.as<MeshScalars>(), M, 1, it, ctx->st);
+      ctx->launches++;
+    }
+    rc = dispatch_iteration(ctx);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->Xm.p, ctx->X.p, sizeof(double) * 4 * ctx->NV, cudaMemcpyDeviceToDevice, ctx->st));
+    KArgs a = make_args(ctx);
+    launch_result_positions(a, ctx->kind[K_CONS].nblk, ctx->Xm.as<double>(), type, ctx->st);
+    if (schedule == 2 && type == 1) launch_glue_schedule(ctx->sc_d.as<MeshScalars>(), M, 0, it, ctx->st);
+    a.X = ctx->Xm.as<double>();  // scaled_jacobian of the result mesh (data.ts.m)
+    launch_scaled_jacobian(a, ctx->kind[K_HEX].nblk, nullptr, ctx->HJs.as<double>(), ctx->st);
+    ctx->launches += 4;
+    CKL();
+    rc = pull_scalars(ctx);
+    if (rc) return rc;
+    bool all = true, changed = false;
+    for (int m = 0; m < M; m++) {
+      if (done[m]) continue;
+      const MeshScalars &S = ctx->sc[m];
+      hexopt_adaptive_report &r = out[m];
+      r.iterations = it + 1;
+      r.min_Jacobian = S.sj_min;
+      r.ave_Jacobian = S.sj_sum / (double)ctx->md[m].nh;
+      r.energy = S.energy / (S.M * 8.0 * (double)ctx->md[m].nh);
+      r.energy_quality = S.eq;
+      r.energy_soft = S.es;
+      r.lamda_glue = S.lamda_G;
+      r.status = S.status;
+      if (S.sj_min > 0) {  // the result mesh is untangled: this mesh stops here
+        r.converged = 1;
+        done[m] = 1;
+        ctx->sc[m].frozen = 1;
+        changed = true;
+      } else {
+        all = false;
+      }
+    }
+    if (all) break;
+    if (changed) {
+      rc = push_scalars(ctx);
+      if (rc) return rc;
+    }
+  }
+  if (rep)
+    for (int m = 0; m < M; m++) rep[m] = out[m];
+  return HEXOPT_OK;
+}
+
+int hexopt_untangle(hexopt_ctx *ctx, const hexopt_slim_params *params, const uint8_t *boundary, int max_iter,
+                    hexopt_untangle_report *rep) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!params || !boundary) return fail(ctx, HEXOPT_ERR_ARG, "untangle: NULL params or boundary flags");
+  if (params->precision != HEXOPT_FP64) return fail(ctx, HEXOPT_ERR_UNSUPPORTED, "untangle runs in HEXOPT_FP64");
+  if (max_iter < 1) return fail(ctx, HEXOPT_ERR_ARG, "untangle: max_iter < 1");
+  const int M = ctx->n_meshes;
+  // the mesh's positions are the boundary-projected positions BV (optimization::assign_constraints)
+  std::vector<double> BV(3 * ctx->NV);
+  rc = hexopt_get_positions(ctx, BV.data());
+  if (rc) return rc;
+  // exploded mesh: hex h owns copies 8h..8h+7 of its corners (mesh-local numbering); copies of one
+  // vertex form its glue group (V_ranges, optimization.cpp:556-575); copies of boundary vertices
+  // are held (known_value_post, :590-615)
+  std::vector<int64_t> nv_e(M), nh_e(M), n_groups(M), nfix(M, 0);
+  std::vector<double> Ve(3 * 8 * (size_t)ctx->NH);
+  std::vector<uint32_t> He(8 * (size_t)ctx->NH);
+  std::vector<int64_t> gptr;
+  std::vector<int32_t> gvs, fix_ids;
+  for (int m = 0; m < M; m++) {
+    const int64_t h0 = ctx->md[m].h_off, nh = ctx->md[m].nh, v0 = ctx->md[m].v_off, nv = ctx->md[m].nv;
+    nv_e[m] = 8 * nh;
+    nh_e[m] = nh;
+    std::vector<int64_t> cnt(nv + 1, 0);
+    for (int64_t h = 0; h < nh; h++)
+      for (int c = 0; c < 8; c++) {
+        const uint32_t v = ctx->H_h[8 * (h0 + h) + c];
+        He[8 * (h0 + h) + c] = (uint32_t)(8 * h + c);
+        for (int d = 0; d < 3; d++) Ve[3 * (8 * (h0 + h) + c) + d] = BV[3 * (v0 + v) + d];
+        cnt[v + 1]++;
+        if (boundary[v0 + v]) { fix_ids.push_back((int32_t)(8 * h + c)); nfix[m]++; }
+      }
+    for (int64_t v = 0; v < nv; v++) cnt[v + 1] += cnt[v];
+    std::vector<int32_t> slot(cnt.begin(), cnt.end() - 1);
+    std::vector<int32_t> mem(8 * nh);
+    for (int64_t h = 0; h < nh; h++)
+      for (int c = 0; c < 8; c++) mem[slot[ctx->H_h[8 * (h0 + h) + c]]++] = (int32_t)(8 * h + c);
+    int64_t groups = 0;
+    for (int64_t v = 0; v < nv; v++) {
+      if (cnt[v + 1] == cnt[v]) continue;  // a vertex no hex uses
+      gptr.push_back((int64_t)gvs.size() - 0);
+      for (int64_t k = cnt[v]; k < cnt[v + 1]; k++) gvs.push_back(mem[k]);
+      groups++;
+    }
+    gptr.push_back((int64_t)gvs.size());
+    n_groups[m] = groups;
+  }
+  // group_ptr per mesh: n_groups[m] + 1 entries, offsets into that mesh's group_vs segment
+  std::vector<int64_t> gptr_local;
+  {
+    size_t k = 0;
+    for (int m = 0; m < M; m++) {
+      const int64_t base = gptr[k];
+      for (int64_t g = 0; g <= n_groups[m]; g++) gptr_local.push_back(gptr[k + g] - base);
+      k += n_groups[m] + 1;
+    }
+  }
+  hexopt_ctx *c = nullptr;
+  rc = hexopt_create(&c, ctx->device);
+  if (rc) return fail(ctx, rc, "untangle: cannot create the exploded-mesh context");
+  struct Guard { hexopt_ctx *c; ~Guard() { hexopt_destroy(c); } } guard{c};
+  auto sub = [&](int code, const char *what) {
+    return fail(ctx, code, "untangle: %s: %s", what, hexopt_last_error(c));
+  };
+  if ((rc = hexopt_upload_meshes(c, M, nv_e.data(), nh_e.data(), Ve.data(), He.data(), nullptr))) return sub(rc, "upload");
+  if ((rc = hexopt_set_fixed(c, nfix.data(), fix_ids.data()))) return sub(rc, "set_fixed");
+  std::vector<double> lg(M, 1e4);
+  if ((rc = hexopt_set_glue(c, n_groups.data(), gptr_local.data(), gvs.data(), lg.data()))) return sub(rc, "set_glue");
+  // reference shapes: compute_referenceMesh(BV, mesh.Hs, all true, Hids, ts.RT, false) (:584)
+  if ((rc = hexopt_set_reference_hexes(c, Ve.data()))) return sub(rc, "set_reference_hexes");
+  // rigidDeformCubes: the starting copies (ts.V = Cubes)
+  launch_rigid_cubes(c->X.as<double>(), c->X32.as<float>(), c->vfix.as<uint8_t>(), c->NH, c->st);
+  c->launches++;
+  {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, HEXOPT_ERR_CUDA, "untangle: rigid cubes: %s", cudaGetErrorString(e));
+  }
+  hexopt_slim_params p = *params;
+  p.cube = 0;
+  if ((rc = hexopt_slim_precompute(c, &p))) return sub(rc, "slim_precompute");
+  std::vector<hexopt_adaptive_report> ar(M);
+  if ((rc = hexopt_slim_solve_adaptive(c, 1, 2, max_iter, ar.data()))) return sub(rc, "slim_solve_adaptive");
+  // the glued positions: each vertex at the mean of its copies (:651-660)
+  KArgs a = make_args(c);
+  CK(cudaMemcpyAsync(c->Xm.p, c->X.p, sizeof(double) * 4 * c->NV, cudaMemcpyDeviceToDevice, c->st));
+  launch_result_positions(a, c->kind[K_CONS].nblk, c->Xm.as<double>(), 1, c->st);
+  CK(c->stage.ensure(sizeof(double) * 3 * c->NV));
+  launch_aos4_to_rows(c->Xm.as<double>(), c->stage.as<double>(), c->NV, c->st);
+  std::vector<double> Xe(3 * (size_t)c->NV);
+  CK(cudaMemcpyAsync(Xe.data(), c->stage.p, sizeof(double) * 3 * c->NV, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int m = 0; m < M; m++) {
+    const int64_t h0 = ctx->md[m].h_off, nh = ctx->md[m].nh, v0 = ctx->md[m].v_off;
+    for (int64_t h = 0; h < nh; h++)
+      for (int cc = 0; cc < 8; cc++) {
+        const uint32_t v = ctx->H_h[8 * (h0 + h) + cc];
+        for (int d = 0; d < 3; d++) BV[3 * (v0 + v) + d] = Xe[3 * (8 * (h0 + h) + cc) + d];
+      }
+  }
+  rc = hexopt_set_positions(ctx, BV.data());
+  if (rc) return rc;
+  std::vector<hexopt_quality> q(M);
+  rc = hexopt_scaled_jacobian(ctx, nullptr, nullptr, q.data());
+  if (rc) return rc;
+  if (rep)
+    for (int m = 0; m < M; m++) {
+      rep[m].success = q[m].min_Jacobian < 0 ? 0 : 1;
+      rep[m].iterations = ar[m].iterations;
+      rep[m].min_Jacobian = q[m].min_Jacobian;
+      rep[m].ave_Jacobian = q[m].ave_Jacobian;
+      rep[m].energy = ar[m].energy;
+      rep[m].lamda_glue = ar[m].lamda_glue;
+    }
   return HEXOPT_OK;
 }
 

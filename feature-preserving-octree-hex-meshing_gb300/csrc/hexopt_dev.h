@@ -36,6 +36,8 @@ struct MeshDesc {
   int64_t c_off, nc;  // corner constraints
   int64_t t_off, nt;  // tangent-plane constraints
   int64_t l_off, nl;  // feature-line constraints (and curve unknowns)
+  int64_t b_off, nb;  // projection points (Tetralize_Set::b / bc)
+  int64_t grp_off, ngrp;  // glue groups (vertex copies tied to their mean)
   int64_t g_off;      // first own-shape slot (hexes with a per-tet rest matrix)
   // block tables of the SLIM launch kinds: first block and block count
   int64_t hblk0, vblk0, cblk0;
@@ -73,6 +75,11 @@ struct MeshScalars {
   double HR;         // Hausdorff ratio threshold (args.Hausdorff_ratio_t)
   double haus_diag, haus_max, haus_ave;
   double adj_eq, adj_es;  // energy_fwd parts
+  // untangling / glue path (add_soft_constraints projection and glue terms, slim_solve2's
+  // adaptive branch)
+  double lamda_P, lamda_G;  // Tetralize_Set::lamda_projection, lamda_glue
+  int32_t glue;             // glue terms on: the feature terms are off (slim_m.cpp:611, 647)
+  int32_t frozen;           // adaptive loop finished for this mesh: later steps leave it in place
 };
 
 }  // namespace hexopt

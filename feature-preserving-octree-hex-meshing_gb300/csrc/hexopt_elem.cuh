@@ -250,4 +250,29 @@ __device__ __forceinline__ void apply_BT(const T Q[3][3], int32_t gs, const doub
   }
 }
 
+// ---------------------------------------------------------------- constraint items
+// The constraint items of a mesh, in order: corners, tangent planes, feature lines, projection
+// points (Tetralize_Set::b / bc), glue groups; e indexes the kind's global arrays.
+enum ConsKind { CK_CORNER = 0, CK_TANGENT = 1, CK_LINE = 2, CK_PROJ = 3, CK_GROUP = 4 };
+struct ConsItem {
+  int kind;
+  int64_t e;
+};
+__device__ __forceinline__ ConsItem cons_item(const MeshDesc &md, int64_t i) {
+  int64_t li = i - md.kitem0[K_CONS];
+  if (li < md.nc) return {CK_CORNER, md.c_off + li};
+  li -= md.nc;
+  if (li < md.nt) return {CK_TANGENT, md.t_off + li};
+  li -= md.nt;
+  if (li < md.nl) return {CK_LINE, md.l_off + li};
+  li -= md.nl;
+  if (li < md.nb) return {CK_PROJ, md.b_off + li};
+  return {CK_GROUP, md.grp_off + (li - md.nb)};
+}
+// Glue group g: members m0..m1-1 of g_vs; coefficient (n / (n-1))^2 of the reference's rows
+// x_j - sum_{k != j} x_k / (n-1) (slim_m.cpp:611-646); 0 for a single member.
+__device__ __forceinline__ double glue_coef(int64_t n) {
+  return n < 2 ? 0.0 : double(n) * double(n) / (double(n - 1) * double(n - 1));
+}
+
 }  // namespace hexopt

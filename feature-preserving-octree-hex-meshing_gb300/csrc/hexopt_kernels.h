@@ -39,6 +39,10 @@ struct KArgs {
   const int32_t *c_ids; const double *c_pos;
   const int32_t *t_ids; double *t_nrm; double *t_dis;
   const int32_t *l_ids; double *l_axis; double *l_orig;
+  const int32_t *b_ids; const double *b_pos;      // projection points and their targets bc
+  const int64_t *g_ptr; const int32_t *g_vs;      // glue groups: member ranges, global vertex ids
+  const uint8_t *vfix;                            // held (known-value) vertices, or null
+  int has_fixed;
   // parameters
   int energy;
   int cg_max_iter;
@@ -77,6 +81,12 @@ template <typename VT> void launch_cg_dir(const KArgs &a, int64_t vblk, cudaStre
 // proximal terms in FP64); `replace` = a replacement inside the CG (accumulate d into dd first,
 // then take the new residual's norms), else the initial residual of the solve.
 void launch_ir_residual(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, bool replace, cudaStream_t st);
+// Held vertices: q = L_ib x_b (element part) for the rhs norm of the known-value solve.
+template <typename VT> void launch_fixed_pre(const KArgs &a, int64_t hblk, int64_t vblk, cudaStream_t st);
+// Result mesh of the adaptive branch: Xm (a copy of X) with glue groups at their means (type 1)
+// or projection points at bc (type 0); glue weight schedules (k_slim.cuh).
+void launch_result_positions(const KArgs &a, int64_t cblk, double *Xm, int type, cudaStream_t st);
+void launch_glue_schedule(MeshScalars *sc, int n, int before, int iter, cudaStream_t st);
 // After the last PCG iteration: the search direction d = fl32(dd + d) (curve entries likewise).
 void launch_ir_final(const KArgs &a, int64_t vblk, cudaStream_t st);
 template <typename ET, typename VT> void launch_ls_energy_pass(const KArgs &a, int64_t hblk, cudaStream_t st);
@@ -91,6 +101,10 @@ constexpr int kLaunchesIrInitial = 2, kLaunchesIrReplace = 4, kLaunchesIrFinal =
 // positions X through the hexes; cube / h_flag as compute_referenceMesh.
 void launch_ref_shapes(const double *P8, const uint32_t *hexv, const double *X, const uint8_t *hflag, int cube,
                        int64_t nh, double *Bref, cudaStream_t st);
+
+// rigidDeformCubes on an exploded mesh (hex h owns vertices 8h..8h+7): hexes with no held corner
+// become the unit cube fitted to their corners (Procrustes with scaling, no reflection).
+void launch_rigid_cubes(double *X, float *X32, const uint8_t *vfix, int64_t nh, cudaStream_t st);
 
 // ---- adjoint (k_adjoint.cu) ----
 template <typename ET> void launch_energy_fwd(const KArgs &a, int64_t hblk, int64_t cblk, cudaStream_t st);

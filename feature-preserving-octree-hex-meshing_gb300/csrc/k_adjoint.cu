@@ -91,32 +91,50 @@ __global__ void __launch_bounds__(256) k_adj_soft(KArgs a) {
   MeshScalars &S = a.sc[sg.mesh];
   double acc[1] = {0};
   if (i < sg.end) {
-    int64_t li = i - md.c_off - md.t_off - md.l_off;
-    int64_t e;
-    if (li < md.nc) {
-      e = md.c_off + li;
-      const int64_t v = md.v_off + a.c_ids[e];
-      const double r0 = a.Xa[4 * v] - a.c_pos[3 * e], r1 = a.Xa[4 * v + 1] - a.c_pos[3 * e + 1], r2 = a.Xa[4 * v + 2] - a.c_pos[3 * e + 2];
-      acc[0] = S.lamda_C * (r0 * r0 + r1 * r1 + r2 * r2);
-      if (BWD) atomic_add3(a.grad, (uint32_t)v, 2 * S.lamda_C * r0, 2 * S.lamda_C * r1, 2 * S.lamda_C * r2);
-    } else if ((li -= md.nc) < md.nt) {
-      e = md.t_off + li;
-      const int64_t v = md.v_off + a.t_ids[e];
-      const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2];
-      const double ad = n0 * a.Xa[4 * v] + n1 * a.Xa[4 * v + 1] + n2 * a.Xa[4 * v + 2] - a.t_dis[e];
-      acc[0] = S.lamda_T * ad * ad;
-      const double g = 2 * S.lamda_T * ad;
-      if (BWD) atomic_add3(a.grad, (uint32_t)v, g * n0, g * n1, g * n2);
-    } else {
-      li -= md.nt;
-      e = md.l_off + li;
-      const int64_t v = md.v_off + a.l_ids[e];
-      const double al = a.aL[e];
-      const double r0 = a.Xa[4 * v] - al * a.l_axis[3 * e] - a.l_orig[3 * e];
-      const double r1 = a.Xa[4 * v + 1] - al * a.l_axis[3 * e + 1] - a.l_orig[3 * e + 1];
-      const double r2 = a.Xa[4 * v + 2] - al * a.l_axis[3 * e + 2] - a.l_orig[3 * e + 2];
-      acc[0] = S.lamda_L * (r0 * r0 + r1 * r1 + r2 * r2);
-      if (BWD) atomic_add3(a.grad, (uint32_t)v, 2 * S.lamda_L * r0, 2 * S.lamda_L * r1, 2 * S.lamda_L * r2);
+    const ConsItem it = cons_item(md, i);
+    const int64_t e = it.e;
+    if (it.kind == CK_GROUP) {
+      // lamda_G (n/(n-1))^2 sum_j |x_j - mean|^2; its gradient 2 c (x_j - mean) (the mean's own
+      // derivative sums to zero over the group)
+      const int64_t m0 = a.g_ptr[e], m1 = a.g_ptr[e + 1];
+      const double c = S.lamda_G * glue_coef(m1 - m0);
+      if (c != 0.0) {
+        double mean[3] = {0, 0, 0};
+        for (int64_t k = m0; k < m1; k++)
+          for (int d = 0; d < 3; d++) mean[d] += a.Xa[4 * (int64_t)a.g_vs[k] + d];
+        for (int d = 0; d < 3; d++) mean[d] /= double(m1 - m0);
+        for (int64_t k = m0; k < m1; k++) {
+          const int64_t v = a.g_vs[k];
+          const double r0 = a.Xa[4 * v] - mean[0], r1 = a.Xa[4 * v + 1] - mean[1], r2 = a.Xa[4 * v + 2] - mean[2];
+          acc[0] += c * (r0 * r0 + r1 * r1 + r2 * r2);
+          if (BWD) atomic_add3(a.grad, (uint32_t)v, 2 * c * r0, 2 * c * r1, 2 * c * r2);
+        }
+      }
+    } else if (!(S.glue && it.kind <= CK_LINE)) {
+      if (it.kind == CK_CORNER || it.kind == CK_PROJ) {
+        const bool pj = it.kind == CK_PROJ;
+        const int64_t v = md.v_off + (pj ? a.b_ids[e] : a.c_ids[e]);
+        const double *cp = pj ? a.b_pos + 3 * e : a.c_pos + 3 * e;
+        const double lc = pj ? S.lamda_P : S.lamda_C;
+        const double r0 = a.Xa[4 * v] - cp[0], r1 = a.Xa[4 * v + 1] - cp[1], r2 = a.Xa[4 * v + 2] - cp[2];
+        acc[0] = lc * (r0 * r0 + r1 * r1 + r2 * r2);
+        if (BWD) atomic_add3(a.grad, (uint32_t)v, 2 * lc * r0, 2 * lc * r1, 2 * lc * r2);
+      } else if (it.kind == CK_TANGENT) {
+        const int64_t v = md.v_off + a.t_ids[e];
+        const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2];
+        const double ad = n0 * a.Xa[4 * v] + n1 * a.Xa[4 * v + 1] + n2 * a.Xa[4 * v + 2] - a.t_dis[e];
+        acc[0] = S.lamda_T * ad * ad;
+        const double g = 2 * S.lamda_T * ad;
+        if (BWD) atomic_add3(a.grad, (uint32_t)v, g * n0, g * n1, g * n2);
+      } else {
+        const int64_t v = md.v_off + a.l_ids[e];
+        const double al = a.aL[e];
+        const double r0 = a.Xa[4 * v] - al * a.l_axis[3 * e] - a.l_orig[3 * e];
+        const double r1 = a.Xa[4 * v + 1] - al * a.l_axis[3 * e + 1] - a.l_orig[3 * e + 1];
+        const double r2 = a.Xa[4 * v + 2] - al * a.l_axis[3 * e + 2] - a.l_orig[3 * e + 2];
+        acc[0] = S.lamda_L * (r0 * r0 + r1 * r1 + r2 * r2);
+        if (BWD) atomic_add3(a.grad, (uint32_t)v, 2 * S.lamda_L * r0, 2 * S.lamda_L * r1, 2 * S.lamda_L * r2);
+      }
     }
   }
   if (BWD) return;

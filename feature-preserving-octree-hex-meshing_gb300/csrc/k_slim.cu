@@ -74,6 +74,17 @@ void launch_ir_residual(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk
   k_ir_soft<<<(unsigned)cblk, a.vthreads, 0, st>>>(a, replace ? 1 : 0);
   if (replace) k_ir_norm<<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
 }
+template <typename VT>
+void launch_fixed_pre(const KArgs &a, int64_t hblk, int64_t vblk, cudaStream_t st) {
+  k_fixed_pre<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+  k_spmv<VT><<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
+}
+void launch_result_positions(const KArgs &a, int64_t cblk, double *Xm, int type, cudaStream_t st) {
+  k_result_positions<<<(unsigned)cblk, a.vthreads, 0, st>>>(a, Xm, type);
+}
+void launch_glue_schedule(MeshScalars *sc, int n, int before, int iter, cudaStream_t st) {
+  k_glue_schedule<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(sc, n, before, iter);
+}
 void launch_ir_final(const KArgs &a, int64_t vblk, cudaStream_t st) {
   k_ir_final<<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
 }
@@ -109,6 +120,7 @@ void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk
   template void launch_cg_start<VT>(const KArgs &, int64_t, cudaStream_t);                       \
   template void launch_cg_iter<VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t, bool); \
   template void launch_cg_dir<VT>(const KArgs &, int64_t, cudaStream_t);                         \
+  template void launch_fixed_pre<VT>(const KArgs &, int64_t, int64_t, cudaStream_t);             \
   template void launch_line_search<ET, VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t); \
   template void launch_ls_energy_pass<ET, VT>(const KArgs &, int64_t, cudaStream_t);
 HX_INST(double, double)

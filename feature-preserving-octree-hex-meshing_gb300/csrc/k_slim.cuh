@@ -286,9 +286,11 @@ __global__ void __launch_bounds__(128, sizeof(ET) == 4 ? 8 : 4) k_spmv(KArgs a) 
 }
 
 // ------------------------------------------------------------------------------- soft terms
-// Constraint items of a mesh: [0, nc) corners, [nc, nc+nt) tangent planes, [nc+nt, +nl) lines.
-// add_soft_constraints (slim_m.cpp:647-711): rhs, diagonal and (FP64 mode; mixed mode forms it
-// in k_ir_soft) the residual at x0 (curve unknowns start at 0).
+// add_soft_constraints (slim_m.cpp:597-714) over the constraint items (cons_item): projection
+// points lamda_P |x - bc|^2 (ts.projection, :600-610); glue groups lamda_G (n/(n-1))^2
+// sum_j |x_j - mean|^2 (ts.glue, :611-646); and, unless the mesh is glued (:647), corners, tangent
+// planes and feature lines with their curve unknowns.  This kernel adds the rhs, the diagonal and
+// (FP64 mode; mixed mode forms it in k_ir_soft) the residual at x0 (curve unknowns start at 0).
 template <typename VT>
 __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
   const Seg sg = a.cseg[blockIdx.x];
@@ -297,21 +299,22 @@ __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
   const MeshDesc md = a.mesh[sg.mesh];
   const MeshScalars &S = a.sc[sg.mesh];
   VT *b = reinterpret_cast<VT *>(a.b), *r = reinterpret_cast<VT *>(a.r), *dg = reinterpret_cast<VT *>(a.diag);
-  int64_t li = i - md.c_off - md.t_off - md.l_off;
-  if (li < md.nc) {
-    const int64_t e = md.c_off + li;
-    const uint32_t v = (uint32_t)(md.v_off + a.c_ids[e]);
-    const double lc = S.lamda_C;
+  const ConsItem it = cons_item(md, i);
+  const int64_t e = it.e;
+  if (S.glue && it.kind <= CK_LINE) return;
+  if (it.kind == CK_CORNER || it.kind == CK_PROJ) {
+    const bool pj = it.kind == CK_PROJ;
+    const uint32_t v = (uint32_t)(md.v_off + (pj ? a.b_ids[e] : a.c_ids[e]));
+    const double lc = pj ? S.lamda_P : S.lamda_C;
+    const double *cp = pj ? a.b_pos + 3 * e : a.c_pos + 3 * e;
     const double *x = a.X + 4 * (int64_t)v;
-    const double c0 = a.c_pos[3 * e], c1 = a.c_pos[3 * e + 1], c2 = a.c_pos[3 * e + 2];
+    const double c0 = cp[0], c1 = cp[1], c2 = cp[2];
     atomic_add3(b, v, VT(lc * c0), VT(lc * c1), VT(lc * c2));
     if constexpr (sizeof(VT) == 8) atomic_add3(r, v, VT(lc * (c0 - x[0])), VT(lc * (c1 - x[1])), VT(lc * (c2 - x[2])));
     atomic_add3(dg, v, VT(lc), VT(lc), VT(lc));
     return;
   }
-  li -= md.nc;
-  if (li < md.nt) {
-    const int64_t e = md.t_off + li;
+  if (it.kind == CK_TANGENT) {
     const uint32_t v = (uint32_t)(md.v_off + a.t_ids[e]);
     const double lt = S.lamda_T;
     const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2], d = a.t_dis[e];
@@ -322,9 +325,25 @@ __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
     atomic_add3(dg, v, VT(lt * n0 * n0), VT(lt * n1 * n1), VT(lt * n2 * n2));
     return;
   }
-  li -= md.nt;
+  if (it.kind == CK_GROUP) {
+    const int64_t m0 = a.g_ptr[e], m1 = a.g_ptr[e + 1];
+    const double c = S.lamda_G * glue_coef(m1 - m0);
+    if (c == 0.0) return;
+    double mean[3] = {0, 0, 0};
+    for (int64_t k = m0; k < m1; k++)
+      for (int d = 0; d < 3; d++) mean[d] += a.X[4 * (int64_t)a.g_vs[k] + d];
+    for (int d = 0; d < 3; d++) mean[d] /= double(m1 - m0);
+    const double w = c * (1.0 - 1.0 / double(m1 - m0));
+    for (int64_t k = m0; k < m1; k++) {
+      const uint32_t v = (uint32_t)a.g_vs[k];
+      const double *x = a.X + 4 * (int64_t)v;
+      if constexpr (sizeof(VT) == 8)
+        atomic_add3(r, v, VT(c * (mean[0] - x[0])), VT(c * (mean[1] - x[1])), VT(c * (mean[2] - x[2])));
+      atomic_add3(dg, v, VT(w), VT(w), VT(w));
+    }
+    return;
+  }
   {
-    const int64_t e = md.l_off + li;
     const uint32_t v = (uint32_t)(md.v_off + a.l_ids[e]);
     const double ll = S.lamda_L;
     const double x0 = a.l_axis[3 * e], x1 = a.l_axis[3 * e + 1], x2 = a.l_axis[3 * e + 2];
@@ -351,17 +370,18 @@ __global__ void __launch_bounds__(256) k_soft_mv(KArgs a) {
   const MeshScalars &S = a.sc[sg.mesh];
   const VT *in = reinterpret_cast<const VT *>(a.p), *in_a = reinterpret_cast<const VT *>(a.pa);
   VT *out = reinterpret_cast<VT *>(a.q), *out_a = reinterpret_cast<VT *>(a.qa);
-  int64_t li = i - md.c_off - md.t_off - md.l_off;
-  if (li < md.nc) {
-    const uint32_t v = (uint32_t)(md.v_off + a.c_ids[md.c_off + li]);
-    const VT lc = VT(S.lamda_C);
+  const ConsItem it = cons_item(md, i);
+  const int64_t e = it.e;
+  if (S.glue && it.kind <= CK_LINE) return;
+  if (it.kind == CK_CORNER || it.kind == CK_PROJ) {
+    const bool pj = it.kind == CK_PROJ;
+    const uint32_t v = (uint32_t)(md.v_off + (pj ? a.b_ids[e] : a.c_ids[e]));
+    const VT lc = VT(pj ? S.lamda_P : S.lamda_C);
     const VT *p = in + 4 * (int64_t)v;
     atomic_add3(out, v, lc * p[0], lc * p[1], lc * p[2]);
     return;
   }
-  li -= md.nc;
-  if (li < md.nt) {
-    const int64_t e = md.t_off + li;
+  if (it.kind == CK_TANGENT) {
     const uint32_t v = (uint32_t)(md.v_off + a.t_ids[e]);
     const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2];
     const VT *p = in + 4 * (int64_t)v;
@@ -369,9 +389,23 @@ __global__ void __launch_bounds__(256) k_soft_mv(KArgs a) {
     atomic_add3(out, v, VT(s * n0), VT(s * n1), VT(s * n2));
     return;
   }
-  li -= md.nt;
+  if (it.kind == CK_GROUP) {
+    const int64_t m0 = a.g_ptr[e], m1 = a.g_ptr[e + 1];
+    const double c = S.lamda_G * glue_coef(m1 - m0);
+    if (c == 0.0) return;
+    double mean[3] = {0, 0, 0};
+    for (int64_t k = m0; k < m1; k++)
+      for (int d = 0; d < 3; d++) mean[d] += double(in[4 * (int64_t)a.g_vs[k] + d]);
+    for (int d = 0; d < 3; d++) mean[d] /= double(m1 - m0);
+    for (int64_t k = m0; k < m1; k++) {
+      const uint32_t v = (uint32_t)a.g_vs[k];
+      const VT *p = in + 4 * (int64_t)v;
+      atomic_add3(out, v, VT(c * (double(p[0]) - mean[0])), VT(c * (double(p[1]) - mean[1])),
+                  VT(c * (double(p[2]) - mean[2])));
+    }
+    return;
+  }
   {
-    const int64_t e = md.l_off + li;
     const uint32_t v = (uint32_t)(md.v_off + a.l_ids[e]);
     const double ll = S.lamda_L;
     const double x0 = a.l_axis[3 * e], x1 = a.l_axis[3 * e + 1], x2 = a.l_axis[3 * e + 2];
@@ -414,6 +448,8 @@ __device__ __forceinline__ void st3(double *Y, int64_t v, V3<double> a) {
 }
 
 // r0 is already formed (local step + soft terms): p = invd r0, delta = 0, q = prox p, norms.
+// Held vertices (known_value_post) drop out of the unknowns: zero residual, direction and
+// preconditioner; the rhs norm is Eigen's over the free rows of b_i - L_ib x_b.
 template <typename VT>
 __global__ void __launch_bounds__(256) k_cg_start(KArgs a) {
   const Seg sg = a.vseg[blockIdx.x];
@@ -427,7 +463,12 @@ __global__ void __launch_bounds__(256) k_cg_start(KArgs a) {
   SumAcc<VT> s_bb, s_rr, s_rp;  // mixed mode: FP32 arithmetic, compensated sums
   for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
     const ItemRef it = item_ref(md, i);
-    if (!it.curve && sizeof(VT) == 4) {
+    if (!it.curve && a.has_fixed && a.vfix[it.idx]) {
+      // a held vertex (known value): not an unknown -- no residual, direction or preconditioner
+      const int64_t v = it.idx;
+      const V3<VT> z{VT(0), VT(0), VT(0)};
+      st3(p, v, z); st3(d, v, z); st3(invd, v, z); st3(q, v, z); st3(r, v, z);
+    } else if (!it.curve && sizeof(VT) == 4) {
       const int64_t v = it.idx;
       const V3<VT> bb = ld3(b, v), rr = ld3(r, v), gg = ld3(dg, v);
       const VT pr = VT(prox);
@@ -445,7 +486,11 @@ __global__ void __launch_bounds__(256) k_cg_start(KArgs a) {
       const int64_t v = it.idx;
       const V3<VT> bb = ld3(b, v), rr = ld3(r, v), gg = ld3(dg, v);
       const double x0 = a.X[4 * v], x1 = a.X[4 * v + 1], x2 = a.X[4 * v + 2];
-      const double b0 = double(bb.x) + prox * x0, b1 = double(bb.y) + prox * x1, b2 = double(bb.z) + prox * x2;
+      double b0 = double(bb.x) + prox * x0, b1 = double(bb.y) + prox * x1, b2 = double(bb.z) + prox * x2;
+      if (a.has_fixed) {  // Eigen's rhs with known values: b_i - L_ib x_b (q holds L x_b, k_fixed_pre)
+        const V3<VT> kq = ld3(q, v);
+        b0 -= double(kq.x); b1 -= double(kq.y); b2 -= double(kq.z);
+      }
       const double i0 = 1.0 / (double(gg.x) + prox), i1 = 1.0 / (double(gg.y) + prox), i2 = 1.0 / (double(gg.z) + prox);
       const double p0 = i0 * double(rr.x), p1 = i1 * double(rr.y), p2 = i2 * double(rr.z);
       st3(p, v, V3<VT>{VT(p0), VT(p1), VT(p2)});
@@ -560,6 +605,7 @@ __global__ void __launch_bounds__(256) k_cg_update(KArgs a) {
       V3<VT> dd = ld3(d, v), rr = ld3(r, v);
       dd.x += alpha * pp.x; dd.y += alpha * pp.y; dd.z += alpha * pp.z;
       rr.x -= alpha * qq.x; rr.y -= alpha * qq.y; rr.z -= alpha * qq.z;
+      if (a.has_fixed && a.vfix[v]) rr = V3<VT>{VT(0), VT(0), VT(0)};
       st3(d, v, dd);
       st3(r, v, rr);
       if (sizeof(VT) == 4) {
@@ -643,6 +689,66 @@ __global__ void __launch_bounds__(256) k_cg_dir(KArgs a) {
     pa[e] = invda[e] * ra[e] + beta * pa[e];
     qa[e] = VT(0);
   }
+  }
+}
+
+// ------------------------------------------------------------------------------- held vertices
+// known_value_post (slim_m.cpp:403-477): p = x_b (the held vertices' positions, 0 on the free
+// ones) and q = 0, so that the element SpMV that follows leaves q = L_ib x_b for k_cg_start.
+template <typename VT>
+__global__ void __launch_bounds__(256) k_fixed_pre(KArgs a) {
+  const Seg sg = a.vseg[blockIdx.x];
+  const MeshDesc md = a.mesh[sg.mesh];
+  if (threadIdx.x == 0) a.sc[sg.mesh].cg_done = 0;
+  VT *p = reinterpret_cast<VT *>(a.p), *q = reinterpret_cast<VT *>(a.q);
+  for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
+    const ItemRef it = item_ref(md, i);
+    if (!it.curve) {
+      const int64_t v = it.idx;
+      const bool fx = a.vfix[v] != 0;
+      st3(p, v, V3<VT>{VT(fx ? a.X[4 * v] : 0.0), VT(fx ? a.X[4 * v + 1] : 0.0), VT(fx ? a.X[4 * v + 2] : 0.0)});
+      st3(q, v, V3<VT>{VT(0), VT(0), VT(0)});
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------- adaptive loop
+// The result mesh slim_solve2's adaptive branch checks (slim_m.cpp:1237-1260): type 1 (gluing)
+// every vertex of a glue group at the mean of its group; type 0 (projection) the projection
+// points at their targets bc.  Xm starts as a copy of X.
+static __global__ void __launch_bounds__(256) k_result_positions(KArgs a, double *Xm, int type) {
+  const Seg sg = a.cseg[blockIdx.x];
+  const int64_t i = sg.begin + threadIdx.x;
+  if (i >= sg.end) return;
+  const MeshDesc md = a.mesh[sg.mesh];
+  const ConsItem it = cons_item(md, i);
+  if (type == 1 && it.kind == CK_GROUP) {
+    const int64_t m0 = a.g_ptr[it.e], m1 = a.g_ptr[it.e + 1];
+    double mean[3] = {0, 0, 0};
+    for (int64_t k = m0; k < m1; k++)
+      for (int d = 0; d < 3; d++) mean[d] += a.X[4 * (int64_t)a.g_vs[k] + d];
+    for (int d = 0; d < 3; d++) mean[d] /= double(m1 - m0);
+    for (int64_t k = m0; k < m1; k++)
+      for (int d = 0; d < 3; d++) Xm[4 * (int64_t)a.g_vs[k] + d] = mean[d];
+  } else if (type == 0 && it.kind == CK_PROJ) {
+    const int64_t v = md.v_off + a.b_ids[it.e];
+    for (int d = 0; d < 3; d++) Xm[4 * v + d] = a.b_pos[3 * it.e + d];
+  }
+}
+
+// Glue weight schedules, one thread per mesh, frozen meshes untouched.  before = 1: slim_solve's
+// doubling at the start of iteration `iter` (lamda_glue *= 2 once iter > 3, while below 1e8,
+// slim_m.cpp:1311-1312); before = 0: slim_solve2's update after an iteration,
+// lamda_glue = min(1e4 max(E_quality / E_soft lamda_glue, 1), 1e16) (slim_m.cpp:1258).
+static __global__ void k_glue_schedule(MeshScalars *sc, int n, int before, int iter) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  MeshScalars &S = sc[m];
+  if (S.frozen) return;
+  if (before) {
+    if (iter > 3 && S.lamda_G < 1e8) S.lamda_G *= 2;
+  } else {
+    S.lamda_G = fmin(1e4 * fmax(S.eq / S.es * S.lamda_G, 1.0), 1e16);
   }
 }
 
@@ -774,9 +880,10 @@ static __global__ void __launch_bounds__(128, 4) k_ir_resid(KArgs a, int replace
   for (int c = 0; c < 8; c++) atomic_add3(r, hv[c], F[c][0], F[c][1], F[c][2]);
 }
 
-// Soft-constraint residual at x = X + dd (curve unknowns a = dda), in FP64: corners
-// lamda_C (c - x), tangent planes lamda_T n (d - n.x), lines lamda_L (o + a t - x) on the vertex
-// rows and lamda_L (t.(x - o) - |t|^2 a) on the curve row (add_soft_constraints' system).
+// Soft-constraint residual at x = X + dd (curve unknowns a = dda), in FP64: corners and
+// projection points lamda (c - x), tangent planes lamda_T n (d - n.x), lines lamda_L (o + a t - x)
+// on the vertex rows and lamda_L (t.(x - o) - |t|^2 a) on the curve row (add_soft_constraints'
+// system).  Glue groups and held vertices are FP64-mode only.
 static __global__ void __launch_bounds__(256) k_ir_soft(KArgs a, int replace) {
   const Seg sg = a.cseg[blockIdx.x];
   const MeshScalars &S = a.sc[sg.mesh];
@@ -785,20 +892,18 @@ static __global__ void __launch_bounds__(256) k_ir_soft(KArgs a, int replace) {
   if (i >= sg.end) return;
   const MeshDesc md = a.mesh[sg.mesh];
   float *r = reinterpret_cast<float *>(a.r);
-  int64_t li = i - md.c_off - md.t_off - md.l_off;
-  int kind;
-  int64_t e;
-  if (li < md.nc) { kind = 0; e = md.c_off + li; }
-  else if ((li -= md.nc) < md.nt) { kind = 1; e = md.t_off + li; }
-  else { kind = 2; e = md.l_off + (li - md.nt); }
-  const int32_t lv = kind == 0 ? a.c_ids[e] : kind == 1 ? a.t_ids[e] : a.l_ids[e];
+  const ConsItem it = cons_item(md, i);
+  const int64_t e = it.e;
+  if (it.kind == CK_GROUP || (S.glue && it.kind <= CK_LINE)) return;
+  const int32_t lv = it.kind == CK_CORNER ? a.c_ids[e] : it.kind == CK_TANGENT ? a.t_ids[e]
+                   : it.kind == CK_LINE ? a.l_ids[e] : a.b_ids[e];
   const int64_t v = md.v_off + lv;
   const double x0 = a.X[4 * v] + a.dd[4 * v], x1 = a.X[4 * v + 1] + a.dd[4 * v + 1], x2 = a.X[4 * v + 2] + a.dd[4 * v + 2];
-  if (kind == 0) {
-    const double lc = S.lamda_C;
-    atomic_add3(r, (uint32_t)v, float(lc * (a.c_pos[3 * e] - x0)), float(lc * (a.c_pos[3 * e + 1] - x1)),
-                float(lc * (a.c_pos[3 * e + 2] - x2)));
-  } else if (kind == 1) {
+  if (it.kind == CK_CORNER || it.kind == CK_PROJ) {
+    const double lc = it.kind == CK_PROJ ? S.lamda_P : S.lamda_C;
+    const double *cp = it.kind == CK_PROJ ? a.b_pos + 3 * e : a.c_pos + 3 * e;
+    atomic_add3(r, (uint32_t)v, float(lc * (cp[0] - x0)), float(lc * (cp[1] - x1)), float(lc * (cp[2] - x2)));
+  } else if (it.kind == CK_TANGENT) {
     const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2];
     const double res = S.lamda_T * (a.t_dis[e] - (n0 * x0 + n1 * x1 + n2 * x2));
     atomic_add3(r, (uint32_t)v, float(res * n0), float(res * n1), float(res * n2));
@@ -1316,7 +1421,7 @@ __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t n
 
 // Soft energy at the current X (round < 0) or at the candidates of `round`; its last block
 // takes the line-search decision for the round (accept the first finite E <= E_old,
-// line_search.cpp:26-47).
+// line_search.cpp:26-47).  Terms as compute_soft_const_energy (slim_m.cpp:735-790).
 template <typename VT>
 __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
   const Seg sg = a.cseg[blockIdx.x];
@@ -1332,36 +1437,61 @@ __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
 #pragma unroll
   for (int j = 0; j < kMaxCand; j++) acc[j] = 0;
   if (i < sg.end) {
-    int64_t li = i - md.c_off - md.t_off - md.l_off;
-    int kind = 0;
-    int64_t e;
-    if (li < md.nc) { e = md.c_off + li; }
-    else if ((li -= md.nc) < md.nt) { kind = 1; e = md.t_off + li; }
-    else { li -= md.nt; kind = 2; e = md.l_off + li; }
-    const int32_t lv = kind == 0 ? a.c_ids[e] : kind == 1 ? a.t_ids[e] : a.l_ids[e];
-    const int64_t v = md.v_off + lv;
-    const double x0 = a.X[4 * v], x1 = a.X[4 * v + 1], x2 = a.X[4 * v + 2];
-    const double d0 = double(d[4 * v]), d1 = double(d[4 * v + 1]), d2 = double(d[4 * v + 2]);
+    const ConsItem it = cons_item(md, i);
+    const int64_t e = it.e;
+    if (it.kind == CK_GROUP) {
+      const int64_t m0 = a.g_ptr[e], m1 = a.g_ptr[e + 1];
+      const double c = S.lamda_G * glue_coef(m1 - m0);
+      if (c != 0.0) {
 #pragma unroll
-    for (int j = 0; j < kMaxCand; j++) {
-      if (j >= nc) break;
-      const double al = round < 0 ? 0.0 : cand_alpha(S, round * nc + j);
-      const double y0 = x0 + al * d0, y1 = x1 + al * d1, y2 = x2 + al * d2;
-      double en;
-      if (kind == 0) {
-        const double e0 = a.c_pos[3 * e] - y0, e1 = a.c_pos[3 * e + 1] - y1, e2 = a.c_pos[3 * e + 2] - y2;
-        en = S.lamda_C * (e0 * e0 + e1 * e1 + e2 * e2);
-      } else if (kind == 1) {
-        const double ad = a.t_nrm[3 * e] * y0 + a.t_nrm[3 * e + 1] * y1 + a.t_nrm[3 * e + 2] * y2 - a.t_dis[e];
-        en = S.lamda_T * ad * ad;
-      } else {
-        const double al_ = double(da[e]);  // a_L = CG solution (curve unknowns start at 0)
-        const double r0 = y0 - al_ * a.l_axis[3 * e] - a.l_orig[3 * e];
-        const double r1 = y1 - al_ * a.l_axis[3 * e + 1] - a.l_orig[3 * e + 1];
-        const double r2 = y2 - al_ * a.l_axis[3 * e + 2] - a.l_orig[3 * e + 2];
-        en = S.lamda_L * (r0 * r0 + r1 * r1 + r2 * r2);
+        for (int j = 0; j < kMaxCand; j++) {
+          if (j >= nc) break;
+          const double al = round < 0 ? 0.0 : cand_alpha(S, round * nc + j);
+          double mean[3] = {0, 0, 0};
+          for (int64_t k = m0; k < m1; k++) {
+            const int64_t v = a.g_vs[k];
+            for (int q = 0; q < 3; q++) mean[q] += a.X[4 * v + q] + al * double(d[4 * v + q]);
+          }
+          for (int q = 0; q < 3; q++) mean[q] /= double(m1 - m0);
+          double en = 0;
+          for (int64_t k = m0; k < m1; k++) {
+            const int64_t v = a.g_vs[k];
+            for (int q = 0; q < 3; q++) {
+              const double r = a.X[4 * v + q] + al * double(d[4 * v + q]) - mean[q];
+              en += r * r;
+            }
+          }
+          acc[j] += c * en;
+        }
       }
-      acc[j] += en;
+    } else if (!(S.glue && it.kind <= CK_LINE)) {
+      const int32_t lv = it.kind == CK_CORNER ? a.c_ids[e] : it.kind == CK_TANGENT ? a.t_ids[e]
+                       : it.kind == CK_LINE ? a.l_ids[e] : a.b_ids[e];
+      const int64_t v = md.v_off + lv;
+      const double x0 = a.X[4 * v], x1 = a.X[4 * v + 1], x2 = a.X[4 * v + 2];
+      const double d0 = double(d[4 * v]), d1 = double(d[4 * v + 1]), d2 = double(d[4 * v + 2]);
+#pragma unroll
+      for (int j = 0; j < kMaxCand; j++) {
+        if (j >= nc) break;
+        const double al = round < 0 ? 0.0 : cand_alpha(S, round * nc + j);
+        const double y0 = x0 + al * d0, y1 = x1 + al * d1, y2 = x2 + al * d2;
+        double en;
+        if (it.kind == CK_CORNER || it.kind == CK_PROJ) {
+          const double *cp = it.kind == CK_PROJ ? a.b_pos + 3 * e : a.c_pos + 3 * e;
+          const double e0 = cp[0] - y0, e1 = cp[1] - y1, e2 = cp[2] - y2;
+          en = (it.kind == CK_PROJ ? S.lamda_P : S.lamda_C) * (e0 * e0 + e1 * e1 + e2 * e2);
+        } else if (it.kind == CK_TANGENT) {
+          const double ad = a.t_nrm[3 * e] * y0 + a.t_nrm[3 * e + 1] * y1 + a.t_nrm[3 * e + 2] * y2 - a.t_dis[e];
+          en = S.lamda_T * ad * ad;
+        } else {
+          const double al_ = double(da[e]);  // a_L = CG solution (curve unknowns start at 0)
+          const double r0 = y0 - al_ * a.l_axis[3 * e] - a.l_orig[3 * e];
+          const double r1 = y1 - al_ * a.l_axis[3 * e + 1] - a.l_orig[3 * e + 1];
+          const double r2 = y2 - al_ * a.l_axis[3 * e + 2] - a.l_orig[3 * e + 2];
+          en = S.lamda_L * (r0 * r0 + r1 * r1 + r2 * r2);
+        }
+        acc[j] += en;
+      }
     }
   }
   __shared__ double smem[kMaxCand][32];
@@ -1414,12 +1544,13 @@ __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
   }
 }
 
-// X += step d; a_L = delta_a
+// X += step d; a_L = delta_a (a mesh whose adaptive loop has finished stays in place)
 template <typename VT>
 __global__ void __launch_bounds__(256) k_ls_apply(KArgs a) {
   const Seg sg = a.vseg[blockIdx.x];
   const MeshDesc md = a.mesh[sg.mesh];
   const MeshScalars &S = a.sc[sg.mesh];
+  if (S.frozen) return;
   for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
   const ItemRef it = item_ref(md, i);
   if (!it.curve) {

@@ -46,6 +46,17 @@ class FaReport(C.Structure):
                 ("hausdorff_diag", C.c_double), ("hausdorff_max", C.c_double), ("hausdorff_ave", C.c_double)]
 
 
+class AdaptiveReport(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("min_Jacobian", C.c_double),
+                ("ave_Jacobian", C.c_double), ("energy", C.c_double), ("energy_quality", C.c_double),
+                ("energy_soft", C.c_double), ("lamda_glue", C.c_double), ("status", C.c_int32), ("pad", C.c_int32)]
+
+
+class UntangleReport(C.Structure):
+    _fields_ = [("success", C.c_int32), ("iterations", C.c_int32), ("min_Jacobian", C.c_double),
+                ("ave_Jacobian", C.c_double), ("energy", C.c_double), ("lamda_glue", C.c_double)]
+
+
 class AABB(C.Structure):
     _fields_ = [("min", C.c_double * 3), ("max", C.c_double * 3)]
 
@@ -72,6 +83,11 @@ SIGNATURES = {
     "hexopt_set_tangents": (C.c_int, [_vp, _i64, _i32, _d, _d]),
     "hexopt_set_lines": (C.c_int, [_vp, _i64, _i32, _d, _d]),
     "hexopt_set_weights": (C.c_int, [_vp, _d, _d, _d]),
+    "hexopt_set_projection": (C.c_int, [_vp, _i64, _i32, _d, _d]),
+    "hexopt_set_glue": (C.c_int, [_vp, _i64, _i64, _i32, _d]),
+    "hexopt_set_fixed": (C.c_int, [_vp, _i64, _i32]),
+    "hexopt_slim_solve_adaptive": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(AdaptiveReport)]),
+    "hexopt_untangle": (C.c_int, [_vp, C.POINTER(SlimParams), _u8, C.c_int, C.POINTER(UntangleReport)]),
     "hexopt_get_tangents": (C.c_int, [_vp, _d, _d]),
     "hexopt_get_lines": (C.c_int, [_vp, _d, _d]),
     "hexopt_set_reference_hexes": (C.c_int, [_vp, _d]),
@@ -242,6 +258,57 @@ class Context:
         f = lambda x: np.ascontiguousarray(np.broadcast_to(np.asarray(x, np.float64), (self.n_meshes,)))
         a, b, c = f(lamda_C), f(lamda_T), f(lamda_L)
         self._ck(self.L.hexopt_set_weights(self.h, ptr(a, _d), ptr(b, _d), ptr(c, _d)), "set_weights")
+
+    def set_projection(self, ids, bc, lamda=None):
+        """Tetralize_Set::b / bc per mesh with weight lamda_projection (scalar or per mesh)."""
+        n, i = self._cat(ids, np.int32)
+        _, c = self._cat(bc, np.float64, 3)
+        lp = None if lamda is None else np.ascontiguousarray(np.broadcast_to(np.asarray(lamda, np.float64),
+                                                                            (self.n_meshes,)))
+        self._ck(self.L.hexopt_set_projection(self.h, ptr(n, _i64), ptr(i, _i32), ptr(c, _d), ptr(lp, _d)),
+                 "set_projection")
+
+    def set_glue(self, groups, lamda=None):
+        """groups: per mesh a list of vertex-id arrays (each a group of copies glued together)."""
+        ng = np.array([len(gs) for gs in groups], np.int64)
+        ptrs, vs = [], []
+        for gs in groups:
+            o = 0
+            ptrs.append(0)
+            for g in gs:
+                o += len(g)
+                ptrs.append(o)
+                vs.append(np.asarray(g, np.int32))
+        ptrs = np.ascontiguousarray(ptrs, np.int64)
+        vs = np.ascontiguousarray(np.concatenate(vs) if vs else np.zeros(1, np.int32), np.int32)
+        lg = None if lamda is None else np.ascontiguousarray(np.broadcast_to(np.asarray(lamda, np.float64),
+                                                                            (self.n_meshes,)))
+        self._ck(self.L.hexopt_set_glue(self.h, ptr(ng, _i64), ptr(ptrs, _i64), ptr(vs, _i32), ptr(lg, _d)),
+                 "set_glue")
+
+    def set_fixed(self, ids):
+        n, i = self._cat(ids, np.int32)
+        self._ck(self.L.hexopt_set_fixed(self.h, ptr(n, _i64), ptr(i, _i32)), "set_fixed")
+
+    def slim_solve_adaptive(self, type_=1, schedule=2, max_iter=50):
+        """slim_solve2 (schedule 2) / slim_solve (schedule 1) with iter_num = -1."""
+        rep = (AdaptiveReport * self.n_meshes)()
+        self._ck(self.L.hexopt_slim_solve_adaptive(self.h, int(type_), int(schedule), int(max_iter), rep),
+                 "slim_solve_adaptive")
+        return [dict(iterations=r.iterations, converged=bool(r.converged), min_J=r.min_Jacobian,
+                     ave_J=r.ave_Jacobian, energy=r.energy, energy_quality=r.energy_quality,
+                     energy_soft=r.energy_soft, lamda_glue=r.lamda_glue, status=r.status) for r in rep]
+
+    def untangle(self, boundary, max_iter=50, energy=3, weight_opt=1.0, **kw):
+        """optimization::pipeline2 on the context's hex meshes (positions = the boundary-projected
+        BV, boundary = one flag per vertex); energy defaults to CONFORMAL, the Tetralize_Set
+        default the reference's gluing runs with.  Positions are replaced by the glued ones."""
+        p = self.params(energy=energy, weight_opt=weight_opt, **kw)
+        b = np.ascontiguousarray(np.asarray(boundary, np.uint8).reshape(-1))
+        rep = (UntangleReport * self.n_meshes)()
+        self._ck(self.L.hexopt_untangle(self.h, C.byref(p), ptr(b, _u8), int(max_iter), rep), "untangle")
+        return [dict(success=bool(r.success), iterations=r.iterations, min_J=r.min_Jacobian, ave_J=r.ave_Jacobian,
+                     energy=r.energy, lamda_glue=r.lamda_glue) for r in rep]
 
     def get_tangents(self, total):
         n = np.empty((total, 3)); d = np.empty(total)

@@ -157,6 +157,60 @@ HEXOPT_API int hexopt_get_lines(hexopt_ctx *ctx, double *axis, double *origin);
  * (optimization.cpp:584); NULL restores the default.  Takes effect at the next precompute. */
 HEXOPT_API int hexopt_set_reference_hexes(hexopt_ctx *ctx, const double *P8);
 
+/* ---- untangling path: Tetralize_Set's projection, glue and known-value terms ----
+ * Projection points (ts.b / ts.bc, ts.projection): per mesh nB[m] vertex ids and targets (nB x
+ * 3) with weight lamda_projection[m] (may be NULL: unchanged); soft term lamda |x - bc|^2
+ * (add_soft_constraints, slim_m.cpp:600-610). */
+HEXOPT_API int hexopt_set_projection(hexopt_ctx *ctx, const int64_t *nB, const int32_t *ids, const double *bc,
+                                     const double *lamda_projection);
+/* Glue groups (ts.glue, V_ranges): per mesh n_groups[m] groups of vertex copies, group_ptr with
+ * n_groups[m] + 1 offsets per mesh into that mesh's part of group_vs (mesh-local vertex ids; a
+ * vertex in at most one group), weight lamda_glue[m] (may be NULL).  Each copy is tied to the
+ * others of its group: lamda (n/(n-1))^2 |x_j - mean|^2 (slim_m.cpp:611-646).  A glued mesh drops
+ * its corner / tangent / line terms (:647); feature lines must be cleared first.  FP64 only. */
+HEXOPT_API int hexopt_set_glue(hexopt_ctx *ctx, const int64_t *n_groups, const int64_t *group_ptr,
+                               const int32_t *group_vs, const double *lamda_glue);
+/* Held vertices (known_value_post, slim_m.cpp:403-477): per mesh nF[m] vertex ids held at their
+ * current positions; the solve runs over the other vertices (and curve unknowns).  FP64 only. */
+HEXOPT_API int hexopt_set_fixed(hexopt_ctx *ctx, const int64_t *nF, const int32_t *ids);
+
+typedef struct hexopt_adaptive_report {
+  int32_t iterations;   /* SLIM iterations this mesh ran */
+  int32_t converged;    /* 1 when its result mesh's minimum scaled Jacobian became > 0 */
+  double min_Jacobian, ave_Jacobian;  /* of the result mesh after its last iteration */
+  double energy, energy_quality, energy_soft;
+  double lamda_glue;    /* glue weight after its last iteration */
+  int32_t status, pad;
+} hexopt_adaptive_report;
+
+/* The iter_num = -1 branch of slim_solve2 (schedule 2, slim_m.cpp:1191-1268) and of slim_solve
+ * (schedule 1, :1293-1394), after slim_precompute: up to max_iter (50 in the reference) SLIM
+ * iterations; after each, the result mesh -- glue groups at their means (type 1) or projection
+ * points at their targets (type 0) -- is checked with scaled_jacobian and a mesh stops once its
+ * minimum is > 0.  Schedule 2 starts lamda_glue at 1e4 and sets it to
+ * min(1e4 max(E_quality / E_soft lamda_glue, 1), 1e16) after each gluing iteration; schedule 1
+ * doubles it before iterations 5, 6, ... while it is below 1e8.  rep: n_meshes or NULL. */
+HEXOPT_API int hexopt_slim_solve_adaptive(hexopt_ctx *ctx, int type, int schedule, int max_iter,
+                                          hexopt_adaptive_report *rep);
+
+typedef struct hexopt_untangle_report {
+  int32_t success;      /* pipeline2's result: the glued mesh's minimum scaled Jacobian is >= 0 */
+  int32_t iterations;   /* SLIM iterations of the gluing solve */
+  double min_Jacobian, ave_Jacobian;  /* of the glued mesh */
+  double energy, lamda_glue;
+} hexopt_untangle_report;
+
+/* optimization::pipeline2 for hex meshes (optimization.cpp:416-434, rigidDeformCubes :456-494,
+ * glueInternalNodes :552-669): every hex gets its own copy of its corners -- the boundary-
+ * flagged vertices' copies held, each other hex replaced by the unit cube Procrustes-fitted to
+ * its corners -- and the copies are glued back by the adaptive gluing solve (schedule 2, at most
+ * max_iter = 50 iterations) with edge-averaged cuboid reference shapes of the input mesh
+ * (compute_referenceMesh(..., false)).  The context's positions (the boundary-projected BV) are
+ * replaced by the glued ones.  params: energy (the reference's Tetralize_Set default is
+ * CONFORMAL), weight_opt, FP64; boundary: one flag per vertex of the batch.  rep: n_meshes. */
+HEXOPT_API int hexopt_untangle(hexopt_ctx *ctx, const hexopt_slim_params *params, const uint8_t *boundary,
+                               int max_iter, hexopt_untangle_report *rep);
+
 /* ---- SLIM ---- */
 HEXOPT_API int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *params);
 /* iters fixed-count SLIM iterations (slim_solve2, slim_m.cpp:1269-1288); rep: n_meshes or NULL */

@@ -4,7 +4,8 @@ reference's OWN FP64 code (oracle/_ref/libhexopt_ref.so, built from the referenc
 
     make -C oracle ref && python tests/golden/make_golden.py [group ...]
 
-Writes tests/golden/*.npz (every group when none is named; groups: base, energies, shapes).  The
+Writes tests/golden/*.npz (every group when none is named; groups: base, energies, shapes,
+untangle).  The
 fixtures are committed; the reference build is not.
 """
 from __future__ import annotations
@@ -114,7 +115,47 @@ def shapes():
     print("cube0", o3)
 
 
+def untangle():
+    """optimization::pipeline2 (rigidDeformCubes + glueInternalNodes, the adaptive gluing solve
+    with CONFORMAL energy and cuboid reference shapes) on jittered grids with inverted hexes and the
+    boundary held: one solved in 1 iteration, one in 2, one that runs all 50 iterations without
+    untangling, and a stretched box grid."""
+    R = O.ref()
+    R.ref_pipeline2.argtypes = [C.c_int64, _d, C.c_int64, _u32, _u8, C.c_double, _d, _d]
+    cases = [("untangle_a", 5, 0.2, 1, None), ("untangle_b", 5, 0.25, 0, None), ("untangle_c", 5, 0.2, 2, None),
+             ("untangle_box", (6, 4, 3), 0.22, 3, (2.0, 1.0, 1.5))]
+    for name, n, sig, seed, hi in cases:
+        if hi is None:
+            V, H = meshgen.grid_hex(n)
+            b = meshgen.grid_boundary_mask(n)
+            V = meshgen.jitter(V, ~b, 1.0 / n, seed, sigma=sig)
+        else:
+            V, H = meshgen.grid_hex(*n, hi=hi)
+            b = meshgen.grid_boundary_mask(*n)
+            V = meshgen.jitter(V, ~b, min(hi[0] / n[0], hi[1] / n[1], hi[2] / n[2]), seed, sigma=sig)
+        bb = np.ascontiguousarray(b.astype(np.uint8))
+        Vo = np.empty_like(V)
+        out = np.empty(4)
+        R.ref_pipeline2(len(V), p(V, _d), len(H), p(H, _u32), p(bb, _u8), 1.0, p(Vo, _d), p(out, _d))
+        # the reference's own spread under 1e-15 relative input noise (4 trials): the adaptive
+        # solve's growing glue weight makes long runs sensitive to rounding
+        diag = np.linalg.norm(V.max(0) - V.min(0))
+        spread, jspread = 0.0, 0.0
+        for k in range(4):
+            Vn = np.ascontiguousarray(V * (1 + np.random.default_rng(k).normal(0, 1e-15, V.shape)))
+            Vk = np.empty_like(V)
+            ok = np.empty(4)
+            R.ref_pipeline2(len(V), p(Vn, _d), len(H), p(H, _u32), p(bb, _u8), 1.0, p(Vk, _d), p(ok, _d))
+            spread = max(spread, float(np.abs(Vk - Vo).max() / diag))
+            jspread = max(jspread, abs(float(ok[1] - out[1])))
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), V=V, H=H, boundary=bb, weight_opt=1.0, V_o=Vo, out=out,
+                            spread=spread, minJ_spread=jspread)
+        print(name, out, "spread", spread, jspread)
+
+
 def main(groups):
+    if "untangle" in groups:
+        untangle()
     if "energies" in groups:
         energies()
     if "shapes" in groups:
@@ -212,4 +253,4 @@ def base():
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["base", "energies", "shapes"])
+    main(sys.argv[1:] or ["base", "energies", "shapes", "untangle"])
