@@ -1114,6 +1114,10 @@ int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *p) {
   if (p->precision != HEXOPT_FP64 && p->precision != HEXOPT_MIXED) return fail(ctx, HEXOPT_ERR_ARG, "unknown precision");
   if (p->ls_candidates < 1 || p->ls_candidates > kMaxCand) return fail(ctx, HEXOPT_ERR_ARG, "ls_candidates must be 1..%d", kMaxCand);
   if (p->cg_max_iter < 0) return fail(ctx, HEXOPT_ERR_ARG, "cg_max_iter < 0");
+  if (p->variant != 0 && p->variant != 1) return fail(ctx, HEXOPT_ERR_ARG, "unknown SLIM variant %d", p->variant);
+  if (p->variant == 1 && (ctx->has_glue || ctx->NB > 0))
+    return fail(ctx, HEXOPT_ERR_UNSUPPORTED,
+                "the modified igl::slim's glue groups and b/bc terms (which no reference caller sets) are not built");
   if (p->precision == HEXOPT_MIXED && (ctx->has_glue || ctx->has_fixed))
     return fail(ctx, HEXOPT_ERR_UNSUPPORTED, "glue groups and held vertices run in HEXOPT_FP64 only");
   ctx->params = *p;
@@ -1129,8 +1133,8 @@ int hexopt_slim_precompute(hexopt_ctx *ctx, const hexopt_slim_params *p) {
   if (rc) return rc;
   for (int m = 0; m < ctx->n_meshes; m++) {
     MeshScalars &S = ctx->sc[m];
-    S.M = p->weight_opt;
-    S.prox = 0.00001 * p->weight_opt;  // slim_m.cpp:1118
+    S.M = p->variant == 1 ? p->weight_opt / 2 : p->weight_opt;  // igl/slim.cpp:1243-1246 halves M
+    S.prox = 0.00001 * p->weight_opt;  // slim_m.cpp:1118, igl/slim.cpp:1240
     S.exp_f = p->exp_factor;
     S.status = 0;
     S.frozen = 0;
@@ -1165,6 +1169,23 @@ int hexopt_slim_m_opt(hexopt_ctx *ctx, const hexopt_slim_params *p, int iters, h
   int rc = hexopt_slim_precompute(ctx, p);
   if (rc) return rc;
   return hexopt_slim_iterate(ctx, iters, rep);
+}
+
+int hexopt_smoothing(hexopt_ctx *ctx, const hexopt_slim_params *params, int outer, int inner,
+                     hexopt_slim_report *rep) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!params || outer < 0 || inner < 0) return fail(ctx, HEXOPT_ERR_ARG, "smoothing: bad arguments");
+  hexopt_slim_params p = *params;
+  p.variant = 1;
+  p.cube = 1;
+  for (int o = 0; o < outer; o++) {
+    rc = hexopt_slim_precompute(ctx, &p);  // compute_referenceMesh(ts.V, ..., true) + slim_precompute
+    if (rc) return rc;
+    rc = hexopt_slim_iterate(ctx, inner, rep);
+    if (rc) return rc;
+  }
+  return HEXOPT_OK;
 }
 
 int hexopt_get_curve_params(hexopt_ctx *ctx, double *a_L) {

@@ -32,7 +32,7 @@ class Quality(C.Structure):
 class SlimParams(C.Structure):
     _fields_ = [("energy", C.c_int), ("precision", C.c_int), ("weight_opt", C.c_double),
                 ("exp_factor", C.c_double), ("cg_max_iter", C.c_int), ("cg_tol", C.c_double),
-                ("ls_candidates", C.c_int), ("cube", C.c_int), ("cg_refine", C.c_int)]
+                ("ls_candidates", C.c_int), ("cube", C.c_int), ("cg_refine", C.c_int), ("variant", C.c_int)]
 
 
 class SlimReport(C.Structure):
@@ -95,6 +95,7 @@ SIGNATURES = {
     "hexopt_slim_iterate": (C.c_int, [_vp, C.c_int, C.POINTER(SlimReport)]),
     "hexopt_slim_m_opt": (C.c_int, [_vp, C.POINTER(SlimParams), C.c_int, C.POINTER(SlimReport)]),
     "hexopt_get_curve_params": (C.c_int, [_vp, _d]),
+    "hexopt_smoothing": (C.c_int, [_vp, C.POINTER(SlimParams), C.c_int, C.c_int, C.POINTER(SlimReport)]),
     "hexopt_set_target": (C.c_int, [_vp, C.c_int, C.c_int64, _d, C.c_int64, _i32]),
     "hexopt_signed_distance": (C.c_int, [_vp, C.c_int, C.c_int64, _d, _d, _i32, _d, _d]),
     "hexopt_set_feature_sets": (C.c_int, [_vp, _i64, _i32, _i64, _i32, _i32, _i64, _i64, _i32, _u8]),
@@ -329,9 +330,9 @@ class Context:
 
     @staticmethod
     def params(precision=FP64, weight_opt=0.001, energy=SYMMETRIC_DIRICHLET, exp_factor=1.0, cg_max_iter=20,
-               cg_tol=1e-8, ls_candidates=4, cube=1, cg_refine=10):
+               cg_tol=1e-8, ls_candidates=4, cube=1, cg_refine=10, variant=0):
         return SlimParams(energy, precision, weight_opt, exp_factor, cg_max_iter, cg_tol, ls_candidates, cube,
-                          cg_refine)
+                          cg_refine, variant)
 
     def slim_m_opt(self, iters, **kw):
         p = self.params(**kw)
@@ -346,6 +347,13 @@ class Context:
     def slim_iterate(self, iters):
         rep = (SlimReport * self.n_meshes)()
         self._ck(self.L.hexopt_slim_iterate(self.h, int(iters), rep), "slim_iterate")
+        return [_rep(r) for r in rep]
+
+    def smoothing(self, outer=3, inner=5, **kw):
+        """The smoothing stage: outer rounds of cube shapes + inner modified-igl::slim iterations."""
+        p = self.params(**kw)
+        rep = (SlimReport * self.n_meshes)()
+        self._ck(self.L.hexopt_smoothing(self.h, C.byref(p), int(outer), int(inner), rep), "smoothing")
         return [_rep(r) for r in rep]
 
     def curve_params(self, total):

@@ -90,6 +90,9 @@ typedef struct hexopt_slim_params {
   int cg_refine;       /* HEXOPT_MIXED only: FP32 PCG iterations between residual replacements, where
                           the accumulated update moves to FP64 and the residual b - A x is
                           re-evaluated from the FP64 positions; <= 0 selects 10 (ignored in FP64) */
+  int variant;         /* 0: the reference's slim_m SLIM (optimization::slim_m_opt); 1: its modified
+                          igl::slim (optimization::slim_opt_igl, extern/libigl/include/igl/
+                          slim.cpp:1190-1288), whose per-tet weight is weight_opt / 2 (:1243-1246) */
 } hexopt_slim_params;
 
 typedef struct hexopt_slim_report {
@@ -219,6 +222,14 @@ HEXOPT_API int hexopt_slim_iterate(hexopt_ctx *ctx, int iters, hexopt_slim_repor
 HEXOPT_API int hexopt_slim_m_opt(hexopt_ctx *ctx, const hexopt_slim_params *params, int iters, hexopt_slim_report *rep);
 /* curve parameters a_L after the last solve (sum of nL) */
 HEXOPT_API int hexopt_get_curve_params(hexopt_ctx *ctx, double *a_L);
+
+/* The smoothing stage (grid_hex_meshing.cpp:2979-3056): `outer` rounds (3 in the reference) of
+ * cube reference shapes at the current positions and `inner` (5) iterations of the modified
+ * igl::slim (optimization::slim_opt_igl, optimization.cpp:970-1005; params.variant is taken as 1,
+ * cube as 1) with whatever soft constraints are set (the stage itself sets none).  rep: the last
+ * round's report per mesh, or NULL. */
+HEXOPT_API int hexopt_smoothing(hexopt_ctx *ctx, const hexopt_slim_params *params, int outer, int inner,
+                                hexopt_slim_report *rep);
 
 /* ---- closest point on a target triangle mesh ----
  * Target of mesh m: triangles TF over TV (mesh-local ids), built into a GPU LBVH with the face,

@@ -114,7 +114,8 @@ class SlimProblem:
 
     def __init__(self, V, H, UV=None, h_flag=None, cube=True, energy=SYMMETRIC_DIRICHLET, weight_opt=0.001,
                  exp_factor=1.0, ids_C=None, C_=None, lamda_C=0.0, ids_T=None, normal_T=None, dis_T=None,
-                 lamda_T=0.0, ids_L=None, Axa_L=None, origin_L=None, lamda_L=0.0):
+                 lamda_T=0.0, ids_L=None, Axa_L=None, origin_L=None, lamda_L=0.0, b=None, bc=None,
+                 lamda_projection=0.0):
         self.V = _f64(V)
         self.UV = _f64(V if UV is None else UV)
         self.H = np.ascontiguousarray(H, dtype=np.uint32)
@@ -131,6 +132,9 @@ class SlimProblem:
         self.Axa_L = _f64(e3 if Axa_L is None else Axa_L).reshape(-1, 3)
         self.origin_L = _f64(e3 if origin_L is None else origin_L).reshape(-1, 3)
         self.lamda_C, self.lamda_T, self.lamda_L = lamda_C, lamda_T, lamda_L
+        self.b = None if b is None else np.ascontiguousarray(b, dtype=np.int32)
+        self.bc = None if bc is None else _f64(bc).reshape(-1, 3)
+        self.lamda_projection = lamda_projection
 
     def struct(self):
         s = orc_slim_problem()
@@ -143,6 +147,9 @@ class SlimProblem:
         s.nL, s.ids_L, s.Axa_L, s.origin_L, s.lamda_L = (len(self.ids_L), _p(self.ids_L, _i32), _p(self.Axa_L, _d),
                                                          _p(self.origin_L, _d), self.lamda_L)
         s.projection, s.nB = 0, 0
+        if self.b is not None:
+            s.projection, s.nB, s.b, s.bc = 1, len(self.b), _p(self.b, _i32), _p(self.bc, _d)
+            s.lamda_projection = self.lamda_projection
         return s
 
 

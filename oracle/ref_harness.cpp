@@ -206,6 +206,99 @@ int ref_pipeline2(int64_t nv, const double *V, int64_t nh, const uint32_t *H, co
   return 0;
 }
 
+// optimization::slim_m_opt(ts, iters, -1) with the projection term on (ts.projection, ts.b /
+// ts.bc, lamda_projection; add_soft_constraints slim_m.cpp:600-610) and no feature constraints.
+int ref_slim_m_opt_proj(int64_t nv, const double *V, int64_t nh, const uint32_t *H, double weight_opt, int64_t nB,
+                        const int32_t *b, const double *bc, double lamda_projection, int iters, double *V_o,
+                        double *out3) {
+  Tetralize_Set ts;
+  ts.V.resize(nv, 3);
+  for (int64_t i = 0; i < nv; i++)
+    for (int d = 0; d < 3; d++) ts.V(i, d) = V[3 * i + d];
+  ts.T.resize(8 * nh, 4);
+  for (int64_t h = 0; h < nh; h++)
+    for (int k = 0; k < 8; k++)
+      for (int j = 0; j < 4; j++) ts.T(8 * h + k, j) = H[8 * h + hex_tetra_table[k][j]];
+  Mesh m = make_hex_mesh(nv, V, nh, H);
+  std::vector<bool> hf(nh, true);
+  std::vector<uint32_t> Hids(nh);
+  for (int64_t h = 0; h < nh; h++) Hids[h] = (uint32_t)h;
+  ts.b.resize(nB);
+  ts.bc.resize(nB, 3);
+  for (int64_t i = 0; i < nB; i++) {
+    ts.b[i] = b[i];
+    for (int d = 0; d < 3; d++) ts.bc(i, d) = bc[3 * i + d];
+  }
+  ts.regionb.resize(0);
+  ts.regionbc.resize(0, 3);
+  ts.energy_type = SYMMETRIC_DIRICHLET;
+  ts.UV = ts.V;
+  ts.projection = true;
+  ts.lamda_projection = lamda_projection;
+  ts.global = true;
+  ts.glue = false;
+  ts.lamda_glue = 0;
+  ts.fc.lamda_C = ts.fc.lamda_T = ts.fc.lamda_L = 0;
+  compute_referenceMesh(ts.UV, m.Hs, hf, Hids, ts.RT, true);
+  optimization opt;
+  opt.weight_opt = weight_opt;
+  opt.slim_m_opt(ts, (uint32_t)iters, -1);
+  for (int64_t i = 0; i < nv; i++)
+    for (int d = 0; d < 3; d++) V_o[3 * i + d] = ts.UV(i, d);
+  out3[0] = opt.energy;
+  out3[1] = opt.engery_quality;
+  out3[2] = opt.engery_soft;
+  return 0;
+}
+
+// The smoothing stage (grid_hex_meshing.cpp:2979-3056) on a hex mesh: `outer` rounds of
+// compute_referenceMesh(ts.V, ..., cube = true) and optimization::slim_opt_igl(ts, inner)
+// (optimization.cpp:970-1005, the modified igl::slim: M = weight_opt / 2), with the stage's empty
+// feature constraints.  out3 = {igl energy / mesh_area of the last solve (printed), min_J, ave_J}.
+int ref_smoothing(int64_t nv, const double *V, int64_t nh, const uint32_t *H, double weight_opt, int outer,
+                  int inner, double *V_out, double *out3) {
+  Mesh m = make_hex_mesh(nv, V, nh, H);
+  Tetralize_Set ts;
+  ts.V.resize(nv, 3);
+  for (int64_t i = 0; i < nv; i++)
+    for (int d = 0; d < 3; d++) ts.V(i, d) = V[3 * i + d];
+  ts.T.resize(8 * nh, 4);
+  for (int64_t h = 0; h < nh; h++)
+    for (int k = 0; k < 8; k++)
+      for (int j = 0; j < 4; j++) ts.T(8 * h + k, j) = H[8 * h + hex_tetra_table[k][j]];
+  Feature_Constraints fc;
+  fc.lamda_C = fc.lamda_L = fc.lamda_T = 0;
+  ts.energy_type = SYMMETRIC_DIRICHLET;
+  ts.UV = ts.V;
+  ts.fc = fc;
+  ts.projection = false;
+  ts.global = true;
+  ts.glue = false;
+  ts.lamda_glue = 0;
+  ts.lamda_region = 0;
+  ts.b.resize(0);
+  ts.bc.resize(0, 3);
+  ts.lamda_b = 0;
+  optimization opt;
+  opt.weight_opt = weight_opt;
+  std::vector<bool> inout(nh, true);
+  std::vector<uint32_t> Hids(nh);
+  for (int64_t h = 0; h < nh; h++) Hids[h] = (uint32_t)h;
+  for (int i = 0; i < outer; i++) {
+    compute_referenceMesh(ts.V, m.Hs, inout, Hids, ts.RT, true);
+    opt.slim_opt_igl(ts, (uint32_t)inner);
+    m.V = ts.V.transpose();
+  }
+  for (int64_t i = 0; i < nv; i++)
+    for (int d = 0; d < 3; d++) V_out[3 * i + d] = ts.V(i, d);
+  Mesh_Quality mq;
+  scaled_jacobian(m, mq);
+  out3[0] = 0;
+  out3[1] = mq.min_Jacobian;
+  out3[2] = mq.ave_Jacobian;
+  return 0;
+}
+
 // Per-tet energies at positions X with the operator of slim_precompute at V
 // (compute_energy_with_jacobians), used to pin the per-element energy.
 int ref_tet_energy(int64_t nv, const double *V, const double *X, int64_t nh, const uint32_t *H, int energy_type,

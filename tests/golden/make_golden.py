@@ -5,7 +5,7 @@ reference's OWN FP64 code (oracle/_ref/libhexopt_ref.so, built from the referenc
     make -C oracle ref && python tests/golden/make_golden.py [group ...]
 
 Writes tests/golden/*.npz (every group when none is named; groups: base, energies, shapes,
-untangle).  The
+untangle, smoothing, projection).  The
 fixtures are committed; the reference build is not.
 """
 from __future__ import annotations
@@ -153,7 +153,45 @@ def untangle():
         print(name, out, "spread", spread, jspread)
 
 
+def smoothing():
+    """The smoothing stage: 3 rounds of cube reference shapes + 5 iterations of the modified
+    igl::slim (slim_opt_igl, M = weight_opt / 2), no soft constraints."""
+    R = O.ref()
+    R.ref_smoothing.argtypes = [C.c_int64, _d, C.c_int64, _u32, C.c_double, C.c_int, C.c_int, _d, _d]
+    V, H, _ = jittered_grid(5, 0.15, 90)
+    Vo = np.empty_like(V)
+    out = np.empty(3)
+    R.ref_smoothing(len(V), p(V, _d), len(H), p(H, _u32), 1.0, 3, 5, p(Vo, _d), p(out, _d))
+    np.savez_compressed(os.path.join(HERE, "smoothing.npz"), V=V, H=H, weight_opt=1.0, outer=3, inner=5, V_o=Vo,
+                        out=out)
+    print("smoothing", out)
+
+
+def projection():
+    """slim_m_opt with the projection term (ts.projection, b / bc, lamda_projection) on a
+    jittered grid: the boundary vertices pulled onto a sphere-ish target, 2 iterations."""
+    R = O.ref()
+    R.ref_slim_m_opt_proj.argtypes = [C.c_int64, _d, C.c_int64, _u32, C.c_double, C.c_int64, _i32, _d, C.c_double,
+                                      C.c_int, _d, _d]
+    V, H, b = jittered_grid(4, 0.1, 95)
+    ids = np.ascontiguousarray(np.nonzero(b)[0][::2].astype(np.int32))
+    c = np.array([0.5, 0.5, 0.5])
+    nrm = V[ids] - c
+    bc = np.ascontiguousarray(c + nrm * (0.6 / np.linalg.norm(nrm, axis=1))[:, None])
+    Vo = np.empty_like(V)
+    out = np.empty(3)
+    R.ref_slim_m_opt_proj(len(V), p(V, _d), len(H), p(H, _u32), 0.001, len(ids), p(ids, _i32), p(bc, _d), 1e3, 2,
+                          p(Vo, _d), p(out, _d))
+    np.savez_compressed(os.path.join(HERE, "slim_projection.npz"), V=V, H=H, b=ids, bc=bc, lamda_projection=1e3,
+                        weight_opt=0.001, iters=2, V_o=Vo, out=out)
+    print("projection", out)
+
+
 def main(groups):
+    if "projection" in groups:
+        projection()
+    if "smoothing" in groups:
+        smoothing()
     if "untangle" in groups:
         untangle()
     if "energies" in groups:
@@ -253,4 +291,4 @@ def base():
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["base", "energies", "shapes", "untangle"])
+    main(sys.argv[1:] or ["base", "energies", "shapes", "untangle", "smoothing", "projection"])

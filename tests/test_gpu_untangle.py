@@ -1,4 +1,4 @@
-"""The untangling path against the reference's own optimization::pipeline2 (tests/golden/
+"""The untangling and smoothing stages against the reference's own optimization::pipeline2 (tests/golden/
 untangle_*.npz, made by oracle/_ref): rigidDeformCubes, then the adaptive gluing solve of
 glueInternalNodes -- per-hex vertex copies, boundary copies held, glue weight schedule of
 slim_solve2, CONFORMAL energy, edge-averaged cuboid reference shapes -- until the glued mesh's
@@ -61,3 +61,37 @@ def test_untangle_batch_equals_individual_runs(hx):
         assert r["success"] == bool(z["out"][0])
         assert np.abs(Vb[off:off + n] - z["V_o"]).max() <= 1e-6 * diag_of(z["V"])
         off += n
+
+
+def test_smoothing_matches_reference(hx):
+    """The smoothing stage (3 rounds of cube shapes + 5 iterations of the modified igl::slim,
+    M = weight_opt / 2) against the reference's own slim_opt_igl loop."""
+    z = load_golden("smoothing")
+    ctx = hx.Context(0)
+    try:
+        ctx.upload([(z["V"], z["H"])])
+        ctx.smoothing(int(z["outer"]), int(z["inner"]), weight_opt=float(z["weight_opt"]), precision=hx.FP64)
+        Vg = ctx.get_positions()
+        q = ctx.scaled_jacobian()[2][0]
+    finally:
+        ctx.close()
+    err = np.abs(Vg - z["V_o"]).max() / diag_of(z["V"])
+    print(f"\n[smoothing] max|dX|/diag {err:.3e}  minJ {q['min']:.8f}/{z['out'][1]:.8f}")
+    assert err <= 1e-6
+    assert abs(q["min"] - z["out"][1]) <= 1e-6
+
+
+def test_projection_term_matches_reference(hx):
+    """Tetralize_Set::projection with lamda_projection 1e3 against the reference's slim_m_opt."""
+    z = load_golden("slim_projection")
+    ctx = hx.Context(0)
+    try:
+        ctx.upload([(z["V"], z["H"])])
+        ctx.set_projection([z["b"]], [z["bc"]], float(z["lamda_projection"]))
+        rep = ctx.slim_m_opt(int(z["iters"]), precision=hx.FP64, weight_opt=float(z["weight_opt"]))
+        Vg = ctx.get_positions()
+    finally:
+        ctx.close()
+    err = np.abs(Vg - z["V_o"]).max() / diag_of(z["V"])
+    assert err <= 1e-6, err
+    np.testing.assert_allclose([rep[0]["energy"], rep[0]["energy_quality"], rep[0]["energy_soft"]], z["out"], rtol=1e-6)

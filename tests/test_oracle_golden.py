@@ -89,6 +89,17 @@ def test_slim_energies_match_reference(oracle, energy):
     np.testing.assert_allclose([info["energy"], info["energy_quality"], info["energy_soft"]], z["out"], rtol=1e-10)
 
 
+def test_projection_term_matches_reference(oracle):
+    """Tetralize_Set::projection: lamda_projection |x_b - bc|^2 (slim_m.cpp:600-610, 740-745)."""
+    z = load_golden("slim_projection")
+    prob = oracle.SlimProblem(z["V"], z["H"], weight_opt=float(z["weight_opt"]), b=z["b"], bc=z["bc"],
+                              lamda_projection=float(z["lamda_projection"]))
+    Vo, aL, info = oracle.slim_m_opt(prob, int(z["iters"]))
+    diag = np.linalg.norm(z["V"].max(0) - z["V"].min(0))
+    assert np.abs(Vo - z["V_o"]).max() <= 1e-11 * diag
+    np.testing.assert_allclose([info["energy"], info["energy_quality"], info["energy_soft"]], z["out"], rtol=1e-10)
+
+
 @pytest.mark.parametrize("name", ["signed_distance", "signed_distance_cyl"])
 def test_signed_distance_pseudonormal_matches_reference(oracle, name):
     z = load_golden(name)
