@@ -206,8 +206,11 @@ def run_ours(args):
     from hexopt import workloads
     precision = hexopt.MIXED if args.precision == "mixed" else hexopt.FP64
     p = workloads.grid_superellipsoid(args.grid, seed=rank)
+    if args.shuffle:
+        p = shuffle_numbering(p, seed=rank)
     nv, nh = len(p["V"]), len(p["H"])
     ctx = hexopt.Context(local)
+    ctx.set_ordering(0 if args.no_morton else 2)
     workloads.load(ctx, [p])
     ctx.fa_begin(lamda0=0.05, precision=precision, weight_opt=0.001)
     tune = ctx.autotune() if not args.no_autotune else None
@@ -300,7 +303,10 @@ def run_ours(args):
            "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
            "config": {"workload": f"grid{args.grid}_superellipsoid: {nh} hexes, {nv} vertices, 200k-triangle "
                                   f"superellipsoid target (float32 coords), Gaussian jitter 0.2h seed {rank}; "
-                                  f"{'mixed FP32/FP64' if mixed else 'plain FP64'}; Hausdorff every iteration "
+                                  f"{'mixed FP32/FP64' if mixed else 'plain FP64'}; "
+                                  f"{'randomly renumbered vertices and hexes; ' if args.shuffle else ''}"
+                                  f"{'caller order on the device' if args.no_morton else 'device order: Morton unless the numbering is coherent'}; "
+                                  f"Hausdorff every iteration "
                                   f"{'on' if do_h else 'off'}; CUDA-graph replay per step",
                       "hexes": nh, "vertices": nv, "replicas": ws,
                       "l2": "inputs larger than L2 (per-tet coefficients and positions exceed 129 MB)",
@@ -325,6 +331,21 @@ def run_ours(args):
     if rank == 0:
         print(json.dumps(out))
     return 0
+
+
+def shuffle_numbering(p, seed=0):
+    """The workload with its vertices and hexes renumbered at random (ids remapped): the numbering
+    an unstructured mesher may hand over."""
+    rng = np.random.default_rng(seed)
+    nv, nh = len(p["V"]), len(p["H"])
+    vp = rng.permutation(nv)
+    inv = np.empty(nv, np.int64)
+    inv[vp] = np.arange(nv)
+    hp = rng.permutation(nh)
+    q = dict(p, V=p["V"][vp], H=inv[p["H"][hp].astype(np.int64)].astype(np.uint32))
+    for k in ("regular", "lines", "corners", "surface"):
+        q[k] = inv[np.asarray(p[k], np.int64)].astype(np.int32)
+    return q
 
 
 def run_c2(args):
@@ -577,6 +598,9 @@ def main():
                          "workload (run with --steps 50); batch: the batching workload; adjoint: the "
                          "differentiation workload")
     ap.add_argument("--batch", type=int, default=256, help="meshes in the batching workload")
+    ap.add_argument("--shuffle", action="store_true", help="renumber the grid's vertices and hexes at random")
+    ap.add_argument("--no-morton", action="store_true",
+                    help="keep the caller's numbering on the device (default: Morton order unless it is coherent)")
     ap.add_argument("--fd-coords", type=int, default=1000, help="coordinates of the adjoint's FD check")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup

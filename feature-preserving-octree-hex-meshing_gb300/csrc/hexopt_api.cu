@@ -133,6 +133,11 @@ struct hexopt_ctx {
   DBuf b_ids, b_pos, g_ptr, g_vs, vfix, Xm;
   std::vector<uint8_t> fixed_h;  // host copy of the held-vertex flags (for argument checks)
   std::vector<uint32_t> H_h;     // host copy of the hexes (mesh-local corner ids), for untangling
+  // device order of the batch (Morton-sorted vertices and hexes); the caller's order at the ABI
+  int ordering = 2;  // 0 caller order, 1 Morton, 2 Morton unless the caller's numbering is coherent
+  bool ordered = false;
+  DBuf vnew2old, vold2new, hnew2old, hold2new;
+  std::vector<int32_t> vold2new_h, hnew2old_h;
   bool has_fixed = false, has_glue = false;
   KindTable kind[8];
   // items per block: hex 128, unknowns 256 x ipt, constraints 256, queries 128
@@ -195,6 +200,50 @@ int fail(hexopt_ctx *c, int code, const char *fmt, ...) {
     if (e_ != cudaSuccess)                                                                    \
       return fail(ctx, HEXOPT_ERR_CUDA, "launch: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, __LINE__); \
   } while (0)
+
+}  // namespace
+
+// Whether the caller's numbering already keeps neighbouring hexes' corners close in memory: in
+// every mesh, the median over hexes of the corner-id span (max - min) and the median jump of the
+// first corner between consecutive hexes both stay within 4 nv^(2/3) -- a 3-D coherent numbering
+// (a structured grid's rows, planes) spans about one plane, nv^(2/3); a random one about nv.
+static bool numbering_coherent(const hexopt_ctx *c, int n_meshes, const int64_t *nv, const int64_t *nh, const uint32_t *H) {
+  int64_t ho = 0;
+  for (int m = 0; m < n_meshes; m++) {
+    const double lim = 4.0 * std::cbrt((double)nv[m] * (double)nv[m]);
+    std::vector<uint32_t> span(nh[m]), jump(nh[m] > 1 ? nh[m] - 1 : 1, 0);
+    for (int64_t h = 0; h < nh[m]; h++) {
+      const uint32_t *q = H + 8 * (ho + h);
+      uint32_t lo = q[0], hi = q[0];
+      for (int k = 1; k < 8; k++) { lo = std::min(lo, q[k]); hi = std::max(hi, q[k]); }
+      span[h] = hi - lo;
+      if (h > 0) {
+        const uint32_t a = q[0], b = H[8 * (ho + h - 1)];
+        jump[h - 1] = a > b ? a - b : b - a;
+      }
+    }
+    std::nth_element(span.begin(), span.begin() + span.size() / 2, span.end());
+    std::nth_element(jump.begin(), jump.begin() + jump.size() / 2, jump.end());
+    if (span[span.size() / 2] > lim || jump[jump.size() / 2] > lim) return false;
+    ho += nh[m];
+  }
+  (void)c;
+  return true;
+}
+
+// device order <-> caller order
+static const int32_t *vn2o(const hexopt_ctx *c) { return c->ordered ? c->vnew2old.as<int32_t>() : nullptr; }
+static const int32_t *vo2n(const hexopt_ctx *c) { return c->ordered ? c->vold2new.as<int32_t>() : nullptr; }
+static const int32_t *hn2o(const hexopt_ctx *c) { return c->ordered ? c->hnew2old.as<int32_t>() : nullptr; }
+static const int32_t *ho2n(const hexopt_ctx *c) { return c->ordered ? c->hold2new.as<int32_t>() : nullptr; }
+// a caller's mesh-local vertex id -> the device's mesh-local id
+static int32_t local_vid(const hexopt_ctx *c, int m, int32_t v) {
+  if (!c->ordered) return v;
+  const int64_t o = c->md[m].v_off;
+  return (int32_t)(c->vold2new_h[o + v] - o);
+}
+
+namespace {
 
 template <typename T>
 cudaError_t upload(DBuf &buf, const T *src, size_t n, cudaStream_t st) {
@@ -775,6 +824,13 @@ int64_t hexopt_num_hexes(const hexopt_ctx *ctx) { return ctx ? ctx->NH : 0; }
 int hexopt_num_meshes(const hexopt_ctx *ctx) { return ctx ? ctx->n_meshes : 0; }
 int64_t hexopt_launch_count(const hexopt_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+int hexopt_set_ordering(hexopt_ctx *ctx, int mode) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  if (mode < 0 || mode > 2) return fail(ctx, HEXOPT_ERR_ARG, "set_ordering: mode must be 0, 1 or 2");
+  ctx->ordering = mode;
+  return HEXOPT_OK;
+}
+
 int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const int64_t *nh, const double *V,
                          const uint32_t *H, const uint8_t *h_flag) {
   if (!ctx) return HEXOPT_ERR_ARG;
@@ -816,42 +872,79 @@ int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const
   ctx->fa_ready = false;
   ctx->haus_ready = false;
   if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
-  // own-shape slots
-  std::vector<int32_t> gs(NH, -1);
-  int64_t ng = 0;
-  if (h_flag)
-    for (int64_t h = 0; h < NH; h++)
-      if (!h_flag[h]) gs[h] = (int32_t)ng++;
-  ctx->NG = ng;
   int64_t vo = 0, ho = 0;
   for (int m = 0; m < n_meshes; m++) {
     ctx->md[m].v_off = vo; ctx->md[m].nv = nv[m];
     ctx->md[m].h_off = ho; ctx->md[m].nh = nh[m];
     vo += nv[m]; ho += nh[m];
   }
-  // positions
   CK(upload(ctx->stage, V, (size_t)NV * 3, ctx->st));
-  CK(ctx->X.ensure(sizeof(double) * 4 * NV));
-  CK(ctx->X32.ensure(sizeof(float) * 8 * NV));
-  launch_rows_to_aos4(ctx->stage.as<double>(), ctx->X.as<double>(), NV, ctx->st);
-  launch_split_pos(ctx->X.as<double>(), ctx->X32.as<float>(), NV, ctx->st);
-  ctx->launches += 1;
-  // hexes -> AoSoA with global ids
-  const int64_t NHp = (NH + 31) / 32 * 32;
   ctx->H_h.assign(H, H + (size_t)NH * 8);
   CK(upload(ctx->stage2, H, (size_t)NH * 8, ctx->st));
+  CK(ctx->X.ensure(sizeof(double) * 4 * NV));
+  CK(ctx->X32.ensure(sizeof(float) * 8 * NV));
+  const int64_t NHp = (NH + 31) / 32 * 32;
   CK(ctx->hexv.ensure(sizeof(uint32_t) * 8 * NHp));
   CK(cudaMemsetAsync(ctx->hexv.p, 0, sizeof(uint32_t) * 8 * NHp, ctx->st));
-  for (int m = 0; m < n_meshes; m++)
-    launch_hex_to_aosoa_mesh(ctx->stage2.as<uint32_t>() + 8 * ctx->md[m].h_off, ctx->md[m].h_off, nh[m],
-                             (uint32_t)ctx->md[m].v_off, ctx->hexv.as<uint32_t>(), ctx->st);
-  ctx->launches += 1 + n_meshes;
-  CK(upload(ctx->gslot, gs.data(), gs.size(), ctx->st));
-  {
-    std::vector<uint8_t> hf(NH, 1);
-    if (h_flag) std::copy(h_flag, h_flag + NH, hf.begin());
-    CK(upload(ctx->hflag_d, hf.data(), hf.size(), ctx->st));
+  ctx->ordered = ctx->ordering == 1 || (ctx->ordering == 2 && !numbering_coherent(ctx, n_meshes, nv, nh, H));
+  ctx->vold2new_h.clear();
+  ctx->hnew2old_h.clear();
+  if (ctx->ordered) {
+    // Morton order of every mesh's vertices and hexes inside its bounding box (device sort)
+    std::vector<double> box(6 * n_meshes);
+    std::vector<int64_t> voff(n_meshes + 1), hoff(n_meshes + 1);
+    for (int m = 0; m < n_meshes; m++) {
+      double *b = &box[6 * m];
+      for (int d = 0; d < 3; d++) { b[d] = INFINITY; b[3 + d] = -INFINITY; }
+      for (int64_t v = ctx->md[m].v_off; v < ctx->md[m].v_off + nv[m]; v++)
+        for (int d = 0; d < 3; d++) { b[d] = std::min(b[d], V[3 * v + d]); b[3 + d] = std::max(b[3 + d], V[3 * v + d]); }
+      voff[m] = ctx->md[m].v_off;
+      hoff[m] = ctx->md[m].h_off;
+    }
+    voff[n_meshes] = NV;
+    hoff[n_meshes] = NH;
+    DBuf box_d, voff_d, hoff_d, scratch;
+    CK(upload(box_d, box.data(), box.size(), ctx->st));
+    CK(upload(voff_d, voff.data(), voff.size(), ctx->st));
+    CK(upload(hoff_d, hoff.data(), hoff.size(), ctx->st));
+    CK(ctx->vnew2old.ensure(sizeof(int32_t) * NV));
+    CK(ctx->vold2new.ensure(sizeof(int32_t) * NV));
+    CK(ctx->hnew2old.ensure(sizeof(int32_t) * NH));
+    CK(ctx->hold2new.ensure(sizeof(int32_t) * NH));
+    const size_t sb = order_scratch_bytes(NV, NH);
+    CK(scratch.ensure(sb));
+    CK(order_batch(ctx->stage.as<double>(), ctx->stage2.as<uint32_t>(), NV, NH, voff_d.as<int64_t>(), hoff_d.as<int64_t>(),
+                   n_meshes, box_d.as<double>(), ctx->vnew2old.as<int32_t>(), ctx->vold2new.as<int32_t>(),
+                   ctx->hnew2old.as<int32_t>(), ctx->hold2new.as<int32_t>(), scratch.p, sb, ctx->st));
+    launch_rows_to_aos4_perm(ctx->stage.as<double>(), ctx->vnew2old.as<int32_t>(), NV, ctx->X.as<double>(), ctx->st);
+    launch_hex_perm(ctx->stage2.as<uint32_t>(), ctx->hnew2old.as<int32_t>(), ctx->vold2new.as<int32_t>(), NH,
+                    hoff_d.as<int64_t>(), voff_d.as<int64_t>(), n_meshes, ctx->hexv.as<uint32_t>(), ctx->st);
+    ctx->vold2new_h.resize(NV);
+    ctx->hnew2old_h.resize(NH);
+    CK(cudaMemcpyAsync(ctx->vold2new_h.data(), ctx->vold2new.p, sizeof(int32_t) * NV, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(ctx->hnew2old_h.data(), ctx->hnew2old.p, sizeof(int32_t) * NH, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));  // the scratch buffers go out of scope
+    ctx->launches += 8;
+  } else {
+    launch_rows_to_aos4(ctx->stage.as<double>(), ctx->X.as<double>(), NV, ctx->st);
+    for (int m = 0; m < n_meshes; m++)
+      launch_hex_to_aosoa_mesh(ctx->stage2.as<uint32_t>() + 8 * ctx->md[m].h_off, ctx->md[m].h_off, nh[m],
+                               (uint32_t)ctx->md[m].v_off, ctx->hexv.as<uint32_t>(), ctx->st);
+    ctx->launches += 1 + n_meshes;
   }
+  launch_split_pos(ctx->X.as<double>(), ctx->X32.as<float>(), NV, ctx->st);
+  ctx->launches += 1;
+  // own-shape slots and h_flag, in the device's hex order
+  std::vector<int32_t> gs(NH, -1);
+  std::vector<uint8_t> hf(NH, 1);
+  int64_t ng = 0;
+  for (int64_t h = 0; h < NH; h++) {
+    const int64_t o = ctx->ordered ? ctx->hnew2old_h[h] : h;
+    if (h_flag && !h_flag[o]) { gs[h] = (int32_t)ng++; hf[h] = 0; }
+  }
+  ctx->NG = ng;
+  CK(upload(ctx->gslot, gs.data(), gs.size(), ctx->st));
+  CK(upload(ctx->hflag_d, hf.data(), hf.size(), ctx->st));
   ctx->has_ref_p8 = false;
   ctx->rest_fixed = false;
   CK(ctx->counters.ensure(sizeof(unsigned) * n_meshes));
@@ -870,7 +963,7 @@ int hexopt_set_positions(hexopt_ctx *ctx, const double *V) {
   if (rc) return rc;
   if (!V) return fail(ctx, HEXOPT_ERR_ARG, "set_positions: NULL");
   CK(upload(ctx->stage, V, (size_t)ctx->NV * 3, ctx->st));
-  launch_rows_to_aos4(ctx->stage.as<double>(), ctx->X.as<double>(), ctx->NV, ctx->st);
+  launch_rows_to_aos4_perm(ctx->stage.as<double>(), vn2o(ctx), ctx->NV, ctx->X.as<double>(), ctx->st);
   launch_split_pos(ctx->X.as<double>(), ctx->X32.as<float>(), ctx->NV, ctx->st);
   ctx->launches += 2;
   CKL();
@@ -882,7 +975,7 @@ int hexopt_get_positions(hexopt_ctx *ctx, double *V) {
   if (rc) return rc;
   if (!V) return fail(ctx, HEXOPT_ERR_ARG, "get_positions: NULL");
   CK(ctx->stage.ensure(sizeof(double) * 3 * ctx->NV));
-  launch_aos4_to_rows(ctx->X.as<double>(), ctx->stage.as<double>(), ctx->NV, ctx->st);
+  launch_aos4_to_rows_perm(ctx->X.as<double>(), vo2n(ctx), ctx->NV, ctx->stage.as<double>(), ctx->st);
   ctx->launches++;
   CK(cudaMemcpyAsync(V, ctx->stage.p, sizeof(double) * 3 * ctx->NV, cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
@@ -901,8 +994,16 @@ int hexopt_scaled_jacobian(hexopt_ctx *ctx, double *V_Js, double *H_Js, hexopt_q
   launch_scaled_jacobian(a, ctx->kind[K_HEX].nblk, vj, ctx->HJs.as<double>(), ctx->st);
   ctx->launches += 2;
   CKL();
-  if (V_Js) CK(cudaMemcpyAsync(V_Js, vj, sizeof(double) * 8 * ctx->NH, cudaMemcpyDeviceToHost, ctx->st));
-  if (H_Js) CK(cudaMemcpyAsync(H_Js, ctx->HJs.p, sizeof(double) * ctx->NH, cudaMemcpyDeviceToHost, ctx->st));
+  if (V_Js || H_Js) CK(ctx->stage.ensure(sizeof(double) * 8 * ctx->NH));
+  if (V_Js) {  // the caller's hex order
+    launch_gather_rows(vj, ho2n(ctx), ctx->NH, 8, ctx->stage.as<double>(), ctx->st);
+    CK(cudaMemcpyAsync(V_Js, ctx->stage.p, sizeof(double) * 8 * ctx->NH, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  if (H_Js) {
+    launch_gather_rows(ctx->HJs.as<double>(), ho2n(ctx), ctx->NH, 1, ctx->stage.as<double>(), ctx->st);
+    CK(cudaMemcpyAsync(H_Js, ctx->stage.p, sizeof(double) * ctx->NH, cudaMemcpyDeviceToHost, ctx->st));
+  }
   rc = pull_scalars(ctx);
   if (rc) return rc;
   if (q)
@@ -926,7 +1027,14 @@ static int set_list(hexopt_ctx *ctx, const int64_t *counts, std::vector<int64_t>
     tot += counts[m];
   }
   dst.assign(counts, counts + ctx->n_meshes);
-  CK(upload(ids_d, ids, (size_t)tot, ctx->st));
+  std::vector<int32_t> mapped(ids, ids + tot);
+  if (ctx->ordered) {
+    int64_t o = 0;
+    for (int m = 0; m < ctx->n_meshes; m++)
+      for (int64_t i = 0; i < counts[m]; i++, o++) mapped[o] = local_vid(ctx, m, mapped[o]);
+  }
+  CK(upload(ids_d, mapped.data(), (size_t)tot, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));  // the mapped copy goes out of scope
   return HEXOPT_OK;
 }
 
@@ -1010,7 +1118,7 @@ int hexopt_set_glue(hexopt_ctx *ctx, const int64_t *n_groups, const int64_t *gro
         const int32_t v = group_vs[vo + (k - pm[0])];
         if (v < 0 || v >= ctx->md[m].nv) return fail(ctx, HEXOPT_ERR_ARG, "mesh %d: glue vertex id out of range", m);
         if (seen[v]++) return fail(ctx, HEXOPT_ERR_ARG, "mesh %d: vertex %d in two glue groups", m, v);
-        gv.push_back((int32_t)(ctx->md[m].v_off + v));
+        gv.push_back((int32_t)(ctx->md[m].v_off + local_vid(ctx, m, v)));
       }
       gp.push_back((int64_t)gv.size());
     }
@@ -1021,7 +1129,8 @@ int hexopt_set_glue(hexopt_ctx *ctx, const int64_t *n_groups, const int64_t *gro
   ctx->NGR = (int64_t)gp.size() - 1;
   ctx->has_glue = ctx->NGR > 0;
   CK(upload(ctx->g_ptr, gp.data(), gp.size(), ctx->st));
-  CK(upload(ctx->g_vs, gv.data(), std::max<size_t>(gv.size(), 1), ctx->st));
+  if (gv.empty()) gv.push_back(0);
+  CK(upload(ctx->g_vs, gv.data(), gv.size(), ctx->st));
   rc = pull_scalars(ctx);
   if (rc) return rc;
   for (int m = 0; m < ctx->n_meshes; m++) {
@@ -1045,7 +1154,7 @@ int hexopt_set_fixed(hexopt_ctx *ctx, const int64_t *nF, const int32_t *ids) {
     for (int64_t i = 0; i < nF[m]; i++) {
       const int32_t v = ids[tot + i];
       if (v < 0 || v >= ctx->md[m].nv) return fail(ctx, HEXOPT_ERR_ARG, "set_fixed: vertex id out of range");
-      ctx->fixed_h[ctx->md[m].v_off + v] = 1;
+      ctx->fixed_h[ctx->md[m].v_off + local_vid(ctx, m, v)] = 1;
     }
     tot += nF[m];
   }
@@ -1096,7 +1205,9 @@ int hexopt_set_reference_hexes(hexopt_ctx *ctx, const double *P8) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
   if (P8) {
-    CK(upload(ctx->ref_p8, P8, (size_t)ctx->NH * 24, ctx->st));
+    CK(upload(ctx->stage, P8, (size_t)ctx->NH * 24, ctx->st));
+    CK(ctx->ref_p8.ensure(sizeof(double) * 24 * ctx->NH));
+    launch_gather_rows(ctx->stage.as<double>(), hn2o(ctx), ctx->NH, 24, ctx->ref_p8.as<double>(), ctx->st);
     ctx->has_ref_p8 = true;
   } else {
     ctx->has_ref_p8 = false;
@@ -1386,8 +1497,9 @@ int hexopt_set_surface(hexopt_ctx *ctx, int mesh, int64_t nf, const int32_t *F) 
   std::vector<uint8_t> used(nv, 0);
   for (int64_t i = 0; i < 3 * nf; i++) {
     if (F[i] < 0 || F[i] >= nv) return fail(ctx, HEXOPT_ERR_ARG, "set_surface: vertex id out of range");
-    G[i] = (int32_t)(F[i] + vo);
-    used[F[i]] = 1;
+    const int32_t lv = local_vid(ctx, mesh, F[i]);
+    G[i] = (int32_t)(lv + vo);
+    used[lv] = 1;
   }
   SurfaceHost &s = ctx->surf[mesh];
   s.nf = nf;
@@ -1405,7 +1517,7 @@ int hexopt_set_surface(hexopt_ctx *ctx, int mesh, int64_t nf, const int32_t *F) 
   CK(cudaStreamSynchronize(ctx->st));
   for (int64_t f = 0; f < nf; f++)
     for (int c = 0; c < 3; c++)
-      for (int d = 0; d < 3; d++) tri[9 * f + 3 * c + d] = Xh[3 * (int64_t)F[3 * f + c] + d];
+      for (int d = 0; d < 3; d++) tri[9 * f + 3 * c + d] = Xh[3 * (int64_t)(G[3 * f + c] - vo) + d];
   StaticBvh tmp;
   rc = build_static_bvh(ctx, tmp, tri, nf);
   if (rc) return rc;
@@ -1831,7 +1943,7 @@ int hexopt_untangle(hexopt_ctx *ctx, const hexopt_slim_params *params, const uin
   // reference shapes: compute_referenceMesh(BV, mesh.Hs, all true, Hids, ts.RT, false) (:584)
   if ((rc = hexopt_set_reference_hexes(c, Ve.data()))) return sub(rc, "set_reference_hexes");
   // rigidDeformCubes: the starting copies (ts.V = Cubes)
-  launch_rigid_cubes(c->X.as<double>(), c->X32.as<float>(), c->vfix.as<uint8_t>(), c->NH, c->st);
+  launch_rigid_cubes(c->hexv.as<uint32_t>(), c->X.as<double>(), c->X32.as<float>(), c->vfix.as<uint8_t>(), c->NH, c->st);
   c->launches++;
   {
     cudaError_t e = cudaGetLastError();
@@ -1847,7 +1959,7 @@ int hexopt_untangle(hexopt_ctx *ctx, const hexopt_slim_params *params, const uin
   CK(cudaMemcpyAsync(c->Xm.p, c->X.p, sizeof(double) * 4 * c->NV, cudaMemcpyDeviceToDevice, c->st));
   launch_result_positions(a, c->kind[K_CONS].nblk, c->Xm.as<double>(), 1, c->st);
   CK(c->stage.ensure(sizeof(double) * 3 * c->NV));
-  launch_aos4_to_rows(c->Xm.as<double>(), c->stage.as<double>(), c->NV, c->st);
+  launch_aos4_to_rows_perm(c->Xm.as<double>(), vo2n(c), c->NV, c->stage.as<double>(), c->st);
   std::vector<double> Xe(3 * (size_t)c->NV);
   CK(cudaMemcpyAsync(Xe.data(), c->stage.p, sizeof(double) * 3 * c->NV, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -1885,7 +1997,7 @@ int hexopt_energy_fwd(hexopt_ctx *ctx, const double *X, double *E) {
   CK(ctx->Xa.ensure(sizeof(double) * 4 * ctx->NV));
   if (X) {
     CK(upload(ctx->stage, X, (size_t)3 * ctx->NV, ctx->st));
-    launch_rows_to_aos4(ctx->stage.as<double>(), ctx->Xa.as<double>(), ctx->NV, ctx->st);
+    launch_rows_to_aos4_perm(ctx->stage.as<double>(), vn2o(ctx), ctx->NV, ctx->Xa.as<double>(), ctx->st);
   } else {
     CK(cudaMemcpyAsync(ctx->Xa.p, ctx->X.p, sizeof(double) * 4 * ctx->NV, cudaMemcpyDeviceToDevice, ctx->st));
   }
@@ -1915,7 +2027,7 @@ int hexopt_energy_bwd(hexopt_ctx *ctx, double *grad) {
   CKL();
   if (grad) {
     CK(ctx->stage.ensure(sizeof(double) * 3 * ctx->NV));
-    launch_aos4_to_rows(ctx->grad.as<double>(), ctx->stage.as<double>(), ctx->NV, ctx->st);
+    launch_aos4_to_rows_perm(ctx->grad.as<double>(), vo2n(ctx), ctx->NV, ctx->stage.as<double>(), ctx->st);
     ctx->launches++;
     CK(cudaMemcpyAsync(grad, ctx->stage.p, sizeof(double) * 3 * ctx->NV, cudaMemcpyDeviceToHost, ctx->st));
   }

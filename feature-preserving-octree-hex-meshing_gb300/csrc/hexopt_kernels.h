@@ -102,9 +102,9 @@ constexpr int kLaunchesIrInitial = 2, kLaunchesIrReplace = 4, kLaunchesIrFinal =
 void launch_ref_shapes(const double *P8, const uint32_t *hexv, const double *X, const uint8_t *hflag, int cube,
                        int64_t nh, double *Bref, cudaStream_t st);
 
-// rigidDeformCubes on an exploded mesh (hex h owns vertices 8h..8h+7): hexes with no held corner
+// rigidDeformCubes on an exploded mesh (every hex owns its 8 corners): hexes with no held corner
 // become the unit cube fitted to their corners (Procrustes with scaling, no reflection).
-void launch_rigid_cubes(double *X, float *X32, const uint8_t *vfix, int64_t nh, cudaStream_t st);
+void launch_rigid_cubes(const uint32_t *hexv, double *X, float *X32, const uint8_t *vfix, int64_t nh, cudaStream_t st);
 
 // ---- adjoint (k_adjoint.cu) ----
 template <typename ET> void launch_energy_fwd(const KArgs &a, int64_t hblk, int64_t cblk, cudaStream_t st);
@@ -124,5 +124,22 @@ void launch_aos4_to_rows(const double *src, double *dst, int64_t n, cudaStream_t
 void launch_split_pos(const double *X, float *X32, int64_t n, cudaStream_t st);
 void launch_hex_to_aosoa_mesh(const uint32_t *src, int64_t h0, int64_t nh, uint32_t voff, uint32_t *dst,
                               cudaStream_t st);
+
+// ---- Morton ordering of the batch (k_order.cu) ----
+// Sorts the vertices (by position) and hexes (by centroid) of every mesh along a Morton curve of
+// the mesh's bounding box (box_d: 6 doubles per mesh), meshes kept contiguous; writes both
+// permutations each way.  rows: caller-order vertex rows (NV x 3), H: caller hexes (mesh-local
+// ids); voff_d / hoff_d: n_meshes + 1 offsets; scratch: order_scratch_bytes(NV, NH) bytes.
+cudaError_t order_batch(const double *rows, const uint32_t *H, int64_t NV, int64_t NH, const int64_t *voff_d,
+                        const int64_t *hoff_d, int n_meshes, const double *box_d, int32_t *vnew2old, int32_t *vold2new,
+                        int32_t *hnew2old, int32_t *hold2new, void *scratch, size_t scratch_bytes, cudaStream_t st);
+size_t order_scratch_bytes(int64_t NV, int64_t NH);
+void launch_hex_perm(const uint32_t *H, const int32_t *hnew2old, const int32_t *vold2new, int64_t nh, const int64_t *hoff,
+                     const int64_t *voff, int n_meshes, uint32_t *hexv, cudaStream_t st);
+// dst[i] = src[perm[i]] (rows of `width` doubles; perm null = copy)
+void launch_gather_rows(const double *src, const int32_t *perm, int64_t n, int width, double *dst, cudaStream_t st);
+// X[i] = rows[new2old[i]] / rows[i] = X[old2new[i]] (null = identity)
+void launch_rows_to_aos4_perm(const double *rows, const int32_t *new2old, int64_t n, double *X, cudaStream_t st);
+void launch_aos4_to_rows_perm(const double *X, const int32_t *old2new, int64_t n, double *rows, cudaStream_t st);
 
 }  // namespace hexopt

@@ -122,25 +122,28 @@ __global__ void __launch_bounds__(128) k_ref_shapes(const double *P8, const uint
 }
 
 // rigidDeformCubes (optimization.cpp:456-494) on the exploded mesh of the untangling path, where
-// hex h owns vertices 8h..8h+7 (its corners, starting at the original mesh's positions): a hex
+// every hex owns its 8 corner vertices (starting at the original mesh's positions): a hex
 // with no held corner is replaced by the unit cube fitted to its corners by igl::procrustes with
 // scaling and without reflection (procrustes.cpp: centred point sets, scale = |Y_c| / |X_c|,
 // R = polar rotation of X_c^T Y_c, t = mean(Y) - scale R^T mean(X)); a hex with a held corner
 // keeps its corners.  X (AoS4) and its FP32 split are rewritten in place.
-__global__ void __launch_bounds__(128) k_rigid_cubes(double *X, float *X32, const uint8_t *vfix, int64_t nh) {
+__global__ void __launch_bounds__(128) k_rigid_cubes(const uint32_t *hexv, double *X, float *X32, const uint8_t *vfix,
+                                                     int64_t nh) {
   const int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (h >= nh) return;
-  const int64_t v0 = 8 * h;
+  int64_t vc[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) vc[c] = hexv[hex_idx(h, c)];
   if (vfix)
     for (int c = 0; c < 8; c++)
-      if (vfix[v0 + c]) return;
+      if (vfix[vc[c]]) return;
   constexpr unsigned bits[8] = {0u, 1u, 3u, 2u, 4u, 5u, 7u, 6u};  // hex_ref_shape (x, y, z) bits
   double Y[8][3], ym[3] = {0, 0, 0};
 #pragma unroll
   for (int c = 0; c < 8; c++)
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      Y[c][d] = X[4 * (v0 + c) + d];
+      Y[c][d] = X[4 * vc[c] + d];
       ym[d] += Y[c][d];
     }
 #pragma unroll
@@ -178,15 +181,15 @@ __global__ void __launch_bounds__(128) k_rigid_cubes(double *X, float *X32, cons
 #pragma unroll
       for (int i = 0; i < 3; i++) acc += (((bits[c] >> i) & 1u) ? 1.0 : 0.0) * R[i][d];
       p[d] = scale * acc + t[d];
-      X[4 * (v0 + c) + d] = p[d];
+      X[4 * vc[c] + d] = p[d];
     }
-    store_split(X32, v0 + c, p[0], p[1], p[2]);
+    store_split(X32, vc[c], p[0], p[1], p[2]);
   }
 }
 
-void launch_rigid_cubes(double *X, float *X32, const uint8_t *vfix, int64_t nh, cudaStream_t st) {
+void launch_rigid_cubes(const uint32_t *hexv, double *X, float *X32, const uint8_t *vfix, int64_t nh, cudaStream_t st) {
   if (nh <= 0) return;
-  k_rigid_cubes<<<(unsigned)((nh + 127) / 128), 128, 0, st>>>(X, X32, vfix, nh);
+  k_rigid_cubes<<<(unsigned)((nh + 127) / 128), 128, 0, st>>>(hexv, X, X32, vfix, nh);
 }
 
 void launch_ref_shapes(const double *P8, const uint32_t *hexv, const double *X, const uint8_t *hflag, int cube,

@@ -72,6 +72,7 @@ SIGNATURES = {
     "hexopt_destroy": (None, [_vp]),
     "hexopt_last_error": (C.c_char_p, [_vp]),
     "hexopt_sync": (C.c_int, [_vp]),
+    "hexopt_set_ordering": (C.c_int, [_vp, C.c_int]),
     "hexopt_upload_meshes": (C.c_int, [_vp, C.c_int, _i64, _i64, _d, _u32, _u8]),
     "hexopt_set_positions": (C.c_int, [_vp, _d]),
     "hexopt_get_positions": (C.c_int, [_vp, _d]),
@@ -194,6 +195,12 @@ class Context:
             raise HexoptError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
 
     # ---- meshes
+    def set_ordering(self, mode=2):
+        """Device order of the next upload: 0 caller order, 1 Morton, 2 (default) Morton unless the
+        caller's numbering is already coherent.  True / False mean 1 / 0."""
+        mode = int(mode) if not isinstance(mode, bool) else int(mode)
+        self._ck(self.L.hexopt_set_ordering(self.h, mode), "set_ordering")
+
     def upload(self, meshes, h_flag=None):
         """meshes: list of (V (nv,3) float64, H (nh,8) uint32)."""
         nv = np.array([len(V) for V, _ in meshes], np.int64)

@@ -123,6 +123,16 @@ HEXOPT_API const char *hexopt_last_error(const hexopt_ctx *ctx);
 /* Synchronises the context's stream. */
 HEXOPT_API int hexopt_sync(hexopt_ctx *ctx);
 
+/* Device order of the meshes uploaded next.  mode 1 sorts every mesh's vertices by the Morton code
+ * of their position and its hexes by that of their centroid, inside the mesh's bounding box, so
+ * corner gathers and scatters of neighbouring hexes share cache lines whatever numbering the
+ * caller uses; 0 keeps the caller's order; 2 (the default) sorts unless the caller's numbering is
+ * already coherent (median corner-id span of a hex and median first-corner jump between
+ * consecutive hexes within 4 nv^(2/3), as a structured grid's row order, which coalesces the
+ * corner gathers better than a Morton curve).  The ABI speaks the caller's order either way:
+ * every vertex id, per-vertex row and per-hex output is mapped at the boundary. */
+HEXOPT_API int hexopt_set_ordering(hexopt_ctx *ctx, int mode);
+
 /* ---- meshes ----
  * Uploads a batch: mesh m has nv[m] vertices and nh[m] hexes; V and H are the meshes' arrays
  * concatenated.  h_flag (may be NULL = all 1) marks hexes whose target is a cube of equal volume
