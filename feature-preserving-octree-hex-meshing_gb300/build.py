@@ -30,7 +30,7 @@ FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", 
 
 
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def _deps():
@@ -45,9 +45,16 @@ def stale() -> bool:
     return any(os.path.getmtime(p) > t for p in _deps())
 
 
+CXX = os.environ.get("CXX", "g++")
+CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
+
+
 def _compile(src: str) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-    cmd = [NVCC, *ARCH, *FLAGS, "-c", src, "-o", obj]
+    obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
+    if src.endswith(".cpp"):  # host-only units
+        cmd = [CXX, *CXXFLAGS, "-c", src, "-o", obj]
+    else:
+        cmd = [NVCC, *ARCH, *FLAGS, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")

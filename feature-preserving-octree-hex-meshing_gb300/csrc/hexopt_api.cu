@@ -1641,6 +1641,71 @@ int hexopt_hausdorff(hexopt_ctx *ctx, int64_t nv0, const double *V0, int64_t nf0
   return HEXOPT_OK;
 }
 
+// Both sides of the uniform-sample check: n samples of each surface against the other's BVH, max
+// and sum / count of the distances below the upper bound D.
+int hexopt_hausdorff_uniform(hexopt_ctx *ctx, int64_t nv0, const double *V0, int64_t nf0, const int32_t *F0, int64_t nv1,
+                             const double *V1, int64_t nf1, const int32_t *F1, int64_t n_samples, uint64_t seed,
+                             double *diag, double *max_dist, double *ave_dist, double *samples0, double *samples1) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  if (nv0 <= 0 || nv1 <= 0 || nf0 <= 0 || nf1 <= 0 || !V0 || !V1 || !F0 || !F1 || n_samples <= 0)
+    return fail(ctx, HEXOPT_ERR_ARG, "hausdorff_uniform: empty mesh or no samples");
+  for (int64_t i = 0; i < 3 * nf0; i++) if (F0[i] < 0 || F0[i] >= nv0) return fail(ctx, HEXOPT_ERR_ARG, "hausdorff_uniform: F0 id out of range");
+  for (int64_t i = 0; i < 3 * nf1; i++) if (F1[i] < 0 || F1[i] >= nv1) return fail(ctx, HEXOPT_ERR_ARG, "hausdorff_uniform: F1 id out of range");
+  CK(cudaSetDevice(ctx->device));
+  // the upper bound: both vertex sets' bbox inflated by 2% of its diagonal (metro_hausdorff.cpp:455-462)
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t v = 0; v < nv0; v++) for (int d = 0; d < 3; d++) { lo[d] = std::min(lo[d], V0[3 * v + d]); hi[d] = std::max(hi[d], V0[3 * v + d]); }
+  for (int64_t v = 0; v < nv1; v++) for (int d = 0; d < 3; d++) { lo[d] = std::min(lo[d], V1[3 * v + d]); hi[d] = std::max(hi[d], V1[3 * v + d]); }
+  const double e0 = hi[0] - lo[0], e1 = hi[1] - lo[1], e2 = hi[2] - lo[2];
+  const double off = std::sqrt(e0 * e0 + e1 * e1 + e2 * e2) * 0.02;
+  const double f0 = e0 + 2 * off, f1 = e1 + 2 * off, f2 = e2 + 2 * off;
+  const double D = std::sqrt(f0 * f0 + f1 * f1 + f2 * f2);
+  std::vector<double> tri0(9 * nf0), tri1(9 * nf1);
+  for (int64_t f = 0; f < nf0; f++) for (int c = 0; c < 3; c++) for (int d = 0; d < 3; d++) tri0[9 * f + 3 * c + d] = V0[3 * (int64_t)F0[3 * f + c] + d];
+  for (int64_t f = 0; f < nf1; f++) for (int c = 0; c < 3; c++) for (int d = 0; d < 3; d++) tri1[9 * f + 3 * c + d] = V1[3 * (int64_t)F1[3 * f + c] + d];
+  StaticBvh B0, B1;
+  int rc = build_static_bvh(ctx, B0, tri0, nf0);
+  if (rc) return rc;
+  rc = build_static_bvh(ctx, B1, tri1, nf1);
+  if (rc) return rc;
+  DBuf Vd0, Vd1, Fd0, Fd1, S0, S1, scratch, dist, stat, out;
+  CK(upload(Vd0, V0, (size_t)3 * nv0, ctx->st));
+  CK(upload(Vd1, V1, (size_t)3 * nv1, ctx->st));
+  CK(upload(Fd0, F0, (size_t)3 * nf0, ctx->st));
+  CK(upload(Fd1, F1, (size_t)3 * nf1, ctx->st));
+  CK(S0.ensure(sizeof(double) * 3 * n_samples));
+  CK(S1.ensure(sizeof(double) * 3 * n_samples));
+  const size_t sb = std::max(sample_scratch_bytes(nf0), sample_scratch_bytes(nf1));
+  CK(scratch.ensure(sb));
+  // the two surfaces draw from disjoint counter ranges: surface 1 starts 3 n_samples after surface 0
+  CK(sample_surface(Vd0.as<double>(), Fd0.as<int32_t>(), nf0, n_samples, seed, S0.as<double>(), scratch.p, sb, ctx->st));
+  CK(sample_surface(Vd1.as<double>(), Fd1.as<int32_t>(), nf1, n_samples, seed + 3ull * (uint64_t)n_samples,
+                    S1.as<double>(), scratch.p, sb, ctx->st));
+  CK(stat.ensure(sizeof(int)));
+  CK(cudaMemsetAsync(stat.p, 0, sizeof(int), ctx->st));
+  CK(out.ensure(sizeof(double) * 6));
+  rc = ep_side(ctx, B1.dev(), S0.as<double>(), nullptr, n_samples, D, out.as<double>(), dist, stat);
+  if (rc) return rc;
+  DBuf dist2;
+  rc = ep_side(ctx, B0.dev(), S1.as<double>(), nullptr, n_samples, D, out.as<double>() + 3, dist2, stat);
+  if (rc) return rc;
+  ctx->launches += 6;
+  double h[6];
+  int st = 0;
+  CK(cudaMemcpyAsync(h, out.p, sizeof h, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(&st, stat.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  if (samples0) CK(cudaMemcpyAsync(samples0, S0.p, sizeof(double) * 3 * n_samples, cudaMemcpyDeviceToHost, ctx->st));
+  if (samples1) CK(cudaMemcpyAsync(samples1, S1.p, sizeof(double) * 3 * n_samples, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (st) return fail(ctx, HEXOPT_ERR_NUMERIC, "hausdorff_uniform: BVH traversal stack overflow");
+  const double mx0 = h[2] > 0 ? h[0] : 0.0, mx1 = h[5] > 0 ? h[3] : 0.0;
+  const double av0 = h[2] > 0 ? h[1] / h[2] : 0.0, av1 = h[5] > 0 ? h[4] / h[5] : 0.0;
+  if (diag) *diag = D;
+  if (max_dist) *max_dist = std::max(mx0, mx1);
+  if (ave_dist) *ave_dist = std::max(av0, av1);
+  return HEXOPT_OK;
+}
+
 int hexopt_point_face_distance(hexopt_ctx *ctx, int64_t np, const double *P, int64_t nv, const double *V, int64_t nf,
                                const int32_t *F, double *dist) {
   if (!ctx) return HEXOPT_ERR_ARG;

@@ -125,6 +125,12 @@ void launch_split_pos(const double *X, float *X32, int64_t n, cudaStream_t st);
 void launch_hex_to_aosoa_mesh(const uint32_t *src, int64_t h0, int64_t nh, uint32_t voff, uint32_t *dst,
                               cudaStream_t st);
 
+// ---- area-uniform surface samples (k_sample.cu) ----
+// n samples of the triangles (V rows, F) drawn with SplitMix64 counters from `seed`, into P (n x 3).
+cudaError_t sample_surface(const double *V, const int32_t *F, int64_t nf, int64_t n, uint64_t seed, double *P,
+                           void *scratch, size_t scratch_bytes, cudaStream_t st);
+size_t sample_scratch_bytes(int64_t nf);
+
 // ---- Morton ordering of the batch (k_order.cu) ----
 // Sorts the vertices (by position) and hexes (by centroid) of every mesh along a Morton curve of
 // the mesh's bounding box (box_d: 6 doubles per mesh), meshes kept contiguous; writes both

@@ -11,7 +11,7 @@ The module-level functions mirror the reference entry points they replace:
     hausdorff_uniform(V0, F0, V1, F1, n)       the same check over n area-uniform samples per surface
 Everything runs on the GPU; a missing library or device raises instead of falling back.
 """
-from ._lib import FP64, MIXED, SYMMETRIC_DIRICHLET, Context, HexoptError, load  # noqa: F401
+from ._lib import FP64, MIXED, SYMMETRIC_DIRICHLET, Context, HexoptError, load, read_hex_mesh, write_hex_mesh  # noqa: F401
 from . import meshgen  # noqa: F401
 
 _ctx = None
@@ -66,24 +66,9 @@ def compute(V0, F0, V1, F1):
 
 
 def hausdorff_uniform(V0, F0, V1, F1, n_samples=10_000, seed=0, ctx=None):
-    """Two-sided Hausdorff over n_samples area-uniform samples of each surface (seeded) instead
-    of the vertices: the sample distance is PointDistanceEP minimised on the GPU, and the rules
-    are those of the vertex mode (metro_hausdorff.cpp:358-506) -- the bbox of both vertex sets
-    inflated by 2% of its diagonal is the upper bound, samples that find no face below it are
-    dropped, max over both sides, ave = the larger of the two means.  Returns (diag, max, ave)."""
-    import numpy as np
+    """Two-sided Hausdorff over n_samples area-uniform samples of each surface instead of the
+    vertices, sampled and evaluated on the device (hexopt_hausdorff_uniform): the sample distance
+    is PointDistanceEP minimised over the other surface, and the rules are those of the vertex mode
+    (metro_hausdorff.cpp:358-506).  Returns (diag, max, ave)."""
     c = ctx or _context()
-    V0 = np.asarray(V0, np.float64); V1 = np.asarray(V1, np.float64)
-    lo = np.minimum(V0.min(0), V1.min(0)); hi = np.maximum(V0.max(0), V1.max(0))
-    e = hi - lo
-    off = np.sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * 0.02
-    e = (hi + off) - (lo - off)
-    D = float(np.sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]))
-    S0 = meshgen.area_samples(V0, np.asarray(F0), n_samples, seed)
-    S1 = meshgen.area_samples(V1, np.asarray(F1), n_samples, seed + 1)
-    d0 = c.point_face_distance(S0, V1, F1)
-    d1 = c.point_face_distance(S1, V0, F0)
-    k0, k1 = d0[d0 < D], d1[d1 < D]
-    mx = max(k0.max(initial=0.0), k1.max(initial=0.0))
-    ave = max(k0.mean() if len(k0) else 0.0, k1.mean() if len(k1) else 0.0)
-    return D, float(mx), float(ave)
+    return c.hausdorff_uniform(V0, F0, V1, F1, n_samples=n_samples, seed=seed)

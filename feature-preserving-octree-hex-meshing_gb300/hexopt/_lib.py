@@ -102,6 +102,8 @@ SIGNATURES = {
     "hexopt_set_feature_sets": (C.c_int, [_vp, _i64, _i32, _i64, _i32, _i32, _i64, _i64, _i32, _u8]),
     "hexopt_project_features": (C.c_int, [_vp]),
     "hexopt_hausdorff": (C.c_int, [_vp, C.c_int64, _d, C.c_int64, _i32, C.c_int64, _d, C.c_int64, _i32, _d, _d, _d]),
+    "hexopt_hausdorff_uniform": (C.c_int, [_vp, C.c_int64, _d, C.c_int64, _i32, C.c_int64, _d, C.c_int64, _i32,
+                                           C.c_int64, C.c_uint64, _d, _d, _d, _d, _d]),
     "hexopt_set_surface": (C.c_int, [_vp, C.c_int, C.c_int64, _i32]),
     "hexopt_hausdorff_meshes": (C.c_int, [_vp, _d, _d, _d]),
     "hexopt_point_face_distance": (C.c_int, [_vp, C.c_int64, _d, C.c_int64, _d, C.c_int64, _i32, _d]),
@@ -120,6 +122,8 @@ SIGNATURES = {
     "hexopt_timer_start": (C.c_int, [_vp]),
     "hexopt_timer_stop": (C.c_int, [_vp, _d]),
     "hexopt_time_stage": (C.c_int, [_vp, C.c_int, C.c_int, _d]),
+    "hexopt_write_hex_mesh": (C.c_int, [C.c_char_p, C.c_int, C.c_int64, _d, C.c_int64, _u32, _u8]),
+    "hexopt_read_hex_mesh": (C.c_int, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _d, _u32]),
     "hexopt_aabb_merge": (None, [C.POINTER(AABB), C.POINTER(AABB)]),
     "hexopt_aabb_squared_distance": (C.c_double, [C.POINTER(AABB), _d]),
     "hexopt_aabb_ray_intersect": (C.c_int, [C.POINTER(AABB), C.POINTER(Ray), _d, _d]),
@@ -151,6 +155,32 @@ def ptr(a, t):
 
 class HexoptError(RuntimeError):
     pass
+
+
+def write_hex_mesh(path, V, H, fmt="mesh", boundary=None):
+    """A hex mesh as the reference writes it: fmt "mesh" (MEDIT) or "vtk" (legacy ASCII, with the
+    boundary flags as point data).  Host only."""
+    L = load()
+    V = np.ascontiguousarray(V, np.float64); H = np.ascontiguousarray(H, np.uint32)
+    b = None if boundary is None else np.ascontiguousarray(np.asarray(boundary, np.uint8))
+    rc = L.hexopt_write_hex_mesh(os.fsencode(path), 0 if fmt == "mesh" else 1, len(V), ptr(V, _d), len(H),
+                                 ptr(H, _u32), ptr(b, _u8))
+    if rc != 0:
+        raise HexoptError(f"write_hex_mesh failed ({rc}): {path}")
+
+
+def read_hex_mesh(path):
+    """(V, H) of a MEDIT .mesh file's Vertices / Hexahedra blocks.  Host only."""
+    L = load()
+    nv, nh = C.c_int64(0), C.c_int64(0)
+    rc = L.hexopt_read_hex_mesh(os.fsencode(path), C.byref(nv), C.byref(nh), None, None)
+    if rc != 0:
+        raise HexoptError(f"read_hex_mesh failed ({rc}): {path}")
+    V = np.empty((nv.value, 3)); H = np.empty((nh.value, 8), np.uint32)
+    rc = L.hexopt_read_hex_mesh(os.fsencode(path), C.byref(nv), C.byref(nh), ptr(V, _d), ptr(H, _u32))
+    if rc != 0:
+        raise HexoptError(f"read_hex_mesh failed ({rc}): {path}")
+    return V, H
 
 
 def point_face_distance_noalloc(P_dev: int, np_: int, V_dev: int, nv: int, F_dev: int, nf: int, dist_dev: int,
@@ -416,6 +446,21 @@ class Context:
         self._ck(self.L.hexopt_hausdorff(self.h, len(V0), ptr(V0, _d), len(F0), ptr(F0, _i32), len(V1), ptr(V1, _d),
                                          len(F1), ptr(F1, _i32), C.byref(dg), C.byref(mx), C.byref(av)), "hausdorff")
         return dg.value, mx.value, av.value
+
+    def hausdorff_uniform(self, V0, F0, V1, F1, n_samples=10_000, seed=0, return_samples=False):
+        """Two-sided Hausdorff over n_samples area-uniform device samples of each surface:
+        (diag, max, ave), plus the two sample arrays when asked."""
+        V0 = np.ascontiguousarray(V0, np.float64); V1 = np.ascontiguousarray(V1, np.float64)
+        F0 = np.ascontiguousarray(F0, np.int32); F1 = np.ascontiguousarray(F1, np.int32)
+        dg, mx, av = C.c_double(), C.c_double(), C.c_double()
+        S0 = np.empty((n_samples, 3)) if return_samples else None
+        S1 = np.empty((n_samples, 3)) if return_samples else None
+        self._ck(self.L.hexopt_hausdorff_uniform(self.h, len(V0), ptr(V0, _d), len(F0), ptr(F0, _i32), len(V1),
+                                                 ptr(V1, _d), len(F1), ptr(F1, _i32), int(n_samples), int(seed),
+                                                 C.byref(dg), C.byref(mx), C.byref(av), ptr(S0, _d), ptr(S1, _d)),
+                 "hausdorff_uniform")
+        out = (dg.value, mx.value, av.value)
+        return out + (S0, S1) if return_samples else out
 
     def set_surface(self, mesh, F):
         F = np.ascontiguousarray(F, np.int32)

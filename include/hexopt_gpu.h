@@ -273,6 +273,18 @@ HEXOPT_API int hexopt_hausdorff_meshes(hexopt_ctx *ctx, double *diag, double *ma
 HEXOPT_API int hexopt_point_face_distance(hexopt_ctx *ctx, int64_t np, const double *P, int64_t nv, const double *V, int64_t nf,
                                const int32_t *F, double *dist);
 
+/* The same two-sided check over n_samples area-uniform random samples of each surface instead of
+ * the vertices (the uniform-sample mode): samples drawn on the device from `seed` with SplitMix64
+ * counters (surface 1 continuing after surface 0's 3 n_samples counters), face picked by
+ * cumulative area, barycentric (1 - sqrt(u1), sqrt(u1)(1 - u2), sqrt(u1) u2); each sample's
+ * distance is PointDistanceEP minimised over the other surface, with the vertex mode's rules --
+ * upper bound = the inflated bbox diagonal, samples reaching it dropped, max over both sides,
+ * ave = the larger mean.  samples0 / samples1 (n_samples x 3 each) receive the samples, or NULL. */
+HEXOPT_API int hexopt_hausdorff_uniform(hexopt_ctx *ctx, int64_t nv0, const double *V0, int64_t nf0, const int32_t *F0,
+                                        int64_t nv1, const double *V1, int64_t nf1, const int32_t *F1,
+                                        int64_t n_samples, uint64_t seed, double *diag, double *max_dist,
+                                        double *ave_dist, double *samples0, double *samples1);
+
 /* ---- the optimiser iteration: one pass of feature_alignment's loop body ----
  * projection -> slim_precompute -> one SLIM iteration -> weight schedule -> scaled Jacobian
  * (-> Hausdorff when do_hausdorff).  lamda0 = feature_weight * MESHRATIO (0.05), upper bound 1e16. */
@@ -330,6 +342,16 @@ HEXOPT_API int64_t hexopt_launch_count(const hexopt_ctx *ctx);
 HEXOPT_API int hexopt_point_face_distance_noalloc(int device, void *stream, int64_t np, const double *P_dev, int64_t nv,
                                                   const double *V_dev, int64_t nf, const int32_t *F_dev,
                                                   double *dist_dev, char *err, size_t err_len);
+
+/* ---- hex-mesh files in the reference's formats (host only, no device) ----
+ * write: format 0 = MEDIT .mesh as h_io::write_hybrid_mesh_MESH (io.cpp:295-325), 1 = legacy
+ * ASCII .vtk as h_io::write_hybrid_mesh_VTK (io.cpp:102-180) with the boundary flags (may be
+ * NULL: all 0) as its "fixed" point data; numbers at iostream's default 6 significant digits.
+ * read: the Vertices / Hexahedra blocks of a .mesh; call with V or H NULL (or *nv, *nh too small)
+ * to get the sizes in *nv, *nh, then again with arrays of those sizes. */
+HEXOPT_API int hexopt_write_hex_mesh(const char *path, int format, int64_t nv, const double *V, int64_t nh,
+                                     const uint32_t *H, const uint8_t *boundary);
+HEXOPT_API int hexopt_read_hex_mesh(const char *path, int64_t *nv, int64_t *nh, double *V, uint32_t *H);
 
 /* ---- aabb.h value types (Ray / AABB, aabb.h:5-115) on the host ---- */
 typedef struct hexopt_aabb { double min[3], max[3]; } hexopt_aabb;

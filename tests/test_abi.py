@@ -5,6 +5,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 from conftest import ROOT
@@ -67,3 +68,25 @@ def test_create_without_device_fails_cleanly(lib):
     h = C.c_void_p()
     assert L.hexopt_create(C.byref(h), 0) != 0
     assert not h.value
+
+
+def test_hex_mesh_files_round_trip(tmp_path):
+    """MEDIT .mesh written as the reference writes it (6 significant digits, 1-based ids) reads
+    back; the .vtk carries the hexes as VTK_HEXAHEDRON cells and the boundary flags."""
+    import hexopt
+    from hexopt import meshgen
+    V, H = meshgen.grid_hex(3, 2, 2, hi=(1.5, 1.0, 0.5))
+    b = meshgen.grid_boundary_mask(3, 2, 2)
+    p = str(tmp_path / "m.mesh")
+    hexopt.write_hex_mesh(p, V, H)
+    V2, H2 = hexopt.read_hex_mesh(p)
+    assert np.array_equal(H2, H)
+    np.testing.assert_allclose(V2, V, rtol=1e-6)
+    txt = open(p).read().split("\n")
+    assert txt[0] == "MeshVersionFormatted 1" and txt[2] == f"Vertices {len(V)}" and txt[-1] == "End"
+    q = str(tmp_path / "m.vtk")
+    hexopt.write_hex_mesh(q, V, H, fmt="vtk", boundary=b)
+    t = open(q).read()
+    assert f"CELLS {len(H)} {9 * len(H)}" in t and t.count("\n12\n") + t.count("\n12") >= len(H)
+    pd = t.split("LOOKUP_TABLE default\n")[1].split()
+    assert [int(x) for x in pd] == b.astype(int).tolist()
