@@ -1,9 +1,12 @@
 // hexopt_api.cu -- host runtime behind the C ABI of include/hexopt_gpu.h.
 //
 // One context = one CUDA stream + one batch of meshes resident in HBM.  Every compute stage is a
-// kernel launch over per-mesh segment tables (no block straddles two meshes, so every reduction
-// is per mesh and deterministic).  The host only uploads inputs, orders launches and downloads
-// results; there is no CPU compute path.
+// kernel launch over per-mesh segment tables (no block straddles two meshes).  The scalar
+// reductions (energies, dot products, minima) are per mesh and summed in a fixed order; the
+// per-vertex scatters (right-hand side, SpMV product, residual, gradient) use float atomics, so
+// positions are not bit-reproducible from run to run (the order of the atomic adds varies).
+// The host only uploads inputs, orders launches and downloads results; there is no CPU compute
+// path.
 #include <cuda_runtime.h>
 #include <cub/device/device_radix_sort.cuh>
 

@@ -18,6 +18,9 @@
 //  * set-up: the first call on a device resolves the scratch's address (cudaGetSymbolAddress,
 //    checked), which loads this file's module and with it the 80 MiB array; a caller that must
 //    not see that happen mid-stream makes one call (any size, e.g. one point) beforehand.
+//    That holds under CUDA's lazy module loading (the default).  With CUDA_MODULE_LOADING=EAGER
+//    the module, and the 80 MiB with it, is loaded on every device when a context first loads
+//    this library, whether or not this entry point is ever called.
 //  * one scratch per device, shared by every call: calls that overlap in time on one device --
 //    from two streams or two host threads -- race on it and give wrong results.  Serialise them
 //    (one stream, or an event between them).  The call itself is synchronous on `stream`.

@@ -333,7 +333,8 @@ HEXOPT_API int64_t hexopt_launch_count(const hexopt_ctx *ctx);
  *   set-up:    the first call on a device resolves the static array's address, which loads it;
  *              when that happens lazily it must come before any stream capture on the device,
  *              so make one small call up front.  The call synchronises `stream` and is not
- *              itself meant to be captured.
+ *              itself meant to be captured.  Under CUDA_MODULE_LOADING=EAGER the 80 MiB are
+ *              reserved on every device as soon as a context loads this library, called or not.
  *   races:     every call on a device shares that one array: calls overlapping in time (two
  *              streams, two host threads) race and give wrong results -- serialise them.
  *   zeroing:   the parts that must start at zero (BVH refit counters, status word) are cleared

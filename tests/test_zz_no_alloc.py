@@ -55,9 +55,13 @@ def test_noalloc_matches_allocating_entry_point(env):
                                          b["F"].data_ptr(), b["F"].shape[0], b["D"].data_ptr(), device=0,
                                          stream=stream)
 
+    before = torch.cuda.mem_get_info(dev)[0]
     call(bufs[0])  # first call on the device: sets the static scratch up
     torch.cuda.synchronize(dev)
     free0 = torch.cuda.mem_get_info(dev)[0]
+    # the static scratch is reserved by this first call under lazy module loading, or was already
+    # when the library was loaded under eager loading; report which
+    print(f"\nfirst no-alloc call changed free device memory by {(before - free0) / 2**20:.1f} MiB")
     call(bufs[1])
     call(bufs[0])
     torch.cuda.synchronize(dev)
