@@ -123,6 +123,7 @@ struct hexopt_ctx {
   // caller): per-hex h_flag, optional reference corners, shapes, and the all-hex slot tables
   DBuf hflag_d, ref_p8, Bref, gslot_all, Bgen_all;
   bool has_ref_p8 = false, rest_fixed = false;
+  bool has_ref_tets = false;  // explicit reference tets (ref_p8 then holds 96 doubles per hex)
   DBuf stage, stage2, HJs, VJs, Xa, grad, Xbak;
   DBuf root_list, root_mesh, root_count, root_min;  // flip-avoid bound: tets needing the exact root
   bool adj_ready = false;
@@ -444,8 +445,12 @@ int build_ref_shapes(hexopt_ctx *ctx) {
     for (int64_t h = 0; h < ctx->NH; h++) id[h] = (int32_t)h;
     CK(upload(ctx->gslot_all, id.data(), id.size(), ctx->st));
   }
-  launch_ref_shapes(ctx->has_ref_p8 ? ctx->ref_p8.as<double>() : nullptr, ctx->hexv.as<uint32_t>(), ctx->X.as<double>(),
-                    ctx->hflag_d.as<uint8_t>(), ctx->params.cube, ctx->NH, ctx->Bref.as<double>(), ctx->st);
+  if (ctx->has_ref_tets)
+    launch_ref_from_tets(ctx->ref_p8.as<double>(), ctx->NH * 8, ctx->Bref.as<double>(), ctx->st);
+  else
+    launch_ref_shapes(ctx->has_ref_p8 ? ctx->ref_p8.as<double>() : nullptr, ctx->hexv.as<uint32_t>(),
+                      ctx->X.as<double>(), ctx->hflag_d.as<uint8_t>(), ctx->params.cube, ctx->NH,
+                      ctx->Bref.as<double>(), ctx->st);
   ctx->launches++;
   CKL();
   return HEXOPT_OK;
@@ -949,6 +954,7 @@ int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const
   CK(upload(ctx->gslot, gs.data(), gs.size(), ctx->st));
   CK(upload(ctx->hflag_d, hf.data(), hf.size(), ctx->st));
   ctx->has_ref_p8 = false;
+  ctx->has_ref_tets = false;
   ctx->rest_fixed = false;
   CK(ctx->counters.ensure(sizeof(unsigned) * n_meshes));
   CK(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned) * n_meshes, ctx->st));
@@ -1212,11 +1218,28 @@ int hexopt_set_reference_hexes(hexopt_ctx *ctx, const double *P8) {
     CK(ctx->ref_p8.ensure(sizeof(double) * 24 * ctx->NH));
     launch_gather_rows(ctx->stage.as<double>(), hn2o(ctx), ctx->NH, 24, ctx->ref_p8.as<double>(), ctx->st);
     ctx->has_ref_p8 = true;
+    ctx->has_ref_tets = false;
   } else {
     ctx->has_ref_p8 = false;
+    ctx->has_ref_tets = false;
   }
   ctx->precomputed = false;
   ctx->tables_epoch++;
+  return HEXOPT_OK;
+}
+
+int hexopt_set_reference_tets(hexopt_ctx *ctx, const double *RT) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!RT) return hexopt_set_reference_hexes(ctx, nullptr);
+  CK(upload(ctx->stage, RT, (size_t)ctx->NH * 96, ctx->st));
+  CK(ctx->ref_p8.ensure(sizeof(double) * 96 * ctx->NH));
+  launch_gather_rows(ctx->stage.as<double>(), hn2o(ctx), ctx->NH, 96, ctx->ref_p8.as<double>(), ctx->st);
+  ctx->has_ref_p8 = true;  // the shapes are fixed by the caller
+  ctx->has_ref_tets = true;
+  ctx->precomputed = false;
+  ctx->tables_epoch++;
+  CKL();
   return HEXOPT_OK;
 }
 

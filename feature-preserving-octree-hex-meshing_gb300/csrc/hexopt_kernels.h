@@ -102,6 +102,8 @@ constexpr int kLaunchesIrInitial = 2, kLaunchesIrReplace = 4, kLaunchesIrFinal =
 void launch_ref_shapes(const double *P8, const uint32_t *hexv, const double *X, const uint8_t *hflag, int cube,
                        int64_t nh, double *Bref, cudaStream_t st);
 
+// Bref from explicit reference tets (ntet x 4 x 3 corners, device order)
+void launch_ref_from_tets(const double *RT, int64_t ntet, double *Bref, cudaStream_t st);
 // rigidDeformCubes on an exploded mesh (every hex owns its 8 corners): hexes with no held corner
 // become the unit cube fitted to their corners (Procrustes with scaling, no reflection).
 void launch_rigid_cubes(const uint32_t *hexv, double *X, float *X32, const uint8_t *vfix, int64_t nh, cudaStream_t st);

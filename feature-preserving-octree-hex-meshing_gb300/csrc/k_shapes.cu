@@ -192,6 +192,31 @@ void launch_rigid_cubes(const uint32_t *hexv, double *X, float *X32, const uint8
   k_rigid_cubes<<<(unsigned)((nh + 127) / 128), 128, 0, st>>>(hexv, X, X32, vfix, nh);
 }
 
+// Bref of every corner tet from explicit reference tets (compute_referenceMesh's output ts.RT:
+// 4 x 3 corner rows per tet, tet 8h + k of hex h in hex_tetra_table order).
+__global__ void __launch_bounds__(128) k_ref_from_tets(const double *RT, int64_t ntet, double *Bref) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntet) return;
+  const double *r = RT + t * 12;
+  double R[3][3], A[3][3];
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+#pragma unroll
+    for (int d = 0; d < 3; d++) R[d][j] = r[3 * (j + 1) + d] - r[d];
+  adj3(R, A);
+  const double dr = fabs(det3(R));
+  const double s = 1.0 / cbrt(dr * dr);
+  double *B = Bref + t * 9;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) B[i * 3 + j] = A[i][j] * s;
+}
+
+void launch_ref_from_tets(const double *RT, int64_t ntet, double *Bref, cudaStream_t st) {
+  if (ntet > 0) k_ref_from_tets<<<(unsigned)((ntet + 127) / 128), 128, 0, st>>>(RT, ntet, Bref);
+}
+
 void launch_ref_shapes(const double *P8, const uint32_t *hexv, const double *X, const uint8_t *hflag, int cube,
                        int64_t nh, double *Bref, cudaStream_t st) {
   if (nh <= 0) return;

@@ -92,6 +92,7 @@ SIGNATURES = {
     "hexopt_get_tangents": (C.c_int, [_vp, _d, _d]),
     "hexopt_get_lines": (C.c_int, [_vp, _d, _d]),
     "hexopt_set_reference_hexes": (C.c_int, [_vp, _d]),
+    "hexopt_set_reference_tets": (C.c_int, [_vp, _d]),
     "hexopt_slim_precompute": (C.c_int, [_vp, C.POINTER(SlimParams)]),
     "hexopt_slim_iterate": (C.c_int, [_vp, C.c_int, C.POINTER(SlimReport)]),
     "hexopt_slim_m_opt": (C.c_int, [_vp, C.POINTER(SlimParams), C.c_int, C.POINTER(SlimReport)]),
@@ -364,6 +365,11 @@ class Context:
         positions at the precompute."""
         P = None if P8 is None else np.ascontiguousarray(P8, np.float64).reshape(-1, 8, 3)
         self._ck(self.L.hexopt_set_reference_hexes(self.h, ptr(P, _d)), "set_reference_hexes")
+
+    def set_reference_tets(self, RT=None):
+        """compute_referenceMesh's reference tets (n_hexes*8 x 4 x 3); None = the default shapes."""
+        R = None if RT is None else np.ascontiguousarray(RT, np.float64).reshape(-1, 4, 3)
+        self._ck(self.L.hexopt_set_reference_tets(self.h, ptr(R, _d)), "set_reference_tets")
 
     @staticmethod
     def params(precision=FP64, weight_opt=0.001, energy=SYMMETRIC_DIRICHLET, exp_factor=1.0, cg_max_iter=20,

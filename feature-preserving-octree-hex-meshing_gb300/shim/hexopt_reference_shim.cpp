@@ -11,12 +11,15 @@
 // (grid_hex_meshing.cpp:3783-3912), stop_criterior_satisfied and hausdorff_ratio_check
 // (:4148-4327) compile and link unchanged and run their optimiser iterations on the GPU.
 //
-// Scope: the forms the feature-alignment loop uses -- symmetric Dirichlet energy over the 8
-// corner tets of each hex (F holds 8 tets per hex in hex_tetra_table order), cube or own-shape
-// reference tets, corner / tangent-plane / feature-line soft constraints, fixed iteration counts.
-// Other forms (adaptive iteration count, glue, projection and region terms, other energies,
-// scaffold post variables, 2-D quad quality) throw std::runtime_error naming the form: there is
-// no CPU fallback behind this file.
+// Scope: every SLIM form the reference's callers use -- the six SLIM energies over the 8 corner
+// tets of each hex (F holds 8 tets per hex in hex_tetra_table order), whatever reference tets
+// ts.RT holds, corner / tangent-plane / feature-line soft constraints, the projection and glue
+// terms, known_value_post, fixed iteration counts and the adaptive (iter_num = -1) branches of
+// slim_solve2 and slim_solve; with HEXOPT_SHIM_SLIM_OPT_IGL, optimization::slim_opt_igl (the
+// modified igl::slim of the smoothing stage).  The conversions themselves are in
+// hexopt_shim_core.h.  Forms no reference caller reaches (region terms, the 2-D quad path, the
+// modified igl::slim's glue groups) throw std::runtime_error naming the form: there is no CPU
+// fallback behind this file.
 //
 // Environment: HEXOPT_DEVICE (CUDA device, default 0); HEXOPT_PRECISION=mixed selects the
 // FP32/FP64 mixed mode (default: plain FP64, the reference's arithmetic).
@@ -25,6 +28,7 @@
 #include "global_functions.h"
 
 #include "hexopt_gpu.h"
+#include "hexopt_shim_core.h"
 
 #include <cmath>
 #include <cstdio>
@@ -92,95 +96,84 @@ static std::vector<int32_t> ids(const Eigen::VectorXi &v) {
   return std::vector<int32_t>(v.data(), v.data() + v.size());
 }
 
-// Hexes from the 8-tets-per-hex list: tet j of hex h starts at corner j (hex_tetra_table[j][0]
-// == j, global_types.h:163-173), and the other three corners must follow the table.
-static std::vector<uint32_t> hexes_from_tets(const Eigen::MatrixXi &F) {
-  if (F.cols() != 4 || F.rows() % 8 != 0) unsupported("a tet list that is not 8 corner tets per hex");
-  const int64_t nh = F.rows() / 8;
-  std::vector<uint32_t> H(8 * (size_t)nh);
-  for (int64_t h = 0; h < nh; h++) {
-    for (int j = 0; j < 8; j++) H[8 * h + j] = (uint32_t)F(8 * h + j, 0);
-    for (int j = 0; j < 8; j++)
-      for (int k = 0; k < 4; k++)
-        if ((uint32_t)F(8 * h + j, k) != H[8 * h + hex_tetra_table[j][k]])
-          unsupported("a tet list that is not 8 corner tets per hex");
-  }
-  return H;
+static std::vector<int32_t> tets_rows(const Eigen::MatrixXi &F) {
+  if (F.cols() != 4) unsupported("a tet list whose rows are not 4 vertices");
+  std::vector<int32_t> T(4 * (size_t)F.rows());
+  for (int64_t i = 0; i < F.rows(); i++)
+    for (int k = 0; k < 4; k++) T[4 * i + k] = F(i, k);
+  return T;
 }
 
-// compute_referenceMesh's per-hex choice (global_functions.cpp:3735-3806), read back from the
-// reference tets: 1 = the corner tets of a cube, 0 = the hex's own corners at V.
-static std::vector<uint8_t> hflags_from_rt(const std::vector<Eigen::MatrixXd> &RT, const Eigen::MatrixXi &F,
-                                           const Eigen::MatrixXd &V) {
-  const int64_t nh = F.rows() / 8;
-  std::vector<uint8_t> flag(nh, 1);
-  if (RT.empty()) return flag;
-  if ((int64_t)RT.size() != F.rows()) unsupported("reference tets whose count differs from the tets'");
-  for (int64_t h = 0; h < nh; h++) {
-    bool cube = true, own = true;
-    for (int j = 0; j < 8 && (cube || own); j++) {
-      const Eigen::MatrixXd &R = RT[8 * h + j];
-      if (R.rows() != 4 || R.cols() != 3) unsupported("reference tets that are not 4 x 3");
-      double a = 0;
-      for (int k = 1; k < 4; k++) a = std::max(a, (R.row(k) - R.row(0)).norm());
-      for (int k = 1; k < 4 && cube; k++)
-        for (int d = 0; d < 3; d++) {
-          const double want = a * (hex_ref_shape[hex_tetra_table[j][k]][d] - hex_ref_shape[hex_tetra_table[j][0]][d]);
-          if (std::fabs(R(k, d) - R(0, d) - want) > 1e-9 * a) { cube = false; break; }
-        }
-      for (int k = 0; k < 4 && own; k++)
-        for (int d = 0; d < 3; d++)
-          if (R(k, d) != V(F(8 * h + j, k), d)) { own = false; break; }
-    }
-    if (!cube && !own) unsupported("reference tets other than cubes or the hex's own shape");
-    flag[h] = cube ? 1 : 0;
+static std::vector<double> rt_rows(const std::vector<Eigen::MatrixXd> &RT, int64_t ntets) {
+  std::vector<double> out;
+  if (RT.empty()) return out;
+  if ((int64_t)RT.size() != ntets) unsupported("reference tets whose count differs from the tets'");
+  out.resize(12 * (size_t)ntets);
+  for (int64_t t = 0; t < ntets; t++) {
+    if (RT[t].rows() != 4 || RT[t].cols() != 3) unsupported("reference tets that are not 4 x 3");
+    for (int j = 0; j < 4; j++)
+      for (int d = 0; d < 3; d++) out[12 * t + 3 * j + d] = RT[t](j, d);
   }
-  return flag;
+  return out;
 }
 
-// Uploads data's mesh, constraints and weights into the SLIM context and runs the precompute.
+// Uploads data's mesh, constraints and weights into the SLIM context and runs the precompute
+// (hexopt_shim_core::load_slim on the plain arrays of data and data.ts).
 static void load(SLIMData &data) {
   Contexts &C = contexts();
   hexopt_ctx *c = get(C.slim);
   const Tetralize_Set &ts = data.ts;
-  if (data.slim_energy != SYMMETRIC_DIRICHLET) unsupported("a SLIM energy other than SYMMETRIC_DIRICHLET");
-  if (ts.projection || data.Projection) unsupported("the projection penalty (Tetralize_Set::projection)");
-  if (ts.glue) unsupported("the glue penalty (Tetralize_Set::glue)");
-  if (ts.known_value_post) unsupported("known_value_post elimination");
   if (ts.regionb.size() > 0 && ts.lamda_region != 0) unsupported("region constraints");
-  const std::vector<uint32_t> H = hexes_from_tets(data.F);
-  const std::vector<uint8_t> hf = hflags_from_rt(ts.RT, data.F, data.V);
-  const int64_t nv = data.V.rows(), nh = (int64_t)H.size() / 8;
-  const std::vector<double> V = rows3(data.V);
   C.loaded = nullptr;
-  ck(c, hexopt_upload_meshes(c, 1, &nv, &nh, V.data(), H.data(), hf.data()), "upload_meshes");
+  const std::vector<int32_t> T = tets_rows(data.F);
+  const std::vector<double> RT = rt_rows(ts.RT, data.F.rows());
+  const std::vector<double> V = rows3(data.V);
+  const std::vector<double> Vo = data.V_o.rows() == data.V.rows() ? rows3(data.V_o) : V;
   const Feature_Constraints &fc = ts.fc;
-  const int64_t nC = fc.ids_C.size(), nT = fc.ids_T.size(), nL = fc.ids_L.size();
-  const std::vector<int32_t> iC = ids(fc.ids_C), iT = ids(fc.ids_T), iL = ids(fc.ids_L);
-  const std::vector<double> Cp = nC ? rows3(fc.C) : std::vector<double>(), Tn = nT ? rows3(fc.normal_T) : std::vector<double>();
-  const std::vector<double> Ta(fc.dis_T.data(), fc.dis_T.data() + nT);
-  const std::vector<double> La = nL ? rows3(fc.Axa_L) : std::vector<double>(), Lo = nL ? rows3(fc.origin_L) : std::vector<double>();
-  ck(c, hexopt_set_corners(c, &nC, iC.data(), Cp.data()), "set_corners");
-  ck(c, hexopt_set_tangents(c, &nT, iT.data(), Tn.data(), Ta.data()), "set_tangents");
-  ck(c, hexopt_set_lines(c, &nL, iL.data(), La.data(), Lo.data()), "set_lines");
-  ck(c, hexopt_set_weights(c, &fc.lamda_C, &fc.lamda_T, &fc.lamda_L), "set_weights");
-  hexopt_slim_params p;
-  std::memset(&p, 0, sizeof p);
-  p.energy = HEXOPT_SYMMETRIC_DIRICHLET;
-  p.precision = precision();
-  p.weight_opt = data.weight_opt;
-  p.exp_factor = data.exp_factor;
-  p.cg_max_iter = 20;
-  p.cg_tol = 1e-8;
-  p.ls_candidates = 1;
-  p.cube = 1;
-  ck(c, hexopt_slim_precompute(c, &p), "slim_precompute");
-  // iterations start from V_init (data.V_o); the precompute snapshot was taken at data.V
-  if (data.V_o.rows() == data.V.rows() && data.V_o != data.V) {
-    const std::vector<double> X = rows3(data.V_o);
-    ck(c, hexopt_set_positions(c, X.data()), "set_positions");
-  }
+  const std::vector<int32_t> iC = ids(fc.ids_C), iT = ids(fc.ids_T), iL = ids(fc.ids_L), ib = ids(data.b);
+  const std::vector<double> Cp = fc.ids_C.size() ? rows3(fc.C) : std::vector<double>();
+  const std::vector<double> Tn = fc.ids_T.size() ? rows3(fc.normal_T) : std::vector<double>();
+  const std::vector<double> Ta(fc.dis_T.data(), fc.dis_T.data() + fc.ids_T.size());
+  const std::vector<double> La = fc.ids_L.size() ? rows3(fc.Axa_L) : std::vector<double>();
+  const std::vector<double> Lo = fc.ids_L.size() ? rows3(fc.origin_L) : std::vector<double>();
+  const std::vector<double> bc = data.b.size() ? rows3(data.bc) : std::vector<double>();
+  std::vector<double> post;
+  if (ts.known_value_post) post = rows3(ts.post_Variables);
+  hexopt_shim_core::SlimSetup st;
+  st.nv = data.V.rows();
+  st.V = V.data();
+  st.V_o = Vo.data();
+  st.ntets = data.F.rows();
+  st.T = T.data();
+  st.RT = RT.empty() ? nullptr : RT.data();
+  st.energy = (int)data.slim_energy;
+  st.precision = precision();
+  st.weight_opt = data.weight_opt;
+  st.nC = (int64_t)iC.size(); st.ids_C = iC.data(); st.C = Cp.data(); st.lamda_C = fc.lamda_C;
+  st.nT = (int64_t)iT.size(); st.ids_T = iT.data(); st.normal_T = Tn.data(); st.dis_T = Ta.data(); st.lamda_T = fc.lamda_T;
+  st.nL = (int64_t)iL.size(); st.ids_L = iL.data(); st.Axa_L = La.data(); st.origin_L = Lo.data(); st.lamda_L = fc.lamda_L;
+  st.projection = ts.projection;
+  st.nB = (int64_t)ib.size(); st.b = ib.data(); st.bc = bc.data(); st.lamda_projection = ts.lamda_projection;
+  st.glue = ts.glue;
+  st.n_ranges = (int64_t)ts.V_ranges.size(); st.V_ranges = ts.V_ranges.data(); st.lamda_glue = ts.lamda_glue;
+  st.known_value_post = ts.known_value_post;
+  st.post_index = ts.post_index;
+  st.post_Variables = post.empty() ? nullptr : post.data();
+  std::string err;
+  const int rc = hexopt_shim_core::load_slim(c, st, err);
+  if (rc == HEXOPT_ERR_UNSUPPORTED) unsupported(err);
+  if (rc != HEXOPT_OK) throw std::runtime_error("hexopt " + err);
   C.loaded = &data;
+}
+
+// The positions (and curve parameters) of the SLIM context back into data.V_o / data.a_L.
+static void download(SLIMData &data) {
+  hexopt_ctx *c = contexts().slim;
+  std::vector<double> X(3 * (size_t)data.V_o.rows());
+  ck(c, hexopt_get_positions(c, X.data()), "get_positions");
+  for (int64_t i = 0; i < data.V_o.rows(); i++)
+    for (int d = 0; d < 3; d++) data.V_o(i, d) = X[3 * i + d];
+  if (data.a_L.size() > 0) ck(c, hexopt_get_curve_params(c, data.a_L.data()), "get_curve_params");
 }
 
 }  // namespace hexopt_shim
@@ -210,11 +203,15 @@ void slim_precompute(Eigen::MatrixXd &V, Eigen::MatrixXi &F, Eigen::MatrixXd &V_
   data.exp_factor = 1.0;
   data.dim = 3;
   load(data);
-  hexopt_ctx *c = contexts().slim;
-  const std::vector<double> X = rows3(data.V_o);
-  double E = 0;
-  ck(c, hexopt_energy_fwd(c, X.data(), &E), "energy_fwd");
-  data.energy = E / data.mesh_area;
+  // data.energy: the start value of the first line search, which recomputes it anyway; the
+  // library's energy_fwd evaluates the symmetric Dirichlet energy
+  if (slim_energy == SYMMETRIC_DIRICHLET && !ts.glue && !ts.projection && !ts.known_value_post) {
+    hexopt_ctx *c = contexts().slim;
+    const std::vector<double> X = rows3(data.V_o);
+    double E = 0;
+    ck(c, hexopt_energy_fwd(c, X.data(), &E), "energy_fwd");
+    data.energy = E / data.mesh_area;
+  }
 }
 
 // The 18-argument overload (slim_m.h:89-100) feeds the projection / region path of slim_opt.
@@ -225,14 +222,32 @@ void slim_precompute(Eigen::MatrixXd &, Eigen::MatrixXi &, Eigen::MatrixXd &, SL
   unsupported("slim_precompute with explicit projection / region arguments");
 }
 
-// slim_m.cpp:1189-1291, fixed-count branch (:1269-1288): iter_num SLIM iterations, the energy
-// printed after each as the reference does.
+// The iter_num = -1 branch of slim_solve2 (schedule 2) / slim_solve (schedule 1): SLIM iterations
+// until the result mesh (glue groups at their means, or projection points at bc) has a positive
+// minimum scaled Jacobian, at most 50, with the glue weight schedules, printing as the reference.
+static Eigen::MatrixXd adaptive(SLIMData &data, int type, int schedule, bool verbose) {
+  hexopt_ctx *c = contexts().slim;
+  hexopt_adaptive_report rep;
+  std::memset(&rep, 0, sizeof rep);
+  ck(c, hexopt_slim_solve_adaptive(c, type, schedule, 50, &rep), "slim_solve_adaptive");
+  data.energy = rep.energy;
+  data.engery_quality = rep.energy_quality;
+  data.engery_soft = rep.energy_soft;
+  data.ts.lamda_glue = rep.lamda_glue;
+  if (verbose) {
+    if (!rep.converged) std::cout << "min J " << rep.min_Jacobian << "; ave J " << rep.ave_Jacobian << std::endl;
+    std::cout << "iterations taken " << rep.iterations << std::endl;
+  }
+  download(data);
+  return data.V_o;
+}
+
+// slim_m.cpp:1189-1291: the fixed-count branch (:1269-1288) prints the energy after each
+// iteration as the reference does; iter_num = -1 runs the adaptive branch (:1191-1268).
 Eigen::MatrixXd slim_solve2(SLIMData &data, int iter_num, int type, bool verbose) {
-  (void)type;
-  (void)verbose;
-  if (iter_num < 0) unsupported("the adaptive iteration count (iter_num == -1)");
   Contexts &C = contexts();
   if (C.loaded != &data) load(data);
+  if (iter_num < 0) return adaptive(data, type, 2, verbose);
   hexopt_ctx *c = C.slim;
   hexopt_slim_report rep;
   std::memset(&rep, 0, sizeof rep);
@@ -245,17 +260,17 @@ Eigen::MatrixXd slim_solve2(SLIMData &data, int iter_num, int type, bool verbose
     data.engery_quality = rep.energy_quality;
     data.engery_soft = rep.energy_soft;
   }
-  std::vector<double> X(3 * (size_t)data.V_o.rows());
-  ck(c, hexopt_get_positions(c, X.data()), "get_positions");
-  for (int64_t i = 0; i < data.V_o.rows(); i++)
-    for (int d = 0; d < 3; d++) data.V_o(i, d) = X[3 * i + d];
-  if (data.a_L.size() > 0) ck(c, hexopt_get_curve_params(c, data.a_L.data()), "get_curve_params");
+  download(data);
   return data.V_o;
 }
 
-// slim_m.cpp:1293-1394 (glue doubling after iteration 3) belongs to the untangling path.
-Eigen::MatrixXd slim_solve(SLIMData &, int, int, bool) {
-  unsupported("slim_solve (the untangling / glue driver)");
+// slim_m.cpp:1293-1394: as slim_solve2, with slim_solve's glue weight doubling in the adaptive
+// branch (:1311-1312).
+Eigen::MatrixXd slim_solve(SLIMData &data, int iter_num, int type, bool verbose) {
+  Contexts &C = contexts();
+  if (C.loaded != &data) load(data);
+  if (iter_num < 0) return adaptive(data, type, 1, verbose);
+  return slim_solve2(data, iter_num, type, verbose);
 }
 
 // metro_hausdorff.cpp:358-506: vertex-sampled two-sided Hausdorff between two triangle meshes
@@ -321,5 +336,58 @@ bool scaled_jacobian(Mesh &hmi, Mesh_Quality &mq) {
   mq.deviation_Jacobian = q.deviation_Jacobian;
   if (q.n_inverted > 0) std::cout << "flipped elements: " << q.n_inverted << std::endl;
   return true;
+}
+#endif
+
+#ifdef HEXOPT_SHIM_SLIM_OPT_IGL
+#include "optimization.h"
+// optimization::slim_opt_igl (optimization.cpp:970-1005) -- the modified igl::slim of the
+// smoothing stage (extern/libigl/include/igl/slim.cpp:1190-1288: M = weight_opt / 2, symmetric
+// Dirichlet) -- compiled in when that definition is removed from optimization.cpp.  The stage's
+// feature constraints are honoured; the igl variant's b / bc, region and Vgroups terms, which
+// the smoothing stage leaves empty, are rejected.
+void optimization::slim_opt_igl(Tetralize_Set &ts, const uint32_t iter) {
+  if (ts.projection || ts.b.size() > 0 || (ts.regionb.size() > 0 && ts.lamda_region != 0) || !ts.Vgroups.empty())
+    unsupported("the modified igl::slim's b / region / Vgroups terms");
+  hexopt_ctx *c = get(contexts().slim);
+  contexts().loaded = nullptr;
+  const std::vector<int32_t> T = tets_rows(ts.T);
+  const std::vector<double> RT = rt_rows(ts.RT, ts.T.rows());
+  const std::vector<double> V = rows3(ts.V);
+  const Feature_Constraints &fc = ts.fc;
+  const std::vector<int32_t> iC = ids(fc.ids_C), iT = ids(fc.ids_T), iL = ids(fc.ids_L);
+  const std::vector<double> Cp = fc.ids_C.size() ? rows3(fc.C) : std::vector<double>();
+  const std::vector<double> Tn = fc.ids_T.size() ? rows3(fc.normal_T) : std::vector<double>();
+  const std::vector<double> Ta(fc.dis_T.data(), fc.dis_T.data() + fc.ids_T.size());
+  const std::vector<double> La = fc.ids_L.size() ? rows3(fc.Axa_L) : std::vector<double>();
+  const std::vector<double> Lo = fc.ids_L.size() ? rows3(fc.origin_L) : std::vector<double>();
+  hexopt_shim_core::SlimSetup st;
+  st.nv = ts.V.rows();
+  st.V = V.data();
+  st.V_o = V.data();
+  st.ntets = ts.T.rows();
+  st.T = T.data();
+  st.RT = RT.empty() ? nullptr : RT.data();
+  st.energy = HEXOPT_SYMMETRIC_DIRICHLET;
+  st.precision = precision();
+  st.weight_opt = weight_opt;
+  st.variant = 1;
+  st.nC = (int64_t)iC.size(); st.ids_C = iC.data(); st.C = Cp.data(); st.lamda_C = fc.lamda_C;
+  st.nT = (int64_t)iT.size(); st.ids_T = iT.data(); st.normal_T = Tn.data(); st.dis_T = Ta.data(); st.lamda_T = fc.lamda_T;
+  st.nL = (int64_t)iL.size(); st.ids_L = iL.data(); st.Axa_L = La.data(); st.origin_L = Lo.data(); st.lamda_L = fc.lamda_L;
+  std::string err;
+  const int rc = hexopt_shim_core::load_slim(c, st, err);
+  if (rc == HEXOPT_ERR_UNSUPPORTED) unsupported(err);
+  if (rc != HEXOPT_OK) throw std::runtime_error("hexopt " + err);
+  hexopt_slim_report rep;
+  std::memset(&rep, 0, sizeof rep);
+  for (uint32_t i = 0; i < iter; i++) {
+    ck(c, hexopt_slim_iterate(c, 1, &rep), "slim_iterate");
+    std::cout << "energy: " << rep.energy << std::endl;  // igl/slim.cpp:1281
+  }
+  std::vector<double> X(3 * (size_t)ts.V.rows());
+  ck(c, hexopt_get_positions(c, X.data()), "get_positions");
+  for (int64_t i = 0; i < ts.V.rows(); i++)
+    for (int d = 0; d < 3; d++) ts.V(i, d) = X[3 * i + d];
 }
 #endif

@@ -169,6 +169,12 @@ HEXOPT_API int hexopt_get_lines(hexopt_ctx *ctx, double *axis, double *origin);
  * as the untangling path builds its shapes from another mesh's positions
  * (optimization.cpp:584); NULL restores the default.  Takes effect at the next precompute. */
 HEXOPT_API int hexopt_set_reference_hexes(hexopt_ctx *ctx, const double *P8);
+/* The reference tets themselves, as compute_referenceMesh writes them into Tetralize_Set::RT:
+ * 4 x 3 corner rows per tet, 8 tets per hex in hex_tetra_table order (n_hexes x 8 x 4 x 3
+ * doubles, the batch's hexes in order).  Any shapes -- cubes, cuboids, a hex's own corners --
+ * are taken as given; the operator of each tet is then grad_tet_ref's (grad.cpp:372-478) at the
+ * tet's positions at the next precompute.  NULL restores the default. */
+HEXOPT_API int hexopt_set_reference_tets(hexopt_ctx *ctx, const double *RT);
 
 /* ---- untangling path: Tetralize_Set's projection, glue and known-value terms ----
  * Projection points (ts.b / ts.bc, ts.projection): per mesh nB[m] vertex ids and targets (nB x

@@ -41,7 +41,7 @@ def _inc():
     ext = os.path.join(REF, "extern")
     return [f"-I{REF}", f"-I{ext}/eigen", f"-I{ext}/libigl/include", f"-I{ext}/geogram/src/lib",
             f"-I{ext}/tbb/include", f"-I{ext}/vcg", f"-I{ext}/libigl/external/embree/include",
-            f"-I{os.path.join(ROOT, 'include')}"]
+            f"-I{os.path.join(ROOT, 'include')}", f"-I{os.path.join(PKG, 'shim')}"]
 
 
 def _compile(out, extra=()):
@@ -107,3 +107,12 @@ def test_signature_drift_is_caught(objs):
     cpu = _unresolved([objs["slim_m"], objs["metro_hausdorff"], objs["global_functions"], *common])
     gpu = _unresolved([bad, objs["gf_local"], *common], objs["lib"])
     assert any("slim_solve2" in s for s in gpu - cpu)
+
+
+def test_shim_compiles_with_slim_opt_igl(objs):
+    """With HEXOPT_SHIM_SLIM_OPT_IGL the shim also defines optimization::slim_opt_igl (for a build
+    that drops the CPU definition from optimization.cpp)."""
+    out = str(objs["dir"] / "shim_igl.o")
+    _compile(out, extra=["-DHEXOPT_SHIM_SLIM_OPT_IGL"])
+    r = subprocess.run(["nm", "-C", "--defined-only", out], capture_output=True, text=True, check=True)
+    assert "optimization::slim_opt_igl(Tetralize_Set&, unsigned int)" in r.stdout
