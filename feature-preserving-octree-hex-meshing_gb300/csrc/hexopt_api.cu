@@ -140,6 +140,7 @@ struct hexopt_ctx {
   // device order of the batch (Morton-sorted vertices and hexes); the caller's order at the ABI
   int ordering = 2;  // 0 caller order, 1 Morton, 2 Morton unless the caller's numbering is coherent
   bool ordered = false;
+  int query_budget = 0;  // per-thread BVH traversal pops before the warp pass (0: the default 128)
   DBuf vnew2old, vold2new, hnew2old, hold2new;
   std::vector<int32_t> vold2new_h, hnew2old_h;
   bool has_fixed = false, has_glue = false;
@@ -719,6 +720,7 @@ ProjArgs make_proj(hexopt_ctx *c, int kind) {
   p.l_ids = c->l_ids.as<int32_t>(); p.l_curve = c->l_curve.as<int32_t>();
   p.l_axis = c->l_axis.as<double>(); p.l_orig = c->l_orig.as<double>();
   p.seed = c->qseed.as<int32_t>();
+  p.budget = c->query_budget;
   return p;
 }
 
@@ -739,6 +741,7 @@ HausArgs make_haus(hexopt_ctx *c, int kind) {
   h.partials = c->partials.as<double>();
   h.counters = c->counters.as<unsigned>();
   h.seed = c->qseed.as<int32_t>() + (kind == K_SURFV ? 2 : 1) * c->qseed_n;
+  h.budget = c->query_budget;
   return h;
 }
 
@@ -1511,6 +1514,26 @@ int hexopt_project_features(hexopt_ctx *ctx) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
   return run_projection(ctx);
+}
+
+int hexopt_set_query_budget(hexopt_ctx *ctx, int pops) {
+  if (!ctx) return HEXOPT_ERR_ARG;
+  if (pops < 0 || pops > (1 << 20)) return fail(ctx, HEXOPT_ERR_ARG, "set_query_budget: pops must be 0..2^20");
+  ctx->query_budget = pops;
+  ctx->tables_epoch++;  // a captured step bakes the budget in
+  return HEXOPT_OK;
+}
+
+int hexopt_query_stats(hexopt_ctx *ctx, int64_t *warp_queries, int64_t *candidates) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  unsigned w = 0, c = 0;
+  if (ctx->ovf_count.p) CK(cudaMemcpyAsync(&w, ctx->ovf_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+  if (ctx->cand_count.p) CK(cudaMemcpyAsync(&c, ctx->cand_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (warp_queries) *warp_queries = w;
+  if (candidates) *candidates = c;
+  return HEXOPT_OK;
 }
 
 // ---------------------------------------------------------------- Hausdorff

@@ -94,6 +94,7 @@ struct ProjArgs {
   // per projection item: the leaf that won its previous query (-1: none), whose FP32 upper
   // bound at the new position seeds the traversal's pruning bound
   int32_t *seed;
+  int budget;  // per-thread traversal pops before the warp pass takes a query over (0: default)
 };
 
 struct HausMesh {
@@ -119,6 +120,7 @@ struct HausArgs {
   double *partials;
   unsigned *counters;
   int32_t *seed;            // per sample item of this side: the previous winning leaf (-1: none)
+  int budget;               // per-thread traversal pops before the warp pass (0: default)
 };
 
 void bvh_morton(const BvhDev &b, const double lo[3], const double hi[3], unsigned long long *keys, cudaStream_t st);

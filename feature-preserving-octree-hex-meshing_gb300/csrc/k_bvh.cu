@@ -785,7 +785,7 @@ __device__ int warp_collect(const BvhDev &b, const double q[3], int32_t *sn, flo
   return __all_sync(0xffffffffu, ok) ? 0 : 1;
 }
 
-constexpr int kThreadBudget = 128;  // pops per query before handing over to the warp pass
+constexpr int kThreadBudget = 128;  // default pops per query before handing over to the warp pass
 __device__ __forceinline__ unsigned warps_total() { return gridDim.x * (blockDim.x >> 5); }
 __device__ __forceinline__ unsigned warp_global() { return blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); }
 
@@ -971,7 +971,7 @@ __global__ void __launch_bounds__(128) k_project(ProjArgs p) {
     proj_entry(p, md, i, q);
     int st = 0;
     seed_bound<0>(t.bvh, p.seed, i, q, ub);
-    if (t.bvh.n > 0) st = thread_collect<0>(t.bvh, q, ub, cl, cb, nc, kThreadBudget);
+    if (t.bvh.n > 0) st = thread_collect<0>(t.bvh, q, ub, cl, cb, nc, p.budget > 0 ? p.budget : kThreadBudget);
     if (st == 2) {
       p.ovf.best[i] = ub;
       push_overflow(p.ovf, i, sg.mesh);
@@ -1195,7 +1195,7 @@ __global__ void __launch_bounds__(128) k_haus_side(HausArgs h) {
     ub = dist_bound<1>(h.hm[sg.mesh].diag);
     seed_bound<1>(*b, h.seed, i, q, ub);
     int st = 0;
-    if (b->n > 0) st = thread_collect<1>(*b, q, ub, cl, cb, nc, kThreadBudget);
+    if (b->n > 0) st = thread_collect<1>(*b, q, ub, cl, cb, nc, h.budget > 0 ? h.budget : kThreadBudget);
     if (st == 2) {
       h.ovf.best[i] = ub;
       push_overflow(h.ovf, i, sg.mesh);

@@ -102,6 +102,8 @@ SIGNATURES = {
     "hexopt_signed_distance": (C.c_int, [_vp, C.c_int, C.c_int64, _d, _d, _i32, _d, _d]),
     "hexopt_set_feature_sets": (C.c_int, [_vp, _i64, _i32, _i64, _i32, _i32, _i64, _i64, _i32, _u8]),
     "hexopt_project_features": (C.c_int, [_vp]),
+    "hexopt_query_stats": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "hexopt_set_query_budget": (C.c_int, [_vp, C.c_int]),
     "hexopt_hausdorff": (C.c_int, [_vp, C.c_int64, _d, C.c_int64, _i32, C.c_int64, _d, C.c_int64, _i32, _d, _d, _d]),
     "hexopt_hausdorff_uniform": (C.c_int, [_vp, C.c_int64, _d, C.c_int64, _i32, C.c_int64, _d, C.c_int64, _i32,
                                            C.c_int64, C.c_uint64, _d, _d, _d, _d, _d]),
@@ -443,6 +445,15 @@ class Context:
 
     def project_features(self):
         self._ck(self.L.hexopt_project_features(self.h), "project_features")
+
+    def set_query_budget(self, pops=0):
+        self._ck(self.L.hexopt_set_query_budget(self.h, int(pops)), "set_query_budget")
+
+    def query_stats(self):
+        """(queries finished by the warp pass, candidate leaves) of the last BVH query pass."""
+        w, c = C.c_int64(), C.c_int64()
+        self._ck(self.L.hexopt_query_stats(self.h, C.byref(w), C.byref(c)), "query_stats")
+        return w.value, c.value
 
     # ---- Hausdorff
     def hausdorff(self, V0, F0, V1, F1):

@@ -264,6 +264,13 @@ HEXOPT_API int hexopt_set_feature_sets(hexopt_ctx *ctx, const int64_t *n_regular
                             const uint8_t *curve_closed);
 /* Recomputes tangent planes and line targets from the current positions. */
 HEXOPT_API int hexopt_project_features(hexopt_ctx *ctx);
+/* Work counters of the last BVH query pass (projection, or a Hausdorff side): the queries that
+ * went past the per-thread traversal budget to the warp-cooperative pass, and the candidate
+ * leaves recorded for exact FP64 evaluation. */
+HEXOPT_API int hexopt_query_stats(hexopt_ctx *ctx, int64_t *warp_queries, int64_t *candidates);
+/* Per-thread traversal budget of the BVH queries: node pops a query may take alone before the
+ * warp-cooperative pass takes it over (0 = the default, 128).  Results do not depend on it. */
+HEXOPT_API int hexopt_set_query_budget(hexopt_ctx *ctx, int pops);
 
 /* ---- Hausdorff (metro_hausdorff.cpp:358-506): vertex-sampled, two-sided ---- */
 HEXOPT_API int hexopt_hausdorff(hexopt_ctx *ctx, int64_t nv0, const double *V0, int64_t nf0, const int32_t *F0, int64_t nv1,
