@@ -64,6 +64,14 @@ void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cu
   k_cg_update<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
   if (with_dir) k_cg_dir<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
 }
+// The vector side of one PCG iteration without its element SpMV (timing).
+template <typename VT>
+void launch_cg_vec(const KArgs &a, int64_t vblk, int64_t cblk, cudaStream_t st) {
+  k_soft_mv<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a);
+  k_cg_alpha<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+  k_cg_update<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+  k_cg_dir<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+}
 template <typename VT>
 void launch_cg_dir(const KArgs &a, int64_t vblk, cudaStream_t st) {
   k_cg_dir<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
@@ -120,6 +128,7 @@ void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk
   template void launch_cg_start<VT>(const KArgs &, int64_t, cudaStream_t);                       \
   template void launch_cg_iter<VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t, bool); \
   template void launch_cg_dir<VT>(const KArgs &, int64_t, cudaStream_t);                         \
+  template void launch_cg_vec<VT>(const KArgs &, int64_t, int64_t, cudaStream_t);                \
   template void launch_fixed_pre<VT>(const KArgs &, int64_t, int64_t, cudaStream_t);             \
   template void launch_line_search<ET, VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t); \
   template void launch_ls_energy_pass<ET, VT>(const KArgs &, int64_t, cudaStream_t);
