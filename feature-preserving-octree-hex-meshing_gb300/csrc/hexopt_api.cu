@@ -140,12 +140,7 @@ struct hexopt_ctx {
   // device order of the batch (Morton-sorted vertices and hexes); the caller's order at the ABI
   int ordering = 2;  // 0 caller order, 1 Morton, 2 Morton unless the caller's numbering is coherent
   bool ordered = false;
-  int query_budget = 0;  // per-thread BVH traversal pops before the warp pass (0: the default 128)
-  bool query_packet = true;  // warp-packet BVH queries (else the per-thread pass + warp pass)
-  // packet order of the query items (projection, Hausdorff side 0, side 1; qseed's layout): a
-  // Morton sort of the query points, made before the first query pass after the item lists change
-  DBuf qperm, qsort;
-  bool qperm_ok[3] = {false, false, false};
+  int query_budget = 0;  // per-thread BVH traversal pops before the warp pass (0: the default 64)
   DBuf vnew2old, vold2new, hnew2old, hold2new;
   std::vector<int32_t> vold2new_h, hnew2old_h;
   bool has_fixed = false, has_glue = false;
@@ -664,8 +659,6 @@ int ensure_query_buffers(hexopt_ctx *ctx) {
   CK(ctx->qseed.ensure(sizeof(int32_t) * 3 * n));
   CK(cudaMemsetAsync(ctx->qseed.p, 0xFF, sizeof(int32_t) * 3 * n, ctx->st));  // -1: no seed yet
   ctx->qseed_n = n;
-  CK(ctx->qperm.ensure(sizeof(int32_t) * 3 * n));
-  for (bool &ok : ctx->qperm_ok) ok = false;
   // up to kQueryCandidates recorded candidates per query on average (a query over its share goes
   // to the exact fallback)
   constexpr int64_t kQueryCandidates = 16;
@@ -728,8 +721,6 @@ ProjArgs make_proj(hexopt_ctx *c, int kind) {
   p.l_axis = c->l_axis.as<double>(); p.l_orig = c->l_orig.as<double>();
   p.seed = c->qseed.as<int32_t>();
   p.budget = c->query_budget;
-  p.packet = c->query_packet ? 1 : 0;
-  p.qperm = c->qperm_ok[0] ? c->qperm.as<int32_t>() : nullptr;
   return p;
 }
 
@@ -749,59 +740,15 @@ HausArgs make_haus(hexopt_ctx *c, int kind) {
   h.surf_vs = c->surf_vs_d.as<int64_t>();
   h.partials = c->partials.as<double>();
   h.counters = c->counters.as<unsigned>();
-  const int region = kind == K_SURFV ? 2 : 1;
-  h.seed = c->qseed.as<int32_t>() + region * c->qseed_n;
+  h.seed = c->qseed.as<int32_t>() + (kind == K_SURFV ? 2 : 1) * c->qseed_n;
   h.budget = c->query_budget;
-  h.packet = c->query_packet ? 1 : 0;
-  h.qperm = c->qperm_ok[region] ? c->qperm.as<int32_t>() + region * c->qseed_n : nullptr;
   return h;
-}
-
-// The packet order of each query kind that lacks one: Morton keys of the query points at the
-// current positions, one radix sort per kind.  Runs outside graph capture (it may allocate its
-// sort workspace); the orders only steer which queries share a warp, never the results.
-int ensure_qperm(hexopt_ctx *ctx) {
-  if (!ctx->query_packet || !ctx->qperm.p) return HEXOPT_OK;
-  const int kinds[3] = {K_PROJ, K_TGTV, K_SURFV};
-  for (int r = 0; r < 3; r++) {
-    if (ctx->qperm_ok[r]) continue;
-    const int k = kinds[r];
-    int64_t n = 0;
-    for (int m = 0; m < ctx->n_meshes; m++) n += ctx->md[m].kcount[k];
-    if (n == 0) { ctx->qperm_ok[r] = true; continue; }
-    bool targets = true;
-    for (int m = 0; m < ctx->n_meshes; m++) targets = targets && (ctx->md[m].kcount[k] == 0 || ctx->tgt[m].set);
-    if (!targets || (k != K_PROJ && !ctx->haus_ready)) continue;  // no key box yet: item order
-    const size_t tmp = sort_pairs_u64_scratch(n);
-    const size_t head = (((size_t)n * 20) + 255) & ~(size_t)255;
-    CK(ctx->qsort.ensure(head + tmp));
-    auto *k_in = ctx->qsort.as<unsigned long long>();
-    auto *k_out = k_in + n;
-    auto *v_in = reinterpret_cast<int32_t *>(k_out + n);
-    if (k == K_PROJ) launch_proj_keys(make_proj(ctx, K_PROJ), ctx->kind[K_PROJ].nblk, k_in, v_in, ctx->st);
-    else launch_haus_keys(make_haus(ctx, k), k == K_TGTV ? 0 : 1, ctx->kind[k].nblk, k_in, v_in, ctx->st);
-    CK(sort_pairs_u64(k_in, k_out, v_in, ctx->qperm.as<int32_t>() + r * ctx->qseed_n, n,
-                      static_cast<char *>(ctx->qsort.p) + head, tmp, ctx->st));
-    ctx->launches += 2;
-    CKL();
-    ctx->qperm_ok[r] = true;
-  }
-  return HEXOPT_OK;
-}
-
-bool capturing(cudaStream_t st) {
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
 }
 
 int run_projection(hexopt_ctx *ctx) {
   if (ctx->NT) {
-    if (!capturing(ctx->st)) {
-      const int rc = ensure_qperm(ctx);
-      if (rc) return rc;
-    }
     launch_project(make_proj(ctx, K_PROJ), ctx->kind[K_PROJ].nblk, ctx->st);
-    ctx->launches += ctx->query_packet ? 4 : 5;
+    ctx->launches += 5;
   }
   if (ctx->NL) {
     launch_curve_project(make_proj(ctx, K_LINE), ctx->kind[K_LINE].nblk, ctx->st);
@@ -818,14 +765,10 @@ int run_hausdorff(hexopt_ctx *ctx) {
                     ctx->kind[K_SURFF].nblk, ctx->block[K_SURFF] * ctx->ipt[K_SURFF], ctx->st);
     ctx->launches += 1;
   }
-  if (!capturing(ctx->st)) {
-    const int rc = ensure_qperm(ctx);
-    if (rc) return rc;
-  }
   launch_haus_bbox(make_haus(ctx, K_SURFV), ctx->kind[K_SURFV].nblk, ctx->st);
   launch_haus_side(make_haus(ctx, K_TGTV), 0, ctx->kind[K_TGTV].nblk, ctx->st);
   launch_haus_side(make_haus(ctx, K_SURFV), 1, ctx->kind[K_SURFV].nblk, ctx->st);
-  ctx->launches += ctx->query_packet ? 11 : 13;
+  ctx->launches += 13;
   CKL();
   return HEXOPT_OK;
 }
@@ -1581,14 +1524,6 @@ int hexopt_set_query_budget(hexopt_ctx *ctx, int pops) {
   return HEXOPT_OK;
 }
 
-int hexopt_set_query_mode(hexopt_ctx *ctx, int mode) {
-  if (!ctx) return HEXOPT_ERR_ARG;
-  if (mode != 0 && mode != 1) return fail(ctx, HEXOPT_ERR_ARG, "set_query_mode: mode must be 0 or 1");
-  ctx->query_packet = mode == 0;
-  ctx->tables_epoch++;  // a captured step bakes the kernels in
-  return HEXOPT_OK;
-}
-
 int hexopt_query_stats(hexopt_ctx *ctx, int64_t *warp_queries, int64_t *candidates) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
@@ -1916,8 +1851,6 @@ int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_r
     rc = prepare_haus(ctx);
     if (rc) return rc;
   }
-  rc = ensure_qperm(ctx);  // before any capture: it may allocate
-  if (rc) return rc;
   if (ctx->use_graph) {
     if (ctx->graph_exec &&
         (ctx->graph_hausdorff != (do_hausdorff != 0) || ctx->graph_tables != ctx->tables_epoch ||

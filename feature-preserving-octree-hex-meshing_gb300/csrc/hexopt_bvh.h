@@ -95,8 +95,6 @@ struct ProjArgs {
   // bound at the new position seeds the traversal's pruning bound
   int32_t *seed;
   int budget;  // per-thread traversal pops before the warp pass takes a query over (0: default)
-  int packet;  // 1: warp-packet traversal in the order qperm; 0: per-thread pass + warp pass
-  const int32_t *qperm;  // packet order of the items (null: item order)
 };
 
 struct HausMesh {
@@ -123,8 +121,6 @@ struct HausArgs {
   unsigned *counters;
   int32_t *seed;            // per sample item of this side: the previous winning leaf (-1: none)
   int budget;               // per-thread traversal pops before the warp pass (0: default)
-  int packet;               // 1: warp-packet traversal in the order qperm; 0: per-thread + warp pass
-  const int32_t *qperm;     // packet order of this side's items (null: item order)
 };
 
 void bvh_morton(const BvhDev &b, const double lo[3], const double hi[3], unsigned long long *keys, cudaStream_t st);
@@ -140,11 +136,6 @@ void bvh_refit_batch(const RefitDev *R, const Seg *seg, const MeshDesc *md, int6
 // both passes of the tangent-plane projection
 void launch_project(const ProjArgs &p, int64_t nblk, cudaStream_t st);
 void launch_curve_project(const ProjArgs &p, int64_t nblk, cudaStream_t st);
-// Morton keys (mesh << 32 | code of the query point in the mesh's target box) and item ids of
-// the projection items / one Hausdorff side's items, for the packet order
-void launch_proj_keys(const ProjArgs &p, int64_t nblk, unsigned long long *keys, int32_t *vals, cudaStream_t st);
-void launch_haus_keys(const HausArgs &h, int side, int64_t nblk, unsigned long long *keys, int32_t *vals,
-                      cudaStream_t st);
 void launch_signed_distance(const TargetDev &t, int64_t np, const double *P, double *S, int32_t *I, double *C,
                             double *N, int *status, cudaStream_t st);
 void launch_haus_bbox(const HausArgs &h, int64_t nblk, cudaStream_t st);

@@ -143,10 +143,6 @@ cudaError_t order_batch(const double *rows, const uint32_t *H, int64_t NV, int64
                         const int64_t *hoff_d, int n_meshes, const double *box_d, int32_t *vnew2old, int32_t *vold2new,
                         int32_t *hnew2old, int32_t *hold2new, void *scratch, size_t scratch_bytes, cudaStream_t st);
 size_t order_scratch_bytes(int64_t NV, int64_t NH);
-// v_out = v_in ordered by the 64-bit keys (stable radix sort); tmp: sort_pairs_u64_scratch(n) bytes
-cudaError_t sort_pairs_u64(const unsigned long long *k_in, unsigned long long *k_out, const int32_t *v_in,
-                           int32_t *v_out, int64_t n, void *tmp, size_t tmp_bytes, cudaStream_t st);
-size_t sort_pairs_u64_scratch(int64_t n);
 void launch_hex_perm(const uint32_t *H, const int32_t *hnew2old, const int32_t *vold2new, int64_t nh, const int64_t *hoff,
                      const int64_t *voff, int n_meshes, uint32_t *hexv, cudaStream_t st);
 // dst[i] = src[perm[i]] (rows of `width` doubles; perm null = copy)

@@ -579,7 +579,12 @@ __device__ int thread_traverse(const BvhDev &b, const double q[3], double &best,
 // distance above the minimum.  A query with more candidates than it may record goes to the
 // exact per-thread search above (the *_fallback kernels).
 constexpr int kQCand = 16;     // candidates a per-thread query may hold
-constexpr int kWarpStack = 1024;
+// The warp pass runs one query per group of kGroup lanes (two per warp): its frontiers are
+// mostly narrower than a warp, so half-warp groups keep more lanes busy and twice the queries in
+// flight per SM for the same shared memory.
+constexpr int kGroup = 16;
+constexpr int kGroupsPerBlock = 128 / kGroup;
+constexpr int kWarpStack = 512;  // frontier entries a group may hold (overflow: exact fallback)
 constexpr int kWarpCand = 64;  // candidates a warp-pass query may hold
 
 __device__ __forceinline__ int warp_excl_scan(int v, int &total) {
@@ -671,50 +676,77 @@ __device__ int thread_collect(const BvhDev &b, const double q[3], float &ub, int
   return ok ? 0 : 1;
 }
 
-// In-order compaction of a warp's shared candidate list to the entries with lo <= ub.
-__device__ __forceinline__ int warp_compact(int32_t *cl, float *cb, int nc, float ub) {
-  const int lane = threadIdx.x & 31;
+// Lanes of this thread's group: the mask, the lane within the group and the group's shift.
+__device__ __forceinline__ unsigned group_shift() { return kGroup == 32 ? 0u : (threadIdx.x & 16u); }
+__device__ __forceinline__ unsigned group_mask() {
+  return kGroup == 32 ? 0xffffffffu : (0xffffu << group_shift());
+}
+__device__ __forceinline__ int group_lane() { return threadIdx.x & (kGroup - 1); }
+__device__ __forceinline__ unsigned group_ballot(bool pred) {
+  return (__ballot_sync(group_mask(), pred) & group_mask()) >> group_shift();
+}
+// Exclusive prefix sum over the group (all its lanes must call it); total = sum.
+__device__ __forceinline__ int group_excl_scan(int v, int &total) {
+  const unsigned gm = group_mask();
+  const int gl = group_lane();
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < kGroup; o <<= 1) {
+    const int y = __shfl_up_sync(gm, x, o, kGroup);
+    if (gl >= o) x += y;
+  }
+  total = __shfl_sync(gm, x, kGroup - 1, kGroup);
+  return x - v;
+}
+
+// In-order compaction of a group's shared candidate list to the entries with lo <= ub.
+__device__ __forceinline__ int group_compact(int32_t *cl, float *cb, int nc, float ub) {
+  const unsigned gm = group_mask();
+  const int gl = group_lane();
   int w = 0;
-  for (int k0 = 0; k0 < nc; k0 += 32) {
-    const int k = k0 + lane;
+  for (int k0 = 0; k0 < nc; k0 += kGroup) {
+    const int k = k0 + gl;
     const bool keep = k < nc && cb[k] <= ub;
-    const unsigned kb = __ballot_sync(0xffffffffu, keep);
+    const unsigned kb = group_ballot(keep);
     const int32_t lk = keep ? cl[k] : 0;
     const float bk = keep ? cb[k] : 0.f;
-    __syncwarp();
+    __syncwarp(gm);
     if (keep) {
-      const int pos = w + __popc(kb & ((1u << lane) - 1u));
+      const int pos = w + __popc(kb & ((1u << gl) - 1u));
       cl[pos] = lk;
       cb[pos] = bk;
     }
     w += __popc(kb);
-    __syncwarp();
+    __syncwarp(gm);
   }
   return w;
 }
 
-// Warp-cooperative collection for the queries left over by the per-thread pass: one query per
-// warp, up to 32 frontier entries per step (one per lane), LIFO frontier and candidate list in
-// shared memory, ub shared by the warp.  Returns 0 when done (cl/cb compacted to lo <= ub),
-// 1 on frontier overflow, 3 when more than kWarpCand candidates remain after compaction.
+// Group-cooperative collection for the queries left over by the per-thread pass: one query per
+// group of kGroup lanes, up to kGroup frontier entries per step (one per lane), LIFO frontier
+// and candidate list in shared memory, ub shared by the group.  Every collective names only
+// the group's lanes, so the two groups of a warp may run different numbers of steps.  Returns
+// 0 when done (cl/cb compacted to lo <= ub), 1 on frontier overflow or a malformed tree,
+// 3 when more than kWarpCand candidates remain after compaction.
 template <int MODE>
-__device__ int warp_collect(const BvhDev &b, const double q[3], int32_t *sn, float *sd, int32_t *cl, float *cb,
-                            float &ub, int &nc) {
-  const int lane = threadIdx.x & 31;
+__device__ int group_collect(const BvhDev &b, const double q[3], int32_t *sn, float *sd, int32_t *cl, float *cb,
+                             float &ub, int &nc) {
+  const unsigned gm = group_mask();
+  const int gl = group_lane();
   const int n = b.n;
   const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
   const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
   bool ok = true, full = false;
   int sz = 1;
   nc = 0;
-  if (lane == 0) { sn[0] = n == 1 ? ~0 : 0; sd[0] = -INFINITY; }
-  __syncwarp();
+  if (gl == 0) { sn[0] = n == 1 ? ~0 : 0; sd[0] = -INFINITY; }
+  __syncwarp(gm);
   for (int guard = 0; sz > 0 && !full && guard < 4 * (2 * n + 64); guard++) {
-    const int take = sz < 32 ? sz : 32;
-    const bool has = lane < take;
-    const int32_t node = has ? sn[sz - take + lane] : 0;
-    const float d = has ? sd[sz - take + lane] : INFINITY;
-    __syncwarp();
+    const int take = sz < kGroup ? sz : kGroup;
+    const bool has = gl < take;
+    const int32_t node = has ? sn[sz - take + gl] : 0;
+    const float d = has ? sd[sz - take + gl] : INFINITY;
+    __syncwarp(gm);
     sz -= take;
     int32_t push[2];
     float pd[2];
@@ -750,19 +782,19 @@ __device__ int warp_collect(const BvhDev &b, const double q[3], int32_t *sn, flo
     // tighten ub by this step's leaves, then record those still within it
     float hm = hi;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) hm = fminf(hm, __shfl_xor_sync(0xffffffffu, hm, o));
+    for (int o = kGroup / 2; o > 0; o >>= 1) hm = fminf(hm, __shfl_xor_sync(gm, hm, o, kGroup));
     ub = fminf(ub, hm);
     const bool rec = cand && lo <= ub;
-    const unsigned rb = __ballot_sync(0xffffffffu, rec);
+    const unsigned rb = group_ballot(rec);
     const int nrec = __popc(rb);
     if (nrec > 0) {
       if (nc + nrec > kWarpCand) {
-        nc = warp_compact(cl, cb, nc, ub);
+        nc = group_compact(cl, cb, nc, ub);
         if (nc + nrec > kWarpCand) full = true;
       }
       if (!full) {
         if (rec) {
-          const int pos = nc + __popc(rb & ((1u << lane) - 1u));
+          const int pos = nc + __popc(rb & ((1u << gl) - 1u));
           cl[pos] = ~node;
           cb[pos] = lo;
         }
@@ -770,163 +802,24 @@ __device__ int warp_collect(const BvhDev &b, const double q[3], int32_t *sn, flo
       }
     }
     int total;
-    const int off = warp_excl_scan(np, total);
+    const int off = group_excl_scan(np, total);
     const int room = kWarpStack - sz;
     for (int k = 0; k < np; k++)
       if (off + k < room) { sn[sz + off + k] = push[k]; sd[sz + off + k] = pd[k]; }
     if (total > room) ok = false;
-    __syncwarp();
+    __syncwarp(gm);
     sz += total < room ? total : room;
   }
-  __syncwarp();
+  __syncwarp(gm);
   if (full) return 3;
   if (sz > 0) ok = false;
-  nc = warp_compact(cl, cb, nc, ub);
-  return __all_sync(0xffffffffu, ok) ? 0 : 1;
+  nc = group_compact(cl, cb, nc, ub);
+  return group_ballot(!ok) ? 1 : 0;
 }
 
-// ---- warp-packet collection ----
-// The warp's lanes hold up to 32 queries against the same tree and walk it together.  A node is
-// expanded once for all lanes of its mask whose bound still reaches the node's box: every lane
-// reads the same 64-byte record (one broadcast load), tests both child boxes against its own
-// query and ub, and the lanes' votes make the child masks.  A leaf child is bounded at once by
-// the lanes that want it (lo / hi as in thread_collect); of two internal children the one that
-// is nearer for most lanes is expanded next and the other waits on the warp's stack with its
-// mask and box (re-tested against the lanes' bounds when popped).  Queries that lie close
-// together -- the query order is a Morton sort of the query points -- share most of their nodes,
-// so one load serves many lanes; unrelated queries cost what divergent per-thread traversals
-// cost.  Each lane records its leaves with lo <= ub in visiting order, so the exact pass that
-// follows returns the sequential search's result for it.  Per lane: 0 done, 1 stack overflow or
-// a malformed tree (the caller sends the query to the exact fallback), 3 more than kQCand
-// candidates remain after compaction (fallback too).
-constexpr int kPStack = 64;
-
-template <int MODE>
-__device__ int packet_collect(const BvhDev &b, bool active, const double q[3], float &ub, int32_t *cl, float *cb,
-                              int &nc, int32_t *sn, unsigned *sm, float *sbox) {
-  const unsigned lane_bit = 1u << (threadIdx.x & 31);
-  const bool leader = (threadIdx.x & 31) == 0;
-  const int n = b.n;
-  nc = 0;
-  if (n == 1) {  // b is the same for every lane of the warp
-    if (active) { cl[0] = 0; cb[0] = -INFINITY; nc = 1; }
-    return 0;
-  }
-  const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
-  const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
-  int st = 0;
-  unsigned alive = __ballot_sync(0xffffffffu, active && n > 1);
-  int32_t node = 0;          // the node to expand next (the root first, unboxed)
-  unsigned mask = alive;
-  bool carry = alive != 0, boxed = false;
-  float bx[6];
-  int sp = 0;
-  const int limit = 4 * (2 * n + 64);
-  for (int guard = 0;; guard++) {
-    if (carry && boxed) {  // a child carried over: re-test it against the bounds tightened since
-      const bool want = (mask & alive & lane_bit) && sqrtf(box_d2f(bx, qf)) - mbox <= ub;
-      mask = __ballot_sync(0xffffffffu, want);
-      carry = mask != 0;
-    }
-    while (!carry && sp > 0) {
-      --sp;
-      const int32_t en = sn[sp];
-      const unsigned em = sm[sp] & alive;
-#pragma unroll
-      for (int k = 0; k < 6; k++) bx[k] = sbox[6 * sp + k];
-      const bool want = (em & lane_bit) && sqrtf(box_d2f(bx, qf)) - mbox <= ub;
-      const unsigned m = __ballot_sync(0xffffffffu, want);
-      if (m) { node = en; mask = m; carry = true; }
-    }
-    __syncwarp();  // every lane has read the popped entry before the leader may reuse its slot
-    if (!carry) break;
-    if (guard >= limit) {  // cannot happen on a well-formed tree (each node is expanded once)
-      if (alive & lane_bit) st = 1;
-      break;
-    }
-    carry = false;
-    const bool in = (mask & lane_bit) != 0;
-    if (node < 0 || node >= n - 1) {
-      if (in) st = 1;
-      alive = __ballot_sync(0xffffffffu, (alive & lane_bit) && st == 0);
-      continue;
-    }
-    const NodeRec r = load_node(b.node, node);
-    if (r.l >= n - 1 || r.r >= n - 1 || ~r.l >= n || ~r.r >= n) {
-      if (in) st = 1;
-      alive = __ballot_sync(0xffffffffu, (alive & lane_bit) && st == 0);
-      continue;
-    }
-    float dl = INFINITY, dr = INFINITY;
-    if (in) {
-      dl = sqrtf(box_d2f(r.lb, qf)) - mbox;
-      dr = sqrtf(box_d2f(r.rb, qf)) - mbox;
-    }
-    const bool wl = in && dl <= ub, wr = in && dr <= ub;
-    const unsigned ml = __ballot_sync(0xffffffffu, wl), mr = __ballot_sync(0xffffffffu, wr);
-    const unsigned both = ml & mr;
-    const unsigned vote = __ballot_sync(0xffffffffu, wl && wr && dl <= dr);
-    const bool left_first = both ? 2 * __popc(vote) >= __popc(both) : ml != 0;
-    // leaf children, in visiting order, bounded now
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-      const bool left = (k == 0) == left_first;
-      const int32_t c = left ? r.l : r.r;
-      const unsigned mc = left ? ml : mr;
-      if (c >= 0 || !(mc & lane_bit) || st != 0) continue;
-      float lo, hi;
-      leaf_bounds<MODE>(b.leafd, ~c, qf, left ? dl : dr, lo, hi);
-      if (lo > ub) continue;
-      ub = fminf(ub, hi);
-      if (nc == kQCand) {
-        int w = 0;
-        for (int j = 0; j < nc; j++)
-          if (cb[j] <= ub) { cl[w] = cl[j]; cb[w] = cb[j]; w++; }
-        nc = w;
-        if (nc == kQCand) { st = 3; continue; }
-      }
-      cl[nc] = ~c;
-      cb[nc] = lo;
-      nc++;
-    }
-    alive = __ballot_sync(0xffffffffu, (alive & lane_bit) && st == 0);
-    // internal children: the first is expanded next, the second waits on the stack
-    const int32_t c0 = left_first ? r.l : r.r, c1 = left_first ? r.r : r.l;
-    const unsigned m0 = (left_first ? ml : mr) & alive, m1 = (left_first ? mr : ml) & alive;
-    const float *b0 = left_first ? r.lb : r.rb, *b1 = left_first ? r.rb : r.lb;
-    const bool go0 = c0 >= 0 && m0, go1 = c1 >= 0 && m1;
-    if (go0 && go1) {
-      if (sp < kPStack) {
-        if (leader) {
-          sn[sp] = c1;
-          sm[sp] = m1;
-#pragma unroll
-          for (int k = 0; k < 6; k++) sbox[6 * sp + k] = b1[k];
-        }
-        sp++;
-      } else {
-        if (m1 & lane_bit) st = 1;
-        alive = __ballot_sync(0xffffffffu, (alive & lane_bit) && st == 0);
-      }
-    }
-    if (go0) {
-      node = c0; mask = m0 & alive; carry = true; boxed = true;
-#pragma unroll
-      for (int k = 0; k < 6; k++) bx[k] = b0[k];
-    } else if (go1) {
-      node = c1; mask = m1 & alive; carry = true; boxed = true;
-#pragma unroll
-      for (int k = 0; k < 6; k++) bx[k] = b1[k];
-    }
-    __syncwarp();
-  }
-  __syncwarp();
-  return active ? st : 0;
-}
-
-constexpr int kThreadBudget = 128;  // default pops per query before handing over to the warp pass
-__device__ __forceinline__ unsigned warps_total() { return gridDim.x * (blockDim.x >> 5); }
-__device__ __forceinline__ unsigned warp_global() { return blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); }
+constexpr int kThreadBudget = 64;  // default pops per query before handing over to the warp pass
+__device__ __forceinline__ unsigned groups_total() { return gridDim.x * (blockDim.x / kGroup); }
+__device__ __forceinline__ unsigned group_global() { return blockIdx.x * (blockDim.x / kGroup) + threadIdx.x / kGroup; }
 
 __device__ __forceinline__ void push_overflow(const Overflow &o, int64_t item, int32_t mesh) {
   const unsigned k = atomicAdd(o.count, 1u);
@@ -972,16 +865,16 @@ __device__ bool store_cands_warp(const CandBuf &c, bool has, int64_t i, int32_t 
   return true;
 }
 
-// Warp pass: one query per warp, candidates already compacted in shared memory.
+// Warp pass: one query per group, candidates already compacted in shared memory.
 __device__ bool store_cands_query(const CandBuf &c, int64_t i, int32_t mesh, const double q[3], const int32_t *cl,
                                   int nc) {
-  const int lane = threadIdx.x & 31;
+  const int gl = group_lane();
   unsigned base = 0;
-  if (lane == 0 && nc > 0) base = atomicAdd(c.count, (unsigned)nc);
-  base = __shfl_sync(0xffffffffu, base, 0);
+  if (gl == 0 && nc > 0) base = atomicAdd(c.count, (unsigned)nc);
+  base = __shfl_sync(group_mask(), base, 0, kGroup);
   if ((int64_t)base + nc > c.cap) return false;
-  for (int j = lane; j < nc; j += 32) { c.leaf[base + j] = cl[j]; c.qi[base + j] = (int32_t)i; }
-  if (lane == 0) store_query(c, i, mesh, q, base, nc);
+  for (int j = gl; j < nc; j += kGroup) { c.leaf[base + j] = cl[j]; c.qi[base + j] = (int32_t)i; }
+  if (gl == 0) store_query(c, i, mesh, q, base, nc);
   return true;
 }
 
@@ -1126,13 +1019,13 @@ __global__ void __launch_bounds__(128) k_project(ProjArgs p) {
 }
 
 __global__ void __launch_bounds__(128) k_project_warp(ProjArgs p) {
-  __shared__ int32_t sn[4][kWarpStack];
-  __shared__ float sd[4][kWarpStack];
-  __shared__ int32_t scl[4][kWarpCand];
-  __shared__ float scb[4][kWarpCand];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ int32_t sn[kGroupsPerBlock][kWarpStack];
+  __shared__ float sd[kGroupsPerBlock][kWarpStack];
+  __shared__ int32_t scl[kGroupsPerBlock][kWarpCand];
+  __shared__ float scb[kGroupsPerBlock][kWarpCand];
+  const int g = threadIdx.x / kGroup, gl = group_lane();
   const unsigned cnt = *p.ovf.count;
-  for (unsigned k = warp_global(); k < cnt; k += warps_total()) {
+  for (unsigned k = group_global(); k < cnt; k += groups_total()) {
     const int64_t i = p.ovf.item[k];
     const int32_t m = p.ovf.mesh[k];
     const MeshDesc md = p.mesh[m];
@@ -1140,45 +1033,14 @@ __global__ void __launch_bounds__(128) k_project_warp(ProjArgs p) {
     proj_entry(p, md, i, q);
     float ub = (float)p.ovf.best[i];
     int nc = 0;
-    const int st = warp_collect<0>(p.tgt[m].bvh, q, sn[w], sd[w], scl[w], scb[w], ub, nc);
-    if (st == 3) {
-      if (lane == 0) push_fallback(p.cand, i, m);
-    } else {
-      if (st == 1 && lane == 0) atomicOr(&p.sc[m].status, 8);
-      if (!store_cands_query(p.cand, i, m, q, scl[w], nc) && lane == 0) push_fallback(p.cand, i, m);
+    const int st = group_collect<0>(p.tgt[m].bvh, q, sn[g], sd[g], scl[g], scb[g], ub, nc);
+    if (st != 0) {  // frontier or candidate overflow: the exact per-thread search
+      if (gl == 0) push_fallback(p.cand, i, m);
+    } else if (!store_cands_query(p.cand, i, m, q, scl[g], nc) && gl == 0) {
+      push_fallback(p.cand, i, m);
     }
-    __syncwarp();
+    __syncwarp(group_mask());
   }
-}
-
-// Packet pass: the block's 128 items in the packet order (qperm: Morton order of the query
-// points; null = item order), 32 queries per warp walking the tree together.
-__global__ void __launch_bounds__(128) k_project_packet(ProjArgs p) {
-  __shared__ int32_t sn[4][kPStack];
-  __shared__ unsigned sm[4][kPStack];
-  __shared__ float sbox[4][6 * kPStack];
-  const Seg sg = p.seg[blockIdx.x];
-  const int w = threadIdx.x >> 5;
-  const int64_t i0 = sg.begin + threadIdx.x;
-  bool has = i0 < sg.end;
-  const int64_t i = has && p.qperm ? (int64_t)p.qperm[i0] : i0;
-  const TargetDev &t = p.tgt[sg.mesh];
-  double q[3] = {0, 0, 0};
-  int32_t cl[kQCand];
-  float cb[kQCand];
-  int nc = 0;
-  float ub = INFINITY;
-  if (has) {
-    proj_entry(p, p.mesh[sg.mesh], i, q);
-    seed_bound<0>(t.bvh, p.seed, i, q, ub);
-  }
-  if (t.bvh.n > 0) {  // the same for the whole block (one mesh)
-    if (packet_collect<0>(t.bvh, has, q, ub, cl, cb, nc, sn[w], sm[w], sbox[w]) != 0) {
-      push_fallback(p.cand, i, sg.mesh);
-      has = false;
-    }
-  }
-  if (!store_cands_warp(p.cand, has, i, sg.mesh, q, cl, cb, nc, ub)) push_fallback(p.cand, i, sg.mesh);
 }
 
 // Winner of each projection query in recorded order (strict improvement), its closest point and
@@ -1381,13 +1243,13 @@ __global__ void __launch_bounds__(128) k_haus_side(HausArgs h) {
 
 template <int SIDE>
 __global__ void __launch_bounds__(128) k_haus_warp(HausArgs h) {
-  __shared__ int32_t sn[4][kWarpStack];
-  __shared__ float sd[4][kWarpStack];
-  __shared__ int32_t scl[4][kWarpCand];
-  __shared__ float scb[4][kWarpCand];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ int32_t sn[kGroupsPerBlock][kWarpStack];
+  __shared__ float sd[kGroupsPerBlock][kWarpStack];
+  __shared__ int32_t scl[kGroupsPerBlock][kWarpCand];
+  __shared__ float scb[kGroupsPerBlock][kWarpCand];
+  const int g = threadIdx.x / kGroup, gl = group_lane();
   const unsigned cnt = *h.ovf.count;
-  for (unsigned k = warp_global(); k < cnt; k += warps_total()) {
+  for (unsigned k = group_global(); k < cnt; k += groups_total()) {
     const int64_t i = h.ovf.item[k];
     const int32_t m = h.ovf.mesh[k];
     double q[3];
@@ -1395,83 +1257,14 @@ __global__ void __launch_bounds__(128) k_haus_warp(HausArgs h) {
     haus_query<SIDE>(h, i, m, q, b);
     float ub = (float)h.ovf.best[i];
     int nc = 0;
-    const int st = warp_collect<1>(*b, q, sn[w], sd[w], scl[w], scb[w], ub, nc);
-    if (st == 3) {
-      if (lane == 0) push_fallback(h.cand, i, m);
-    } else {
-      if (st == 1 && lane == 0) atomicOr(&h.sc[m].status, 8);
-      if (!store_cands_query(h.cand, i, m, q, scl[w], nc) && lane == 0) push_fallback(h.cand, i, m);
+    const int st = group_collect<1>(*b, q, sn[g], sd[g], scl[g], scb[g], ub, nc);
+    if (st != 0) {  // frontier or candidate overflow: the exact per-thread search
+      if (gl == 0) push_fallback(h.cand, i, m);
+    } else if (!store_cands_query(h.cand, i, m, q, scl[g], nc) && gl == 0) {
+      push_fallback(h.cand, i, m);
     }
-    __syncwarp();
+    __syncwarp(group_mask());
   }
-}
-
-// Packet pass of one Hausdorff side (k_project_packet's scheme, PointDistanceEP bounds).
-template <int SIDE>
-__global__ void __launch_bounds__(128) k_haus_packet(HausArgs h) {
-  __shared__ int32_t sn[4][kPStack];
-  __shared__ unsigned sm[4][kPStack];
-  __shared__ float sbox[4][6 * kPStack];
-  const Seg sg = h.seg[blockIdx.x];
-  const int w = threadIdx.x >> 5;
-  const int64_t i0 = sg.begin + threadIdx.x;
-  bool has = i0 < sg.end;
-  const int64_t i = has && h.qperm ? (int64_t)h.qperm[i0] : i0;
-  const BvhDev *b = SIDE == 0 ? &h.surf[sg.mesh] : &h.tgt[sg.mesh].bvh;
-  double q[3] = {0, 0, 0};
-  int32_t cl[kQCand];
-  float cb[kQCand];
-  int nc = 0;
-  float ub = dist_bound<1>(h.hm[sg.mesh].diag);
-  if (has) {
-    haus_query<SIDE>(h, i, sg.mesh, q, b);
-    seed_bound<1>(*b, h.seed, i, q, ub);
-  }
-  if (b->n > 0) {  // the same for the whole block (one mesh)
-    if (packet_collect<1>(*b, has, q, ub, cl, cb, nc, sn[w], sm[w], sbox[w]) != 0) {
-      push_fallback(h.cand, i, sg.mesh);
-      has = false;
-    }
-  }
-  if (!store_cands_warp(h.cand, has, i, sg.mesh, q, cl, cb, nc, ub)) push_fallback(h.cand, i, sg.mesh);
-}
-
-// ---- packet order: Morton codes of the query points in the mesh's target box ----
-__device__ __forceinline__ unsigned long long query_key(int32_t mesh, const BvhDev &b, const double q[3]) {
-  uint32_t code = 0;
-  if (b.n > 1) {
-    const NodeRec r = load_node(b.node, 0);
-    uint32_t c[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      const float lo = fminf(r.lb[d], r.rb[d]), hi = fmaxf(r.lb[3 + d], r.rb[3 + d]);
-      const float ext = hi - lo;
-      const float t = ext > 0.f ? (float(q[d]) - lo) / ext : 0.f;
-      c[d] = (uint32_t)fminf(fmaxf(t * 1024.f, 0.f), 1023.f);
-    }
-    code = (expand_bits(c[0]) << 2) | (expand_bits(c[1]) << 1) | expand_bits(c[2]);
-  }
-  return ((unsigned long long)(uint32_t)mesh << 32) | code;
-}
-__global__ void __launch_bounds__(128) k_proj_keys(ProjArgs p, unsigned long long *keys, int32_t *vals) {
-  const Seg sg = p.seg[blockIdx.x];
-  const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
-  double q[3];
-  proj_entry(p, p.mesh[sg.mesh], i, q);
-  keys[i] = query_key(sg.mesh, p.tgt[sg.mesh].bvh, q);
-  vals[i] = (int32_t)i;
-}
-template <int SIDE>
-__global__ void __launch_bounds__(128) k_haus_keys(HausArgs h, unsigned long long *keys, int32_t *vals) {
-  const Seg sg = h.seg[blockIdx.x];
-  const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
-  double q[3];
-  const BvhDev *b;
-  haus_query<SIDE>(h, i, sg.mesh, q, b);
-  keys[i] = query_key(sg.mesh, h.tgt[sg.mesh].bvh, q);
-  vals[i] = (int32_t)i;
 }
 
 // Per-sample distance from the recorded candidates: PointDistanceEP's bound test against the
@@ -1638,12 +1431,8 @@ void launch_project(const ProjArgs &p, int64_t nblk, cudaStream_t st) {
   cudaMemsetAsync(p.ovf.count, 0, sizeof(unsigned), st);
   cudaMemsetAsync(p.cand.count, 0, sizeof(unsigned), st);
   cudaMemsetAsync(p.cand.fb_count, 0, sizeof(unsigned), st);
-  if (p.packet) {
-    k_project_packet<<<(unsigned)nblk, 128, 0, st>>>(p);
-  } else {
-    k_project<<<(unsigned)nblk, 128, 0, st>>>(p);
-    k_project_warp<<<kWarpGrid, 128, 0, st>>>(p);
-  }
+  k_project<<<(unsigned)nblk, 128, 0, st>>>(p);
+  k_project_warp<<<kWarpGrid, 128, 0, st>>>(p);
   k_cand_eval<0, 0><<<kEvalGrid, 128, 0, st>>>(p.cand, p.tgt, nullptr);
   k_project_finish<<<(unsigned)nblk, 128, 0, st>>>(p);
   k_project_fallback<<<kWarpGrid, 128, 0, st>>>(p);
@@ -1663,38 +1452,20 @@ void launch_haus_side(const HausArgs &h, int side, int64_t nblk, cudaStream_t st
   cudaMemsetAsync(h.cand.count, 0, sizeof(unsigned), st);
   cudaMemsetAsync(h.cand.fb_count, 0, sizeof(unsigned), st);
   if (side == 0) {  // target samples against the boundary surface
-    if (h.packet) {
-      k_haus_packet<0><<<(unsigned)nblk, 128, 0, st>>>(h);
-    } else {
-      k_haus_side<0><<<(unsigned)nblk, 128, 0, st>>>(h);
-      k_haus_warp<0><<<kWarpGrid, 128, 0, st>>>(h);
-    }
+    k_haus_side<0><<<(unsigned)nblk, 128, 0, st>>>(h);
+    k_haus_warp<0><<<kWarpGrid, 128, 0, st>>>(h);
     k_cand_eval<1, 1><<<kEvalGrid, 128, 0, st>>>(h.cand, h.tgt, h.surf);
     k_haus_finish<0><<<(unsigned)nblk, 128, 0, st>>>(h);
     k_haus_fallback<0><<<kWarpGrid, 128, 0, st>>>(h);
     k_haus_reduce<0><<<(unsigned)nblk, 128, 0, st>>>(h);
   } else {  // surface samples against the target
-    if (h.packet) {
-      k_haus_packet<1><<<(unsigned)nblk, 128, 0, st>>>(h);
-    } else {
-      k_haus_side<1><<<(unsigned)nblk, 128, 0, st>>>(h);
-      k_haus_warp<1><<<kWarpGrid, 128, 0, st>>>(h);
-    }
+    k_haus_side<1><<<(unsigned)nblk, 128, 0, st>>>(h);
+    k_haus_warp<1><<<kWarpGrid, 128, 0, st>>>(h);
     k_cand_eval<1, 0><<<kEvalGrid, 128, 0, st>>>(h.cand, h.tgt, h.surf);
     k_haus_finish<1><<<(unsigned)nblk, 128, 0, st>>>(h);
     k_haus_fallback<1><<<kWarpGrid, 128, 0, st>>>(h);
     k_haus_reduce<1><<<(unsigned)nblk, 128, 0, st>>>(h);
   }
-}
-
-void launch_proj_keys(const ProjArgs &p, int64_t nblk, unsigned long long *keys, int32_t *vals, cudaStream_t st) {
-  if (nblk > 0) k_proj_keys<<<(unsigned)nblk, 128, 0, st>>>(p, keys, vals);
-}
-void launch_haus_keys(const HausArgs &h, int side, int64_t nblk, unsigned long long *keys, int32_t *vals,
-                      cudaStream_t st) {
-  if (nblk <= 0) return;
-  if (side == 0) k_haus_keys<0><<<(unsigned)nblk, 128, 0, st>>>(h, keys, vals);
-  else k_haus_keys<1><<<(unsigned)nblk, 128, 0, st>>>(h, keys, vals);
 }
 
 }  // namespace hexopt

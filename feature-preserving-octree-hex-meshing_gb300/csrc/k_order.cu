@@ -137,17 +137,6 @@ size_t order_scratch_bytes(int64_t NV, int64_t NH) {
                                   (int32_t *)nullptr, (int32_t *)nullptr, (int)n, 0, 64, (cudaStream_t)0);
   return (((size_t)n * 20 + 255) & ~(size_t)255) + tb;
 }
-cudaError_t sort_pairs_u64(const unsigned long long *k_in, unsigned long long *k_out, const int32_t *v_in,
-                           int32_t *v_out, int64_t n, void *tmp, size_t tmp_bytes, cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
-  return cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, k_in, k_out, v_in, v_out, (int)n, 0, 64, st);
-}
-size_t sort_pairs_u64_scratch(int64_t n) {
-  size_t tb = 0;
-  cub::DeviceRadixSort::SortPairs(nullptr, tb, (unsigned long long *)nullptr, (unsigned long long *)nullptr,
-                                  (int32_t *)nullptr, (int32_t *)nullptr, (int)(n > 0 ? n : 1), 0, 64, (cudaStream_t)0);
-  return tb;
-}
 void launch_hex_perm(const uint32_t *H, const int32_t *hnew2old, const int32_t *vold2new, int64_t nh, const int64_t *hoff,
                      const int64_t *voff, int n_meshes, uint32_t *hexv, cudaStream_t st) {
   if (nh > 0) k_hex_perm<<<grid_of(nh), 256, 0, st>>>(H, hnew2old, vold2new, nh, hoff, voff, n_meshes, hexv);

@@ -104,7 +104,6 @@ SIGNATURES = {
     "hexopt_project_features": (C.c_int, [_vp]),
     "hexopt_query_stats": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "hexopt_set_query_budget": (C.c_int, [_vp, C.c_int]),
-    "hexopt_set_query_mode": (C.c_int, [_vp, C.c_int]),
     "hexopt_hausdorff": (C.c_int, [_vp, C.c_int64, _d, C.c_int64, _i32, C.c_int64, _d, C.c_int64, _i32, _d, _d, _d]),
     "hexopt_hausdorff_uniform": (C.c_int, [_vp, C.c_int64, _d, C.c_int64, _i32, C.c_int64, _d, C.c_int64, _i32,
                                            C.c_int64, C.c_uint64, _d, _d, _d, _d, _d]),
@@ -449,10 +448,6 @@ class Context:
 
     def set_query_budget(self, pops=0):
         self._ck(self.L.hexopt_set_query_budget(self.h, int(pops)), "set_query_budget")
-
-    def set_query_mode(self, mode=0):
-        """0: warp-packet BVH queries (default); 1: per-thread queries with a warp pass."""
-        self._ck(self.L.hexopt_set_query_mode(self.h, int(mode)), "set_query_mode")
 
     def query_stats(self):
         """(queries finished by the warp pass, candidate leaves) of the last BVH query pass."""

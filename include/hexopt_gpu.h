@@ -265,17 +265,13 @@ HEXOPT_API int hexopt_set_feature_sets(hexopt_ctx *ctx, const int64_t *n_regular
 /* Recomputes tangent planes and line targets from the current positions. */
 HEXOPT_API int hexopt_project_features(hexopt_ctx *ctx);
 /* Work counters of the last BVH query pass (projection, or a Hausdorff side): the queries that
- * went past the per-thread traversal budget to the warp-cooperative pass (0 in the packet
- * mode), and the candidate leaves recorded for exact FP64 evaluation. */
+ * went past the per-thread traversal budget to the warp-cooperative pass, and the candidate
+ * leaves recorded for exact FP64 evaluation. */
 HEXOPT_API int hexopt_query_stats(hexopt_ctx *ctx, int64_t *warp_queries, int64_t *candidates);
 /* Per-thread traversal budget of the BVH queries: node pops a query may take alone before the
- * warp-cooperative pass takes it over (0 = the default, 128).  Results do not depend on it. */
+ * group-cooperative pass takes it over (0 = the default, 64).  Results do not depend on it. */
 HEXOPT_API int hexopt_set_query_budget(hexopt_ctx *ctx, int pops);
-/* How the projection and Hausdorff queries walk their BVH: 0 (default) = warp packets, the
- * queries of a warp (taken in the Morton order of their points) walking the tree together;
- * 1 = one query per thread, handing queries over the per-thread budget to a warp-cooperative
- * pass.  Results do not depend on the mode. */
-HEXOPT_API int hexopt_set_query_mode(hexopt_ctx *ctx, int mode);
+
 
 /* ---- Hausdorff (metro_hausdorff.cpp:358-506): vertex-sampled, two-sided ---- */
 HEXOPT_API int hexopt_hausdorff(hexopt_ctx *ctx, int64_t nv0, const double *V0, int64_t nf0, const int32_t *F0, int64_t nv1,

@@ -245,16 +245,16 @@ def test_hausdorff_meshes_matches_oracle(ctx, hx, oracle):
     assert abs(mx[0] - ref[1]) <= 1e-5 * ref[0] and abs(av[0] - ref[2]) <= 1e-5 * ref[0]
 
 
-@pytest.mark.parametrize("mode", [0, 1])
-def test_seeded_queries_match_oracle(ctx, hx, oracle, mode):
+@pytest.mark.parametrize("budget", [0, 8])
+def test_seeded_queries_match_oracle(ctx, hx, oracle, budget):
     """Projection and Hausdorff queries start their pruning bound from the leaf that won the
     query's previous search.  After the points move (a little, then far, so seeds go stale), the
     tangent planes and the two-sided Hausdorff still equal the oracle's exact search, with the
-    queries walking the trees in warp packets (mode 0) or one per thread (mode 1)."""
+    default per-thread budget and with one that hands nearly every query to the warp pass."""
     from hexopt import workloads
     p = workloads.cylinder()
     workloads.load(ctx, [p])
-    ctx.set_query_mode(mode)
+    ctx.set_query_budget(budget)
     reg = np.asarray(p["regular"], np.int64)
     rng = np.random.default_rng(12)
     for step, amp in enumerate([0.0, 1e-3, 2e-3, 5e-2]):
@@ -268,31 +268,33 @@ def test_seeded_queries_match_oracle(ctx, hx, oracle, mode):
         dg, mx, av = ctx.hausdorff_meshes()
         ref = oracle.hausdorff(p["TV"], p["TF"], V, p["surface"])
         assert abs(mx[0] - ref[1]) <= 1e-9 * ref[0] and abs(av[0] - ref[2]) <= 1e-9 * ref[0], step
-    ctx.set_query_mode(0)
+    ctx.set_query_budget(0)
 
 
-def test_packet_queries_match_per_thread_queries(ctx, hx, oracle):
-    """The warp-packet traversal (Morton-ordered queries, 32 per warp walking the tree together)
-    and the per-thread traversal give the same tangent planes and Hausdorff distances on a
-    2-mesh batch of jittered grids whose boundaries start far from their superellipsoid targets
-    (long traversals, partial warps at the mesh ends), and both match the oracle's search on a
-    sample of the projection queries."""
+def test_query_budget_does_not_change_results(ctx, hx, oracle):
+    """The per-thread traversal budget only decides which pass finishes a query: every query
+    per-thread (a budget above any traversal), most of them in the warp-cooperative pass
+    (budget 16) and the default give the same tangent planes and Hausdorff distances on a
+    2-mesh batch of jittered grids whose boundaries start far from their superellipsoid
+    targets, and they match the oracle's search on a sample of the projection queries."""
     from hexopt import workloads
     ps = [workloads.grid_box_superellipsoid((23, 17, 29), 0.2, 3, 20000, 4.0),
           workloads.grid_box_superellipsoid((31, 26, 19), 0.2, 4, 30000, 2.5)]
     workloads.load(ctx, ps)
     out = {}
-    for mode in (1, 0):
-        ctx.set_query_mode(mode)
+    for budget in (1 << 20, 16, 0):
+        ctx.set_query_budget(budget)
         ctx.project_features()
         tot = sum(len(p["regular"]) for p in ps)
         nrm, dis = ctx.get_tangents(tot)
-        out[mode] = (nrm, dis, ctx.hausdorff_meshes())
-    ctx.set_query_mode(0)
-    np.testing.assert_allclose(out[0][0], out[1][0], rtol=0, atol=1e-12)
-    np.testing.assert_allclose(out[0][1], out[1][1], rtol=0, atol=1e-12)
-    for k in range(3):
-        np.testing.assert_allclose(out[0][2][k], out[1][2][k], rtol=1e-12, atol=0)
+        out[budget] = (nrm, dis, ctx.hausdorff_meshes(), ctx.query_stats())
+    ctx.set_query_budget(0)
+    assert out[16][3][0] > 0 and out[1 << 20][3][0] == 0  # warp-pass queries of the last pass
+    for b in (16, 1 << 20):
+        np.testing.assert_allclose(out[b][0], out[0][0], rtol=0, atol=1e-12)
+        np.testing.assert_allclose(out[b][1], out[0][1], rtol=0, atol=1e-12)
+        for k in range(3):
+            np.testing.assert_allclose(out[b][2][k], out[0][2][k], rtol=1e-12, atol=0)
     p = ps[0]
     reg = np.asarray(p["regular"], np.int64)
     sel = np.random.default_rng(5).choice(len(reg), 500, replace=False)
