@@ -147,7 +147,7 @@ struct hexopt_ctx {
   KindTable kind[8];
   // items per block: hex 128, unknowns 256 x ipt, constraints 256, queries 128
   int block[8] = {128, 256, 256, 128, 128, 128, 128, 128};  // K_CONS follows K_VERT's size
-  int ipt[8] = {1, 4, 1, 1, 1, 1, 1, 1};                     // items per thread of each kind
+  int ipt[8] = {1, 8, 1, 1, 1, 1, 1, 1};                     // items per thread of each kind
   // SLIM
   hexopt_slim_params params{};
   bool precomputed = false;
@@ -356,6 +356,7 @@ KArgs make_args(hexopt_ctx *c) {
   a.hseg = c->kind[K_HEX].dev.as<Seg>();
   a.vseg = c->kind[K_VERT].dev.as<Seg>();
   a.cseg = c->kind[K_CONS].dev.as<Seg>();
+  a.hblk = c->kind[K_HEX].nblk;
   a.partials = c->partials.as<double>();
   a.counters = c->counters.as<unsigned>();
   a.hexv = c->hexv.as<uint32_t>();
@@ -2158,6 +2159,10 @@ int hexopt_set_block_size(hexopt_ctx *ctx, int kind, int threads) {
   } else if (kind == 1) {
     if (threads != 64 && threads != 128 && threads != 256) return fail(ctx, HEXOPT_ERR_ARG, "vertex block size must be 64, 128 or 256");
     ctx->block[K_VERT] = threads;
+  } else if (kind == 2) {
+    if (threads != 1 && threads != 2 && threads != 4 && threads != 8 && threads != 16)
+      return fail(ctx, HEXOPT_ERR_ARG, "vertex items per thread must be 1, 2, 4, 8 or 16");
+    ctx->ipt[K_VERT] = threads;
   } else {
     return fail(ctx, HEXOPT_ERR_ARG, "unknown kind");
   }
@@ -2166,8 +2171,9 @@ int hexopt_set_block_size(hexopt_ctx *ctx, int kind, int threads) {
   return HEXOPT_OK;
 }
 
-// Times one SLIM iteration for each (hex block, vertex block, line-search candidates) setting on
-// a copy of the positions, keeps the fastest, restores the positions and scalars.
+// Times one SLIM iteration for each (hex block, vertex block, vertices per thread, line-search
+// candidates) setting on a copy of the positions, keeps the fastest, restores the positions and
+// scalars.
 int hexopt_autotune(hexopt_ctx *ctx) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
@@ -2177,19 +2183,20 @@ int hexopt_autotune(hexopt_ctx *ctx) {
   rc = pull_scalars(ctx);
   if (rc) return rc;
   const std::vector<MeshScalars> sc0 = ctx->sc;
-  const int hb[2] = {64, 128}, vb[2] = {128, 256};
+  const int hb[2] = {64, 128}, vb[2] = {128, 256}, vi[2] = {4, 8};
   // candidate counts whose energy-pass variants run without register spills in each mode
   const int lc[3] = {1, 2, ctx->mixed ? 4 : 2};
   float best = INFINITY;
-  int bh = ctx->block[K_HEX], bv = ctx->block[K_VERT], bl = ctx->params.ls_candidates;
+  int bh = ctx->block[K_HEX], bv = ctx->block[K_VERT], bi = ctx->ipt[K_VERT], bl = ctx->params.ls_candidates;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   for (int i = 0; i < 2; i++)
-    for (int j = 0; j < 2; j++)
+    for (int j = 0; j < 4; j++)
       for (int k = 0; k < 3; k++) {
         ctx->block[K_HEX] = hb[i];
-        ctx->block[K_VERT] = vb[j];
+        ctx->block[K_VERT] = vb[j & 1];
+        ctx->ipt[K_VERT] = vi[j >> 1];
         ctx->params.ls_candidates = lc[k];
         rc = rebuild_tables(ctx);
         if (rc) return rc;
@@ -2206,12 +2213,13 @@ int hexopt_autotune(hexopt_ctx *ctx) {
           CK(cudaEventSynchronize(e1));
           CK(cudaEventElapsedTime(&ms, e0, e1));
         }
-        if (ms < best) { best = ms; bh = hb[i]; bv = vb[j]; bl = lc[k]; }
+        if (ms < best) { best = ms; bh = hb[i]; bv = vb[j & 1]; bi = vi[j >> 1]; bl = lc[k]; }
       }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   ctx->block[K_HEX] = bh;
   ctx->block[K_VERT] = bv;
+  ctx->ipt[K_VERT] = bi;
   ctx->params.ls_candidates = bl;
   rc = rebuild_tables(ctx);
   if (rc) return rc;
@@ -2224,10 +2232,11 @@ int hexopt_autotune(hexopt_ctx *ctx) {
   return HEXOPT_OK;
 }
 
-int hexopt_get_tuning(const hexopt_ctx *ctx, int *hex_block, int *vert_block, int *ls_candidates) {
+int hexopt_get_tuning(const hexopt_ctx *ctx, int *hex_block, int *vert_block, int *vert_items, int *ls_candidates) {
   if (!ctx) return HEXOPT_ERR_ARG;
   if (hex_block) *hex_block = ctx->block[K_HEX];
   if (vert_block) *vert_block = ctx->block[K_VERT];
+  if (vert_items) *vert_items = ctx->ipt[K_VERT];
   if (ls_candidates) *ls_candidates = ctx->params.ls_candidates;
   return HEXOPT_OK;
 }

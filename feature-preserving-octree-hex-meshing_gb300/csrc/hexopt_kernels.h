@@ -13,6 +13,7 @@ struct KArgs {
   const MeshDesc *mesh;
   MeshScalars *sc;
   const Seg *hseg, *vseg, *cseg;
+  int64_t hblk;  // hex blocks: an element-SpMV launch's blocks past them run the soft terms
   double *partials;
   unsigned *counters;
   // geometry
@@ -94,7 +95,7 @@ template <typename ET, typename VT> void launch_ls_energy_pass(const KArgs &a, i
 template <typename ET, typename VT> void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st);
 
 // Launches per call of the launchers above (for the launch count).
-constexpr int kLaunchesCgIter = 5;
+constexpr int kLaunchesCgIter = 4;  // element + soft SpMV, alpha, update, direction
 constexpr int kLaunchesIrInitial = 2, kLaunchesIrReplace = 4, kLaunchesIrFinal = 1;
 
 // ---- reference shapes (k_shapes.cu) ----

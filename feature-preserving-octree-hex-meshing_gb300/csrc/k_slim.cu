@@ -58,8 +58,7 @@ void launch_cg_start(const KArgs &a, int64_t nblk, cudaStream_t st) {
 }
 template <typename VT>
 void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st, bool with_dir) {
-  k_spmv<VT><<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
-  k_soft_mv<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a);
+  k_spmv<VT><<<(unsigned)(hblk + cblk), a.hthreads, 0, st>>>(a);  // element and soft terms
   k_cg_alpha<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
   k_cg_update<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
   if (with_dir) k_cg_dir<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);

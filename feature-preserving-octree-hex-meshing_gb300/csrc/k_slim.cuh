@@ -205,6 +205,60 @@ __global__ void __launch_bounds__(128, sizeof(ET) == 4 ? 5 : 1) k_local(KArgs a)
   if (PRE && degenerate) atomicOr(&a.sc[sg.mesh].status, 2);
 }
 
+// q += S p for the soft-constraint block of L: item i of a constraint segment
+template <typename VT>
+__device__ __forceinline__ void soft_mv_item(const KArgs &a, const Seg &sg, int64_t i) {
+  const MeshDesc md = a.mesh[sg.mesh];
+  const MeshScalars &S = a.sc[sg.mesh];
+  const VT *in = reinterpret_cast<const VT *>(a.p), *in_a = reinterpret_cast<const VT *>(a.pa);
+  VT *out = reinterpret_cast<VT *>(a.q), *out_a = reinterpret_cast<VT *>(a.qa);
+  const ConsItem it = cons_item(md, i);
+  const int64_t e = it.e;
+  if (S.glue && it.kind <= CK_LINE) return;
+  if (it.kind == CK_CORNER || it.kind == CK_PROJ) {
+    const bool pj = it.kind == CK_PROJ;
+    const uint32_t v = (uint32_t)(md.v_off + (pj ? a.b_ids[e] : a.c_ids[e]));
+    const VT lc = VT(pj ? S.lamda_P : S.lamda_C);
+    const VT *p = in + 4 * (int64_t)v;
+    atomic_add3(out, v, lc * p[0], lc * p[1], lc * p[2]);
+    return;
+  }
+  if (it.kind == CK_TANGENT) {
+    const uint32_t v = (uint32_t)(md.v_off + a.t_ids[e]);
+    const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2];
+    const VT *p = in + 4 * (int64_t)v;
+    const double s = S.lamda_T * (n0 * double(p[0]) + n1 * double(p[1]) + n2 * double(p[2]));
+    atomic_add3(out, v, VT(s * n0), VT(s * n1), VT(s * n2));
+    return;
+  }
+  if (it.kind == CK_GROUP) {
+    const int64_t m0 = a.g_ptr[e], m1 = a.g_ptr[e + 1];
+    const double c = S.lamda_G * glue_coef(m1 - m0);
+    if (c == 0.0) return;
+    double mean[3] = {0, 0, 0};
+    for (int64_t k = m0; k < m1; k++)
+      for (int d = 0; d < 3; d++) mean[d] += double(in[4 * (int64_t)a.g_vs[k] + d]);
+    for (int d = 0; d < 3; d++) mean[d] /= double(m1 - m0);
+    for (int64_t k = m0; k < m1; k++) {
+      const uint32_t v = (uint32_t)a.g_vs[k];
+      const VT *p = in + 4 * (int64_t)v;
+      atomic_add3(out, v, VT(c * (double(p[0]) - mean[0])), VT(c * (double(p[1]) - mean[1])),
+                  VT(c * (double(p[2]) - mean[2])));
+    }
+    return;
+  }
+  {
+    const uint32_t v = (uint32_t)(md.v_off + a.l_ids[e]);
+    const double ll = S.lamda_L;
+    const double x0 = a.l_axis[3 * e], x1 = a.l_axis[3 * e + 1], x2 = a.l_axis[3 * e + 2];
+    const VT *p = in + 4 * (int64_t)v;
+    const double pa = double(in_a[e]);
+    atomic_add3(out, v, VT(ll * (double(p[0]) - x0 * pa)), VT(ll * (double(p[1]) - x1 * pa)),
+                VT(ll * (double(p[2]) - x2 * pa)));
+    out_a[e] += VT(ll * (-(x0 * double(p[0]) + x1 * double(p[1]) + x2 * double(p[2])) + (x0 * x0 + x1 * x1 + x2 * x2) * pa));
+  }
+}
+
 // ------------------------------------------------------------------------------- SpMV
 // q += K p over the element terms: J' = E(p) B', Q = C' J', forces G = Q B'^T (the cube scale
 // is folded into C').  crow points at the hex's coefficient of row 0 (tet 0, component 0); the
@@ -239,8 +293,16 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // ids and directions, so the coefficient stream (70% of the bytes) is in flight while the
 // dependent gathers wait; other warps (a mesh tail, or a batch mesh not starting on a multiple
 // of 32 hexes) read the coefficients from global memory.
+// Blocks past a.hblk (launched by the PCG iteration) apply the soft terms of one constraint
+// segment each: they run in the SpMV's tail instead of a launch of their own.
 template <typename ET>
 __global__ void __launch_bounds__(128, sizeof(ET) == 4 ? 8 : 4) k_spmv(KArgs a) {
+  if (blockIdx.x >= a.hblk) {
+    const Seg cs = a.cseg[blockIdx.x - a.hblk];
+    if (a.sc[cs.mesh].cg_done) return;
+    for (int64_t i = cs.begin + threadIdx.x; i < cs.end; i += blockDim.x) soft_mv_item<ET>(a, cs, i);
+    return;
+  }
   const Seg sg = a.hseg[blockIdx.x];
   if (a.sc[sg.mesh].cg_done) return;
   const int64_t h = sg.begin + threadIdx.x;
@@ -359,62 +421,13 @@ __global__ void __launch_bounds__(256) k_soft_rhs(KArgs a) {
   }
 }
 
-// q += S p for the soft-constraint block of L
+// The soft terms alone (the element SpMV launch runs them in its trailing blocks).
 template <typename VT>
 __global__ void __launch_bounds__(256) k_soft_mv(KArgs a) {
   const Seg sg = a.cseg[blockIdx.x];
   if (a.sc[sg.mesh].cg_done) return;
   const int64_t i = sg.begin + threadIdx.x;
-  if (i >= sg.end) return;
-  const MeshDesc md = a.mesh[sg.mesh];
-  const MeshScalars &S = a.sc[sg.mesh];
-  const VT *in = reinterpret_cast<const VT *>(a.p), *in_a = reinterpret_cast<const VT *>(a.pa);
-  VT *out = reinterpret_cast<VT *>(a.q), *out_a = reinterpret_cast<VT *>(a.qa);
-  const ConsItem it = cons_item(md, i);
-  const int64_t e = it.e;
-  if (S.glue && it.kind <= CK_LINE) return;
-  if (it.kind == CK_CORNER || it.kind == CK_PROJ) {
-    const bool pj = it.kind == CK_PROJ;
-    const uint32_t v = (uint32_t)(md.v_off + (pj ? a.b_ids[e] : a.c_ids[e]));
-    const VT lc = VT(pj ? S.lamda_P : S.lamda_C);
-    const VT *p = in + 4 * (int64_t)v;
-    atomic_add3(out, v, lc * p[0], lc * p[1], lc * p[2]);
-    return;
-  }
-  if (it.kind == CK_TANGENT) {
-    const uint32_t v = (uint32_t)(md.v_off + a.t_ids[e]);
-    const double n0 = a.t_nrm[3 * e], n1 = a.t_nrm[3 * e + 1], n2 = a.t_nrm[3 * e + 2];
-    const VT *p = in + 4 * (int64_t)v;
-    const double s = S.lamda_T * (n0 * double(p[0]) + n1 * double(p[1]) + n2 * double(p[2]));
-    atomic_add3(out, v, VT(s * n0), VT(s * n1), VT(s * n2));
-    return;
-  }
-  if (it.kind == CK_GROUP) {
-    const int64_t m0 = a.g_ptr[e], m1 = a.g_ptr[e + 1];
-    const double c = S.lamda_G * glue_coef(m1 - m0);
-    if (c == 0.0) return;
-    double mean[3] = {0, 0, 0};
-    for (int64_t k = m0; k < m1; k++)
-      for (int d = 0; d < 3; d++) mean[d] += double(in[4 * (int64_t)a.g_vs[k] + d]);
-    for (int d = 0; d < 3; d++) mean[d] /= double(m1 - m0);
-    for (int64_t k = m0; k < m1; k++) {
-      const uint32_t v = (uint32_t)a.g_vs[k];
-      const VT *p = in + 4 * (int64_t)v;
-      atomic_add3(out, v, VT(c * (double(p[0]) - mean[0])), VT(c * (double(p[1]) - mean[1])),
-                  VT(c * (double(p[2]) - mean[2])));
-    }
-    return;
-  }
-  {
-    const uint32_t v = (uint32_t)(md.v_off + a.l_ids[e]);
-    const double ll = S.lamda_L;
-    const double x0 = a.l_axis[3 * e], x1 = a.l_axis[3 * e + 1], x2 = a.l_axis[3 * e + 2];
-    const VT *p = in + 4 * (int64_t)v;
-    const double pa = double(in_a[e]);
-    atomic_add3(out, v, VT(ll * (double(p[0]) - x0 * pa)), VT(ll * (double(p[1]) - x1 * pa)),
-                VT(ll * (double(p[2]) - x2 * pa)));
-    out_a[e] += VT(ll * (-(x0 * double(p[0]) + x1 * double(p[1]) + x2 * double(p[2])) + (x0 * x0 + x1 * x1 + x2 * x2) * pa));
-  }
+  if (i < sg.end) soft_mv_item<VT>(a, sg, i);
 }
 
 // ------------------------------------------------------------------------------- CG vectors
@@ -851,7 +864,7 @@ static __global__ void __launch_bounds__(128, 4) k_ir_resid(KArgs a, int replace
   const int32_t gs = a.gslot[h];
   float Eh[12][3], El[12][3];
   hex_edges_split_df(a.X32, hv, Eh, El);
-  {
+  if (replace) {  // the FP64 update dd (zero for the initial residual)
     float P[8][3];
 #pragma unroll
     for (int c = 0; c < 8; c++) {

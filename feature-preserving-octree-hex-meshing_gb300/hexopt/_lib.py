@@ -120,7 +120,8 @@ SIGNATURES = {
     "hexopt_energy_bwd": (C.c_int, [_vp, _d]),
     "hexopt_set_block_size": (C.c_int, [_vp, C.c_int, C.c_int]),
     "hexopt_autotune": (C.c_int, [_vp]),
-    "hexopt_get_tuning": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "hexopt_get_tuning": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int)]),
     "hexopt_launch_count": (C.c_int64, [_vp]),
     "hexopt_timer_start": (C.c_int, [_vp]),
     "hexopt_timer_stop": (C.c_int, [_vp, _d]),
@@ -537,9 +538,9 @@ class Context:
 
     def autotune(self):
         self._ck(self.L.hexopt_autotune(self.h), "autotune")
-        a, b, c = C.c_int(), C.c_int(), C.c_int()
-        self.L.hexopt_get_tuning(self.h, C.byref(a), C.byref(b), C.byref(c))
-        return dict(hex_block=a.value, vertex_block=b.value, ls_candidates=c.value)
+        a, b, v, c = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self.L.hexopt_get_tuning(self.h, C.byref(a), C.byref(b), C.byref(v), C.byref(c))
+        return dict(hex_block=a.value, vertex_block=b.value, vertex_items=v.value, ls_candidates=c.value)
 
     def sync(self):
         self._ck(self.L.hexopt_sync(self.h), "sync")

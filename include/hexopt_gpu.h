@@ -313,9 +313,15 @@ HEXOPT_API int hexopt_energy_fwd(hexopt_ctx *ctx, const double *X, double *E);
 HEXOPT_API int hexopt_energy_bwd(hexopt_ctx *ctx, double *grad);
 
 /* ---- launch tuning ---- */
-HEXOPT_API int hexopt_set_block_size(hexopt_ctx *ctx, int kind, int threads); /* kind 0 hex, 1 vertex */
+/* kind 0: threads per hex block (32, 64, 128); 1: threads per vertex block (64, 128, 256);
+ * 2: vertices per thread of the vertex kernels (1, 2, 4, 8, 16; default 8) */
+HEXOPT_API int hexopt_set_block_size(hexopt_ctx *ctx, int kind, int threads);
+/* Times one SLIM iteration per setting (hex block 64/128, vertex block 128/256, 4/8 vertices per
+ * thread, 1/2/4 line-search candidates) on the live problem and keeps the fastest; positions and
+ * solver state are restored.  Needs slim_precompute (or fa_begin) first. */
 HEXOPT_API int hexopt_autotune(hexopt_ctx *ctx);
-HEXOPT_API int hexopt_get_tuning(const hexopt_ctx *ctx, int *hex_block, int *vert_block, int *ls_candidates);
+HEXOPT_API int hexopt_get_tuning(const hexopt_ctx *ctx, int *hex_block, int *vert_block, int *vert_items,
+                                 int *ls_candidates);
 /* CUDA-event timing on the context's stream: start records an event, stop records a second one,
  * synchronises and returns the elapsed milliseconds between them. */
 HEXOPT_API int hexopt_timer_start(hexopt_ctx *ctx);
