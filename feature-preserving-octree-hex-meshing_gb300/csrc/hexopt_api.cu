@@ -118,7 +118,7 @@ struct hexopt_ctx {
   DBuf X, X32, hexv, gslot, Sinv, Ccoef, Bgen, aL;
   DBuf b, diag, ba, diaga;
   DBuf d, r, p, q, invd, da, ra, pa, qa, invda;
-  DBuf Rrot, dd, dda;  // mixed mode's FP64 refinement: stored rotations, FP64 update accumulator
+  DBuf Rrot, dd, dda, ddf;  // mixed mode's FP64 refinement: stored rotations, FP64 update (+ its FP32 copy)
   // general reference shapes (compute_referenceMesh with cube = 0, or reference corners set by the
   // caller): per-hex h_flag, optional reference corners, shapes, and the all-hex slot tables
   DBuf hflag_d, ref_p8, Bref, gslot_all, Bgen_all;
@@ -379,6 +379,7 @@ KArgs make_args(hexopt_ctx *c) {
   a.Rrot = c->Rrot.as<float>();
   a.dd = c->dd.as<double>();
   a.dda = c->dda.as<double>();
+  a.ddf = c->ddf.as<float>();
   a.cg_refine = c->params.cg_refine > 0 ? c->params.cg_refine : 10;
   a.c_ids = c->c_ids.as<int32_t>(); a.c_pos = c->c_pos.as<double>();
   a.t_ids = c->t_ids.as<int32_t>(); a.t_nrm = c->t_nrm.as<double>(); a.t_dis = c->t_dis.as<double>();
@@ -420,6 +421,7 @@ int alloc_vectors(hexopt_ctx *ctx) {
     CK(ctx->Rrot.ensure(nt * 9 * sizeof(float)));
     CK(ctx->dd.ensure(nv4 * sizeof(double)));
     CK(ctx->dda.ensure(nl * sizeof(double)));
+    CK(ctx->ddf.ensure(nv4 * sizeof(float)));
   }
   // every corner tet may need the exact root: the list holds all of them
   const size_t nroot = (size_t)ctx->NH * 8;

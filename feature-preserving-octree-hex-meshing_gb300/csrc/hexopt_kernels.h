@@ -36,6 +36,7 @@ struct KArgs {
   // the update accumulated in FP64 between residual replacements (vertices AoS4, curve entries)
   float *Rrot;
   double *dd, *dda;
+  float *ddf;  // fl32(dd) per vertex (AoS4), written with dd: the residual pass's corner gathers
   // constraints
   const int32_t *c_ids; const double *c_pos;
   const int32_t *t_ids; double *t_nrm; double *t_dis;

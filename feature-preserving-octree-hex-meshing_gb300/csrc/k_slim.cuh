@@ -806,7 +806,7 @@ __device__ __forceinline__ void hex_edges_split_df(const float *X32, const uint3
 // X's double-float edges, Elo their lo part plus the edges of dd (both small next to Eh).
 template <int K>
 __device__ __forceinline__ void ir_tet(const KArgs &a, int64_t h, int32_t gs, const float Eh12[12][3],
-                                       const float El12[12][3], float F[8][3]) {
+                                       const float El12[12][3], const float *rrow, float F[8][3]) {
   float Eh[3][3], El[3][3];
   tet_E12<K>(Eh12, Eh);
   tet_E12<K>(El12, El);
@@ -826,7 +826,7 @@ __device__ __forceinline__ void ir_tet(const KArgs &a, int64_t h, int32_t gs, co
       for (int r = 0; r < 3; r++) {
         const float jh = __fmul_rn(Eh[r][j], sg);
         const float jl = __fadd_rn(__fmaf_rn(Eh[r][j], sg, -jh), __fmul_rn(El[r][j], sg));
-        res[r][ax] = __fsub_rn(__fsub_rn(a.Rrot[tet_idx<9>(h, K, r * 3 + ax)], jh), jl);
+        res[r][ax] = __fsub_rn(__fsub_rn(rrow[(K * 9 + r * 3 + ax) * 32], jh), jl);
       }
     }
 #pragma unroll
@@ -843,7 +843,7 @@ __device__ __forceinline__ void ir_tet(const KArgs &a, int64_t h, int32_t gs, co
         double jv = 0;
 #pragma unroll
         for (int k = 0; k < 3; k++) jv += (double(Eh[r][k]) + double(El[r][k])) * B[k * 3 + cc];
-        res[r][cc] = float(double(a.Rrot[tet_idx<9>(h, K, r * 3 + cc)]) - jv);
+        res[r][cc] = float(double(rrow[(K * 9 + r * 3 + cc) * 32]) - jv);
       }
 #pragma unroll
     for (int i = 0; i < 6; i++) c[i] = Cc[tet_idx<6>(h, K, i)];
@@ -854,40 +854,59 @@ __device__ __forceinline__ void ir_tet(const KArgs &a, int64_t h, int32_t gs, co
 }
 
 // r += element residual at X + dd (r starts at -prox dd, or at 0 for the initial residual).
+// A warp whose 32 hexes fill one AoSoA tile copies the tile's 8 x 9 rotations (9 KB, contiguous)
+// into shared memory with cp.async before its dependent corner gathers, as k_spmv does with C'.
 static __global__ void __launch_bounds__(128, 4) k_ir_resid(KArgs a, int replace) {
   const Seg sg = a.hseg[blockIdx.x];
   if (replace && a.sc[sg.mesh].cg_done) return;
   const int64_t h = sg.begin + threadIdx.x;
+  const float *rrow = a.Rrot + tet_idx<9>(h, 0, 0);  // row (K, i) at rrow[(K * 9 + i) * 32]
+  bool staged = false;  // every lane of a staged warp is active
+  {
+    __shared__ __align__(16) float rs[4][72 * 32];  // blockDim.x <= 128
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t hw = sg.begin + 32 * w;
+    if ((hw & 31) == 0 && hw + 32 <= sg.end && w < 4) {
+      const float *src = a.Rrot + tet_idx<9>(hw, 0, 0);  // 2304 floats, 16-byte aligned
+#pragma unroll
+      for (int i = 0; i < 18; i++) cp_async16(&rs[w][(i * 32 + lane) * 4], src + (i * 32 + lane) * 4);
+      rrow = &rs[w][lane];
+      staged = true;
+    }
+  }
   if (h >= sg.end) return;
   uint32_t hv[8];
   load_hex(a.hexv, h, hv);
   const int32_t gs = a.gslot[h];
   float Eh[12][3], El[12][3];
   hex_edges_split_df(a.X32, hv, Eh, El);
-  if (replace) {  // the FP64 update dd (zero for the initial residual)
+  if (replace) {  // the update dd at FP32 (zero for the initial residual)
     float P[8][3];
 #pragma unroll
     for (int c = 0; c < 8; c++) {
-      const double2 u = __ldg(reinterpret_cast<const double2 *>(a.dd + 4 * (int64_t)hv[c]));
-      const double w = __ldg(a.dd + 4 * (int64_t)hv[c] + 2);
-      P[c][0] = float(u.x); P[c][1] = float(u.y); P[c][2] = float(w);
+      const float4 u = __ldg(reinterpret_cast<const float4 *>(a.ddf) + hv[c]);
+      P[c][0] = u.x; P[c][1] = u.y; P[c][2] = u.z;
     }
 #pragma unroll
     for (int e = 0; e < 12; e++)
 #pragma unroll
       for (int r = 0; r < 3; r++) El[e][r] = __fadd_rn(El[e][r], P[hex_edge_hi(e)][r] - P[hex_edge_lo(e)][r]);
   }
+  if (staged) {
+    cp_async_wait_all();
+    __syncwarp();
+  }
   float F[8][3];
 #pragma unroll
   for (int c = 0; c < 8; c++) F[c][0] = F[c][1] = F[c][2] = 0.f;
-  ir_tet<0>(a, h, gs, Eh, El, F);
-  ir_tet<1>(a, h, gs, Eh, El, F);
-  ir_tet<2>(a, h, gs, Eh, El, F);
-  ir_tet<3>(a, h, gs, Eh, El, F);
-  ir_tet<4>(a, h, gs, Eh, El, F);
-  ir_tet<5>(a, h, gs, Eh, El, F);
-  ir_tet<6>(a, h, gs, Eh, El, F);
-  ir_tet<7>(a, h, gs, Eh, El, F);
+  ir_tet<0>(a, h, gs, Eh, El, rrow, F);
+  ir_tet<1>(a, h, gs, Eh, El, rrow, F);
+  ir_tet<2>(a, h, gs, Eh, El, rrow, F);
+  ir_tet<3>(a, h, gs, Eh, El, rrow, F);
+  ir_tet<4>(a, h, gs, Eh, El, rrow, F);
+  ir_tet<5>(a, h, gs, Eh, El, rrow, F);
+  ir_tet<6>(a, h, gs, Eh, El, rrow, F);
+  ir_tet<7>(a, h, gs, Eh, El, rrow, F);
   float *r = reinterpret_cast<float *>(a.r);
 #pragma unroll
   for (int c = 0; c < 8; c++) atomic_add3(r, hv[c], F[c][0], F[c][1], F[c][2]);
@@ -951,6 +970,7 @@ static __global__ void __launch_bounds__(256) k_ir_acc(KArgs a) {
       u.x += double(dv.x); u.y += double(dv.y); w += double(dv.z);
       *reinterpret_cast<double2 *>(a.dd + 4 * v) = u;
       a.dd[4 * v + 2] = w;
+      st3(a.ddf, v, V3<float>{float(u.x), float(u.y), float(w)});
       st3(d, v, V3<float>{0.f, 0.f, 0.f});
       st3(r, v, V3<float>{float(-prox * u.x), float(-prox * u.y), float(-prox * w)});
     } else {

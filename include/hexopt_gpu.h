@@ -45,7 +45,7 @@ extern "C" {
 #define HEXOPT_ERR_CUDA 2        /* a CUDA call failed */
 #define HEXOPT_ERR_STATE 3       /* call order (e.g. iterate before precompute) */
 #define HEXOPT_ERR_NUMERIC 4     /* NaN/Inf or degenerate element detected on the device */
-#define HEXOPT_ERR_UNSUPPORTED 5 /* option outside what this build implements */
+#define HEXOPT_ERR_UNSUPPORTED 5 /* option outside what the library implements */
 #define HEXOPT_ERR_NOMEM 6       /* device allocation failed */
 
 /* ---- per-mesh device status bits (hexopt_slim_report.status) ---- */
