@@ -140,7 +140,7 @@ def spmv_bytes_per_hex(mixed: bool) -> float:
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_spmv<float> launch per hex,
 # from an ncu capture on the 96^3 grid (working set above L2; traffic grows with the hex count).
-SPMV_DRAM_BYTES_PER_HEX_MIXED = (231.139328e6 + 12.921088e6) / 96 ** 3
+SPMV_DRAM_BYTES_PER_HEX_MIXED = (234.636544e6 + 13.034496e6) / 96 ** 3
 
 
 def cpu_baseline(steps=None, budget_s=12.0):

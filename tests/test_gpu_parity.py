@@ -380,12 +380,14 @@ def test_autotune_preserves_results(ctx, hx):
 def test_vertex_items_per_thread_preserve_results(ctx, hx, precision):
     """The vertex kernels' items per thread (1 .. 16) only change the launch shape and the order
     of the block partial sums: on a two-mesh batch whose vertex counts are no multiple of any
-    block, positions after 3 SLIM iterations agree to rounding (the float atomics of the element
-    scatter already reorder sums from run to run; the truncated CG and the line search amplify
-    such differences, most in mixed precision) and the iteration counts match."""
+    block, positions after 3 SLIM iterations agree to rounding and the iteration counts match.
+    Reordered sums can flip a backtracking decision of the line search (an O(step) difference)
+    where energies tie to rounding: FP64 runs on meshes with inverted tets (jitter 0.2h), mixed
+    precision, whose rounding is 1e-7, on mildly jittered ones (0.05h) where full steps pass."""
     from hexopt import workloads
-    ps = [workloads.grid_box_superellipsoid((13, 9, 11), 0.2, 7, 4000, 4.0),
-          workloads.grid_box_superellipsoid((7, 15, 10), 0.2, 8, 4000, 2.5)]
+    sig = 0.2 if precision == "fp64" else 0.05
+    ps = [workloads.grid_box_superellipsoid((13, 9, 11), sig, 7, 4000, 4.0),
+          workloads.grid_box_superellipsoid((7, 15, 10), sig, 8, 4000, 2.5)]
     prec = hx.FP64 if precision == "fp64" else hx.MIXED
     out = {}
     for ipt in (1, 4, 16):
