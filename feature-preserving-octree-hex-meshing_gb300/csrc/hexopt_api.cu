@@ -177,6 +177,12 @@ struct hexopt_ctx {
   hexopt_slim_params graph_params{};
   double graph_lamda0 = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // asynchronous position transfers: one copy stream each way (an upload never queues behind a
+  // download), staging buffers each way, and the events that order them against the compute
+  // stream (input copied / consumed, output staged / copied)
+  cudaStream_t ust = nullptr, dst = nullptr;
+  cudaEvent_t in_ready = nullptr, in_free = nullptr, out_ready = nullptr, out_done = nullptr;
+  DBuf in_stage, out_stage;
 };
 
 namespace {
@@ -819,8 +825,14 @@ void hexopt_destroy(hexopt_ctx *ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->ust) cudaStreamSynchronize(ctx->ust);
+  if (ctx->dst) cudaStreamSynchronize(ctx->dst);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  for (cudaEvent_t e : {ctx->in_ready, ctx->in_free, ctx->out_ready, ctx->out_done})
+    if (e) cudaEventDestroy(e);
+  if (ctx->ust) cudaStreamDestroy(ctx->ust);
+  if (ctx->dst) cudaStreamDestroy(ctx->dst);
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
 }
@@ -830,6 +842,8 @@ const char *hexopt_last_error(const hexopt_ctx *ctx) { return ctx ? ctx->err.c_s
 int hexopt_sync(hexopt_ctx *ctx) {
   if (!ctx) return HEXOPT_ERR_ARG;
   CK(cudaStreamSynchronize(ctx->st));
+  if (ctx->ust) CK(cudaStreamSynchronize(ctx->ust));
+  if (ctx->dst) CK(cudaStreamSynchronize(ctx->dst));
   return HEXOPT_OK;
 }
 
@@ -982,6 +996,52 @@ int hexopt_set_positions(hexopt_ctx *ctx, const double *V) {
   launch_split_pos(ctx->X.as<double>(), ctx->X32.as<float>(), ctx->NV, ctx->st);
   ctx->launches += 2;
   CKL();
+  return HEXOPT_OK;
+}
+
+static cudaError_t ensure_copy_streams(hexopt_ctx *ctx) {
+  if (ctx->ust) return cudaSuccess;
+  cudaError_t e = cudaStreamCreateWithFlags(&ctx->ust, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->dst, cudaStreamNonBlocking);
+  for (cudaEvent_t *ev : {&ctx->in_ready, &ctx->in_free, &ctx->out_ready, &ctx->out_done})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  return e;
+}
+
+int hexopt_set_positions_async(hexopt_ctx *ctx, const double *V) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!V) return fail(ctx, HEXOPT_ERR_ARG, "set_positions_async: NULL");
+  CK(ensure_copy_streams(ctx));
+  CK(ctx->in_stage.ensure(sizeof(double) * 3 * ctx->NV));
+  // the copy waits until the previous input has been consumed, the compute stream until it lands
+  CK(cudaStreamWaitEvent(ctx->ust, ctx->in_free, 0));
+  CK(cudaMemcpyAsync(ctx->in_stage.p, V, sizeof(double) * 3 * ctx->NV, cudaMemcpyHostToDevice, ctx->ust));
+  CK(cudaEventRecord(ctx->in_ready, ctx->ust));
+  CK(cudaStreamWaitEvent(ctx->st, ctx->in_ready, 0));
+  launch_rows_to_aos4_perm(ctx->in_stage.as<double>(), vn2o(ctx), ctx->NV, ctx->X.as<double>(), ctx->st);
+  launch_split_pos(ctx->X.as<double>(), ctx->X32.as<float>(), ctx->NV, ctx->st);
+  ctx->launches += 2;
+  CKL();
+  CK(cudaEventRecord(ctx->in_free, ctx->st));
+  return HEXOPT_OK;
+}
+
+int hexopt_get_positions_async(hexopt_ctx *ctx, double *V) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!V) return fail(ctx, HEXOPT_ERR_ARG, "get_positions_async: NULL");
+  CK(ensure_copy_streams(ctx));
+  CK(ctx->out_stage.ensure(sizeof(double) * 3 * ctx->NV));
+  // stage the positions after the work queued so far, once the previous copy has left the stage
+  CK(cudaStreamWaitEvent(ctx->st, ctx->out_done, 0));
+  launch_aos4_to_rows_perm(ctx->X.as<double>(), vo2n(ctx), ctx->NV, ctx->out_stage.as<double>(), ctx->st);
+  ctx->launches++;
+  CKL();
+  CK(cudaEventRecord(ctx->out_ready, ctx->st));
+  CK(cudaStreamWaitEvent(ctx->dst, ctx->out_ready, 0));
+  CK(cudaMemcpyAsync(V, ctx->out_stage.p, sizeof(double) * 3 * ctx->NV, cudaMemcpyDeviceToHost, ctx->dst));
+  CK(cudaEventRecord(ctx->out_done, ctx->dst));
   return HEXOPT_OK;
 }
 
@@ -2302,6 +2362,7 @@ int hexopt_timer_start(hexopt_ctx *ctx) {
 
 int hexopt_timer_stop(hexopt_ctx *ctx, double *ms) {
   if (!ctx || !ctx->ev0) return HEXOPT_ERR_ARG;
+  if (ctx->dst) CK(cudaStreamWaitEvent(ctx->st, ctx->out_done, 0));  // asynchronous downloads included
   CK(cudaEventRecord(ctx->ev1, ctx->st));
   CK(cudaEventSynchronize(ctx->ev1));
   float f = 0;

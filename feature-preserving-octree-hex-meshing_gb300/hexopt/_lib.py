@@ -76,6 +76,8 @@ SIGNATURES = {
     "hexopt_upload_meshes": (C.c_int, [_vp, C.c_int, _i64, _i64, _d, _u32, _u8]),
     "hexopt_set_positions": (C.c_int, [_vp, _d]),
     "hexopt_get_positions": (C.c_int, [_vp, _d]),
+    "hexopt_set_positions_async": (C.c_int, [_vp, _d]),
+    "hexopt_get_positions_async": (C.c_int, [_vp, _d]),
     "hexopt_num_vertices": (C.c_int64, [_vp]),
     "hexopt_num_hexes": (C.c_int64, [_vp]),
     "hexopt_num_meshes": (C.c_int, [_vp]),
@@ -259,6 +261,20 @@ class Context:
         out = np.empty((int(sum(self.nv)), 3))
         self._ck(self.L.hexopt_get_positions(self.h, ptr(out, _d)), "get_positions")
         return out
+
+    def set_positions_async(self, V):
+        """Queue an upload of V (C-contiguous float64, nv x 3): V must stay alive and unchanged
+        until sync() returns (page-locked memory lets the copy overlap the computation)."""
+        if not (isinstance(V, np.ndarray) and V.dtype == np.float64 and V.flags.c_contiguous):
+            raise ValueError("set_positions_async needs a C-contiguous float64 array")
+        self._ck(self.L.hexopt_set_positions_async(self.h, ptr(V, _d)), "set_positions_async")
+
+    def get_positions_async(self, out):
+        """Queue a download of the positions into out (C-contiguous float64, nv x 3), complete
+        after sync()."""
+        if not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.flags.c_contiguous):
+            raise ValueError("get_positions_async needs a C-contiguous float64 array")
+        self._ck(self.L.hexopt_get_positions_async(self.h, ptr(out, _d)), "get_positions_async")
 
     def scaled_jacobian(self, per_corner=False):
         NH = int(sum(self.nh))

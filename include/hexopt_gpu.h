@@ -141,6 +141,17 @@ HEXOPT_API int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t
                          const uint32_t *H, const uint8_t *h_flag);
 HEXOPT_API int hexopt_set_positions(hexopt_ctx *ctx, const double *V);
 HEXOPT_API int hexopt_get_positions(hexopt_ctx *ctx, double *V);
+/* Asynchronous forms for streaming positions through the optimiser: the host <-> device copies
+ * run on the context's upload and download streams and overlap the computation queued on its
+ * compute stream.
+ * set_positions_async: V (nv x 3, caller order) is read after the call returns, so it must stay
+ * valid and unchanged until hexopt_sync returns; the positions take effect for the work queued
+ * after the call.
+ * get_positions_async: the positions after the work queued so far, written into V (nv x 3,
+ * caller order) once the copy completes (hexopt_sync, or hexopt_timer_stop, waits for it).
+ * Page-locked host buffers let the copies overlap; pageable ones still give correct results. */
+HEXOPT_API int hexopt_set_positions_async(hexopt_ctx *ctx, const double *V);
+HEXOPT_API int hexopt_get_positions_async(hexopt_ctx *ctx, double *V);
 HEXOPT_API int64_t hexopt_num_vertices(const hexopt_ctx *ctx);
 HEXOPT_API int64_t hexopt_num_hexes(const hexopt_ctx *ctx);
 HEXOPT_API int hexopt_num_meshes(const hexopt_ctx *ctx);

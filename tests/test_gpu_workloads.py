@@ -255,3 +255,48 @@ def test_adjoint_96_all_coordinates_match_central_differences(hx):
     print(f"\n[adjoint 96^3] aggregate rel err {rel:.3e} over {len(gf)} coordinates; "
           f"steps used: {sorted(set(steps))}")
     assert rel <= 1e-4
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_async_position_transfers_match_synchronous(hx, graph):
+    """Streaming positions through the optimiser with the asynchronous transfers (uploads and
+    downloads on the copy stream, overlapping the steps; one synchronisation at the end) gives,
+    step for step, the positions of the synchronous set_positions / fa_step / get_positions
+    sequence, with and without graph replay.  Page-locked buffers (torch) and pageable numpy
+    buffers both work."""
+    import torch
+    from hexopt import workloads
+    p = workloads.grid_superellipsoid(n=16, n_tri=4000)
+    rng = np.random.default_rng(3)
+    h = 1.0 / 16
+    inputs = [np.ascontiguousarray(p["V"] + (0.02 * h * k) * rng.standard_normal(p["V"].shape) *
+                                   np.isin(np.arange(len(p["V"])), p["regular"], invert=True)[:, None])
+              for k in range(4)]
+    ctx = hx.Context(0)
+    try:
+        workloads.load(ctx, [p])
+        ctx.use_graph(graph)
+        ctx.fa_begin(lamda0=0.05, precision=hx.FP64, weight_opt=0.001)
+        ref = []
+        for V in inputs:
+            ctx.set_positions(V)
+            ctx.fa_step(hausdorff=True, report=False)
+            ref.append(ctx.get_positions())
+        for pinned in (True, False):
+            if pinned:
+                ins = [torch.from_numpy(V).pin_memory().numpy() for V in inputs]
+                outs = [torch.empty(V.shape, dtype=torch.float64).pin_memory().numpy() for V in inputs]
+            else:
+                ins = [V.copy() for V in inputs]
+                outs = [np.empty_like(V) for V in inputs]
+            ctx.fa_begin(lamda0=0.05, precision=hx.FP64, weight_opt=0.001)
+            for V, out in zip(ins, outs):
+                ctx.set_positions_async(V)
+                ctx.fa_step(hausdorff=True, report=False)
+                ctx.get_positions_async(out)
+            ctx.sync()
+            d = float(np.linalg.norm(p["V"].max(0) - p["V"].min(0)))
+            for k, (a, b) in enumerate(zip(outs, ref)):
+                assert np.abs(a - b).max() <= 1e-9 * d, (pinned, k, float(np.abs(a - b).max()))
+    finally:
+        ctx.close()
