@@ -1587,15 +1587,17 @@ int hexopt_set_query_budget(hexopt_ctx *ctx, int pops) {
   return HEXOPT_OK;
 }
 
-int hexopt_query_stats(hexopt_ctx *ctx, int64_t *warp_queries, int64_t *candidates) {
+int hexopt_query_stats(hexopt_ctx *ctx, int64_t *warp_queries, int64_t *candidates, int64_t *fallbacks) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
-  unsigned w = 0, c = 0;
+  unsigned w = 0, c = 0, f = 0;
   if (ctx->ovf_count.p) CK(cudaMemcpyAsync(&w, ctx->ovf_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
   if (ctx->cand_count.p) CK(cudaMemcpyAsync(&c, ctx->cand_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+  if (ctx->fb_count.p) CK(cudaMemcpyAsync(&f, ctx->fb_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
   if (warp_queries) *warp_queries = w;
   if (candidates) *candidates = c;
+  if (fallbacks) *fallbacks = f;
   return HEXOPT_OK;
 }
 

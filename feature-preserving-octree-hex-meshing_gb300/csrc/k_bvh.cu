@@ -584,7 +584,7 @@ constexpr int kQCand = 16;     // candidates a per-thread query may hold
 // flight per SM for the same shared memory.
 constexpr int kGroup = 16;
 constexpr int kGroupsPerBlock = 128 / kGroup;
-constexpr int kWarpStack = 512;  // frontier entries a group may hold (overflow: exact fallback)
+constexpr int kWarpStack = 256;  // frontier entries a group may hold (overflow: exact fallback)
 constexpr int kWarpCand = 64;  // candidates a warp-pass query may hold
 
 __device__ __forceinline__ int warp_excl_scan(int v, int &total) {
@@ -1004,21 +1004,18 @@ __global__ void __launch_bounds__(128) k_project(ProjArgs p) {
     int st = 0;
     seed_bound<0>(t.bvh, p.seed, i, q, ub);
     if (t.bvh.n > 0) st = thread_collect<0>(t.bvh, q, ub, cl, cb, nc, p.budget > 0 ? p.budget : kThreadBudget);
-    if (st == 2) {
+    if (st != 0) {
+      // over budget, stack or candidate list: the cooperative pass restarts the query from the
+      // root under the bound found so far (any leaf's upper bound bounds the minimum)
       p.ovf.best[i] = ub;
       push_overflow(p.ovf, i, sg.mesh);
       has = false;
-    } else if (st == 3) {
-      push_fallback(p.cand, i, sg.mesh);
-      has = false;
-    } else if (st == 1) {
-      atomicOr(&p.sc[sg.mesh].status, 8);
     }
   }
   if (!store_cands_warp(p.cand, has, i, sg.mesh, q, cl, cb, nc, ub)) push_fallback(p.cand, i, sg.mesh);
 }
 
-__global__ void __launch_bounds__(128) k_project_warp(ProjArgs p) {
+__global__ void __launch_bounds__(128, 8) k_project_warp(ProjArgs p) {
   __shared__ int32_t sn[kGroupsPerBlock][kWarpStack];
   __shared__ float sd[kGroupsPerBlock][kWarpStack];
   __shared__ int32_t scl[kGroupsPerBlock][kWarpCand];
@@ -1227,22 +1224,19 @@ __global__ void __launch_bounds__(128) k_haus_side(HausArgs h) {
     seed_bound<1>(*b, h.seed, i, q, ub);
     int st = 0;
     if (b->n > 0) st = thread_collect<1>(*b, q, ub, cl, cb, nc, h.budget > 0 ? h.budget : kThreadBudget);
-    if (st == 2) {
+    if (st != 0) {
+      // over budget, stack or candidate list: the cooperative pass restarts the query from the
+      // root under the bound found so far (any leaf's upper bound bounds the minimum)
       h.ovf.best[i] = ub;
       push_overflow(h.ovf, i, sg.mesh);
       has = false;
-    } else if (st == 3) {
-      push_fallback(h.cand, i, sg.mesh);
-      has = false;
-    } else if (st == 1) {
-      atomicOr(&h.sc[sg.mesh].status, 8);
     }
   }
   if (!store_cands_warp(h.cand, has, i, sg.mesh, q, cl, cb, nc, ub)) push_fallback(h.cand, i, sg.mesh);
 }
 
 template <int SIDE>
-__global__ void __launch_bounds__(128) k_haus_warp(HausArgs h) {
+__global__ void __launch_bounds__(128, 8) k_haus_warp(HausArgs h) {
   __shared__ int32_t sn[kGroupsPerBlock][kWarpStack];
   __shared__ float sd[kGroupsPerBlock][kWarpStack];
   __shared__ int32_t scl[kGroupsPerBlock][kWarpCand];
@@ -1424,7 +1418,7 @@ void bvh_refit(const BvhDev &b, float *box, const int32_t *parent, unsigned *cou
   k_refit<<<(b.n + 127) / 128, 128, 0, st>>>(b, box, parent, counters, leafd);
   if (b.n > 1) k_pack<<<(b.n + 254) / 256, 256, 0, st>>>(b.n, b.child, box, node);
 }
-static const unsigned kWarpGrid = 912;  // persistent warp-pass grid (152 SMs x 6 blocks of 4 warps)
+static const unsigned kWarpGrid = 1216;  // persistent warp-pass grid (152 SMs x 8 blocks of 4 warps)
 static const unsigned kEvalGrid = 152 * 8;  // dense exact pass: grid-stride over the candidates
 void launch_project(const ProjArgs &p, int64_t nblk, cudaStream_t st) {
   if (nblk <= 0) return;

@@ -104,7 +104,7 @@ SIGNATURES = {
     "hexopt_signed_distance": (C.c_int, [_vp, C.c_int, C.c_int64, _d, _d, _i32, _d, _d]),
     "hexopt_set_feature_sets": (C.c_int, [_vp, _i64, _i32, _i64, _i32, _i32, _i64, _i64, _i32, _u8]),
     "hexopt_project_features": (C.c_int, [_vp]),
-    "hexopt_query_stats": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "hexopt_query_stats": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "hexopt_set_query_budget": (C.c_int, [_vp, C.c_int]),
     "hexopt_hausdorff": (C.c_int, [_vp, C.c_int64, _d, C.c_int64, _i32, C.c_int64, _d, C.c_int64, _i32, _d, _d, _d]),
     "hexopt_hausdorff_uniform": (C.c_int, [_vp, C.c_int64, _d, C.c_int64, _i32, C.c_int64, _d, C.c_int64, _i32,
@@ -467,10 +467,11 @@ class Context:
         self._ck(self.L.hexopt_set_query_budget(self.h, int(pops)), "set_query_budget")
 
     def query_stats(self):
-        """(queries finished by the warp pass, candidate leaves) of the last BVH query pass."""
-        w, c = C.c_int64(), C.c_int64()
-        self._ck(self.L.hexopt_query_stats(self.h, C.byref(w), C.byref(c)), "query_stats")
-        return w.value, c.value
+        """(queries handed to the cooperative pass, candidate leaves, exact fallbacks) of the last
+        BVH query pass."""
+        w, c, f = C.c_int64(), C.c_int64(), C.c_int64()
+        self._ck(self.L.hexopt_query_stats(self.h, C.byref(w), C.byref(c), C.byref(f)), "query_stats")
+        return w.value, c.value, f.value
 
     # ---- Hausdorff
     def hausdorff(self, V0, F0, V1, F1):

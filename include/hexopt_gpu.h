@@ -276,9 +276,10 @@ HEXOPT_API int hexopt_set_feature_sets(hexopt_ctx *ctx, const int64_t *n_regular
 /* Recomputes tangent planes and line targets from the current positions. */
 HEXOPT_API int hexopt_project_features(hexopt_ctx *ctx);
 /* Work counters of the last BVH query pass (projection, or a Hausdorff side): the queries that
- * went past the per-thread traversal budget to the warp-cooperative pass, and the candidate
- * leaves recorded for exact FP64 evaluation. */
-HEXOPT_API int hexopt_query_stats(hexopt_ctx *ctx, int64_t *warp_queries, int64_t *candidates);
+ * went past the per-thread traversal budget to the group-cooperative pass, the candidate leaves
+ * recorded for exact FP64 evaluation, and the queries finished by the exact per-thread search
+ * after a frontier or candidate overflow. */
+HEXOPT_API int hexopt_query_stats(hexopt_ctx *ctx, int64_t *warp_queries, int64_t *candidates, int64_t *fallbacks);
 /* Per-thread traversal budget of the BVH queries: node pops a query may take alone before the
  * group-cooperative pass takes it over (0 = the default, 64).  Results do not depend on it. */
 HEXOPT_API int hexopt_set_query_budget(hexopt_ctx *ctx, int pops);
