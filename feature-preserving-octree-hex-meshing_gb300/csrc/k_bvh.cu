@@ -615,12 +615,16 @@ __device__ __forceinline__ void seed_bound(const BvhDev &b, const int32_t *seed,
   ub = fminf(ub, hi);
 }
 
-// Per-thread collection with at most `budget` pops.  Returns 0 when done, 1 on stack overflow
-// (candidates may miss subtrees), 2 when the budget ran out (ub stays a valid bound), 3 when more
-// than kQCand candidates remain after compaction.
+// Per-thread collection with at most `budget` pops.  The stack is the thread's column of a
+// block-shared array (entry k at sn[k * kBlockThreads]), kTStack entries deep: the per-pop pushes
+// and pops stay in shared memory instead of local memory.  Returns 0 when done, 1 on stack
+// overflow (candidates may miss subtrees), 2 when the budget ran out (ub stays a valid bound), 3
+// when more than kQCand candidates remain after compaction; ub stays a valid bound in every case.
+constexpr int kTStack = 32;
+constexpr int kBlockThreads = 128;
 template <int MODE>
 __device__ int thread_collect(const BvhDev &b, const double q[3], float &ub, int32_t *cl, float *cb, int &nc,
-                              int budget) {
+                              int budget, int32_t *sn, float *sd) {
   const int n = b.n;
   nc = 0;
   if (n == 1) {
@@ -631,16 +635,15 @@ __device__ int thread_collect(const BvhDev &b, const double q[3], float &ub, int
   }
   const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
   const float mbox = 1e-6f * (1.f + fabsf(qf[0]) + fabsf(qf[1]) + fabsf(qf[2]));
-  int32_t sn[kStack];
-  float sd[kStack];
+  constexpr int S = kBlockThreads;
   int sp = 0, pops = 0;
   bool ok = true;
-  sn[sp] = 0; sd[sp] = 0.f; sp++;
+  sn[0] = 0; sd[0] = 0.f; sp++;
   while (sp > 0) {
     if (pops >= budget) return 2;
     --sp;
-    const int32_t node = sn[sp];
-    const float d = sd[sp];
+    const int32_t node = sn[sp * S];
+    const float d = sd[sp * S];
     pops++;
     if (d > ub) continue;
     if (node < 0) {
@@ -670,8 +673,8 @@ __device__ int thread_collect(const BvhDev &b, const double q[3], float &ub, int
     const bool lnear = dl <= dr;
     const int32_t nearc = lnear ? r.l : r.r, farc = lnear ? r.r : r.l;
     const float dn = lnear ? dl : dr, df = lnear ? dr : dl;
-    if (df <= ub) { if (sp < kStack) { sn[sp] = farc; sd[sp] = df; sp++; } else ok = false; }
-    if (dn <= ub) { if (sp < kStack) { sn[sp] = nearc; sd[sp] = dn; sp++; } else ok = false; }
+    if (df <= ub) { if (sp < kTStack) { sn[sp * S] = farc; sd[sp * S] = df; sp++; } else return 1; }
+    if (dn <= ub) { if (sp < kTStack) { sn[sp * S] = nearc; sd[sp * S] = dn; sp++; } else return 1; }
   }
   return ok ? 0 : 1;
 }
@@ -988,7 +991,9 @@ __device__ __forceinline__ int64_t proj_entry(const ProjArgs &p, const MeshDesc 
   return e;
 }
 
-__global__ void __launch_bounds__(128) k_project(ProjArgs p) {
+__global__ void __launch_bounds__(kBlockThreads) k_project(ProjArgs p) {
+  __shared__ int32_t s_sn[kTStack][kBlockThreads];
+  __shared__ float s_sd[kTStack][kBlockThreads];
   const Seg sg = p.seg[blockIdx.x];
   const int64_t i = sg.begin + threadIdx.x;
   bool has = i < sg.end;
@@ -1003,7 +1008,9 @@ __global__ void __launch_bounds__(128) k_project(ProjArgs p) {
     proj_entry(p, md, i, q);
     int st = 0;
     seed_bound<0>(t.bvh, p.seed, i, q, ub);
-    if (t.bvh.n > 0) st = thread_collect<0>(t.bvh, q, ub, cl, cb, nc, p.budget > 0 ? p.budget : kThreadBudget);
+    if (t.bvh.n > 0)
+      st = thread_collect<0>(t.bvh, q, ub, cl, cb, nc, p.budget > 0 ? p.budget : kThreadBudget, &s_sn[0][threadIdx.x],
+                             &s_sd[0][threadIdx.x]);
     if (st != 0) {
       // over budget, stack or candidate list: the cooperative pass restarts the query from the
       // root under the bound found so far (any leaf's upper bound bounds the minimum)
@@ -1208,7 +1215,9 @@ __device__ __forceinline__ void haus_query(const HausArgs &h, int64_t i, int32_t
 }
 
 template <int SIDE>
-__global__ void __launch_bounds__(128) k_haus_side(HausArgs h) {
+__global__ void __launch_bounds__(kBlockThreads) k_haus_side(HausArgs h) {
+  __shared__ int32_t s_sn[kTStack][kBlockThreads];
+  __shared__ float s_sd[kTStack][kBlockThreads];
   const Seg sg = h.seg[blockIdx.x];
   const int64_t i = sg.begin + threadIdx.x;
   bool has = i < sg.end;
@@ -1223,7 +1232,9 @@ __global__ void __launch_bounds__(128) k_haus_side(HausArgs h) {
     ub = dist_bound<1>(h.hm[sg.mesh].diag);
     seed_bound<1>(*b, h.seed, i, q, ub);
     int st = 0;
-    if (b->n > 0) st = thread_collect<1>(*b, q, ub, cl, cb, nc, h.budget > 0 ? h.budget : kThreadBudget);
+    if (b->n > 0)
+      st = thread_collect<1>(*b, q, ub, cl, cb, nc, h.budget > 0 ? h.budget : kThreadBudget, &s_sn[0][threadIdx.x],
+                             &s_sd[0][threadIdx.x]);
     if (st != 0) {
       // over budget, stack or candidate list: the cooperative pass restarts the query from the
       // root under the bound found so far (any leaf's upper bound bounds the minimum)
