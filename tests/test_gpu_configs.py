@@ -11,13 +11,16 @@ Bars (the criteria the optimiser is held to):
   minimum scaled J      within 1e-4 (both modes)
   Hausdorff max         within 1e-5 of the bbox diagonal (both modes)
   weight schedule       lamda within 1e-6 relative (FP64)
-  mixed positions       64^3 grid: 5e-5 of the diagonal, lamda 1e-3 relative; cube minus
-                        cylinder: 1e-5, lamda 1e-4.  Mixed precision rounds the local step's
+  mixed positions       5e-5 of the diagonal on both workloads; lamda 1e-3 relative (64^3 grid)
+                        and 1e-4 (cube minus cylinder).  Mixed precision rounds the local step's
                         coefficients at FP32 resolution, and the FP64 path itself moves by
-                        ~1e-5 of the diagonal on the 64^3 grid after 3 iterations when its input
-                        is perturbed at that resolution (2^-24 h, printed by the test): the
-                        truncated 20-iteration CG and the line search amplify such
-                        perturbations.  The mixed bars sit a few times above that sensitivity.
+                        ~1e-5 of the diagonal after 3 iterations when its input is perturbed at
+                        that resolution (2^-24 h, printed by the tests): the truncated
+                        20-iteration CG and the line search amplify such perturbations.  The
+                        mixed result also moves from run to run (the float atomics of the
+                        element scatter sum in launch order): 5e-6 to 1.2e-5 of the diagonal
+                        on the cube minus cylinder over repeated runs.  The mixed bars sit a few
+                        times above both.
 Each test prints the measured errors.
 """
 import numpy as np
@@ -114,5 +117,13 @@ def test_feature_alignment_grid64_vs_oracle(hx, grid64, mode):
 def test_feature_alignment_cube_minus_cylinder_vs_oracle(hx, c2, mode):
     ref = oracle_loop("c2", c2, 3)
     Vg, r = run_gpu(hx, c2, 3, hx.FP64 if mode == "fp64" else hx.MIXED)
-    check(f"cube_minus_cylinder {mode}", c2, Vg, r, ref, 1e-6 if mode == "fp64" else 1e-5,
+    if mode == "mixed":  # the FP64 path's own response to an input perturbed at FP32 resolution
+        h = 1.0 / 64
+        free = np.ones(len(c2["V"]), bool)
+        free[np.asarray(c2["corners"], np.int64)] = False
+        noise = np.random.default_rng(2).normal(0, 2.0 ** -24 * h, c2["V"].shape) * free[:, None]
+        Vn, rn = run_gpu(hx, c2, 3, hx.FP64, V0=c2["V"] + noise)
+        print(f"\n[cube_minus_cylinder fp64, input noise 2^-24 h] max|dX|/diag "
+              f"{np.abs(Vn - ref['V']).max() / diag_of(c2['V']):.3e}  lamda rel {abs(rn['lamda'] - ref['lam']) / ref['lam']:.3e}")
+    check(f"cube_minus_cylinder {mode}", c2, Vg, r, ref, 1e-6 if mode == "fp64" else 5e-5,
           1e-6 if mode == "fp64" else 1e-4)
