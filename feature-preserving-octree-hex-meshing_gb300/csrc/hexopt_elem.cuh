@@ -250,6 +250,57 @@ __device__ __forceinline__ void apply_BT(const T Q[3][3], int32_t gs, const doub
   }
 }
 
+// Runtime-K forms of the corner-tet maps, for loops over the 8 tets that are not unrolled (one
+// copy of the per-tet code): the cube-corner permutation becomes select chains, never a dynamic
+// index into a register array, and every value equals the compile-time form's bit for bit.
+template <typename T>
+__device__ __forceinline__ void apply_B_rt(int K, const T E[3][3], int32_t gs, const double *B, T s, T J[3][3]) {
+  if (gs < 0) {
+    const int a0 = edge_axis(K, 0), a1 = edge_axis(K, 1);
+    const T s0 = T(edge_sign(K, 0)) * s, s1 = T(edge_sign(K, 1)) * s, s2 = T(edge_sign(K, 2)) * s;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const T v0 = E[r][0] * s0, v1 = E[r][1] * s1, v2 = E[r][2] * s2;
+      J[r][0] = a0 == 0 ? v0 : a1 == 0 ? v1 : v2;
+      J[r][1] = a0 == 1 ? v0 : a1 == 1 ? v1 : v2;
+      J[r][2] = a0 == 2 ? v0 : a1 == 2 ? v1 : v2;
+    }
+  } else {
+    gen_J<0>(E, B, J);
+  }
+}
+template <typename T>
+__device__ __forceinline__ void apply_BT_rt(int K, const T Q[3][3], int32_t gs, const double *B, T s, T G[3][3]) {
+  if (gs < 0) {
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int a = edge_axis(K, j);
+      const T sg = T(edge_sign(K, j)) * s;
+#pragma unroll
+      for (int r = 0; r < 3; r++) G[r][j] = (a == 0 ? Q[r][0] : a == 1 ? Q[r][1] : Q[r][2]) * sg;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int r = 0; r < 3; r++) G[r][j] = Q[r][0] * T(B[j * 3 + 0]) + Q[r][1] * T(B[j * 3 + 1]) + Q[r][2] * T(B[j * 3 + 2]);
+  }
+}
+// Edge matrix of corner tet K from a thread's column of 12-edge frames (entry e * 3 + r at
+// col[(e * 3 + r) * stride]).
+template <typename T>
+__device__ __forceinline__ void tet_E_rt(int K, const T *col, int stride, T E[3][3]) {
+  const int c0 = tet_v(K, 0);
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int cj = tet_v(K, j + 1);
+    const int e = hex_edge_id(c0, cj);
+    const T sg = cj > c0 ? T(1) : T(-1);
+#pragma unroll
+    for (int r = 0; r < 3; r++) E[r][j] = sg * col[(e * 3 + r) * stride];
+  }
+}
+
 // ---------------------------------------------------------------- constraint items
 // The constraint items of a mesh, in order: corners, tangent planes, feature lines, projection
 // points (Tetralize_Set::b / bc), glue groups; e indexes the kind's global arrays.

@@ -72,12 +72,17 @@ __global__ void __launch_bounds__(128) k_precompute(KArgs a) {
 // also scatters the initial residual r0 = b - A x0 = sum_t M W^T W (R - J) B^T (formed per
 // element, so it carries no cancellation); mixed mode stores R instead and forms r0 in k_ir_resid
 // from the FP64 positions.
-template <typename ET, int K, bool PRE>
-__device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs, const ET E12[12][3], ET M, ET exp_f,
-                                          int energy, const uint32_t hv[8], bool &degenerate) {
+// K is a run-time index (the 8 tets run as a loop that is not unrolled, so the SVD and weight
+// code exists once: unrolled, the kernel outgrew the instruction cache); the hex's 12-edge frame
+// and corner ids come from the thread's columns of block-shared arrays (stride kLocalThreads).
+constexpr int kLocalThreads = 128;
+template <typename ET, bool PRE>
+__device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs, int K, const ET *e12col, ET M,
+                                          ET exp_f, int energy, const uint32_t *hvcol, bool &degenerate) {
   ET *gb = reinterpret_cast<ET *>(a.b), *gr = reinterpret_cast<ET *>(a.r), *gd = reinterpret_cast<ET *>(a.diag);
+  auto hvk = [&](int c) { return hvcol[c * kLocalThreads]; };
   ET E[3][3];
-  tet_E12<K>(E12, E);
+  tet_E_rt(K, e12col, kLocalThreads, E);
   ET *Sinv = reinterpret_cast<ET *>(a.Sinv);
   double *B = gs >= 0 ? a.Bgen + ((int64_t)gs * 8 + K) * 9 : nullptr;
   ET is;
@@ -107,7 +112,7 @@ __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs,
     is = Sinv[tet_idx<1>(h, K, 0)];
   }
   ET J[3][3];
-  apply_B<K>(E, gs, B, is, J);
+  apply_B_rt(K, E, gs, B, is, J);
   ET R[3][3], U[3][3], s[3], Vm[3][3], m[3];
   polar_svd3(J, R, U, s, Vm);
   slim_weights(energy, exp_f, s, U, Vm, m, R);
@@ -122,15 +127,15 @@ __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs,
   c[5] = U[1][0] * U[2][0] * m0 + U[1][1] * U[2][1] * m1 + U[1][2] * U[2][2] * m2;
   ET Q[3][3], G[3][3];
   sym_mul(c, R, Q);
-  apply_BT<K>(Q, gs, B, is, G);
+  apply_BT_rt(K, Q, gs, B, is, G);
   {
     ET s0 = 0, s1 = 0, s2 = 0;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      atomic_add3(gb, hv[tet_v(K, j + 1)], G[0][j], G[1][j], G[2][j]);
+      atomic_add3(gb, hvk(tet_v(K, j + 1)), G[0][j], G[1][j], G[2][j]);
       s0 += G[0][j]; s1 += G[1][j]; s2 += G[2][j];
     }
-    atomic_add3(gb, hv[tet_v(K, 0)], -s0, -s1, -s2);
+    atomic_add3(gb, hvk(tet_v(K, 0)), -s0, -s1, -s2);
   }
   if constexpr (sizeof(ET) == 4) {
     // mixed mode: the rotation is kept for the residual evaluations of the refined PCG (k_ir_*),
@@ -146,14 +151,14 @@ __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs,
 #pragma unroll
       for (int j = 0; j < 3; j++) R[i][j] -= J[i][j];
     sym_mul(c, R, Q);
-    apply_BT<K>(Q, gs, B, is, G);
+    apply_BT_rt(K, Q, gs, B, is, G);
     ET s0 = 0, s1 = 0, s2 = 0;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      atomic_add3(gr, hv[tet_v(K, j + 1)], G[0][j], G[1][j], G[2][j]);
+      atomic_add3(gr, hvk(tet_v(K, j + 1)), G[0][j], G[1][j], G[2][j]);
       s0 += G[0][j]; s1 += G[1][j]; s2 += G[2][j];
     }
-    atomic_add3(gr, hv[tet_v(K, 0)], -s0, -s1, -s2);
+    atomic_add3(gr, hvk(tet_v(K, 0)), -s0, -s1, -s2);
   }
   ET *C = reinterpret_cast<ET *>(a.Ccoef);
   ET w[4];
@@ -173,7 +178,7 @@ __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs,
     w[0] = g0[0] * g0[0] + g0[1] * g0[1] + g0[2] * g0[2];
   }
 #pragma unroll
-  for (int j = 0; j < 4; j++) atomic_add3(gd, hv[tet_v(K, j)], w[j] * c[0], w[j] * c[1], w[j] * c[2]);
+  for (int j = 0; j < 4; j++) atomic_add3(gd, hvk(tet_v(K, j)), w[j] * c[0], w[j] * c[1], w[j] * c[2]);
 }
 
 // Each corner tet scatters its right-hand-side, residual and diagonal contributions straight to
@@ -182,26 +187,31 @@ __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs,
 // (96 registers, ~100 B of spills): more warps hide the FP32 SVD's latency (1.47 -> 1.20 ms at
 // 2.1M hexes).
 template <typename ET, bool PRE>
-__global__ void __launch_bounds__(128, sizeof(ET) == 4 ? 5 : 1) k_local(KArgs a) {
+__global__ void __launch_bounds__(kLocalThreads, sizeof(ET) == 4 ? 5 : 1) k_local(KArgs a) {
+  __shared__ ET e12s[36][kLocalThreads];
+  __shared__ uint32_t hvs[8][kLocalThreads];
   const Seg sg = a.hseg[blockIdx.x];
   const int64_t h = sg.begin + threadIdx.x;
   if (h >= sg.end) return;
   const MeshScalars &S = a.sc[sg.mesh];
   const ET M = ET(S.M), exp_f = ET(S.exp_f);
-  uint32_t hv[8];
-  load_hex(a.hexv, h, hv);
+  {
+    uint32_t hv[8];
+    load_hex(a.hexv, h, hv);
+    ET E12[12][3];
+    hex_edges_mode<ET>(a, hv, E12);
+#pragma unroll
+    for (int c = 0; c < 8; c++) hvs[c][threadIdx.x] = hv[c];
+#pragma unroll
+    for (int e = 0; e < 12; e++)
+#pragma unroll
+      for (int r = 0; r < 3; r++) e12s[e * 3 + r][threadIdx.x] = E12[e][r];
+  }
   const int32_t gs = a.gslot[h];
-  ET E12[12][3];
-  hex_edges_mode<ET>(a, hv, E12);
   bool degenerate = false;
-  local_tet<ET, 0, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 1, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 2, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 3, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 4, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 5, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 6, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
-  local_tet<ET, 7, PRE>(a, h, gs, E12, M, exp_f, a.energy, hv, degenerate);
+#pragma unroll 1
+  for (int K = 0; K < 8; K++)
+    local_tet<ET, PRE>(a, h, gs, K, &e12s[0][threadIdx.x], M, exp_f, a.energy, &hvs[0][threadIdx.x], degenerate);
   if (PRE && degenerate) atomicOr(&a.sc[sg.mesh].status, 2);
 }
 
@@ -1307,7 +1317,6 @@ template <typename ET, typename VT>
 __global__ void __launch_bounds__(128, sizeof(ET) == 4 ? 4 : 1) k_ls_bound(KArgs a) {
   const Seg sg = a.hseg[blockIdx.x];
   const int64_t h = sg.begin + threadIdx.x;
-  const MeshDesc md = a.mesh[sg.mesh];
   MeshScalars &S = a.sc[sg.mesh];
   double eq[1] = {0};
   unsigned need = 0;  // bit K: corner tet K needs the exact root
