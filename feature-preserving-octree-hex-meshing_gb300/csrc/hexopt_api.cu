@@ -69,7 +69,7 @@ struct KindTable {
 };
 
 struct StaticBvh {  // device LBVH over a fixed triangle set
-  DBuf child, parent, box, leaf_face, tri, counters, node, leafd;
+  DBuf child, parent, box, leaf_face, tri, counters, node, leafd, onode;
   int32_t n = 0;
   BvhDev dev() const {
     BvhDev b{};
@@ -80,6 +80,7 @@ struct StaticBvh {  // device LBVH over a fixed triangle set
     b.tri = tri.as<double>();
     b.node = node.as<float4>();
     b.leafd = leafd.as<float4>();
+    b.onode = onode.as<float4>();
     return b;
   }
 };
@@ -89,7 +90,7 @@ struct TargetHost {
   int64_t nv = 0, nf = 0;
   std::vector<double> TV;
   StaticBvh bvh;
-  DBuf TVd, FN, VNc, ENc, curve_ptr, curve_vs, curve_closed;
+  DBuf TVd, FN, VNc, ENc, EP, curve_ptr, curve_vs, curve_closed;
   int64_t n_curves = 0;
   double lo[3], hi[3];
   std::vector<int64_t> ref_vs;  // vertices referenced by a face (target-local ids)
@@ -140,7 +141,7 @@ struct hexopt_ctx {
   // device order of the batch (Morton-sorted vertices and hexes); the caller's order at the ABI
   int ordering = 2;  // 0 caller order, 1 Morton, 2 Morton unless the caller's numbering is coherent
   bool ordered = false;
-  int query_budget = 0;  // per-thread BVH traversal pops before the warp pass (0: the default 64)
+  int query_budget = 0;  // per-thread BVH traversal pops before the warp pass (0: the defaults below)
   DBuf vnew2old, vold2new, hnew2old, hold2new;
   std::vector<int32_t> vold2new_h, hnew2old_h;
   bool has_fixed = false, has_glue = false;
@@ -556,7 +557,8 @@ void fill_report(const MeshScalars &S, int64_t nh, hexopt_slim_report &r) {
 }
 
 // ------------------------------------------------------------------ BVH builds
-int build_static_bvh(hexopt_ctx *ctx, StaticBvh &B, const std::vector<double> &tri, int64_t nf) {
+// oriented: also the oriented node records (trees that the target queries walk)
+int build_static_bvh(hexopt_ctx *ctx, StaticBvh &B, const std::vector<double> &tri, int64_t nf, bool oriented) {
   B.n = (int32_t)nf;
   if (nf == 0) return HEXOPT_OK;
   CK(upload(B.tri, tri.data(), tri.size(), ctx->st));
@@ -577,7 +579,12 @@ int build_static_bvh(hexopt_ctx *ctx, StaticBvh &B, const std::vector<double> &t
   CK(cudaMemsetAsync(B.counters.p, 0, sizeof(unsigned) * std::max<int64_t>(nf - 1, 1), ctx->st));
   CK(B.node.ensure(sizeof(float4) * 4 * std::max<int64_t>(nf - 1, 1)));
   CK(B.leafd.ensure(sizeof(float4) * 3 * nf));
-  DBuf keys, keys2, tmp;
+  DBuf keys, keys2, tmp, range, obb;
+  if (oriented && nf > 1) {
+    CK(range.ensure(sizeof(int32_t) * 2 * (nf - 1)));
+    CK(obb.ensure(sizeof(float4) * 4 * (2 * nf - 1)));
+    CK(B.onode.ensure(sizeof(float4) * 8 * (nf - 1)));
+  }
   CK(keys.ensure(sizeof(unsigned long long) * nf));
   CK(keys2.ensure(sizeof(unsigned long long) * nf));
   BvhDev bd = B.dev();
@@ -586,11 +593,16 @@ int build_static_bvh(hexopt_ctx *ctx, StaticBvh &B, const std::vector<double> &t
   CK(cub::DeviceRadixSort::SortKeys(nullptr, tb, keys.as<unsigned long long>(), keys2.as<unsigned long long>(), (int)nf, 0, 64, ctx->st));
   CK(tmp.ensure(tb));
   CK(cub::DeviceRadixSort::SortKeys(tmp.p, tb, keys.as<unsigned long long>(), keys2.as<unsigned long long>(), (int)nf, 0, 64, ctx->st));
-  bvh_karras((int)nf, keys2.as<unsigned long long>(), B.child.as<int32_t>(), B.parent.as<int32_t>(), B.leaf_face.as<int32_t>(), ctx->st);
+  bvh_karras((int)nf, keys2.as<unsigned long long>(), B.child.as<int32_t>(), B.parent.as<int32_t>(), B.leaf_face.as<int32_t>(), ctx->st,
+             range.as<int32_t>());
   bd = B.dev();
   bvh_refit(bd, B.box.as<float>(), B.parent.as<int32_t>(), B.counters.as<unsigned>(), B.node.as<float4>(),
             B.leafd.as<float4>(), ctx->st);
   ctx->launches += 5;
+  if (oriented && nf > 1) {
+    bvh_orient(bd, range.as<int32_t>(), obb.as<float4>(), B.onode.as<float4>(), ctx->st);
+    ctx->launches += 3;
+  }
   CKL();
   CK(cudaStreamSynchronize(ctx->st));
   return HEXOPT_OK;
@@ -606,6 +618,7 @@ int upload_targets_table(hexopt_ctx *ctx) {
       t.TV = h.TVd.as<double>();
       t.tri = h.bvh.tri.as<double>();
       t.FN = h.FN.as<double>();
+      t.EP = h.EP.as<double>();
       t.VNc = h.VNc.as<double>();
       t.ENc = h.ENc.as<double>();
       t.curve_ptr = h.curve_ptr.as<int64_t>();
@@ -729,7 +742,7 @@ ProjArgs make_proj(hexopt_ctx *c, int kind) {
   p.l_ids = c->l_ids.as<int32_t>(); p.l_curve = c->l_curve.as<int32_t>();
   p.l_axis = c->l_axis.as<double>(); p.l_orig = c->l_orig.as<double>();
   p.seed = c->qseed.as<int32_t>();
-  p.budget = c->query_budget;
+  p.budget = c->query_budget > 0 ? c->query_budget : 128;  // no benchmark projection query needs more
   return p;
 }
 
@@ -750,7 +763,7 @@ HausArgs make_haus(hexopt_ctx *c, int kind) {
   h.partials = c->partials.as<double>();
   h.counters = c->counters.as<unsigned>();
   h.seed = c->qseed.as<int32_t>() + (kind == K_SURFV ? 2 : 1) * c->qseed_n;
-  h.budget = c->query_budget;
+  h.budget = c->query_budget > 0 ? c->query_budget : 96;  // side 0's long queries do better cooperatively
   return h;
 }
 
@@ -1477,8 +1490,12 @@ int hexopt_set_target(hexopt_ctx *ctx, int mesh, int64_t nv, const double *TV, i
   CK(upload(t.FN, FN.data(), FN.size(), ctx->st));
   CK(upload(t.VNc, VNc.data(), VNc.size(), ctx->st));
   CK(upload(t.ENc, ENc.data(), ENc.size(), ctx->st));
-  rc = build_static_bvh(ctx, t.bvh, tri, nf);
+  rc = build_static_bvh(ctx, t.bvh, tri, nf, true);
   if (rc) return rc;
+  CK(t.EP.ensure(sizeof(double) * 16 * nf));
+  launch_ep_faces(t.bvh.tri.as<double>(), nf, t.EP.as<double>(), ctx->st);
+  ctx->launches++;
+  CKL();
   t.set = true;
   // referenced target vertices for the Hausdorff side 0 list
   t.ref_vs.clear();
@@ -1633,7 +1650,7 @@ int hexopt_set_surface(hexopt_ctx *ctx, int mesh, int64_t nf, const int32_t *F) 
     for (int c = 0; c < 3; c++)
       for (int d = 0; d < 3; d++) tri[9 * f + 3 * c + d] = Xh[3 * (int64_t)(G[3 * f + c] - vo) + d];
   StaticBvh tmp;
-  rc = build_static_bvh(ctx, tmp, tri, nf);
+  rc = build_static_bvh(ctx, tmp, tri, nf, false);
   if (rc) return rc;
   // adopt the topology (child / parent / leaf order); boxes are refitted from X on use
   std::swap(s.child.p, tmp.child.p); std::swap(s.child.bytes, tmp.child.bytes);
@@ -1726,9 +1743,9 @@ int hexopt_hausdorff(hexopt_ctx *ctx, int64_t nv0, const double *V0, int64_t nf0
   for (int64_t v = 0; v < nv0; v++) if (u0[v]) r0.push_back(v);
   for (int64_t v = 0; v < nv1; v++) if (u1[v]) r1.push_back(v);
   StaticBvh B0, B1;
-  int rc = build_static_bvh(ctx, B0, tri0, nf0);
+  int rc = build_static_bvh(ctx, B0, tri0, nf0, false);
   if (rc) return rc;
-  rc = build_static_bvh(ctx, B1, tri1, nf1);
+  rc = build_static_bvh(ctx, B1, tri1, nf1, false);
   if (rc) return rc;
   DBuf P0, P1, I0, I1, dist, stat, out;
   CK(upload(P0, V0, (size_t)3 * nv0, ctx->st));
@@ -1778,9 +1795,9 @@ int hexopt_hausdorff_uniform(hexopt_ctx *ctx, int64_t nv0, const double *V0, int
   for (int64_t f = 0; f < nf0; f++) for (int c = 0; c < 3; c++) for (int d = 0; d < 3; d++) tri0[9 * f + 3 * c + d] = V0[3 * (int64_t)F0[3 * f + c] + d];
   for (int64_t f = 0; f < nf1; f++) for (int c = 0; c < 3; c++) for (int d = 0; d < 3; d++) tri1[9 * f + 3 * c + d] = V1[3 * (int64_t)F1[3 * f + c] + d];
   StaticBvh B0, B1;
-  int rc = build_static_bvh(ctx, B0, tri0, nf0);
+  int rc = build_static_bvh(ctx, B0, tri0, nf0, false);
   if (rc) return rc;
-  rc = build_static_bvh(ctx, B1, tri1, nf1);
+  rc = build_static_bvh(ctx, B1, tri1, nf1, false);
   if (rc) return rc;
   DBuf Vd0, Vd1, Fd0, Fd1, S0, S1, scratch, dist, stat, out;
   CK(upload(Vd0, V0, (size_t)3 * nv0, ctx->st));
@@ -1830,7 +1847,7 @@ int hexopt_point_face_distance(hexopt_ctx *ctx, int64_t np, const double *P, int
   std::vector<double> tri(9 * nf);
   for (int64_t f = 0; f < nf; f++) for (int c = 0; c < 3; c++) for (int d = 0; d < 3; d++) tri[9 * f + 3 * c + d] = V[3 * (int64_t)F[3 * f + c] + d];
   StaticBvh B;
-  int rc = build_static_bvh(ctx, B, tri, nf);
+  int rc = build_static_bvh(ctx, B, tri, nf, false);
   if (rc) return rc;
   DBuf Pd, Dd, stat;
   CK(upload(Pd, P, (size_t)3 * np, ctx->st));

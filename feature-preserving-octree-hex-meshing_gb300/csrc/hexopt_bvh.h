@@ -25,6 +25,9 @@ struct BvhDev {
   // per leaf (sorted order), 48 B: first vertex and the two edges from it in FP32 -- the
   // screening data of the leaf's triangle
   const float4 *leafd;
+  // static trees only (null otherwise): 128-byte internal node records with both children's
+  // oriented boxes -- rows of an orthonormal frame and the extents along them -- and ids
+  const float4 *onode;
 };
 
 // Per-mesh refit view of a dynamic (hex-boundary) surface tree: the tree and the buffers the
@@ -72,6 +75,9 @@ struct TargetDev {
   const double *TV;       // target vertices, rows of 3
   const double *tri;      // 9 doubles per face
   const double *FN;       // face normals (3 per face)
+  // per face, 16 doubles: PointDistanceEP's set-up of the face (edges scaled by the dominant
+  // normal component, unit normal, plane offset, double area, dominant axis), formed once
+  const double *EP;
   const double *VNc;      // angle-weighted vertex normal of each corner (9 per face)
   const double *ENc;      // uniform edge normal of the edge opposite each corner (9 per face)
   const int64_t *curve_ptr;
@@ -124,8 +130,12 @@ struct HausArgs {
 };
 
 void bvh_morton(const BvhDev &b, const double lo[3], const double hi[3], unsigned long long *keys, cudaStream_t st);
+// range (optional, 2 per internal node): the node's first and last leaf in sorted order
 void bvh_karras(int n, const unsigned long long *keys, int32_t *child, int32_t *parent, int32_t *leaf_face,
-                cudaStream_t st);
+                cudaStream_t st, int32_t *range = nullptr);
+// oriented boxes of every node of a fitted static tree (obb: (2n - 1) x 64 B scratch) and the
+// 128-byte oriented records built from them
+void bvh_orient(const BvhDev &b, const int32_t *range, float4 *obb, float4 *onode, cudaStream_t st);
 // refit boxes bottom-up and rewrite the packed node records
 void bvh_refit(const BvhDev &b, float *box, const int32_t *parent, unsigned *counters, float4 *node, float4 *leafd,
                cudaStream_t st);
@@ -145,5 +155,7 @@ void launch_ep_points(const BvhDev &b, const double *P, const int64_t *ids, int6
                       int *status, cudaStream_t st);
 void launch_maxmean(const double *dist, int64_t n, double upper, double *out3, cudaStream_t st);
 void launch_fa_haus_flag(MeshScalars *sc, const HausMesh *hm, int n, cudaStream_t st);
+// PointDistanceEP's per-face set-up of a static triangle set (tri: 9 doubles per face)
+void launch_ep_faces(const double *tri, int64_t nf, double *EP, cudaStream_t st);
 
 }  // namespace hexopt

@@ -5,7 +5,8 @@
 //    radix-sorted (CUB), internal nodes from the longest common prefix, boxes fitted bottom-up
 //    with per-node arrival counters.  Boxes are FP32, rounded outward, so every distance lower
 //    bound stays conservative.  Dynamic surfaces (the hex mesh boundary) keep the topology and
-//    are refitted from the current positions.
+//    are refitted from the current positions; static trees (the targets) also get an oriented
+//    box per node (principal axes of its vertices), which the target queries prune with.
 //  * closest point: Ericson's point-triangle test in FP64 (as igl::point_simplex_squared_distance)
 //    under a depth-first traversal with nearest-child-first order and strict-improvement updates
 //    (AABB::squared_distance, AABB.cpp:366-445); pseudonormal of the winning face restates
@@ -67,7 +68,8 @@ __device__ __forceinline__ int lcp(const unsigned long long *k, int n, int i, in
   return __clzll(k[i] ^ k[j]);
 }
 
-__global__ void k_karras(int n, const unsigned long long *keys, int32_t *child, int32_t *parent, int32_t *leaf_face) {
+__global__ void k_karras(int n, const unsigned long long *keys, int32_t *child, int32_t *parent, int32_t *leaf_face,
+                         int32_t *range) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) leaf_face[i] = (int32_t)(keys[i] & 0xffffffffull);
   if (i >= n - 1) return;
@@ -91,6 +93,7 @@ __global__ void k_karras(int n, const unsigned long long *keys, int32_t *child, 
   }
   const int gamma = i + s * d + (d < 0 ? d : 0);
   const int lo = i < j ? i : j, hi = i < j ? j : i;
+  if (range) { range[2 * i] = lo; range[2 * i + 1] = hi; }  // the node's leaves, sorted order
   const int32_t left = (lo == gamma) ? ~gamma : gamma;
   const int32_t right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
   child[2 * i] = left;
@@ -181,6 +184,192 @@ __global__ void k_refit_batch(const RefitDev *R, const Seg *seg, const MeshDesc 
   const int32_t k = (int32_t)(i - md[sg.mesh].kitem0[K_SURFF]);
   if (k >= r.b.n) return;
   refit_leaf(r.b, r.box, r.parent, r.counters, r.leafd, r.node, k);
+}
+
+// ------------------------------------------------------------------------------- oriented boxes
+// Static trees (the targets) also carry an oriented box per node: rows a0..a2 of an orthonormal
+// frame rounded to FP32 and extents [lo_k, hi_k] of the node's vertices along them, formed in
+// FP64 with the stored rows and rounded outward, so lo_k <= a_k . x <= hi_k for every point x of
+// every triangle below the node.  A leaf takes its triangle's frame (first edge, in-plane normal
+// to it, normal: zero thickness); an internal node of at most kObbLeaves leaves the principal axes
+// of its vertices, and keeps them only where they enclose less volume than the axis-aligned box
+// (which larger nodes always use).  Queries that start well away from a curved surface reach
+// many more tilted axis-aligned boxes than oriented ones: on a 200k-triangle superellipsoid with
+// queries on the faces of a cube around it, about a third of the internal nodes.
+constexpr int kObbLeaves = 1024;
+
+// Eigenvectors of a symmetric 3x3 matrix (cyclic Jacobi rotations, FP64), as the columns of v.
+__device__ void sym3_eigvecs(double a[3][3], double v[3][3]) {
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) v[r][c] = r == c ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 16; sweep++) {
+    const double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    const double dia = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+    if (!(off > 1e-30 * dia)) break;
+    for (int pq = 0; pq < 3; pq++) {
+      const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+      const double apq = a[p][q];
+      if (apq == 0.0) continue;
+      const double th = (a[q][q] - a[p][p]) / (2.0 * apq);
+      const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+      const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+      for (int k = 0; k < 3; k++) {  // columns p, q of a J
+        const double akp = a[k][p], akq = a[k][q];
+        a[k][p] = c * akp - sn * akq;
+        a[k][q] = sn * akp + c * akq;
+      }
+      for (int k = 0; k < 3; k++) {  // rows p, q of J^T a
+        const double apk = a[p][k], aqk = a[q][k];
+        a[p][k] = c * apk - sn * aqk;
+        a[q][k] = sn * apk + c * aqk;
+      }
+      for (int k = 0; k < 3; k++) {
+        const double vkp = v[k][p], vkq = v[k][q];
+        v[k][p] = c * vkp - sn * vkq;
+        v[k][q] = sn * vkp + c * vkq;
+      }
+    }
+  }
+}
+
+// Extents of points along the stored (FP32) rows, in FP64; rounded outward by obb_store.
+struct ObbAcc {
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  double scale = 1.0;
+  __device__ void add(const float a[3][3], const double p[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double u = double(a[k][0]) * p[0] + double(a[k][1]) * p[1] + double(a[k][2]) * p[2];
+      mn[k] = fmin(mn[k], u);
+      mx[k] = fmax(mx[k], u);
+    }
+    scale = fmax(scale, 1.0 + fabs(p[0]) + fabs(p[1]) + fabs(p[2]));
+  }
+};
+
+// 64-byte node box: (a0, a1.x), (a1.yz, a2.xy), (a2.z, lo), (hi, id -- set when packed)
+__device__ void obb_store(float4 *o, const float a[3][3], const ObbAcc &acc) {
+  float lo[3], hi[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {  // the FP64 extents carry at most a few ulps of |p|_1
+    lo[k] = __double2float_rd(acc.mn[k] - 1e-12 * acc.scale);
+    hi[k] = __double2float_ru(acc.mx[k] + 1e-12 * acc.scale);
+  }
+  o[0] = make_float4(a[0][0], a[0][1], a[0][2], a[1][0]);
+  o[1] = make_float4(a[1][1], a[1][2], a[2][0], a[2][1]);
+  o[2] = make_float4(a[2][2], lo[0], lo[1], lo[2]);
+  o[3] = make_float4(hi[0], hi[1], hi[2], 0.f);
+}
+
+__device__ __forceinline__ void unit_rows(float a[3][3]) {
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) a[r][c] = r == c ? 1.f : 0.f;
+}
+
+// leaves (sorted order): the triangle's own frame, or the coordinate axes if it is degenerate
+__global__ void k_obb_leaf(BvhDev b, float4 *obb) {
+  const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= b.n) return;
+  double p[3][3];
+  face_pts(b, b.leaf_face[k], p);
+  const double e1[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+  const double e2[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+  const double nr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+  const double l1 = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+  const double l2 = sqrt(e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2]);
+  const double ln = sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
+  float a[3][3];
+  unit_rows(a);
+  if (l1 > 0.0 && ln > 1e-9 * l1 * l2) {
+    const double u[3] = {e1[0] / l1, e1[1] / l1, e1[2] / l1}, w[3] = {nr[0] / ln, nr[1] / ln, nr[2] / ln};
+    const double v[3] = {w[1] * u[2] - w[2] * u[1], w[2] * u[0] - w[0] * u[2], w[0] * u[1] - w[1] * u[0]};
+    for (int c = 0; c < 3; c++) { a[0][c] = float(u[c]); a[1][c] = float(v[c]); a[2][c] = float(w[c]); }
+  }
+  ObbAcc acc;
+  for (int c = 0; c < 3; c++) acc.add(a, p[c]);
+  obb_store(obb + 4 * (int64_t)(b.n - 1 + k), a, acc);
+}
+
+// internal nodes: principal axes of the vertices below (up to kObbLeaves leaves) where they
+// enclose less volume than the axis-aligned box, else that box
+__global__ void k_obb_node(BvhDev b, const int32_t *range, float4 *obb) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.n - 1) return;
+  const float *bx = b.box + 6 * (int64_t)i;
+  float a[3][3];
+  unit_rows(a);
+  ObbAcc acc;
+  for (int k = 0; k < 3; k++) { acc.mn[k] = bx[k]; acc.mx[k] = bx[3 + k]; }
+  acc.scale = 0.0;  // the box's floats are kept as they are
+  const int32_t lo = range[2 * i], hi = range[2 * i + 1];
+  if (lo >= 0 && hi < b.n && hi - lo + 1 <= kObbLeaves) {
+    double p[3][3];
+    face_pts(b, b.leaf_face[lo], p);
+    const double o[3] = {p[0][0], p[0][1], p[0][2]};
+    double s1[3] = {0, 0, 0}, s2[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int32_t k = lo; k <= hi; k++) {
+      face_pts(b, b.leaf_face[k], p);
+      for (int c = 0; c < 3; c++) {
+        const double d[3] = {p[c][0] - o[0], p[c][1] - o[1], p[c][2] - o[2]};
+        for (int r = 0; r < 3; r++) {
+          s1[r] += d[r];
+          for (int t = 0; t < 3; t++) s2[r][t] += d[r] * d[t];
+        }
+      }
+    }
+    const double cnt = 3.0 * double(hi - lo + 1);
+    double cv[3][3], v[3][3];
+    for (int r = 0; r < 3; r++)
+      for (int t = 0; t < 3; t++) cv[r][t] = s2[r][t] / cnt - (s1[r] / cnt) * (s1[t] / cnt);
+    sym3_eigvecs(cv, v);
+    float ar[3][3];
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) ar[r][c] = float(v[c][r]);
+    ObbAcc oa;
+    for (int32_t k = lo; k <= hi; k++) {
+      face_pts(b, b.leaf_face[k], p);
+      for (int c = 0; c < 3; c++) oa.add(ar, p[c]);
+    }
+    // compare enclosed volumes (extents padded so that flat boxes still compare)
+    const double pad = 1e-9 * oa.scale;
+    double vo = 1.0, va = 1.0;
+    for (int k = 0; k < 3; k++) {
+      vo *= oa.mx[k] - oa.mn[k] + pad;
+      va *= double(bx[3 + k]) - double(bx[k]) + pad;
+    }
+    if (vo < va) {
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) a[r][c] = ar[r][c];
+      acc = oa;
+    }
+  }
+  obb_store(obb + 4 * (int64_t)i, a, acc);
+}
+
+// 128-byte oriented node records: both children's boxes, each with the child's id in its last lane
+__global__ void k_opack(int n, const int32_t *child, const float4 *obb, float4 *onode) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  for (int s = 0; s < 2; s++) {
+    const int32_t c = child[2 * i + s];
+    float4 *o = onode + 8 * (int64_t)i + 4 * s;
+    if (c >= 0 ? c >= n - 1 : ~c >= n) {  // malformed: an unbounded box, reported when visited
+      o[0] = make_float4(1.f, 0.f, 0.f, 0.f);
+      o[1] = make_float4(1.f, 0.f, 0.f, 0.f);
+      o[2] = make_float4(1.f, -INFINITY, -INFINITY, -INFINITY);
+      o[3] = make_float4(INFINITY, INFINITY, INFINITY, __int_as_float(c));
+      continue;
+    }
+    const float4 *f = obb + 4 * (int64_t)(c >= 0 ? c : n - 1 + ~c);
+    o[0] = f[0];
+    o[1] = f[1];
+    o[2] = f[2];
+    float4 t = f[3];
+    t.w = __int_as_float(c);
+    o[3] = t;
+  }
 }
 
 // ------------------------------------------------------------------------------- queries
@@ -403,6 +592,47 @@ __device__ void ep_setup(const double P[3][3], EPFace &e) {
   e.darea = sqrt(ndot(x, x));
 }
 
+// The set-up above, stored per face (16 doubles) and read back: the same bits as forming it anew.
+__device__ __forceinline__ void ep_store(const EPFace &e, double *o) {
+  double2 *w = reinterpret_cast<double2 *>(o);
+  w[0] = make_double2(e.edge[0][0], e.edge[0][1]);
+  w[1] = make_double2(e.edge[0][2], e.edge[1][0]);
+  w[2] = make_double2(e.edge[1][1], e.edge[1][2]);
+  w[3] = make_double2(e.edge[2][0], e.edge[2][1]);
+  w[4] = make_double2(e.edge[2][2], e.dir[0]);
+  w[5] = make_double2(e.dir[1], e.dir[2]);
+  w[6] = make_double2(e.off, e.darea);
+  w[7] = make_double2(double(e.axis), 0.0);
+}
+__device__ __forceinline__ void ep_load(const double *o, const double P[3][3], EPFace &e) {
+  const double2 *w = reinterpret_cast<const double2 *>(o);
+  const double2 w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2), w3 = __ldg(w + 3), w4 = __ldg(w + 4),
+                w5 = __ldg(w + 5), w6 = __ldg(w + 6), w7 = __ldg(w + 7);
+#pragma unroll
+  for (int c = 0; c < 3; c++)
+#pragma unroll
+    for (int d = 0; d < 3; d++) e.p[c][d] = P[c][d];
+  e.edge[0][0] = w0.x; e.edge[0][1] = w0.y; e.edge[0][2] = w1.x;
+  e.edge[1][0] = w1.y; e.edge[1][1] = w2.x; e.edge[1][2] = w2.y;
+  e.edge[2][0] = w3.x; e.edge[2][1] = w3.y; e.edge[2][2] = w4.x;
+  e.dir[0] = w4.y; e.dir[1] = w5.x; e.dir[2] = w5.y;
+  e.off = w6.x; e.darea = w6.y;
+  e.axis = int(w7.x);
+}
+
+__global__ void k_ep_faces(const double *tri, int64_t nf, double *EP) {
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  double P[3][3];
+#pragma unroll
+  for (int c = 0; c < 3; c++)
+#pragma unroll
+    for (int d = 0; d < 3; d++) P[c][d] = tri[f * 9 + c * 3 + d];
+  EPFace e;
+  ep_setup(P, e);
+  ep_store(e, EP + 16 * f);
+}
+
 __device__ __forceinline__ double ps_dist(const double q[3], const double *v1, const double *v2) {
   double e[3], qv[3], pp[3];
   nsub3(v2, v1, e);
@@ -452,6 +682,43 @@ __device__ __forceinline__ NodeRec load_node(const float4 *node, int32_t i) {
   r.rb[0] = b.z; r.rb[1] = b.w; r.rb[2] = c.x; r.rb[3] = c.y; r.rb[4] = c.z; r.rb[5] = c.w;
   r.l = __float_as_int(d.x); r.r = __float_as_int(d.y);
   return r;
+}
+
+// Lower bound of the distance from qf to anything inside an oriented box (one half of a 128-byte
+// record).  The rows are orthonormal to FP32 rounding (norm <= 1 + 2e-7), the projections carry
+// a few ulps of |q|_1 and qf differs from the FP64 query by an ulp: mob = 2e-6 (1 + |qf|_1) and
+// the relative factor cover all of it.
+__device__ __forceinline__ float obb_dist(const float4 &f0, const float4 &f1, const float4 &f2, const float4 &f3,
+                                          const float qf[3], float mob) {
+  const float u0 = f0.x * qf[0] + f0.y * qf[1] + f0.z * qf[2];
+  const float u1 = f0.w * qf[0] + f1.x * qf[1] + f1.y * qf[2];
+  const float u2 = f1.z * qf[0] + f1.w * qf[1] + f2.x * qf[2];
+  const float e0 = fmaxf(fmaxf(f2.y - u0, u0 - f3.x), 0.f);
+  const float e1 = fmaxf(fmaxf(f2.z - u1, u1 - f3.y), 0.f);
+  const float e2 = fmaxf(fmaxf(f2.w - u2, u2 - f3.z), 0.f);
+  return sqrtf(e0 * e0 + e1 * e1 + e2 * e2) * (1.f - 1e-6f) - mob;
+}
+
+// Both children of internal node `node` with their lower bounds: oriented records (OB, static
+// trees) or axis-aligned ones.  mbox = 1e-6 (1 + |qf|_1).
+template <bool OB>
+__device__ __forceinline__ void node_children(const BvhDev &b, int32_t node, const float qf[3], float mbox,
+                                              int32_t &l, int32_t &r, float &dl, float &dr) {
+  if constexpr (OB) {
+    const float4 *o = b.onode + 8 * (int64_t)node;
+    const float4 a0 = __ldg(o), a1 = __ldg(o + 1), a2 = __ldg(o + 2), a3 = __ldg(o + 3);
+    const float4 b0 = __ldg(o + 4), b1 = __ldg(o + 5), b2 = __ldg(o + 6), b3 = __ldg(o + 7);
+    dl = obb_dist(a0, a1, a2, a3, qf, 2.f * mbox);
+    dr = obb_dist(b0, b1, b2, b3, qf, 2.f * mbox);
+    l = __float_as_int(a3.w);
+    r = __float_as_int(b3.w);
+  } else {
+    const NodeRec rec = load_node(b.node, node);
+    dl = sqrtf(box_d2f(rec.lb, qf)) - mbox;
+    dr = sqrtf(box_d2f(rec.rb, qf)) - mbox;
+    l = rec.l;
+    r = rec.r;
+  }
 }
 
 // Exact FP64 evaluation of one leaf against the running best.  MODE 0: closest point (squared
@@ -517,7 +784,7 @@ __device__ __forceinline__ void add_cand(const BvhDev &b, const double q[3], int
 
 // Per-thread depth-first traversal with at most `budget` pops.  Returns 0 when done, 1 on stack
 // overflow (result may be incomplete), 2 when the budget ran out (best is a valid upper bound).
-template <int MODE>
+template <int MODE, bool OB>
 __device__ int thread_traverse(const BvhDev &b, const double q[3], double &best, int32_t &bf, double bc[3],
                                int budget) {
   const int n = b.n;
@@ -557,12 +824,12 @@ __device__ int thread_traverse(const BvhDev &b, const double q[3], double &best,
       continue;
     }
     if (node >= n - 1) { ok = false; continue; }
-    const NodeRec r = load_node(b.node, node);
-    if (r.l >= n - 1 || r.r >= n - 1 || ~r.l >= n || ~r.r >= n) { ok = false; continue; }
-    const float dl = sqrtf(box_d2f(r.lb, qf)) - mbox;
-    const float dr = sqrtf(box_d2f(r.rb, qf)) - mbox;
+    int32_t cl_, cr_;
+    float dl, dr;
+    node_children<OB>(b, node, qf, mbox, cl_, cr_, dl, dr);
+    if (cl_ >= n - 1 || cr_ >= n - 1 || ~cl_ >= n || ~cr_ >= n) { ok = false; continue; }
     const bool lnear = dl <= dr;
-    const int32_t nearc = lnear ? r.l : r.r, farc = lnear ? r.r : r.l;
+    const int32_t nearc = lnear ? cl_ : cr_, farc = lnear ? cr_ : cl_;
     const float dn = lnear ? dl : dr, df = lnear ? dr : dl;
     if (df <= ub) { if (sp < kStack) { sn[sp] = farc; sd[sp] = df; sp++; } else ok = false; }
     if (dn <= ub) { if (sp < kStack) { sn[sp] = nearc; sd[sp] = dn; sp++; } else ok = false; }
@@ -622,7 +889,7 @@ __device__ __forceinline__ void seed_bound(const BvhDev &b, const int32_t *seed,
 // when more than kQCand candidates remain after compaction; ub stays a valid bound in every case.
 constexpr int kTStack = 32;
 constexpr int kBlockThreads = 128;
-template <int MODE>
+template <int MODE, bool OB>
 __device__ int thread_collect(const BvhDev &b, const double q[3], float &ub, int32_t *cl, float *cb, int &nc,
                               int budget, int32_t *sn, float *sd) {
   const int n = b.n;
@@ -666,12 +933,12 @@ __device__ int thread_collect(const BvhDev &b, const double q[3], float &ub, int
       continue;
     }
     if (node >= n - 1) { ok = false; continue; }
-    const NodeRec r = load_node(b.node, node);
-    if (r.l >= n - 1 || r.r >= n - 1 || ~r.l >= n || ~r.r >= n) { ok = false; continue; }
-    const float dl = sqrtf(box_d2f(r.lb, qf)) - mbox;
-    const float dr = sqrtf(box_d2f(r.rb, qf)) - mbox;
+    int32_t cl_, cr_;
+    float dl, dr;
+    node_children<OB>(b, node, qf, mbox, cl_, cr_, dl, dr);
+    if (cl_ >= n - 1 || cr_ >= n - 1 || ~cl_ >= n || ~cr_ >= n) { ok = false; continue; }
     const bool lnear = dl <= dr;
-    const int32_t nearc = lnear ? r.l : r.r, farc = lnear ? r.r : r.l;
+    const int32_t nearc = lnear ? cl_ : cr_, farc = lnear ? cr_ : cl_;
     const float dn = lnear ? dl : dr, df = lnear ? dr : dl;
     if (df <= ub) { if (sp < kTStack) { sn[sp * S] = farc; sd[sp * S] = df; sp++; } else return 1; }
     if (dn <= ub) { if (sp < kTStack) { sn[sp * S] = nearc; sd[sp * S] = dn; sp++; } else return 1; }
@@ -731,7 +998,7 @@ __device__ __forceinline__ int group_compact(int32_t *cl, float *cb, int nc, flo
 // the group's lanes, so the two groups of a warp may run different numbers of steps.  Returns
 // 0 when done (cl/cb compacted to lo <= ub), 1 on frontier overflow or a malformed tree,
 // 3 when more than kWarpCand candidates remain after compaction.
-template <int MODE>
+template <int MODE, bool OB>
 __device__ int group_collect(const BvhDev &b, const double q[3], int32_t *sn, float *sd, int32_t *cl, float *cb,
                              float &ub, int &nc) {
   const unsigned gm = group_mask();
@@ -767,16 +1034,16 @@ __device__ int group_collect(const BvhDev &b, const double q[3], int32_t *sn, fl
           ok = false;
         }
       } else if (node < n - 1) {
-        const NodeRec r = load_node(b.node, node);
-        if (r.l >= n - 1 || r.r >= n - 1 || ~r.l >= n || ~r.r >= n) {
+        int32_t cl_, cr_;
+        float dl, dr;
+        node_children<OB>(b, node, qf, mbox, cl_, cr_, dl, dr);
+        if (cl_ >= n - 1 || cr_ >= n - 1 || ~cl_ >= n || ~cr_ >= n) {
           ok = false;
         } else {
-          const float dl = sqrtf(box_d2f(r.lb, qf)) - mbox;
-          const float dr = sqrtf(box_d2f(r.rb, qf)) - mbox;
           const bool lnear = dl <= dr;
           const float dn = lnear ? dl : dr, df = lnear ? dr : dl;
-          if (df <= ub) { push[np] = lnear ? r.r : r.l; pd[np] = df; np++; }
-          if (dn <= ub) { push[np] = lnear ? r.l : r.r; pd[np] = dn; np++; }
+          if (df <= ub) { push[np] = lnear ? cr_ : cl_; pd[np] = df; np++; }
+          if (dn <= ub) { push[np] = lnear ? cl_ : cr_; pd[np] = dn; np++; }
         }
       } else {
         ok = false;
@@ -820,7 +1087,7 @@ __device__ int group_collect(const BvhDev &b, const double q[3], int32_t *sn, fl
   return group_ballot(!ok) ? 1 : 0;
 }
 
-constexpr int kThreadBudget = 64;  // default pops per query before handing over to the warp pass
+constexpr int kThreadBudget = 96;  // pops per query before the warp pass when the caller gives none
 __device__ __forceinline__ unsigned groups_total() { return gridDim.x * (blockDim.x / kGroup); }
 __device__ __forceinline__ unsigned group_global() { return blockIdx.x * (blockDim.x / kGroup) + threadIdx.x / kGroup; }
 
@@ -902,7 +1169,8 @@ __global__ void __launch_bounds__(128) k_cand_eval(CandBuf c, const TargetDev *t
       c.x[e] = ndot(r, r);
     } else {
       EPFace fe;
-      ep_setup(P, fe);
+      if (SRC == 0 && tgt[m].EP) ep_load(tgt[m].EP + 16 * (int64_t)b.leaf_face[c.leaf[e]], P, fe);
+      else ep_setup(P, fe);
       double x = INFINITY;
       point_distance_ep(fe, q, x);
       c.x[e] = x;
@@ -1009,7 +1277,7 @@ __global__ void __launch_bounds__(kBlockThreads) k_project(ProjArgs p) {
     int st = 0;
     seed_bound<0>(t.bvh, p.seed, i, q, ub);
     if (t.bvh.n > 0)
-      st = thread_collect<0>(t.bvh, q, ub, cl, cb, nc, p.budget > 0 ? p.budget : kThreadBudget, &s_sn[0][threadIdx.x],
+      st = thread_collect<0, true>(t.bvh, q, ub, cl, cb, nc, p.budget > 0 ? p.budget : kThreadBudget, &s_sn[0][threadIdx.x],
                              &s_sd[0][threadIdx.x]);
     if (st != 0) {
       // over budget, stack or candidate list: the cooperative pass restarts the query from the
@@ -1037,7 +1305,7 @@ __global__ void __launch_bounds__(128, 8) k_project_warp(ProjArgs p) {
     proj_entry(p, md, i, q);
     float ub = (float)p.ovf.best[i];
     int nc = 0;
-    const int st = group_collect<0>(p.tgt[m].bvh, q, sn[g], sd[g], scl[g], scb[g], ub, nc);
+    const int st = group_collect<0, true>(p.tgt[m].bvh, q, sn[g], sd[g], scl[g], scb[g], ub, nc);
     if (st != 0) {  // frontier or candidate overflow: the exact per-thread search
       if (gl == 0) push_fallback(p.cand, i, m);
     } else if (!store_cands_query(p.cand, i, m, q, scl[g], nc) && gl == 0) {
@@ -1091,7 +1359,7 @@ __global__ void __launch_bounds__(128) k_project_fallback(ProjArgs p) {
     const int64_t e = proj_entry(p, md, i, q);
     double best = INFINITY, c[3] = {0, 0, 0};
     int32_t f = -1;
-    if (t.bvh.n > 0 && thread_traverse<0>(t.bvh, q, best, f, c, 1 << 30) != 0) atomicOr(&p.sc[m].status, 8);
+    if (t.bvh.n > 0 && thread_traverse<0, true>(t.bvh, q, best, f, c, 1 << 30) != 0) atomicOr(&p.sc[m].status, 8);
     write_tangent(p, t, e, f, c);
   }
 }
@@ -1104,7 +1372,7 @@ __global__ void __launch_bounds__(128) k_signed_distance(TargetDev t, int64_t np
   const double q[3] = {P[3 * i], P[3 * i + 1], P[3 * i + 2]};
   double best = INFINITY, c[3] = {0, 0, 0}, n[3] = {0, 0, 0};
   int32_t f = -1;
-  if (t.bvh.n > 0 && thread_traverse<0>(t.bvh, q, best, f, c, 1 << 30) != 0) atomicOr(status, 8);
+  if (t.bvh.n > 0 && thread_traverse<0, true>(t.bvh, q, best, f, c, 1 << 30) != 0) atomicOr(status, 8);
   double s = 1;
   if (f >= 0) {
     pseudonormal(t, f, c, n);
@@ -1233,7 +1501,7 @@ __global__ void __launch_bounds__(kBlockThreads) k_haus_side(HausArgs h) {
     seed_bound<1>(*b, h.seed, i, q, ub);
     int st = 0;
     if (b->n > 0)
-      st = thread_collect<1>(*b, q, ub, cl, cb, nc, h.budget > 0 ? h.budget : kThreadBudget, &s_sn[0][threadIdx.x],
+      st = thread_collect<1, SIDE == 1>(*b, q, ub, cl, cb, nc, h.budget > 0 ? h.budget : kThreadBudget, &s_sn[0][threadIdx.x],
                              &s_sd[0][threadIdx.x]);
     if (st != 0) {
       // over budget, stack or candidate list: the cooperative pass restarts the query from the
@@ -1262,7 +1530,7 @@ __global__ void __launch_bounds__(128, 8) k_haus_warp(HausArgs h) {
     haus_query<SIDE>(h, i, m, q, b);
     float ub = (float)h.ovf.best[i];
     int nc = 0;
-    const int st = group_collect<1>(*b, q, sn[g], sd[g], scl[g], scb[g], ub, nc);
+    const int st = group_collect<1, SIDE == 1>(*b, q, sn[g], sd[g], scl[g], scb[g], ub, nc);
     if (st != 0) {  // frontier or candidate overflow: the exact per-thread search
       if (gl == 0) push_fallback(h.cand, i, m);
     } else if (!store_cands_query(h.cand, i, m, q, scl[g], nc) && gl == 0) {
@@ -1307,7 +1575,7 @@ __global__ void __launch_bounds__(128) k_haus_fallback(HausArgs h) {
     double dist = h.hm[m].diag;
     int32_t fd = -1;
     double cd[3];
-    if (b->n > 0 && thread_traverse<1>(*b, q, dist, fd, cd, 1 << 30) != 0) atomicOr(&h.sc[m].status, 8);
+    if (b->n > 0 && thread_traverse<1, SIDE == 1>(*b, q, dist, fd, cd, 1 << 30) != 0) atomicOr(&h.sc[m].status, 8);
     h.dist[i] = dist;
   }
 }
@@ -1357,7 +1625,7 @@ __global__ void __launch_bounds__(128) k_ep_points(BvhDev b, const double *P, co
   double d = upper;
   int32_t fd = -1;
   double cd[3];
-  if (b.n > 0 && thread_traverse<1>(b, q, d, fd, cd, 1 << 30) != 0) atomicOr(status, 8);
+  if (b.n > 0 && thread_traverse<1, false>(b, q, d, fd, cd, 1 << 30) != 0) atomicOr(status, 8);
   dist[i] = d;
 }
 
@@ -1407,6 +1675,9 @@ void launch_ep_points(const BvhDev &b, const double *P, const int64_t *ids, int6
 void launch_maxmean(const double *dist, int64_t n, double upper, double *out3, cudaStream_t st) {
   k_maxmean<<<1, 1024, 0, st>>>(dist, n, upper, out3);
 }
+void launch_ep_faces(const double *tri, int64_t nf, double *EP, cudaStream_t st) {
+  if (nf > 0) k_ep_faces<<<(unsigned)((nf + 127) / 128), 128, 0, st>>>(tri, nf, EP);
+}
 void launch_fa_haus_flag(MeshScalars *sc, const HausMesh *hm, int n, cudaStream_t st) {
   k_fa_haus_flag<<<(n + 127) / 128, 128, 0, st>>>(sc, hm, n);
 }
@@ -1416,8 +1687,14 @@ void bvh_morton(const BvhDev &b, const double lo[3], const double hi[3], unsigne
   if (b.n > 0) k_morton<<<(b.n + 255) / 256, 256, 0, st>>>(b, lo[0], lo[1], lo[2], inv[0], inv[1], inv[2], keys);
 }
 void bvh_karras(int n, const unsigned long long *keys, int32_t *child, int32_t *parent, int32_t *leaf_face,
-                cudaStream_t st) {
-  if (n > 0) k_karras<<<(n + 255) / 256, 256, 0, st>>>(n, keys, child, parent, leaf_face);
+                cudaStream_t st, int32_t *range) {
+  if (n > 0) k_karras<<<(n + 255) / 256, 256, 0, st>>>(n, keys, child, parent, leaf_face, range);
+}
+void bvh_orient(const BvhDev &b, const int32_t *range, float4 *obb, float4 *onode, cudaStream_t st) {
+  if (b.n < 2) return;
+  k_obb_leaf<<<(b.n + 127) / 128, 128, 0, st>>>(b, obb);
+  k_obb_node<<<(b.n + 126) / 128, 128, 0, st>>>(b, range, obb);
+  k_opack<<<(b.n + 126) / 128, 128, 0, st>>>(b.n, b.child, obb, onode);
 }
 void bvh_refit_batch(const RefitDev *R, const Seg *seg, const MeshDesc *md, int64_t nblk, int threads,
                      cudaStream_t st) {

@@ -281,7 +281,8 @@ HEXOPT_API int hexopt_project_features(hexopt_ctx *ctx);
  * after a frontier or candidate overflow. */
 HEXOPT_API int hexopt_query_stats(hexopt_ctx *ctx, int64_t *warp_queries, int64_t *candidates, int64_t *fallbacks);
 /* Per-thread traversal budget of the BVH queries: node pops a query may take alone before the
- * group-cooperative pass takes it over (0 = the default, 64).  Results do not depend on it. */
+ * group-cooperative pass takes it over (0 = the defaults: 128 for the projection, 96 for the
+ * Hausdorff sides).  Results do not depend on it. */
 HEXOPT_API int hexopt_set_query_budget(hexopt_ctx *ctx, int pops);
 
 
