@@ -68,6 +68,14 @@ struct KindTable {
   int64_t nblk = 0;
 };
 
+// One set of BVH query buffers: the overflow list of the cooperative pass, per-sample distances,
+// the batched exact evaluation's candidate lists and the fallback list.
+struct QueryBufs {
+  DBuf ovf_item, ovf_mesh, ovf_count, ovf_best, ovf_face, ovf_pt, hdist;
+  DBuf cand_leaf, cand_qi, cand_x, cand_d, cand_count, q_off, q_cnt, qpos, q_mesh, fb_count, fb_item, fb_mesh;
+  int64_t cand_cap = 0;
+};
+
 struct StaticBvh {  // device LBVH over a fixed triangle set
   DBuf child, parent, box, leaf_face, tri, counters, node, leafd, onode;
   int32_t n = 0;
@@ -158,10 +166,9 @@ struct hexopt_ctx {
   std::vector<SurfaceHost> surf;
   DBuf tgt_d, surf_d, refit_d, hm_d, tgt_vs_d, surf_vs_d;
   int64_t n_surf_faces = 0;  // surface faces of the batch (items of K_SURFF)
-  DBuf ovf_item, ovf_mesh, ovf_count, ovf_best, ovf_face, ovf_pt, hdist;
-  // batched exact evaluation of the BVH queries (shared by projection and both Hausdorff sides)
-  DBuf cand_leaf, cand_qi, cand_x, cand_d, cand_count, q_off, q_cnt, qpos, q_mesh, fb_count, fb_item, fb_mesh;
-  int64_t cand_cap = 0;
+  // BVH query buffers, two sets: set 0 serves the projection and Hausdorff side 1, set 1 Hausdorff
+  // side 0, so that the two sides run at the same time
+  QueryBufs qb[2];
   DBuf qseed;           // previous winning leaf per query: projection, Hausdorff side 0, side 1
   int64_t qseed_n = 0;  // items per region of qseed
   std::vector<int64_t> tgt_vs_cnt, surf_vs_cnt;
@@ -184,6 +191,13 @@ struct hexopt_ctx {
   cudaStream_t ust = nullptr, dst = nullptr;
   cudaEvent_t in_ready = nullptr, in_free = nullptr, out_ready = nullptr, out_done = nullptr;
   DBuf in_stage, out_stage;
+  // the end of a step forks three ways (Hausdorff side 1 on st, side 0 and the SJ check on their
+  // own streams) and joins before the Hausdorff combine; each branch reduces into its own region
+  // of the partials and counters (region 0: the step's kernels and the SJ check, 1: side 1 and
+  // the bbox, 2: side 0)
+  cudaStream_t hs0 = nullptr, hsj = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_bbox = nullptr, ev_side0 = nullptr, ev_sj = nullptr;
+  int64_t part_region = 0;  // doubles per partials region
 };
 
 namespace {
@@ -351,7 +365,8 @@ int rebuild_tables(hexopt_ctx *ctx) {
     maxblk = std::max(maxblk, ctx->kind[k].nblk);
     CK(upload(ctx->kind[k].dev, ctx->kind[k].segs.data(), ctx->kind[k].segs.size(), ctx->st));
   }
-  CK(ctx->partials.ensure(sizeof(double) * (size_t)(maxblk + 1) * kMaxCand));
+  ctx->part_region = (maxblk + 1) * kMaxCand;
+  CK(ctx->partials.ensure(sizeof(double) * (size_t)ctx->part_region * 3));
   CK(upload(ctx->md_d, ctx->md.data(), ctx->md.size(), ctx->st));
   return ensure_query_buffers(ctx);
 }
@@ -671,68 +686,70 @@ int ensure_query_buffers(hexopt_ctx *ctx) {
     for (int m = 0; m < ctx->n_meshes; m++) tot += ctx->md[m].kcount[k];
     n = std::max(n, tot);
   }
-  CK(ctx->ovf_item.ensure(sizeof(int64_t) * n));
-  CK(ctx->ovf_mesh.ensure(sizeof(int32_t) * n));
-  CK(ctx->ovf_count.ensure(sizeof(unsigned)));
-  CK(ctx->ovf_best.ensure(sizeof(double) * n));
-  CK(ctx->ovf_face.ensure(sizeof(int32_t) * n));
-  CK(ctx->ovf_pt.ensure(sizeof(double) * 3 * n));
-  CK(ctx->hdist.ensure(sizeof(double) * n));
   CK(ctx->qseed.ensure(sizeof(int32_t) * 3 * n));
   CK(cudaMemsetAsync(ctx->qseed.p, 0xFF, sizeof(int32_t) * 3 * n, ctx->st));  // -1: no seed yet
   ctx->qseed_n = n;
   // up to kQueryCandidates recorded candidates per query on average (a query over its share goes
   // to the exact fallback)
   constexpr int64_t kQueryCandidates = 16;
-  ctx->cand_cap = kQueryCandidates * n;
-  CK(ctx->cand_leaf.ensure(sizeof(int32_t) * ctx->cand_cap));
-  CK(ctx->cand_qi.ensure(sizeof(int32_t) * ctx->cand_cap));
-  CK(ctx->cand_x.ensure(sizeof(double) * ctx->cand_cap));
-  CK(ctx->cand_d.ensure(sizeof(double) * ctx->cand_cap));
-  CK(ctx->cand_count.ensure(sizeof(unsigned)));
-  CK(ctx->q_off.ensure(sizeof(int32_t) * n));
-  CK(ctx->q_cnt.ensure(sizeof(int32_t) * n));
-  CK(ctx->qpos.ensure(sizeof(double) * 3 * n));
-  CK(ctx->q_mesh.ensure(sizeof(int32_t) * n));
-  CK(ctx->fb_count.ensure(sizeof(unsigned)));
-  CK(ctx->fb_item.ensure(sizeof(int64_t) * n));
-  CK(ctx->fb_mesh.ensure(sizeof(int32_t) * n));
+  for (QueryBufs &q : ctx->qb) {
+    CK(q.ovf_item.ensure(sizeof(int64_t) * n));
+    CK(q.ovf_mesh.ensure(sizeof(int32_t) * n));
+    CK(q.ovf_count.ensure(sizeof(unsigned)));
+    CK(q.ovf_best.ensure(sizeof(double) * n));
+    CK(q.ovf_face.ensure(sizeof(int32_t) * n));
+    CK(q.ovf_pt.ensure(sizeof(double) * 3 * n));
+    CK(q.hdist.ensure(sizeof(double) * n));
+    q.cand_cap = kQueryCandidates * n;
+    CK(q.cand_leaf.ensure(sizeof(int32_t) * q.cand_cap));
+    CK(q.cand_qi.ensure(sizeof(int32_t) * q.cand_cap));
+    CK(q.cand_x.ensure(sizeof(double) * q.cand_cap));
+    CK(q.cand_d.ensure(sizeof(double) * q.cand_cap));
+    CK(q.cand_count.ensure(sizeof(unsigned)));
+    CK(q.q_off.ensure(sizeof(int32_t) * n));
+    CK(q.q_cnt.ensure(sizeof(int32_t) * n));
+    CK(q.qpos.ensure(sizeof(double) * 3 * n));
+    CK(q.q_mesh.ensure(sizeof(int32_t) * n));
+    CK(q.fb_count.ensure(sizeof(unsigned)));
+    CK(q.fb_item.ensure(sizeof(int64_t) * n));
+    CK(q.fb_mesh.ensure(sizeof(int32_t) * n));
+  }
   return HEXOPT_OK;
 }
 
-CandBuf make_cand(hexopt_ctx *c) {
+CandBuf make_cand(const QueryBufs &q) {
   CandBuf b{};
-  b.leaf = c->cand_leaf.as<int32_t>();
-  b.qi = c->cand_qi.as<int32_t>();
-  b.x = c->cand_x.as<double>();
-  b.d = c->cand_d.as<double>();
-  b.count = c->cand_count.as<unsigned>();
-  b.cap = c->cand_cap;
-  b.q_off = c->q_off.as<int32_t>();
-  b.q_cnt = c->q_cnt.as<int32_t>();
-  b.qpos = c->qpos.as<double>();
-  b.q_mesh = c->q_mesh.as<int32_t>();
-  b.fb_count = c->fb_count.as<unsigned>();
-  b.fb_item = c->fb_item.as<int64_t>();
-  b.fb_mesh = c->fb_mesh.as<int32_t>();
+  b.leaf = q.cand_leaf.as<int32_t>();
+  b.qi = q.cand_qi.as<int32_t>();
+  b.x = q.cand_x.as<double>();
+  b.d = q.cand_d.as<double>();
+  b.count = q.cand_count.as<unsigned>();
+  b.cap = q.cand_cap;
+  b.q_off = q.q_off.as<int32_t>();
+  b.q_cnt = q.q_cnt.as<int32_t>();
+  b.qpos = q.qpos.as<double>();
+  b.q_mesh = q.q_mesh.as<int32_t>();
+  b.fb_count = q.fb_count.as<unsigned>();
+  b.fb_item = q.fb_item.as<int64_t>();
+  b.fb_mesh = q.fb_mesh.as<int32_t>();
   return b;
 }
 
-Overflow make_ovf(hexopt_ctx *c) {
+Overflow make_ovf(const QueryBufs &q) {
   Overflow o{};
-  o.item = c->ovf_item.as<int64_t>();
-  o.mesh = c->ovf_mesh.as<int32_t>();
-  o.count = c->ovf_count.as<unsigned>();
-  o.best = c->ovf_best.as<double>();
-  o.face = c->ovf_face.as<int32_t>();
-  o.pt = c->ovf_pt.as<double>();
+  o.item = q.ovf_item.as<int64_t>();
+  o.mesh = q.ovf_mesh.as<int32_t>();
+  o.count = q.ovf_count.as<unsigned>();
+  o.best = q.ovf_best.as<double>();
+  o.face = q.ovf_face.as<int32_t>();
+  o.pt = q.ovf_pt.as<double>();
   return o;
 }
 
 ProjArgs make_proj(hexopt_ctx *c, int kind) {
   ProjArgs p{};
-  p.ovf = make_ovf(c);
-  p.cand = make_cand(c);
+  p.ovf = make_ovf(c->qb[0]);
+  p.cand = make_cand(c->qb[0]);
   p.seg = c->kind[kind].dev.as<Seg>();
   p.mesh = c->md_d.as<MeshDesc>();
   p.sc = c->sc_d.as<MeshScalars>();
@@ -748,9 +765,10 @@ ProjArgs make_proj(hexopt_ctx *c, int kind) {
 
 HausArgs make_haus(hexopt_ctx *c, int kind) {
   HausArgs h{};
-  h.ovf = make_ovf(c);
-  h.cand = make_cand(c);
-  h.dist = c->hdist.as<double>();
+  const int set = kind == K_TGTV ? 1 : 0, region = kind == K_TGTV ? 2 : 1;  // side 0: set 1, region 2
+  h.ovf = make_ovf(c->qb[set]);
+  h.cand = make_cand(c->qb[set]);
+  h.dist = c->qb[set].hdist.as<double>();
   h.seg = c->kind[kind].dev.as<Seg>();
   h.mesh = c->md_d.as<MeshDesc>();
   h.sc = c->sc_d.as<MeshScalars>();
@@ -760,8 +778,8 @@ HausArgs make_haus(hexopt_ctx *c, int kind) {
   h.X = c->X.as<double>();
   h.tgt_vs = c->tgt_vs_d.as<int64_t>();
   h.surf_vs = c->surf_vs_d.as<int64_t>();
-  h.partials = c->partials.as<double>();
-  h.counters = c->counters.as<unsigned>();
+  h.partials = c->partials.as<double>() + region * c->part_region;
+  h.counters = c->counters.as<unsigned>() + region * c->n_meshes;
   h.seed = c->qseed.as<int32_t>() + (kind == K_SURFV ? 2 : 1) * c->qseed_n;
   h.budget = c->query_budget > 0 ? c->query_budget : 96;  // side 0's long queries do better cooperatively
   return h;
@@ -780,17 +798,54 @@ int run_projection(hexopt_ctx *ctx) {
   return HEXOPT_OK;
 }
 
-int run_hausdorff(hexopt_ctx *ctx) {
+static cudaError_t ensure_side_streams(hexopt_ctx *ctx) {
+  if (ctx->hs0) return cudaSuccess;
+  cudaError_t e = cudaStreamCreateWithFlags(&ctx->hs0, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->hsj, cudaStreamNonBlocking);
+  for (cudaEvent_t *ev : {&ctx->ev_fork, &ctx->ev_bbox, &ctx->ev_side0, &ctx->ev_sj})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  return e;
+}
+
+// The scaled-Jacobian check of a step (fast FP32 screen in mixed mode, the bit-exact pass in FP64).
+static void launch_step_sj(hexopt_ctx *ctx, cudaStream_t s) {
+  KArgs a = make_args(ctx);
+  if (ctx->mixed) launch_sj_check(a, ctx->kind[K_HEX].nblk, s);
+  else launch_scaled_jacobian(a, ctx->kind[K_HEX].nblk, nullptr, ctx->HJs.as<double>(), s);
+  ctx->launches += 3;
+}
+
+// Both Hausdorff sides at the current positions, side 0 (with the refit of the hex-boundary trees
+// it searches) on a second stream, side 1 on the context's stream; with_sj also runs the step's
+// SJ check on a third.  The branches share only the bbox diagonal (written before either side
+// starts) and join before the two sides' results are combined.  Inside a capture the branches
+// become parallel graph branches.
+int run_hausdorff(hexopt_ctx *ctx, bool with_sj) {
+  CK(ensure_side_streams(ctx));
+  cudaStream_t st = ctx->st, s0 = ctx->hs0;
+  CK(cudaEventRecord(ctx->ev_fork, st));
+  if (with_sj) {
+    CK(cudaStreamWaitEvent(ctx->hsj, ctx->ev_fork, 0));
+    launch_step_sj(ctx, ctx->hsj);
+    CK(cudaEventRecord(ctx->ev_sj, ctx->hsj));
+  }
+  CK(cudaStreamWaitEvent(s0, ctx->ev_fork, 0));
   // refit every mesh's surface tree at the current positions, one launch for the batch
   if (ctx->n_surf_faces > 0) {
     bvh_refit_batch(ctx->refit_d.as<RefitDev>(), ctx->kind[K_SURFF].dev.as<Seg>(), ctx->md_d.as<MeshDesc>(),
-                    ctx->kind[K_SURFF].nblk, ctx->block[K_SURFF] * ctx->ipt[K_SURFF], ctx->st);
+                    ctx->kind[K_SURFF].nblk, ctx->block[K_SURFF] * ctx->ipt[K_SURFF], s0);
     ctx->launches += 1;
   }
-  launch_haus_bbox(make_haus(ctx, K_SURFV), ctx->kind[K_SURFV].nblk, ctx->st);
-  launch_haus_side(make_haus(ctx, K_TGTV), 0, ctx->kind[K_TGTV].nblk, ctx->st);
-  launch_haus_side(make_haus(ctx, K_SURFV), 1, ctx->kind[K_SURFV].nblk, ctx->st);
-  ctx->launches += 13;
+  launch_haus_bbox(make_haus(ctx, K_SURFV), ctx->kind[K_SURFV].nblk, st);
+  CK(cudaEventRecord(ctx->ev_bbox, st));
+  CK(cudaStreamWaitEvent(s0, ctx->ev_bbox, 0));
+  launch_haus_side(make_haus(ctx, K_TGTV), 0, ctx->kind[K_TGTV].nblk, s0);
+  CK(cudaEventRecord(ctx->ev_side0, s0));
+  launch_haus_side(make_haus(ctx, K_SURFV), 1, ctx->kind[K_SURFV].nblk, st);
+  CK(cudaStreamWaitEvent(st, ctx->ev_side0, 0));
+  if (with_sj) CK(cudaStreamWaitEvent(st, ctx->ev_sj, 0));
+  launch_haus_combine(ctx->hm_d.as<HausMesh>(), ctx->n_meshes, st);
+  ctx->launches += 14;
   CKL();
   return HEXOPT_OK;
 }
@@ -844,6 +899,12 @@ void hexopt_destroy(hexopt_ctx *ctx) {
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (cudaEvent_t e : {ctx->in_ready, ctx->in_free, ctx->out_ready, ctx->out_done})
     if (e) cudaEventDestroy(e);
+  if (ctx->hs0) cudaStreamSynchronize(ctx->hs0);
+  if (ctx->hsj) cudaStreamSynchronize(ctx->hsj);
+  for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_bbox, ctx->ev_side0, ctx->ev_sj})
+    if (e) cudaEventDestroy(e);
+  if (ctx->hs0) cudaStreamDestroy(ctx->hs0);
+  if (ctx->hsj) cudaStreamDestroy(ctx->hsj);
   if (ctx->ust) cudaStreamDestroy(ctx->ust);
   if (ctx->dst) cudaStreamDestroy(ctx->dst);
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -857,6 +918,8 @@ int hexopt_sync(hexopt_ctx *ctx) {
   CK(cudaStreamSynchronize(ctx->st));
   if (ctx->ust) CK(cudaStreamSynchronize(ctx->ust));
   if (ctx->dst) CK(cudaStreamSynchronize(ctx->dst));
+  if (ctx->hs0) CK(cudaStreamSynchronize(ctx->hs0));
+  if (ctx->hsj) CK(cudaStreamSynchronize(ctx->hsj));
   return HEXOPT_OK;
 }
 
@@ -989,8 +1052,8 @@ int hexopt_upload_meshes(hexopt_ctx *ctx, int n_meshes, const int64_t *nv, const
   ctx->has_ref_p8 = false;
   ctx->has_ref_tets = false;
   ctx->rest_fixed = false;
-  CK(ctx->counters.ensure(sizeof(unsigned) * n_meshes));
-  CK(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned) * n_meshes, ctx->st));
+  CK(ctx->counters.ensure(sizeof(unsigned) * 3 * n_meshes));  // three regions (see part_region)
+  CK(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned) * 3 * n_meshes, ctx->st));
   int rc = rebuild_tables(ctx);
   if (rc) return rc;
   CK(upload(ctx->sc_d, ctx->sc.data(), ctx->sc.size(), ctx->st));
@@ -1608,9 +1671,10 @@ int hexopt_query_stats(hexopt_ctx *ctx, int64_t *warp_queries, int64_t *candidat
   int rc = check_ctx(ctx);
   if (rc) return rc;
   unsigned w = 0, c = 0, f = 0;
-  if (ctx->ovf_count.p) CK(cudaMemcpyAsync(&w, ctx->ovf_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
-  if (ctx->cand_count.p) CK(cudaMemcpyAsync(&c, ctx->cand_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
-  if (ctx->fb_count.p) CK(cudaMemcpyAsync(&f, ctx->fb_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+  const QueryBufs &q = ctx->qb[0];  // the projection, or Hausdorff side 1
+  if (q.ovf_count.p) CK(cudaMemcpyAsync(&w, q.ovf_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+  if (q.cand_count.p) CK(cudaMemcpyAsync(&c, q.cand_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+  if (q.fb_count.p) CK(cudaMemcpyAsync(&f, q.fb_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
   if (warp_queries) *warp_queries = w;
   if (candidates) *candidates = c;
@@ -1693,7 +1757,7 @@ int hexopt_hausdorff_meshes(hexopt_ctx *ctx, double *diag, double *max_dist, dou
     rc = prepare_haus(ctx);
     if (rc) return rc;
   }
-  rc = run_hausdorff(ctx);
+  rc = run_hausdorff(ctx, false);
   if (rc) return rc;
   std::vector<HausMesh> hm(ctx->n_meshes);
   CK(cudaMemcpyAsync(hm.data(), ctx->hm_d.p, sizeof(HausMesh) * ctx->n_meshes, cudaMemcpyDeviceToHost, ctx->st));
@@ -1907,16 +1971,9 @@ static int fa_enqueue(hexopt_ctx *ctx, int do_hausdorff) {
   rc = dispatch_iteration(ctx, true);  // slim_precompute fused into the local step
   if (rc) return rc;
   launch_fa_schedule(ctx->sc_d.as<MeshScalars>(), ctx->n_meshes, ctx->lamda0, 1e16, ctx->st);
-  KArgs a = make_args(ctx);
-  if (ctx->mixed) {
-    launch_sj_check(a, ctx->kind[K_HEX].nblk, ctx->st);
-    ctx->launches += 3;
-  } else {
-    launch_scaled_jacobian(a, ctx->kind[K_HEX].nblk, nullptr, ctx->HJs.as<double>(), ctx->st);
-    ctx->launches += 3;
-  }
+  if (!do_hausdorff) launch_step_sj(ctx, ctx->st);
   if (do_hausdorff) {
-    rc = run_hausdorff(ctx);
+    rc = run_hausdorff(ctx, true);  // the SJ check runs beside the two sides
     if (rc) return rc;
     launch_fa_haus_flag(ctx->sc_d.as<MeshScalars>(), ctx->hm_d.as<HausMesh>(), ctx->n_meshes, ctx->st);
     ctx->launches++;

@@ -151,6 +151,8 @@ void launch_signed_distance(const TargetDev &t, int64_t np, const double *P, dou
 void launch_haus_bbox(const HausArgs &h, int64_t nblk, cudaStream_t st);
 // both passes of one Hausdorff side (per-sample distances into h.dist) and its reduction
 void launch_haus_side(const HausArgs &h, int side, int64_t nblk, cudaStream_t st);
+// after both sides: each mesh's Hausdorff max and mean from the two sides' results
+void launch_haus_combine(HausMesh *hm, int n, cudaStream_t st);
 void launch_ep_points(const BvhDev &b, const double *P, const int64_t *ids, int64_t n, double upper, double *dist,
                       int *status, cudaStream_t st);
 void launch_maxmean(const double *dist, int64_t n, double upper, double *out3, cudaStream_t st);

@@ -1606,10 +1606,6 @@ __global__ void __launch_bounds__(256) k_haus_reduce(HausArgs h) {
     if (threadIdx.x == 0) {
       hm.side_max[SIDE] = -m;
       hm.side_mean[SIDE] = s / c;
-      if (SIDE == 1) {
-        hm.max_dist = fmax(hm.side_max[0], hm.side_max[1]);
-        hm.ave_dist = fmax(hm.side_mean[1], hm.side_mean[0]);
-      }
       h.counters[sg.mesh] = 0;
     }
   }
@@ -1644,6 +1640,14 @@ __global__ void __launch_bounds__(1024) k_maxmean(const double *dist, int64_t n,
 }
 
 // Max_dis_satisified after a Hausdorff check (stop_criterior_satisfied, :4160-4176)
+// Both sides reduced (they may run concurrently): the mesh's Hausdorff max and mean.
+__global__ void k_haus_combine(HausMesh *hm, int n) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  hm[m].max_dist = fmax(hm[m].side_max[0], hm[m].side_max[1]);
+  hm[m].ave_dist = fmax(hm[m].side_mean[1], hm[m].side_mean[0]);
+}
+
 __global__ void k_fa_haus_flag(MeshScalars *sc, const HausMesh *hm, int n) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= n) return;
@@ -1677,6 +1681,9 @@ void launch_maxmean(const double *dist, int64_t n, double upper, double *out3, c
 }
 void launch_ep_faces(const double *tri, int64_t nf, double *EP, cudaStream_t st) {
   if (nf > 0) k_ep_faces<<<(unsigned)((nf + 127) / 128), 128, 0, st>>>(tri, nf, EP);
+}
+void launch_haus_combine(HausMesh *hm, int n, cudaStream_t st) {
+  if (n > 0) k_haus_combine<<<(n + 127) / 128, 128, 0, st>>>(hm, n);
 }
 void launch_fa_haus_flag(MeshScalars *sc, const HausMesh *hm, int n, cudaStream_t st) {
   k_fa_haus_flag<<<(n + 127) / 128, 128, 0, st>>>(sc, hm, n);

@@ -562,6 +562,10 @@ __global__ void __launch_bounds__(256) k_cg_start(KArgs a) {
   }
 }
 
+// Items whose loads a mixed-mode vector kernel issues together before using them: the plain loop
+// waits for each item's loads in turn.
+constexpr int kChunk = 2;
+
 // alpha = abs_new / (p . q)
 template <typename VT>
 __global__ void __launch_bounds__(256) k_cg_alpha(KArgs a) {
@@ -572,6 +576,28 @@ __global__ void __launch_bounds__(256) k_cg_alpha(KArgs a) {
   const VT *p = reinterpret_cast<const VT *>(a.p), *q = reinterpret_cast<const VT *>(a.q);
   double acc[1] = {0};
   SumAcc<VT> pq;  // mixed mode: compensated FP32 dot product
+  if constexpr (sizeof(VT) == 4) {
+    // kChunk items' loads issued together, then summed in the item order of the loop below (a
+    // curve entry as a vertex with zero y, z: adding 0 * 0 leaves the compensated sum unchanged)
+    const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
+    for (int64_t i0 = sg.begin + threadIdx.x; i0 < sg.end; i0 += kChunk * blockDim.x) {
+      V3<VT> pp[kChunk], qq[kChunk];
+#pragma unroll
+      for (int k = 0; k < kChunk; k++) {
+        const int64_t i = i0 + k * blockDim.x;
+        pp[k] = qq[k] = V3<VT>{VT(0), VT(0), VT(0)};
+        if (i < sg.end) {
+          const ItemRef it = item_ref(md, i);
+          if (!it.curve) { pp[k] = ld3(p, it.idx); qq[k] = ld3(q, it.idx); }
+          else { pp[k].x = pa[it.idx]; qq[k].x = qa[it.idx]; }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kChunk; k++) {
+        pq.add_prod(pp[k].x, qq[k].x); pq.add_prod(pp[k].y, qq[k].y); pq.add_prod(pp[k].z, qq[k].z);
+      }
+    }
+  } else
   for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
     const ItemRef it = item_ref(md, i);
     if (!it.curve) {
@@ -617,6 +643,60 @@ __global__ void __launch_bounds__(256) k_cg_update(KArgs a) {
   const VT alpha = VT(S.alpha);
   double acc[2] = {0, 0};
   SumAcc<VT> s_rr, s_rz;  // mixed mode: compensated FP32 dot products
+  if constexpr (sizeof(VT) == 4) {
+    // kChunk items' loads together, then the update and the sums in the loop's item order (a
+    // curve entry in the x lane, y and z zero; its r.r and r.z gain only 0 * 0 terms)
+    VT *r = reinterpret_cast<VT *>(a.r), *d = reinterpret_cast<VT *>(a.d);
+    const VT *p = reinterpret_cast<const VT *>(a.p), *q = reinterpret_cast<const VT *>(a.q);
+    const VT *invd = reinterpret_cast<const VT *>(a.invd);
+    VT *ra = reinterpret_cast<VT *>(a.ra), *da = reinterpret_cast<VT *>(a.da);
+    const VT *pa = reinterpret_cast<const VT *>(a.pa), *qa = reinterpret_cast<const VT *>(a.qa);
+    const VT *invda = reinterpret_cast<const VT *>(a.invda);
+    for (int64_t i0 = sg.begin + threadIdx.x; i0 < sg.end; i0 += kChunk * blockDim.x) {
+      V3<VT> pp[kChunk], qq[kChunk], id[kChunk], dd[kChunk], rr[kChunk];
+      int64_t ix[kChunk];
+      int kind[kChunk];  // 0 none, 1 vertex, 2 curve entry
+#pragma unroll
+      for (int k = 0; k < kChunk; k++) {
+        const int64_t i = i0 + k * blockDim.x;
+        const V3<VT> z{VT(0), VT(0), VT(0)};
+        pp[k] = qq[k] = id[k] = dd[k] = rr[k] = z;
+        kind[k] = 0;
+        ix[k] = 0;
+        if (i < sg.end) {
+          const ItemRef it = item_ref(md, i);
+          ix[k] = it.idx;
+          if (!it.curve) {
+            kind[k] = 1;
+            pp[k] = ld3(p, it.idx); qq[k] = ld3(q, it.idx); id[k] = ld3(invd, it.idx);
+            dd[k] = ld3(d, it.idx); rr[k] = ld3(r, it.idx);
+          } else {
+            kind[k] = 2;
+            pp[k].x = pa[it.idx]; qq[k].x = qa[it.idx]; id[k].x = invda[it.idx];
+            dd[k].x = da[it.idx]; rr[k].x = ra[it.idx];
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kChunk; k++) {
+        if (kind[k] == 0) continue;
+        V3<VT> de = dd[k], re = rr[k];
+        de.x += alpha * pp[k].x; de.y += alpha * pp[k].y; de.z += alpha * pp[k].z;
+        re.x -= alpha * qq[k].x; re.y -= alpha * qq[k].y; re.z -= alpha * qq[k].z;
+        if (kind[k] == 1) {
+          if (a.has_fixed && a.vfix[ix[k]]) re = V3<VT>{VT(0), VT(0), VT(0)};
+          st3(d, ix[k], de);
+          st3(r, ix[k], re);
+        } else {
+          da[ix[k]] = de.x;
+          ra[ix[k]] = re.x;
+          re.y = re.z = VT(0);
+        }
+        s_rr.add_prod(re.x, re.x); s_rr.add_prod(re.y, re.y); s_rr.add_prod(re.z, re.z);
+        s_rz.add_prod(re.x, id[k].x * re.x); s_rz.add_prod(re.y, id[k].y * re.y); s_rz.add_prod(re.z, id[k].z * re.z);
+      }
+    }
+  } else
   for (int64_t i = sg.begin + threadIdx.x; i < sg.end; i += blockDim.x) {
     const ItemRef it = item_ref(md, i);
     if (!it.curve) {
