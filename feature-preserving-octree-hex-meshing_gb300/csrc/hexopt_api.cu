@@ -197,6 +197,7 @@ struct hexopt_ctx {
   // the bbox, 2: side 0)
   cudaStream_t hs0 = nullptr, hsj = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_bbox = nullptr, ev_side0 = nullptr, ev_sj = nullptr;
+  cudaEvent_t ev_pfork = nullptr, ev_proj = nullptr;  // the projection beside the local step
   int64_t part_region = 0;  // doubles per partials region
 };
 
@@ -502,16 +503,31 @@ int run_precompute(hexopt_ctx *ctx) {
   return HEXOPT_OK;
 }
 
+int run_projection(hexopt_ctx *ctx, cudaStream_t s = nullptr);
+static cudaError_t ensure_side_streams(hexopt_ctx *ctx);
+
 template <typename ET, typename VT>
-int run_iteration(hexopt_ctx *ctx, bool pre) {
+int run_iteration(hexopt_ctx *ctx, bool pre, bool project) {
   KArgs a = make_args(ctx);
   cudaStream_t st = ctx->st;
+  if (project) {
+    // the feature projection (tangent planes and line targets for the soft terms) beside the
+    // local step, which reads only positions and writes only the elastic terms; joined before
+    // the soft terms are assembled
+    CK(ensure_side_streams(ctx));
+    CK(cudaEventRecord(ctx->ev_pfork, st));
+    CK(cudaStreamWaitEvent(ctx->hs0, ctx->ev_pfork, 0));
+    int rc = run_projection(ctx, ctx->hs0);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev_proj, ctx->hs0));
+  }
   const size_t nv4 = (size_t)ctx->NV * 4;
   CK(cudaMemsetAsync(ctx->b.p, 0, nv4 * sizeof(VT), st));
   CK(cudaMemsetAsync(ctx->diag.p, 0, nv4 * sizeof(VT), st));
   CK(cudaMemsetAsync(ctx->r.p, 0, nv4 * sizeof(VT), st));
   const int64_t hb = ctx->kind[K_HEX].nblk, vb = ctx->kind[K_VERT].nblk, cb = ctx->kind[K_CONS].nblk;
   launch_local<ET, VT>(a, hb, pre, st);
+  if (project) CK(cudaStreamWaitEvent(st, ctx->ev_proj, 0));
   launch_soft_rhs<VT>(a, cb, st);
   ctx->launches += 2;
   if (ctx->has_fixed) {  // q = L_ib x_b for the known-value solve's rhs norm
@@ -552,8 +568,8 @@ int run_iteration(hexopt_ctx *ctx, bool pre) {
 int dispatch_precompute(hexopt_ctx *ctx) {
   return ctx->mixed ? run_precompute<float, float>(ctx) : run_precompute<double, double>(ctx);
 }
-int dispatch_iteration(hexopt_ctx *ctx, bool pre = false) {
-  return ctx->mixed ? run_iteration<float, float>(ctx, pre) : run_iteration<double, double>(ctx, pre);
+int dispatch_iteration(hexopt_ctx *ctx, bool pre = false, bool project = false) {
+  return ctx->mixed ? run_iteration<float, float>(ctx, pre, project) : run_iteration<double, double>(ctx, pre, project);
 }
 
 // SLIMData::energy is the accepted total divided by mesh_area = sum of M over the tets
@@ -785,13 +801,14 @@ HausArgs make_haus(hexopt_ctx *c, int kind) {
   return h;
 }
 
-int run_projection(hexopt_ctx *ctx) {
+int run_projection(hexopt_ctx *ctx, cudaStream_t s) {
+  if (!s) s = ctx->st;
   if (ctx->NT) {
-    launch_project(make_proj(ctx, K_PROJ), ctx->kind[K_PROJ].nblk, ctx->st);
+    launch_project(make_proj(ctx, K_PROJ), ctx->kind[K_PROJ].nblk, s);
     ctx->launches += 5;
   }
   if (ctx->NL) {
-    launch_curve_project(make_proj(ctx, K_LINE), ctx->kind[K_LINE].nblk, ctx->st);
+    launch_curve_project(make_proj(ctx, K_LINE), ctx->kind[K_LINE].nblk, s);
     ctx->launches++;
   }
   CKL();
@@ -802,7 +819,7 @@ static cudaError_t ensure_side_streams(hexopt_ctx *ctx) {
   if (ctx->hs0) return cudaSuccess;
   cudaError_t e = cudaStreamCreateWithFlags(&ctx->hs0, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->hsj, cudaStreamNonBlocking);
-  for (cudaEvent_t *ev : {&ctx->ev_fork, &ctx->ev_bbox, &ctx->ev_side0, &ctx->ev_sj})
+  for (cudaEvent_t *ev : {&ctx->ev_fork, &ctx->ev_bbox, &ctx->ev_side0, &ctx->ev_sj, &ctx->ev_pfork, &ctx->ev_proj})
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   return e;
 }
@@ -901,7 +918,7 @@ void hexopt_destroy(hexopt_ctx *ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->hs0) cudaStreamSynchronize(ctx->hs0);
   if (ctx->hsj) cudaStreamSynchronize(ctx->hsj);
-  for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_bbox, ctx->ev_side0, ctx->ev_sj})
+  for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_bbox, ctx->ev_side0, ctx->ev_sj, ctx->ev_pfork, ctx->ev_proj})
     if (e) cudaEventDestroy(e);
   if (ctx->hs0) cudaStreamDestroy(ctx->hs0);
   if (ctx->hsj) cudaStreamDestroy(ctx->hsj);
@@ -1962,13 +1979,13 @@ static bool same_params(const hexopt_slim_params &a, const hexopt_slim_params &b
 }
 
 static int fa_enqueue(hexopt_ctx *ctx, int do_hausdorff) {
-  int rc = run_projection(ctx);
-  if (rc) return rc;
+  int rc = 0;
   if (ctx->rest_fixed && !ctx->has_ref_p8) {  // compute_referenceMesh(ts.UV, ...) of this step
     rc = build_ref_shapes(ctx);
     if (rc) return rc;
   }
-  rc = dispatch_iteration(ctx, true);  // slim_precompute fused into the local step
+  // the projection runs beside the local step (slim_precompute fused into it)
+  rc = dispatch_iteration(ctx, true, true);
   if (rc) return rc;
   launch_fa_schedule(ctx->sc_d.as<MeshScalars>(), ctx->n_meshes, ctx->lamda0, 1e16, ctx->st);
   if (!do_hausdorff) launch_step_sj(ctx, ctx->st);
