@@ -183,11 +183,12 @@ __device__ __forceinline__ void local_tet(const KArgs &a, int64_t h, int32_t gs,
 
 // Each corner tet scatters its right-hand-side, residual and diagonal contributions straight to
 // the vertex vectors (float atomics): holding 8 corners x 3 vectors per hex in registers would
-// halve the occupancy of this latency-bound kernel.  Mixed mode runs 5 blocks of 128 per SM
-// (96 registers, ~100 B of spills): more warps hide the FP32 SVD's latency (1.47 -> 1.20 ms at
-// 2.1M hexes).
+// halve the occupancy of this latency-bound kernel.  Mixed mode runs 9 blocks of 128 per SM
+// (56 registers, 72 B of spills; the shared-memory columns allow no tenth block): with the tets
+// as a run-time loop more warps hide the FP32 SVD's dependency chains, 1.19 ms at 5 blocks,
+// 1.10 at 6, 1.05 at 7, 1.01 at 8, 0.98 at 9 for 2.1M hexes.
 template <typename ET, bool PRE>
-__global__ void __launch_bounds__(kLocalThreads, sizeof(ET) == 4 ? 5 : 1) k_local(KArgs a) {
+__global__ void __launch_bounds__(kLocalThreads, sizeof(ET) == 4 ? 9 : 1) k_local(KArgs a) {
   __shared__ ET e12s[36][kLocalThreads];
   __shared__ uint32_t hvs[8][kLocalThreads];
   const Seg sg = a.hseg[blockIdx.x];
