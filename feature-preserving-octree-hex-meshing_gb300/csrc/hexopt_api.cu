@@ -196,6 +196,7 @@ struct hexopt_ctx {
   // of the partials and counters (region 0: the step's kernels and the SJ check, 1: side 1 and
   // the bbox, 2: side 0)
   cudaStream_t hs0 = nullptr, hsj = nullptr;
+  cudaStream_t lsb = nullptr;  // captures the body of the line search's WHILE node
   cudaEvent_t ev_fork = nullptr, ev_bbox = nullptr, ev_side0 = nullptr, ev_sj = nullptr;
   cudaEvent_t ev_pfork = nullptr, ev_proj = nullptr;  // the projection beside the local step
   int64_t part_region = 0;  // doubles per partials region
@@ -425,6 +426,7 @@ KArgs make_args(hexopt_ctx *c) {
   a.root_count = c->root_count.as<unsigned>();
   a.root_min = c->root_min.as<unsigned long long>();
   a.ls_active = c->root_count.as<unsigned>() + 1;
+  a.ls_round = c->root_count.as<unsigned>() + 2;
   a.n_meshes = c->n_meshes;
   return a;
 }
@@ -450,10 +452,10 @@ int alloc_vectors(hexopt_ctx *ctx) {
   const size_t nroot = (size_t)ctx->NH * 8;
   CK(ctx->root_list.ensure(nroot * sizeof(uint32_t)));
   CK(ctx->root_mesh.ensure(nroot * sizeof(int32_t)));
-  CK(ctx->root_count.ensure(2 * sizeof(unsigned)));  // [0] root-list length, [1] line searches open
+  CK(ctx->root_count.ensure(3 * sizeof(unsigned)));  // [0] root-list length, [1] line searches open, [2] round
   CK(ctx->root_min.ensure(sizeof(unsigned long long) * ctx->n_meshes));
   {
-    CK(cudaMemsetAsync(ctx->root_count.p, 0, 2 * sizeof(unsigned), ctx->st));
+    CK(cudaMemsetAsync(ctx->root_count.p, 0, 3 * sizeof(unsigned), ctx->st));
     std::vector<double> inf(ctx->n_meshes, INFINITY);
     CK(cudaMemcpyAsync(ctx->root_min.p, inf.data(), sizeof(double) * ctx->n_meshes, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
@@ -558,9 +560,13 @@ int run_iteration(hexopt_ctx *ctx, bool pre, bool project) {
     launch_ir_final(a, vb, st);
     ctx->launches += kLaunchesIrFinal;
   }
-  launch_line_search<ET, VT>(a, hb, vb, cb, st);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(st, &cs));
+  CK(ensure_side_streams(ctx));
+  CK((launch_line_search<ET, VT>(a, hb, vb, cb, st, ctx->lsb)));
   const int rounds = (kHalvings + 1 + ctx->params.ls_candidates - 1) / ctx->params.ls_candidates;
-  ctx->launches += 5 + 2 * rounds;
+  // captured: the rounds are a WHILE node, counted here as one iteration (3 kernels)
+  ctx->launches += cs == cudaStreamCaptureStatusActive ? 5 + 3 : 5 + 2 * rounds;
   CKL();
   return HEXOPT_OK;
 }
@@ -819,6 +825,7 @@ static cudaError_t ensure_side_streams(hexopt_ctx *ctx) {
   if (ctx->hs0) return cudaSuccess;
   cudaError_t e = cudaStreamCreateWithFlags(&ctx->hs0, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->hsj, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->lsb, cudaStreamNonBlocking);
   for (cudaEvent_t *ev : {&ctx->ev_fork, &ctx->ev_bbox, &ctx->ev_side0, &ctx->ev_sj, &ctx->ev_pfork, &ctx->ev_proj})
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   return e;
@@ -922,6 +929,7 @@ void hexopt_destroy(hexopt_ctx *ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->hs0) cudaStreamDestroy(ctx->hs0);
   if (ctx->hsj) cudaStreamDestroy(ctx->hsj);
+  if (ctx->lsb) cudaStreamDestroy(ctx->lsb);
   if (ctx->ust) cudaStreamDestroy(ctx->ust);
   if (ctx->dst) cudaStreamDestroy(ctx->dst);
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -2022,7 +2030,10 @@ int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_r
       rc = fa_enqueue(ctx, do_hausdorff);
       cudaGraph_t gg = nullptr;
       cudaError_t e = cudaStreamEndCapture(ctx->st, &gg);
-      if (rc) return rc;
+      if (rc) {  // a failed capture is discarded, never launched
+        if (gg) cudaGraphDestroy(gg);
+        return rc;
+      }
       if (e != cudaSuccess) return fail(ctx, HEXOPT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
       g = gg;
       CK(cudaGraphInstantiate(&ctx->graph_exec, g, 0));

@@ -66,7 +66,10 @@ struct KArgs {
   unsigned long long *root_min;
   // meshes whose line search has not accepted a step yet (later candidate passes exit when 0)
   unsigned *ls_active;
+  // the line-search round of a graph's WHILE loop (passes launched with round kRoundFromDevice)
+  unsigned *ls_round;
 };
+constexpr int kRoundFromDevice = -2;
 
 template <typename ET, typename VT> void launch_precompute(const KArgs &a, int64_t nblk, cudaStream_t st);
 // fused local step; pre = also take the volume snapshot (slim_precompute) at the current X
@@ -93,7 +96,11 @@ void launch_glue_schedule(MeshScalars *sc, int n, int before, int iter, cudaStre
 // After the last PCG iteration: the search direction d = fl32(dd + d) (curve entries likewise).
 void launch_ir_final(const KArgs &a, int64_t vblk, cudaStream_t st);
 template <typename ET, typename VT> void launch_ls_energy_pass(const KArgs &a, int64_t hblk, cudaStream_t st);
-template <typename ET, typename VT> void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st);
+// body: with st capturing into a graph, a second stream that is not; the candidate rounds then
+// become a WHILE node that stops once every mesh has accepted (otherwise fixed rounds that no-op)
+template <typename ET, typename VT>
+cudaError_t launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st,
+                               cudaStream_t body = nullptr);
 
 // Launches per call of the launchers above (for the launch count).
 constexpr int kLaunchesCgIter = 4;  // element + soft SpMV, alpha, update, direction

@@ -95,27 +95,77 @@ void launch_glue_schedule(MeshScalars *sc, int n, int before, int iter, cudaStre
 void launch_ir_final(const KArgs &a, int64_t vblk, cudaStream_t st) {
   k_ir_final<<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
 }
+// One round of candidate passes: the elastic energies, then the soft energies whose last block
+// takes the round's decision (round = kRoundFromDevice: the round counter on the device).
 template <typename ET, typename VT>
-void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st) {
+static void launch_ls_round(const KArgs &a, int r, int64_t hblk, int64_t cblk, cudaStream_t st) {
+  switch (a.ls_cand) {
+    case 1: launch_ls_energy_nc<ET, VT, 1>(a, r, hblk, st); break;
+    case 2: launch_ls_energy_nc<ET, VT, 2>(a, r, hblk, st); break;
+    case 3: launch_ls_energy_nc<ET, VT, 3>(a, r, hblk, st); break;
+    case 4: launch_ls_energy_nc<ET, VT, 4>(a, r, hblk, st); break;
+    case 5: launch_ls_energy_nc<ET, VT, 5>(a, r, hblk, st); break;
+    case 6: launch_ls_energy_nc<ET, VT, 6>(a, r, hblk, st); break;
+    case 7: launch_ls_energy_nc<ET, VT, 7>(a, r, hblk, st); break;
+    default: launch_ls_energy_nc<ET, VT, 8>(a, r, hblk, st); break;
+  }
+  k_ls_soft<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a, r);
+}
+
+// The end of a WHILE iteration: next round, and another iteration only while a mesh is still
+// searching and rounds remain (at most `rounds` iterations however the flags stand).
+static __global__ void k_ls_next(KArgs a, cudaGraphConditionalHandle h, int rounds) {
+  const unsigned r = *a.ls_round + 1;
+  *a.ls_round = r;
+  cudaGraphSetConditional(h, (*a.ls_active > 0 && (int)r < rounds) ? 1u : 0u);
+}
+
+template <typename ET, typename VT>
+cudaError_t launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st,
+                               cudaStream_t body) {
   k_ls_bound<ET, VT><<<(unsigned)hblk, a.hthreads, 0, st>>>(a);
   k_ls_roots<VT><<<152 * 4, 128, 0, st>>>(a);
-  k_ls_bound_finish<<<(unsigned)a.n_meshes, 128, 0, st>>>(a, a.n_meshes);
+  k_ls_bound_finish<<<(unsigned)a.n_meshes, 128, 0, st>>>(a, a.n_meshes);  // also round = 0
   k_ls_soft<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a, -1);
   const int rounds = (kHalvings + 1 + a.ls_cand - 1) / a.ls_cand;
-  for (int r = 0; r < rounds; r++) {
-    switch (a.ls_cand) {
-      case 1: launch_ls_energy_nc<ET, VT, 1>(a, r, hblk, st); break;
-      case 2: launch_ls_energy_nc<ET, VT, 2>(a, r, hblk, st); break;
-      case 3: launch_ls_energy_nc<ET, VT, 3>(a, r, hblk, st); break;
-      case 4: launch_ls_energy_nc<ET, VT, 4>(a, r, hblk, st); break;
-      case 5: launch_ls_energy_nc<ET, VT, 5>(a, r, hblk, st); break;
-      case 6: launch_ls_energy_nc<ET, VT, 6>(a, r, hblk, st); break;
-      case 7: launch_ls_energy_nc<ET, VT, 7>(a, r, hblk, st); break;
-      default: launch_ls_energy_nc<ET, VT, 8>(a, r, hblk, st); break;
-    }
-    k_ls_soft<VT><<<(unsigned)cblk, a.vthreads, 0, st>>>(a, r);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  if (body && cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) == cudaSuccess &&
+      cs == cudaStreamCaptureStatusActive) {
+    // a WHILE node whose body runs one round: the graph stops at the first round that leaves no
+    // mesh searching, instead of launching rounds - 1 passes that only check a flag.  Any
+    // failure from here on is returned, so that the caller discards the capture: a body without
+    // its k_ls_next would never clear the condition.
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &np);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t bg = np.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(body, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    launch_ls_round<ET, VT>(a, kRoundFromDevice, hblk, cblk, body);
+    k_ls_next<<<1, 1, 0, body>>>(a, h, rounds);
+    const cudaError_t le = cudaGetLastError();
+    e = cudaStreamEndCapture(body, &bg);
+    if (le != cudaSuccess) return le;
+    if (e != cudaSuccess) return e;
+    k_ls_apply<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+    return cudaGetLastError();
   }
+  for (int r = 0; r < rounds; r++) launch_ls_round<ET, VT>(a, r, hblk, cblk, st);
   k_ls_apply<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
+  return cudaSuccess;
 }
 
 // explicit instantiations for the two modes
@@ -129,7 +179,7 @@ void launch_line_search(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk
   template void launch_cg_dir<VT>(const KArgs &, int64_t, cudaStream_t);                         \
   template void launch_cg_vec<VT>(const KArgs &, int64_t, int64_t, cudaStream_t);                \
   template void launch_fixed_pre<VT>(const KArgs &, int64_t, int64_t, cudaStream_t);             \
-  template void launch_line_search<ET, VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t); \
+  template cudaError_t launch_line_search<ET, VT>(const KArgs &, int64_t, int64_t, int64_t, cudaStream_t, cudaStream_t); \
   template void launch_ls_energy_pass<ET, VT>(const KArgs &, int64_t, cudaStream_t);
 HX_INST(double, double)
 HX_INST(float, float)

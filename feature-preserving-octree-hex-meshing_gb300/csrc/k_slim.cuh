@@ -1380,7 +1380,7 @@ static __global__ void __launch_bounds__(128) k_ls_bound_finish(KArgs a, int n_m
   double g[1];
   gather_partials_sums<1>(a.partials, md.hblk0, md.nhblk, 1, g, smem);
   if (threadIdx.x == 0) {
-    if (m == 0) { *a.root_count = 0; *a.ls_active = (unsigned)n_meshes; }
+    if (m == 0) { *a.root_count = 0; *a.ls_active = (unsigned)n_meshes; *a.ls_round = 0; }
     MeshScalars &S = a.sc[m];
     S.old_eq = g[0];
     S.ls_done = 0;
@@ -1472,6 +1472,7 @@ template <typename ET, typename VT, int NC>
 __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t nseg) {
   __shared__ double smem[NC][32];
   if (*a.ls_active == 0) return;  // every mesh has accepted its step
+  if (round == kRoundFromDevice) round = (int)*a.ls_round;
   for (int64_t sb = blockIdx.x; sb < nseg; sb += gridDim.x) {
     const Seg sg = a.hseg[sb];
     MeshScalars &S = a.sc[sg.mesh];
@@ -1548,6 +1549,7 @@ __global__ void __launch_bounds__(128) k_ls_energy(KArgs a, int round, int64_t n
 template <typename VT>
 __global__ void __launch_bounds__(256) k_ls_soft(KArgs a, int round) {
   const Seg sg = a.cseg[blockIdx.x];
+  if (round == kRoundFromDevice) round = (int)*a.ls_round;
   if (round >= 0 && *a.ls_active == 0) return;  // every mesh has accepted its step
   MeshScalars &S = a.sc[sg.mesh];
   if (round >= 0 && S.ls_done) return;
