@@ -214,7 +214,11 @@ def run_ours(args):
     workloads.load(ctx, [p])
     ctx.fa_begin(lamda0=0.05, precision=precision, weight_opt=0.001)
     tune = ctx.autotune() if not args.no_autotune else None
-    ctx.use_graph(True)
+    # every later fa_begin keeps the tuned candidates per line-search pass (fa_begin takes the
+    # parameters it is given)
+    ls = dict(ls_candidates=tune["ls_candidates"]) if tune else {}
+    graph_mode = 2 if args.graph_fixed_rounds else True
+    ctx.use_graph(graph_mode)
     do_h = not args.no_hausdorff
     for _ in range(args.warmup):
         ctx.fa_step(hausdorff=do_h, report=False)
@@ -235,26 +239,32 @@ def run_ours(args):
     ms = max_over_ranks(tdist, ms)
     rep = ctx.fa_step(hausdorff=do_h)[0]  # report of the state after the timed steps
     value = ws * args.steps / (ms / 1e3)
-    # ---------------- e2e: host buffers in pinned memory; every step uploads its positions, steps
-    # and downloads the resulting positions through the C ABI's asynchronous transfers (copy
-    # stream, overlapping the previous / next step's computation); the stop event waits for the
-    # last download
+    # ---------------- e2e: the same optimisation from the same start, with the positions held in
+    # pinned host memory: every step uploads them, steps, downloads the result into the same host
+    # buffer and waits for it, so step k + 1's input is step k's output read back from the host
+    # (the transfers are on the critical path; nothing overlaps them).  W warm-up steps likewise
+    # (the graph is captured there), then K timed steps; the stop event waits for the last download
     import torch
-    Vin = torch.from_numpy(np.ascontiguousarray(p["V"])).pin_memory()
-    Vout = torch.empty((nv, 3), dtype=torch.float64).pin_memory()
-    vin, vout = Vin.numpy(), Vout.numpy()
-    ctx.fa_begin(lamda0=0.05, precision=precision, weight_opt=0.001)
-    ctx.fa_step(hausdorff=do_h, report=False)  # re-capture the graph outside the timed region
-    ctx.sync()
+    Vh = torch.from_numpy(np.ascontiguousarray(p["V"])).pin_memory()
+    vh = Vh.numpy()
+    ctx.set_positions(np.ascontiguousarray(p["V"]))
+    ctx.fa_begin(lamda0=0.05, precision=precision, weight_opt=0.001, **ls)
+
+    def e2e_step():
+        ctx.set_positions_async(vh)
+        ctx.fa_step(hausdorff=do_h, report=False)
+        ctx.get_positions_async(vh)
+        ctx.sync()  # the next step's input is this download
+
+    for _ in range(args.warmup):
+        e2e_step()
     barrier(tdist)
     ctx.timer_start()
     for _ in range(args.steps):
-        ctx.set_positions_async(vin)
-        ctx.fa_step(hausdorff=do_h, report=False)
-        ctx.get_positions_async(vout)
+        e2e_step()
     e2e_ms = max_over_ranks(tdist, ctx.timer_stop())
     e2e = ws * args.steps / (e2e_ms / 1e3)
-    e2e_ok = bool(np.isfinite(vout).all())
+    e2e_ok = bool(np.isfinite(vh).all())
     # ---------------- FP64 plain path on the same input (the mixed vs FP64 comparison), same steps
     out_extra = {}
     if not args.skip_compare:
@@ -262,11 +272,11 @@ def run_ours(args):
         res = {}
         for name, prec in (("fp64", hexopt.FP64), ("mixed", hexopt.MIXED)):
             ctx.set_positions(p["V"])
-            ctx.fa_begin(lamda0=0.05, precision=prec, weight_opt=0.001)
-            ctx.use_graph(True)
+            ctx.fa_begin(lamda0=0.05, precision=prec, weight_opt=0.001, **ls)
+            ctx.use_graph(graph_mode)
             ctx.fa_step(hausdorff=do_h, report=False)  # capture
             ctx.set_positions(p["V"])
-            ctx.fa_begin(lamda0=0.05, precision=prec, weight_opt=0.001)
+            ctx.fa_begin(lamda0=0.05, precision=prec, weight_opt=0.001, **ls)
             ctx.timer_start()
             for _ in range(cmp_steps):
                 ctx.fa_step(hausdorff=do_h, report=False)
@@ -295,7 +305,7 @@ def run_ours(args):
         del res
     # ---------------- roofline of the dominant kernel (element SpMV of the PCG)
     ctx.set_positions(p["V"])
-    ctx.fa_begin(lamda0=0.05, precision=precision, weight_opt=0.001)
+    ctx.fa_begin(lamda0=0.05, precision=precision, weight_opt=0.001, **ls)
     spmv_ms = ctx.time_stage(0, reps=50)
     mixed = precision == hexopt.MIXED
     achieved = spmv_bytes_per_hex(mixed) * nh / (spmv_ms / 1e3) / 1e9
@@ -320,7 +330,8 @@ def run_ours(args):
            "gpu_launches": launches,
            "clocks": clk,
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nv * 3 * 8,
-                   "d2h_bytes_per_step": nv * 3 * 8, "overlapped": True, "result_finite": e2e_ok},
+                   "d2h_bytes_per_step": nv * 3 * 8, "chained": True, "overlapped": False,
+                   "result_finite": e2e_ok},
            "roofline": {"bound": "hbm", "kernel": "k_spmv (element SpMV of the PCG)", "achieved": achieved,
                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": SPMV_DRAM_BYTES_PER_HEX_MIXED * nh if mixed else None,
@@ -599,6 +610,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-hausdorff", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--graph-fixed-rounds", action="store_true",
+                    help="line-search rounds as fixed launches in the step graph (for per-kernel profilers)")
     ap.add_argument("--skip-compare", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=GRID_N,

@@ -177,6 +177,7 @@ struct hexopt_ctx {
   double lamda0 = 0.05, HR = 0.005;
   bool fa_ready = false;
   bool use_graph = false;
+  bool graph_conditionals = true;  // the line-search rounds as a WHILE node when captured
   cudaGraphExec_t graph_exec = nullptr;
   bool graph_hausdorff = false;
   int64_t graph_launches = 0;
@@ -563,10 +564,10 @@ int run_iteration(hexopt_ctx *ctx, bool pre, bool project) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   CK(cudaStreamIsCapturing(st, &cs));
   CK(ensure_side_streams(ctx));
-  CK((launch_line_search<ET, VT>(a, hb, vb, cb, st, ctx->lsb)));
+  CK((launch_line_search<ET, VT>(a, hb, vb, cb, st, ctx->graph_conditionals ? ctx->lsb : nullptr)));
   const int rounds = (kHalvings + 1 + ctx->params.ls_candidates - 1) / ctx->params.ls_candidates;
   // captured: the rounds are a WHILE node, counted here as one iteration (3 kernels)
-  ctx->launches += cs == cudaStreamCaptureStatusActive ? 5 + 3 : 5 + 2 * rounds;
+  ctx->launches += cs == cudaStreamCaptureStatusActive && ctx->graph_conditionals ? 5 + 3 : 5 + 2 * rounds;
   CKL();
   return HEXOPT_OK;
 }
@@ -906,7 +907,7 @@ int hexopt_create(hexopt_ctx **out, int device) {
   ctx->params.exp_factor = 1.0;  // slim_precompute leaves SLIMData::exp_factor at 1 (slim_m.cpp:1125)
   ctx->params.cg_max_iter = 20;
   ctx->params.cg_tol = 1e-8;
-  ctx->params.ls_candidates = 4;
+  ctx->params.ls_candidates = 1;
   ctx->params.cube = 1;
   *out = ctx;
   return HEXOPT_OK;
@@ -2073,6 +2074,13 @@ int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_r
 
 int hexopt_use_graph(hexopt_ctx *ctx, int on) {
   if (!ctx) return HEXOPT_ERR_ARG;
+  if (on < 0 || on > 2) return fail(ctx, HEXOPT_ERR_ARG, "use_graph: on must be 0, 1 or 2");
+  const bool cond = on == 1;
+  if (ctx->graph_exec && cond != ctx->graph_conditionals) {  // the captured form changes
+    cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+  }
+  ctx->graph_conditionals = cond;
   ctx->use_graph = on != 0;
   if (!ctx->use_graph && ctx->graph_exec) {
     cudaGraphExecDestroy(ctx->graph_exec);

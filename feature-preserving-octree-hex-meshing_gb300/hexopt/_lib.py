@@ -392,7 +392,7 @@ class Context:
 
     @staticmethod
     def params(precision=FP64, weight_opt=0.001, energy=SYMMETRIC_DIRICHLET, exp_factor=1.0, cg_max_iter=20,
-               cg_tol=1e-8, ls_candidates=4, cube=1, cg_refine=10, variant=0):
+               cg_tol=1e-8, ls_candidates=1, cube=1, cg_refine=10, variant=0):
         return SlimParams(energy, precision, weight_opt, exp_factor, cg_max_iter, cg_tol, ls_candidates, cube,
                           cg_refine, variant)
 
@@ -535,7 +535,9 @@ class Context:
         return out
 
     def use_graph(self, on=True):
-        self._ck(self.L.hexopt_use_graph(self.h, int(bool(on))), "use_graph")
+        """True / 1: replay each step as a CUDA graph (line-search rounds as a WHILE node); 2: the
+        same with fixed line-search launches (profilable per kernel); False / 0: eager."""
+        self._ck(self.L.hexopt_use_graph(self.h, 2 if on == 2 else int(bool(on))), "use_graph")
 
     # ---- adjoint
     def energy_fwd(self, X=None):

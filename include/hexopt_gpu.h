@@ -85,7 +85,9 @@ typedef struct hexopt_slim_params {
                           the reference */
   int cg_max_iter;     /* 20 (slim_m.cpp:495) */
   double cg_tol;       /* 1e-8 (slim_m.cpp:494) */
-  int ls_candidates;   /* step sizes evaluated per line-search pass, 1..8 (same result, fewer passes) */
+  int ls_candidates;   /* step sizes evaluated per line-search pass, 1..8: the same result either way;
+                          more per pass means fewer passes but more work per pass (1 is fastest when
+                          the first steps are usually accepted, as on the benchmark workloads) */
   int cube;            /* compute_referenceMesh 'cube' flag: 1 in feature alignment */
   int cg_refine;       /* HEXOPT_MIXED only: FP32 PCG iterations between residual replacements, where
                           the accumulated update moves to FP64 and the residual b - A x is
@@ -317,7 +319,9 @@ HEXOPT_API int hexopt_hausdorff_uniform(hexopt_ctx *ctx, int64_t nv0, const doub
  * (-> Hausdorff when do_hausdorff).  lamda0 = feature_weight * MESHRATIO (0.05), upper bound 1e16. */
 HEXOPT_API int hexopt_fa_begin(hexopt_ctx *ctx, const hexopt_slim_params *params, double lamda0, double hausdorff_ratio_t);
 HEXOPT_API int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_report *rep);
-/* Captures one step (without report download) in a CUDA graph and replays it; 1 = on. */
+/* Captures one step (without report download) in a CUDA graph and replays it.  on: 0 = off,
+ * 1 = on (the line-search rounds become a conditional WHILE node), 2 = on with the rounds as
+ * fixed launches (a graph whose kernel nodes a per-kernel profiler can capture). */
 HEXOPT_API int hexopt_use_graph(hexopt_ctx *ctx, int on);
 
 /* ---- adjoint of the total energy (symmetric Dirichlet over corner tets + soft terms) ----

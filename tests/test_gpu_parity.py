@@ -307,8 +307,10 @@ def test_query_budget_does_not_change_results(ctx, hx, oracle):
 
 
 # ------------------------------------------------------------------ feature alignment
-@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("graph", [False, True, 2])
 def test_feature_alignment_cylinder_vs_oracle(ctx, hx, graph):
+    """Eager steps, graph replays with the line-search rounds as a WHILE node (True) and as fixed
+    launches (2) against the oracle's feature-alignment loop."""
     import fa_oracle
     from hexopt import workloads
     p = workloads.cylinder()
@@ -324,6 +326,30 @@ def test_feature_alignment_cylinder_vs_oracle(ctx, hx, graph):
     assert r[0]["lamda"] == pytest.approx(lam, rel=1e-6)
     assert r[0]["energy"] == pytest.approx(info["energy"], rel=1e-6)
     assert r[0]["hausdorff_max"] > 0
+
+
+def test_line_search_while_node_matches_eager(ctx, hx):
+    """Starts whose line searches reject candidates (a heavily jittered grid): graph replays with
+    the rounds as a WHILE node, graph replays with fixed rounds and eager steps take the same
+    halvings and reach the same positions (FP64; up to the float-atomic order of the scatters)."""
+    from hexopt import workloads
+    prec, precision = hx.FP64, "fp64"
+    # the oracle's loop on this start halves the step once, in its 5th iteration
+    p = workloads.grid_box_superellipsoid((6, 5, 7), 0.3, 7, 2000, 3.0)
+    out = {}
+    for graph in (False, True, 2):
+        workloads.load(ctx, [p])
+        ctx.use_graph(graph)
+        ctx.fa_begin(lamda0=0.05, precision=prec, weight_opt=0.001)
+        hv = [ctx.fa_step(hausdorff=True)[0]["halvings"] for _ in range(6)]
+        ctx.use_graph(False)
+        out[graph] = (ctx.get_positions(), hv)
+    print(precision, "halvings per step", out[False][1])
+    assert max(out[False][1]) > 0
+    tol = 1e-9 * diag_of(p["V"])
+    for g in (True, 2):
+        assert out[g][1] == out[False][1]
+        assert np.abs(out[g][0] - out[False][0]).max() <= tol
 
 
 def test_feature_alignment_grid_vs_oracle(ctx, hx):
