@@ -1,7 +1,9 @@
 // hexopt_api.cu -- host runtime behind the C ABI of include/hexopt_gpu.h.
 //
-// One context = one CUDA stream + one batch of meshes resident in HBM.  Every compute stage is a
-// kernel launch over per-mesh segment tables (no block straddles two meshes).  The scalar
+// One context = one compute stream (with two copy streams for the asynchronous transfers and the
+// side streams of a step's parallel branches, all ordered against it by events) + one batch of
+// meshes resident in HBM.  Every compute stage is a kernel launch over per-mesh segment tables
+// (no block straddles two meshes).  The scalar
 // reductions (energies, dot products, minima) are per mesh and summed in a fixed order; the
 // per-vertex scatters (right-hand side, SpMV product, residual, gradient) use float atomics, so
 // positions are not bit-reproducible from run to run (the order of the atomic adds varies).
