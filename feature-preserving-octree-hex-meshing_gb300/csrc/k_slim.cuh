@@ -1355,8 +1355,14 @@ __device__ __forceinline__ void tet_edges_dir(const KArgs &a, const uint32_t hv[
 // Dense exact pass over the recorded tets: the reference's smallest positive root in FP64, one
 // tet per thread, reduced per mesh by atomicMin on the bits of the (non-negative) root.
 template <typename VT>
+// Each thread keeps the minimum of its entries per mesh (flushed when the mesh changes); at the
+// end a warp whose lanes all hold the same mesh takes one atomic instead of 32, which keeps the
+// single-mesh case off one contended word.  Roots are non-negative, so their bit patterns order
+// like the doubles.
 __global__ void __launch_bounds__(128) k_ls_roots(KArgs a) {
   const unsigned n = *a.root_count;
+  int32_t mesh = -1;
+  unsigned long long best = ~0ull;
   for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
     const uint32_t code = a.root_list[e];
     const int64_t h = code >> 3;
@@ -1365,7 +1371,27 @@ __global__ void __launch_bounds__(128) k_ls_roots(KArgs a) {
     double E[3][3], D[3][3];
     tet_edges_dir<VT>(a, hv, (int)(code & 7), E, D);
     const double r = min_pos_root(E, D);
-    atomicMin(a.root_min + a.root_mesh[e], (unsigned long long)__double_as_longlong(r));
+    const int32_t m = a.root_mesh[e];
+    if (m != mesh) {
+      if (mesh >= 0) atomicMin(a.root_min + mesh, best);
+      mesh = m;
+      best = ~0ull;
+    }
+    const unsigned long long rb = (unsigned long long)__double_as_longlong(r);
+    best = rb < best ? rb : best;
+  }
+  const int32_t m0 = __shfl_sync(0xffffffffu, mesh, 0);
+  const bool same = __all_sync(0xffffffffu, mesh == m0 || mesh < 0);
+  if (same && m0 >= 0) {
+    unsigned long long w = best;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long y = __shfl_xor_sync(0xffffffffu, w, o);
+      w = y < w ? y : w;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMin(a.root_min + m0, w);
+  } else if (!same && mesh >= 0) {
+    atomicMin(a.root_min + mesh, best);
   }
 }
 
