@@ -44,9 +44,28 @@ void launch_local(const KArgs &a, int64_t nblk, bool pre, cudaStream_t st) {
   if (pre) k_local<ET, true><<<(unsigned)nblk, a.hthreads, 0, st>>>(a);
   else k_local<ET, false><<<(unsigned)nblk, a.hthreads, 0, st>>>(a);
 }
+// Persistent blocks of k_spmv_pipe: the resident blocks of the whole device, at most one warp
+// per 32-hex unit.
+static int spmv_pipe_blocks(const KArgs &a) {
+  static int resident = 0;
+  if (resident == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmv_pipe, kPipeWarps * 32, 0);
+    resident = std::max(1, sms * per_sm);
+  }
+  const int64_t units = a.hblk * (a.hthreads / 32);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(resident, (units + kPipeWarps - 1) / kPipeWarps));
+}
+static void launch_spmv_pipe(const KArgs &a, int64_t cblk, cudaStream_t st) {
+  const int npipe = spmv_pipe_blocks(a);
+  k_spmv_pipe<<<(unsigned)(npipe + cblk), kPipeWarps * 32, 0, st>>>(a, npipe, a.hthreads / 32);
+}
 template <typename ET, typename VT>
 void launch_spmv_elems(const KArgs &a, int64_t nblk, cudaStream_t st) {
-  k_spmv<ET><<<(unsigned)nblk, a.hthreads, 0, st>>>(a);
+  if constexpr (sizeof(ET) == 4) launch_spmv_pipe(a, 0, st);
+  else k_spmv<ET><<<(unsigned)nblk, a.hthreads, 0, st>>>(a);
 }
 template <typename VT>
 void launch_soft_rhs(const KArgs &a, int64_t nblk, cudaStream_t st) {
@@ -58,7 +77,8 @@ void launch_cg_start(const KArgs &a, int64_t nblk, cudaStream_t st) {
 }
 template <typename VT>
 void launch_cg_iter(const KArgs &a, int64_t hblk, int64_t vblk, int64_t cblk, cudaStream_t st, bool with_dir) {
-  k_spmv<VT><<<(unsigned)(hblk + cblk), a.hthreads, 0, st>>>(a);  // element and soft terms
+  if constexpr (sizeof(VT) == 4) launch_spmv_pipe(a, cblk, st);  // element and soft terms
+  else k_spmv<VT><<<(unsigned)(hblk + cblk), a.hthreads, 0, st>>>(a);
   k_cg_alpha<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
   k_cg_update<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);
   if (with_dir) k_cg_dir<VT><<<(unsigned)vblk, a.vthreads, 0, st>>>(a);

@@ -358,6 +358,108 @@ __global__ void __launch_bounds__(128, sizeof(ET) == 4 ? 8 : 4) k_spmv(KArgs a) 
   for (int c = 0; c < 8; c++) atomic_add3(q, hv[c], F[c][0], F[c][1], F[c][2]);
 }
 
+// Mixed mode, persistent and software-pipelined form of k_spmv (same sums per hex).  A unit is
+// the 32 hexes one warp of k_spmv takes (unit u: segment u / upseg, hexes 32 (u % upseg) on);
+// each warp walks the units with a stride of every warp of the grid.  While it computes unit k,
+// the coefficient tile of unit k+1 (cp.async into the warp's other shared-memory stage), unit
+// k+1's corner ids and cg_done flag, and unit k+2's segment are in flight, so a unit waits only
+// for its L2 direction gathers.  Units that do not fill an aligned tile read their coefficients
+// from global memory.  Blocks from npipe on apply the soft terms of one constraint segment each.
+constexpr int kPipeWarps = 4;
+struct PipeUnit {
+  int64_t hb, he;  // hex range (hb >= he: nothing to do)
+  int32_t mesh;
+};
+__device__ __forceinline__ PipeUnit pipe_unit(const KArgs &a, int64_t u, int64_t nunits, int upseg) {
+  PipeUnit r{0, 0, 0};
+  if (u < nunits) {
+    const Seg s = a.hseg[u / upseg];
+    r.hb = s.begin + 32 * (u % upseg);
+    r.he = min(s.end, r.hb + 32);
+    r.mesh = s.mesh;
+  }
+  return r;
+}
+static __global__ void __launch_bounds__(kPipeWarps * 32, 4) k_spmv_pipe(KArgs a, int npipe, int upseg) {
+  if ((int)blockIdx.x >= npipe) {
+    const Seg cs = a.cseg[blockIdx.x - npipe];
+    if (a.sc[cs.mesh].cg_done) return;
+    for (int64_t i = cs.begin + threadIdx.x; i < cs.end; i += blockDim.x) soft_mv_item<float>(a, cs, i);
+    return;
+  }
+  __shared__ __align__(16) float cs[kPipeWarps][2][48 * 32];  // 48 KB
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float *C = reinterpret_cast<const float *>(a.Ccoef);
+  const float *p = reinterpret_cast<const float *>(a.p);
+  float *q = reinterpret_cast<float *>(a.q);
+  const int64_t nunits = a.hblk * upseg, stride = (int64_t)npipe * kPipeWarps;
+  int64_t u = (int64_t)blockIdx.x * kPipeWarps + w;
+  // stage the coefficient tile of unit t into cs[w][st]; false when it reads global memory
+  auto stage = [&](const PipeUnit &t, int st) -> bool {
+    if ((t.hb & 31) != 0 || t.he - t.hb != 32) return false;
+    const float *src = C + tet_idx<6>(t.hb, 0, 0);  // 1536 floats, 16-byte aligned
+#pragma unroll
+    for (int i = 0; i < 12; i++) cp_async16(&cs[w][st][(i * 32 + lane) * 4], src + (i * 32 + lane) * 4);
+    return true;
+  };
+  auto load_ids = [&](const PipeUnit &t, uint32_t hv[8]) -> int32_t {
+    const int64_t h = t.hb + lane;
+    if (h < t.he) {
+      load_hex(a.hexv, h, hv);
+      return a.gslot[h];
+    }
+#pragma unroll
+    for (int c = 0; c < 8; c++) hv[c] = 0;
+    return -1;
+  };
+  PipeUnit cur = pipe_unit(a, u, nunits, upseg), nxt = pipe_unit(a, u + stride, nunits, upseg);
+  uint32_t hv[8];
+  int32_t gs = load_ids(cur, hv);
+  int done = cur.hb < cur.he ? a.sc[cur.mesh].cg_done : 1;
+  bool staged = stage(cur, 0);
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  for (int st = 0; u < nunits; u += stride, st ^= 1) {
+    // in flight while this unit computes: unit k+2's segment, unit k+1's ids, flag and tile
+    const PipeUnit nn = pipe_unit(a, u + 2 * stride, nunits, upseg);
+    uint32_t hn[8];
+    const int32_t gs_n = load_ids(nxt, hn);
+    const int done_n = nxt.hb < nxt.he ? a.sc[nxt.mesh].cg_done : 1;
+    const bool staged_n = stage(nxt, st ^ 1);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    const int64_t h = cur.hb + lane;
+    const bool live = !done && h < cur.he;
+    float E12[12][3];
+    if (live) hex_edges_vec(p, hv, E12);
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    __syncwarp();
+    if (live) {
+      const float *crow = staged ? &cs[w][st][lane] : C + tet_idx<6>(h, 0, 0);
+      float F[8][3];
+#pragma unroll
+      for (int c = 0; c < 8; c++) F[c][0] = F[c][1] = F[c][2] = 0.f;
+      spmv_tet<float, 0>(a, gs, E12, crow, F);
+      spmv_tet<float, 1>(a, gs, E12, crow, F);
+      spmv_tet<float, 2>(a, gs, E12, crow, F);
+      spmv_tet<float, 3>(a, gs, E12, crow, F);
+      spmv_tet<float, 4>(a, gs, E12, crow, F);
+      spmv_tet<float, 5>(a, gs, E12, crow, F);
+      spmv_tet<float, 6>(a, gs, E12, crow, F);
+      spmv_tet<float, 7>(a, gs, E12, crow, F);
+#pragma unroll
+      for (int c = 0; c < 8; c++) atomic_add3(q, hv[c], F[c][0], F[c][1], F[c][2]);
+    }
+    __syncwarp();  // every lane is done with stage st before the next iteration refills it
+    cur = nxt;
+    nxt = nn;
+#pragma unroll
+    for (int c = 0; c < 8; c++) hv[c] = hn[c];
+    gs = gs_n;
+    done = done_n;
+    staged = staged_n;
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // ------------------------------------------------------------------------------- soft terms
 // add_soft_constraints (slim_m.cpp:597-714) over the constraint items (cons_item): projection
 // points lamda_P |x - bc|^2 (ts.projection, :600-610); glue groups lamda_G (n/(n-1))^2
