@@ -138,9 +138,9 @@ def spmv_bytes_per_hex(mixed: bool) -> float:
     return 32 + 8 * 6 * w + 4 * w + 2 * 4 * w
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_spmv<float> launch per hex,
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_spmv_pipe launch per hex,
 # from an ncu capture on the 96^3 grid (working set above L2; traffic grows with the hex count).
-SPMV_DRAM_BYTES_PER_HEX_MIXED = (234.636544e6 + 13.034496e6) / 96 ** 3
+SPMV_DRAM_BYTES_PER_HEX_MIXED = (234.301184e6 + 10.387712e6) / 96 ** 3
 
 
 def cpu_baseline(steps=None, budget_s=12.0):
@@ -332,7 +332,7 @@ def run_ours(args):
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nv * 3 * 8,
                    "d2h_bytes_per_step": nv * 3 * 8, "chained": True, "overlapped": False,
                    "result_finite": e2e_ok},
-           "roofline": {"bound": "hbm", "kernel": "k_spmv (element SpMV of the PCG)", "achieved": achieved,
+           "roofline": {"bound": "hbm", "kernel": "k_spmv_pipe (element SpMV of the PCG)", "achieved": achieved,
                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": SPMV_DRAM_BYTES_PER_HEX_MIXED * nh if mixed else None,
                         "peak_kind": peak_kind, "kernel_ms": spmv_ms,
