@@ -193,6 +193,9 @@ struct hexopt_ctx {
   // stream (input copied / consumed, output staged / copied)
   cudaStream_t ust = nullptr, dst = nullptr;
   cudaEvent_t in_ready = nullptr, in_free = nullptr, out_ready = nullptr, out_done = nullptr;
+  // recorded by each feature-alignment step once its line search has applied the step (an event
+  // record node in the step's graph): the positions are final from there on
+  cudaEvent_t ev_xfinal = nullptr;
   DBuf in_stage, out_stage;
   // the end of a step forks three ways (Hausdorff side 1 on st, side 0 and the SJ check on their
   // own streams) and joins before the Hausdorff combine; each branch reduces into its own region
@@ -924,7 +927,7 @@ void hexopt_destroy(hexopt_ctx *ctx) {
   if (ctx->dst) cudaStreamSynchronize(ctx->dst);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-  for (cudaEvent_t e : {ctx->in_ready, ctx->in_free, ctx->out_ready, ctx->out_done})
+  for (cudaEvent_t e : {ctx->in_ready, ctx->in_free, ctx->out_ready, ctx->out_done, ctx->ev_xfinal})
     if (e) cudaEventDestroy(e);
   if (ctx->hs0) cudaStreamSynchronize(ctx->hs0);
   if (ctx->hsj) cudaStreamSynchronize(ctx->hsj);
@@ -1998,6 +2001,11 @@ static int fa_enqueue(hexopt_ctx *ctx, int do_hausdorff) {
   // the projection runs beside the local step (slim_precompute fused into it)
   rc = dispatch_iteration(ctx, true, true);
   if (rc) return rc;
+  if (!ctx->ev_xfinal) CK(cudaEventCreateWithFlags(&ctx->ev_xfinal, cudaEventDisableTiming));
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(ctx->st, &cs));
+  if (cs == cudaStreamCaptureStatusActive) CK(cudaEventRecordWithFlags(ctx->ev_xfinal, ctx->st, cudaEventRecordExternal));
+  else CK(cudaEventRecord(ctx->ev_xfinal, ctx->st));
   launch_fa_schedule(ctx->sc_d.as<MeshScalars>(), ctx->n_meshes, ctx->lamda0, 1e16, ctx->st);
   if (!do_hausdorff) launch_step_sj(ctx, ctx->st);
   if (do_hausdorff) {
@@ -2010,7 +2018,35 @@ static int fa_enqueue(hexopt_ctx *ctx, int do_hausdorff) {
   return HEXOPT_OK;
 }
 
+static int fa_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_report *rep, double *V);
+
 int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_report *rep) {
+  return fa_step(ctx, do_hausdorff, rep, nullptr);
+}
+
+int hexopt_feature_alignment_step_get(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_report *rep, double *V) {
+  if (ctx && !V) return fail(ctx, HEXOPT_ERR_ARG, "feature_alignment_step_get: NULL");
+  return fa_step(ctx, do_hausdorff, rep, V);
+}
+
+// The step's download, queued right after the step: staged and copied on the download stream
+// once the step's positions are final (ev_xfinal), beside the step's SJ check and Hausdorff
+// passes; later work on the compute stream waits until the staging kernel has read X.
+static int fa_queue_download(hexopt_ctx *ctx, double *V) {
+  CK(ensure_copy_streams(ctx));
+  CK(ctx->out_stage.ensure(sizeof(double) * 3 * ctx->NV));
+  CK(cudaStreamWaitEvent(ctx->dst, ctx->ev_xfinal, 0));
+  launch_aos4_to_rows_perm(ctx->X.as<double>(), vo2n(ctx), ctx->NV, ctx->out_stage.as<double>(), ctx->dst);
+  ctx->launches++;
+  CKL();
+  CK(cudaEventRecord(ctx->out_ready, ctx->dst));
+  CK(cudaStreamWaitEvent(ctx->st, ctx->out_ready, 0));
+  CK(cudaMemcpyAsync(V, ctx->out_stage.p, sizeof(double) * 3 * ctx->NV, cudaMemcpyDeviceToHost, ctx->dst));
+  CK(cudaEventRecord(ctx->out_done, ctx->dst));
+  return HEXOPT_OK;
+}
+
+static int fa_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_report *rep, double *V) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
   if (!ctx->fa_ready) return fail(ctx, HEXOPT_ERR_STATE, "feature_alignment_step before fa_begin");
@@ -2053,6 +2089,10 @@ int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_r
     ctx->launches += ctx->graph_launches;
   } else {
     rc = fa_enqueue(ctx, do_hausdorff);
+    if (rc) return rc;
+  }
+  if (V) {
+    rc = fa_queue_download(ctx, V);
     if (rc) return rc;
   }
   if (rep) {

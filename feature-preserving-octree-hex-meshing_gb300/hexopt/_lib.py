@@ -117,6 +117,7 @@ SIGNATURES = {
                                                      C.c_size_t]),
     "hexopt_fa_begin": (C.c_int, [_vp, C.POINTER(SlimParams), C.c_double, C.c_double]),
     "hexopt_feature_alignment_step": (C.c_int, [_vp, C.c_int, C.POINTER(FaReport)]),
+    "hexopt_feature_alignment_step_get": (C.c_int, [_vp, C.c_int, C.POINTER(FaReport), _d]),
     "hexopt_use_graph": (C.c_int, [_vp, C.c_int]),
     "hexopt_energy_fwd": (C.c_int, [_vp, _d, _d]),
     "hexopt_energy_bwd": (C.c_int, [_vp, _d]),
@@ -520,9 +521,18 @@ class Context:
         p = self.params(**kw)
         self._ck(self.L.hexopt_fa_begin(self.h, C.byref(p), lamda0, hausdorff_ratio_t), "fa_begin")
 
-    def fa_step(self, hausdorff=False, report=True):
+    def fa_step(self, hausdorff=False, report=True, out=None):
+        """One feature-alignment step.  out (C-contiguous float64, nv x 3): also queue the download
+        of the step's positions in the same call, overlapped with the step's quality and
+        Hausdorff passes; complete after sync()."""
         rep = (FaReport * self.n_meshes)() if report else None
-        self._ck(self.L.hexopt_feature_alignment_step(self.h, int(bool(hausdorff)), rep), "feature_alignment_step")
+        if out is None:
+            self._ck(self.L.hexopt_feature_alignment_step(self.h, int(bool(hausdorff)), rep), "feature_alignment_step")
+        else:
+            if not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.flags.c_contiguous):
+                raise ValueError("fa_step(out=...) needs a C-contiguous float64 array")
+            self._ck(self.L.hexopt_feature_alignment_step_get(self.h, int(bool(hausdorff)), rep, ptr(out, _d)),
+                     "feature_alignment_step_get")
         if not report:
             return None
         out = []

@@ -319,6 +319,13 @@ HEXOPT_API int hexopt_hausdorff_uniform(hexopt_ctx *ctx, int64_t nv0, const doub
  * (-> Hausdorff when do_hausdorff).  lamda0 = feature_weight * MESHRATIO (0.05), upper bound 1e16. */
 HEXOPT_API int hexopt_fa_begin(hexopt_ctx *ctx, const hexopt_slim_params *params, double lamda0, double hausdorff_ratio_t);
 HEXOPT_API int hexopt_feature_alignment_step(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_report *rep);
+/* The same step with the download of its result queued in the same call: V (nv x 3 float64, the
+ * caller's vertex order, as hexopt_get_positions_async) receives the positions the step's line
+ * search produced.  They are staged and copied on the download stream as soon as the line search
+ * has applied its step, beside the step's scaled-Jacobian check and Hausdorff passes, instead of
+ * after them; complete after hexopt_sync.  V must stay alive until then (page-locked memory lets
+ * the copy overlap the computation). */
+HEXOPT_API int hexopt_feature_alignment_step_get(hexopt_ctx *ctx, int do_hausdorff, hexopt_fa_report *rep, double *V);
 /* Captures one step (without report download) in a CUDA graph and replays it.  on: 0 = off,
  * 1 = on (the line-search rounds become a conditional WHILE node), 2 = on with the rounds as
  * fixed launches (a graph whose kernel nodes a per-kernel profiler can capture). */

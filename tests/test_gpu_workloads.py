@@ -262,7 +262,9 @@ def test_async_position_transfers_match_synchronous(hx, graph):
     """Streaming positions through the optimiser with the asynchronous transfers (uploads and
     downloads on the copy stream, overlapping the steps; one synchronisation at the end) gives,
     step for step, the positions of the synchronous set_positions / fa_step / get_positions
-    sequence, with and without graph replay.  Page-locked buffers (torch) and pageable numpy
+    sequence, with and without graph replay, whether the download is a call of its own or is
+    queued inside the step's call (fa_step(out=...), staged beside the step's tail), and when each
+    step's input is the previous step's download.  Page-locked buffers (torch) and pageable numpy
     buffers both work."""
     import torch
     from hexopt import workloads
@@ -289,14 +291,37 @@ def test_async_position_transfers_match_synchronous(hx, graph):
             else:
                 ins = [V.copy() for V in inputs]
                 outs = [np.empty_like(V) for V in inputs]
-            ctx.fa_begin(lamda0=0.05, precision=hx.FP64, weight_opt=0.001)
-            for V, out in zip(ins, outs):
-                ctx.set_positions_async(V)
-                ctx.fa_step(hausdorff=True, report=False)
-                ctx.get_positions_async(out)
-            ctx.sync()
             d = float(np.linalg.norm(p["V"].max(0) - p["V"].min(0)))
-            for k, (a, b) in enumerate(zip(outs, ref)):
-                assert np.abs(a - b).max() <= 1e-9 * d, (pinned, k, float(np.abs(a - b).max()))
+            # the download queued by a separate call after the step, then inside the step's own
+            # call (staged once the line search has applied the step, beside the step's tail)
+            for fused in (False, True):
+                ctx.fa_begin(lamda0=0.05, precision=hx.FP64, weight_opt=0.001)
+                for out in outs:
+                    out.fill(np.nan)
+                for V, out in zip(ins, outs):
+                    ctx.set_positions_async(V)
+                    if fused:
+                        ctx.fa_step(hausdorff=True, report=False, out=out)
+                    else:
+                        ctx.fa_step(hausdorff=True, report=False)
+                        ctx.get_positions_async(out)
+                ctx.sync()
+                for k, (a, b) in enumerate(zip(outs, ref)):
+                    assert np.abs(a - b).max() <= 1e-9 * d, (pinned, fused, k, float(np.abs(a - b).max()))
+            # chained as the end-to-end loop runs it: each step's input is the previous download
+            ctx.fa_begin(lamda0=0.05, precision=hx.FP64, weight_opt=0.001)
+            chain = ins[0].copy() if not pinned else torch.from_numpy(ins[0].copy()).pin_memory().numpy()
+            got = []
+            for _ in range(3):
+                ctx.set_positions_async(chain)
+                ctx.fa_step(hausdorff=True, report=False, out=chain)
+                ctx.sync()
+                got.append(chain.copy())
+            ctx.fa_begin(lamda0=0.05, precision=hx.FP64, weight_opt=0.001)
+            ctx.set_positions(ins[0])
+            for k in range(3):
+                ctx.fa_step(hausdorff=True, report=False)
+                want = ctx.get_positions()
+                assert np.abs(got[k] - want).max() <= 1e-9 * d, (pinned, "chained", k, float(np.abs(got[k] - want).max()))
     finally:
         ctx.close()
